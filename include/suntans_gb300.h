@@ -1,0 +1,144 @@
+/*
+ * suntans_gb300.h -- C ABI of the GB300 elliptic solvers for SUNTANS.
+ *
+ * Drop-in replacements for the two conjugate-gradient solves of the SUNTANS
+ * reference (ofringer/suntans, main/phys.c):
+ *
+ *   static void CGSolveQ(REAL **q, REAL **src, REAL **c, gridT *grid, physT *phys,
+ *                        propT *prop, int myproc, int numprocs, MPI_Comm comm);
+ *        declared main/phys.c:50-52, defined main/phys.c:2411-2550
+ *   static void CGSolve(gridT *grid, physT *phys, propT *prop, int myproc,
+ *                       int numprocs, MPI_Comm comm);
+ *        declared main/phys.c:45-46, defined main/phys.c:3086-3217
+ *
+ * Every entry point takes plain pointers and sizes.  The 3-D fields are the
+ * reference's own jagged arrays: row i of q, src, c and dzz points at Nk[i]
+ * doubles (cell index order), row j of dzf at Nke[j] doubles.  The solves run
+ * on one GPU as a single partition: the reference's halo exchanges
+ * (ISendRecvCellData2D/3D, main/sendrecv.c:134-217) have nothing to exchange
+ * and its MPI_Reduce + MPI_Bcast inner products (main/phys.c:3290-3291,
+ * 3315-3316) become in-kernel reductions.  There is no CPU fallback: without a
+ * usable CUDA device every entry point returns SGPU_NO_DEVICE.
+ *
+ * Adapter for the reference's own signatures (gridT/physT/propT) and the
+ * two-line call-site patch: INTEGRATION.md and suntans_gb300/shim/.
+ */
+#ifndef SUNTANS_GB300_H
+#define SUNTANS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (every entry point returns one) */
+#define SGPU_OK 0          /* converged (or eps == 0 at start, as the reference) */
+#define SGPU_MAXITER 1     /* maxiters reached without convergence; x is the last iterate */
+#define SGPU_BREAKDOWN 2   /* p.Ap == 0 or a non-finite scalar; the solve stopped */
+#define SGPU_TIMEOUT 3     /* a device-side barrier wait hit its time limit */
+#define SGPU_OOM 4         /* device or pinned allocation failed */
+#define SGPU_BAD_GRID 5    /* grid description fails validation (message: sgpu_last_error) */
+#define SGPU_BAD_ARG 6     /* null pointer or out-of-range parameter */
+#define SGPU_CUDA_ERROR 7  /* a CUDA call failed (message: sgpu_last_error) */
+#define SGPU_NO_DEVICE 8   /* no CUDA device, or the library was built without one */
+
+/* The part of gridT (main/grid.h:32-149) the two solves read and that does not
+ * change between time steps.  Arrays are copied at sgpu_create; the caller
+ * keeps ownership. */
+typedef struct sgpu_grid_desc {
+  int Nc, Ne, maxfaces, Nkmax;
+  const int *nfaces;   /* [Nc]             gridT.nfaces                         */
+  const int *neigh;    /* [Nc*maxfaces]    gridT.neigh, -1 = no neighbour       */
+  const int *face;     /* [Nc*maxfaces]    gridT.face                           */
+  const int *Nk;       /* [Nc]             gridT.Nk                             */
+  const int *Nke;      /* [Ne]             gridT.Nke                            */
+  const int *cellp;    /* [celldist[2]]    gridT.cellp                          */
+  const int *celldist; /* [3]              gridT.celldist                       */
+  const double *Ac;    /* [Nc]             gridT.Ac                             */
+  const double *df;    /* [Ne]             gridT.df                             */
+  const double *dg;    /* [Ne]             gridT.dg                             */
+} sgpu_grid_desc;
+
+/* The propT fields (main/phys.h:183-203) the two solves read. */
+typedef struct sgpu_props {
+  int qprecond;     /* 0 none, 1 diagonal scaling (OperatorQC), 2 column tridiagonal */
+  int qmaxiters;
+  double qepsilon;
+  int hprecond;     /* 0 none, 1 Jacobi */
+  int maxiters;
+  double epsilon;
+  double resnorm;   /* 0: qprecond 0/1 and hprecond 0 stop on the absolute norm */
+  double grav, theta, dt;
+} sgpu_props;
+
+/* Per-solve report (not in the reference, which returns void). */
+typedef struct sgpu_stats {
+  int status;
+  int niters;        /* solver iterations executed */
+  double eps, eps0;  /* last eps and its normaliser: converged iff sqrt(eps/eps0) < tol */
+  double ms_solve;   /* device time of the solve kernel (CUDA events) */
+  double ms_total;   /* wall time of the call, copies included */
+  long long unknowns;/* N_q = sum (Nk - ctop) over computational cells, or N_h */
+} sgpu_stats;
+
+typedef struct sgpu_context sgpu_context;
+
+/* Builds the device copy of one grid on CUDA device `device` (the context's
+ * device stays current only inside calls).  Replaces nothing in the reference:
+ * it is the one-time upload the reference never needed (its grid lives in host
+ * memory).  Returns SGPU_BAD_GRID with a message for inconsistent input. */
+int sgpu_create(const sgpu_grid_desc *grid, int device, sgpu_context **out);
+int sgpu_destroy(sgpu_context *ctx);
+const char *sgpu_last_error(const sgpu_context *ctx);
+const char *sgpu_status_string(int status);
+
+/* CGSolveQ drop-in (main/phys.c:2411-2550).
+ *   ctop[Nc]            gridT.ctop            (changes every step)
+ *   dzz[Nc][Nk]         gridT.dzz             (changes every step)
+ *   dzf[Ne][Nke]        gridT.dzf             (changes every step)
+ *   D[Ne]               phys->D = df/dg       (set by ComputeQSource, phys.c:2392)
+ *   q[Nc][Nk]           phys->qc: warm start in, solution out (computational cells,
+ *                       k in [ctop, Nk)); other entries untouched, as in the reference
+ *   src[Nc][Nk]         phys->stmp: right-hand side.  The reference destroys it (uses it
+ *                       as p); this call leaves it unchanged, which no caller can observe
+ *   c[Nc][Nk]           preconditioner buffer: read only at type-3 boundary cells for
+ *                       qprecond 1 (the reference reads whatever the buffer holds there).
+ *                       Not written (the reference's buffer aliases its residual).
+ */
+int sgpu_cgsolveq(sgpu_context *ctx, const int *ctop, const double *const *dzz, const double *const *dzf,
+                  const double *D, double *const *q, const double *const *src, const double *const *c,
+                  const sgpu_props *prop, sgpu_stats *stats);
+
+/* CGSolve drop-in (main/phys.c:3086-3217).
+ *   D[Ne]      phys->D = sum_k E dzf (UPredictor, main/phys.c:2935-2937)
+ *   h[Nc]      phys->h: type-3 boundary values in; solution out at computational cells
+ *   htmp[Nc]   phys->htmp: right-hand side (left unchanged; the reference destroys it) */
+int sgpu_cgsolve(sgpu_context *ctx, const double *D, double *h, const double *htmp,
+                 const sgpu_props *prop, sgpu_stats *stats);
+
+/* Staged forms of the same two solves, for callers that keep inputs resident:
+ * upload (host -> HBM), solve (HBM only; repeatable on the same inputs), and
+ * download (HBM -> host, computational cells / active levels only). */
+int sgpu_q_upload(sgpu_context *ctx, const int *ctop, const double *const *dzz, const double *const *dzf,
+                  const double *D, const double *const *q, const double *const *src, const double *const *c);
+int sgpu_q_solve(sgpu_context *ctx, const sgpu_props *prop, sgpu_stats *stats);
+int sgpu_q_download(sgpu_context *ctx, double *const *q);
+int sgpu_h_upload(sgpu_context *ctx, const double *D, const double *h, const double *htmp);
+int sgpu_h_solve(sgpu_context *ctx, const sgpu_props *prop, sgpu_stats *stats);
+int sgpu_h_download(sgpu_context *ctx, double *h);
+
+/* Device-side barrier wait limit in nanoseconds (default 2e9).  A wait that
+ * runs out ends the solve with SGPU_TIMEOUT instead of hanging. */
+int sgpu_set_timeout_ns(sgpu_context *ctx, long long ns);
+
+/* Number of CTAs the persistent kernels are launched with (0 = one full wave,
+ * the default).  For experiments and tests of the reduction order. */
+int sgpu_set_grid(sgpu_context *ctx, int ctas);
+
+/* The CUDA stream (cudaStream_t) every call of this context runs on, so that a
+ * caller can order its own work or record timing events around the solves. */
+void *sgpu_stream(sgpu_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

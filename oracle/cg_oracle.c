@@ -1,0 +1,471 @@
+/*
+ * cg_oracle.c -- TEST INFRASTRUCTURE ONLY (the "port" oracle).
+ *
+ * A plain-C restatement, on flat arrays, of the SUNTANS elliptic solves:
+ * the nonhydrostatic pressure PCG (CGSolveQ and its helpers) and the
+ * free-surface PCG (CGSolve and its helpers) from the reference's main/phys.c,
+ * plus the Thomas solver from main/util.c.  Every function cites the reference
+ * lines it follows.  The operation order of each floating-point expression is
+ * the reference's, and the file is compiled with -ffp-contract=off, so on the
+ * same inputs it returns the same bits as the reference built with gcc -O2
+ * (tests/test_oracle.py checks this against oracle/_ref where the reference
+ * sources are present, and against the committed golden vectors everywhere).
+ *
+ * Deviations from the reference, all at the call boundary, none in arithmetic:
+ *  - the qprecond=1 preconditioner buffer c is the caller's own array; in the
+ *    reference the call site passes phys->stmp3, which is also the residual r
+ *    inside CGSolveQ (main/phys.c:1280 with main/phys.c:2419), so the final
+ *    rescale divides by the converged residual.  Here c never aliases r.
+ *  - scratch arrays are private to each call instead of physT fields.
+ *
+ * The product never links this file; the CUDA path is checked against it.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "cg_oracle.h"
+
+typedef struct {
+  long *coff;   /* [Nc+1] offsets of cell columns in the ragged arrays */
+  long *eoff;   /* [Ne+1] offsets of edge columns in dzf               */
+  long n3;      /* sum(Nk)                                             */
+} layout_t;
+
+static void layout_make(const sgo_grid *g, layout_t *L) {
+  int i, j;
+  L->coff = (long *)malloc(sizeof(long) * (g->Nc + 1));
+  L->eoff = (long *)malloc(sizeof(long) * (g->Ne + 1));
+  L->coff[0] = 0;
+  for (i = 0; i < g->Nc; i++) L->coff[i + 1] = L->coff[i] + g->Nk[i];
+  L->eoff[0] = 0;
+  for (j = 0; j < g->Ne; j++) L->eoff[j + 1] = L->eoff[j] + g->Nke[j];
+  L->n3 = L->coff[g->Nc];
+}
+static void layout_free(layout_t *L) { free(L->coff); free(L->eoff); }
+
+#define X3(a, i, k) (a)[L->coff[(i)] + (k)]
+#define DZZ(i, k) g->dzz[L->coff[(i)] + (k)]
+#define DZF(j, k) g->dzf[L->eoff[(j)] + (k)]
+/* fcoef row (i,nf) has Nk[i] entries and starts at maxfaces*coff[i] + nf*Nk[i] */
+#define FC(i, nf, k) fcoef[(long)g->maxfaces * L->coff[(i)] + (long)(nf) * g->Nk[(i)] + (k)]
+
+/* Inner product over computational cells: main/phys.c:3304-3319 (InnerProduct3).
+   Sequential sum in cellp order; the serial MPI_Reduce/MPI_Bcast are copies. */
+static double inner3(const sgo_grid *g, const layout_t *L, const double *x, const double *y) {
+  double mysum = 0;
+  int iptr, i, k;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) mysum += X3(x, i, k) * X3(y, i, k);
+  }
+  return mysum;
+}
+
+/* main/phys.c:3280-3294 (InnerProduct) */
+static double inner2(const sgo_grid *g, const double *x, const double *y) {
+  double mysum = 0;
+  int iptr, i;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    mysum += x[i] * y[i];
+  }
+  return mysum;
+}
+
+static int kmin_of(const sgo_grid *g, int i, int nc) {
+  return g->ctop[nc] > g->ctop[i] ? g->ctop[nc] : g->ctop[i];
+}
+
+/* QCoefficients: main/phys.c:3420-3471. coef has the ragged cell layout. */
+static void qcoef_impl(const sgo_grid *g, const layout_t *L, const double *D, const double *c,
+                       int qprecond, double *coef, double *fcoef) {
+  int iptr, i, k, nf, nc, ne, kmin;
+  if (qprecond == 1) {
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      X3(coef, i, g->ctop[i]) = g->Ac[i] / DZZ(i, g->ctop[i]) / X3(c, i, g->ctop[i]);
+      for (k = g->ctop[i] + 1; k < g->Nk[i]; k++)
+        X3(coef, i, k) = 2 * g->Ac[i] / (DZZ(i, k) + DZZ(i, k - 1)) / (X3(c, i, k) * X3(c, i, k - 1));
+      for (nf = 0; nf < g->nfaces[i]; nf++)
+        if ((nc = g->neigh[i * g->maxfaces + nf]) != -1) {
+          ne = g->face[i * g->maxfaces + nf];
+          kmin = kmin_of(g, i, nc);
+          for (k = kmin; k < g->Nke[ne]; k++)
+            FC(i, nf, k) = DZZ(i, k) * D[ne] / (X3(c, i, k) * X3(c, nc, k));
+        }
+    }
+  } else {
+    /* the reference loops over all Nc cells here, not only computational ones */
+    for (i = 0; i < g->Nc; i++) {
+      X3(coef, i, g->ctop[i]) = g->Ac[i] / DZZ(i, g->ctop[i]);
+      for (k = g->ctop[i] + 1; k < g->Nk[i]; k++)
+        X3(coef, i, k) = 2 * g->Ac[i] / (DZZ(i, k) + DZZ(i, k - 1));
+    }
+  }
+}
+
+/* OperatorQ: main/phys.c:3486-3536 */
+static void opq_impl(const sgo_grid *g, const layout_t *L, const double *D, const double *coef,
+                     const double *x, double *y) {
+  int iptr, i, k, nf, nc, ne, kmin;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(y, i, k) = 0;
+    for (nf = 0; nf < g->nfaces[i]; nf++)
+      if ((nc = g->neigh[i * g->maxfaces + nf]) != -1) {
+        ne = g->face[i * g->maxfaces + nf];
+        kmin = kmin_of(g, i, nc);
+        for (k = kmin; k < g->Nke[ne]; k++)
+          X3(y, i, k) += (X3(x, nc, k) - X3(x, i, k)) * DZF(ne, k) * D[ne];
+      }
+    for (k = g->ctop[i] + 1; k < g->Nk[i] - 1; k++)
+      X3(y, i, k) += X3(coef, i, k) * X3(x, i, k - 1) - (X3(coef, i, k) + X3(coef, i, k + 1)) * X3(x, i, k) +
+                     X3(coef, i, k + 1) * X3(x, i, k + 1);
+    if (g->ctop[i] < g->Nk[i] - 1) {
+      k = g->ctop[i];
+      X3(y, i, k) += (-2 * X3(coef, i, k) - X3(coef, i, k + 1)) * X3(x, i, k) + X3(coef, i, k + 1) * X3(x, i, k + 1);
+      k = g->Nk[i] - 1;
+      X3(y, i, k) += X3(coef, i, k) * X3(x, i, k - 1) - X3(coef, i, k) * X3(x, i, k);
+    } else
+      X3(y, i, g->ctop[i]) -= 2.0 * X3(coef, i, g->ctop[i]) * X3(x, i, g->ctop[i]);
+  }
+}
+
+/* OperatorQC: main/phys.c:3364-3409 */
+static void opqc_impl(const sgo_grid *g, const layout_t *L, const double *coef, const double *fcoef,
+                      const double *x, double *y) {
+  int iptr, i, k, nf, nc, ne, kmin;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(y, i, k) = -X3(x, i, k);
+    for (nf = 0; nf < g->nfaces[i]; nf++)
+      if ((nc = g->neigh[i * g->maxfaces + nf]) != -1) {
+        ne = g->face[i * g->maxfaces + nf];
+        kmin = kmin_of(g, i, nc);
+        for (k = kmin; k < g->Nke[ne]; k++) X3(y, i, k) += X3(x, nc, k) * FC(i, nf, k);
+      }
+    for (k = g->ctop[i] + 1; k < g->Nk[i] - 1; k++)
+      X3(y, i, k) += X3(coef, i, k) * X3(x, i, k - 1) + X3(coef, i, k + 1) * X3(x, i, k + 1);
+    if (g->ctop[i] < g->Nk[i] - 1) {
+      k = g->ctop[i];
+      X3(y, i, k) += X3(coef, i, k + 1) * X3(x, i, k + 1);
+      k = g->Nk[i] - 1;
+      X3(y, i, k) += X3(coef, i, k) * X3(x, i, k - 1);
+    }
+  }
+}
+
+/* ConditionQ: main/phys.c:3629-3687.  a[] is the reference's phys->a scratch. */
+static void condq_impl(const sgo_grid *g, const layout_t *L, const double *D, double *x) {
+  int iptr, i, k, nf, nc, ne, kmin;
+  double *a = (double *)malloc(sizeof(double) * (g->Nkmax + 2));
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(x, i, k) = 0;
+    for (nf = 0; nf < g->nfaces[i]; nf++)
+      if ((nc = g->neigh[i * g->maxfaces + nf]) != -1) {
+        ne = g->face[i * g->maxfaces + nf];
+        kmin = kmin_of(g, i, nc);
+        for (k = kmin; k < g->Nke[ne]; k++) X3(x, i, k) += DZZ(i, k) * D[ne];
+      }
+    a[g->ctop[i]] = g->Ac[i] / DZZ(i, g->ctop[i]);
+    for (k = g->ctop[i] + 1; k < g->Nk[i]; k++) a[k] = 2 * g->Ac[i] / (DZZ(i, k) + DZZ(i, k - 1));
+    for (k = g->ctop[i] + 1; k < g->Nk[i] - 1; k++) X3(x, i, k) += (a[k] + a[k + 1]);
+    if (g->ctop[i] < g->Nk[i] - 1) {
+      k = g->ctop[i];
+      X3(x, i, k) += 2 * a[k] + a[k + 1];
+      k = g->Nk[i] - 1;
+      X3(x, i, k) += a[k];
+    }
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) {
+      if (X3(x, i, k) <= 0) X3(x, i, k) = 1;
+      X3(x, i, k) = sqrt(X3(x, i, k));
+    }
+  }
+  free(a);
+}
+
+/* TriSolve: main/util.c:185-203 (Thomas algorithm; overwrites b and d). */
+static void trisolve(double *a, double *b, double *c, double *d, double *u, int N) {
+  int k;
+  for (k = 1; k < N; k++) {
+    b[k] -= a[k] * c[k - 1] / b[k - 1];
+    d[k] -= a[k] * d[k - 1] / b[k - 1];
+  }
+  u[N - 1] = d[N - 1] / b[N - 1];
+  for (k = N - 2; k >= 0; k--) u[k] = d[k] / b[k] - c[k] * u[k + 1] / b[k];
+}
+
+/* Preconditioner: main/phys.c:3577-3619 */
+static void precond_impl(const sgo_grid *g, const layout_t *L, const double *coef, const double *x,
+                         double *xc) {
+  int iptr, i, k, n = g->Nkmax + 2;
+  double *a = (double *)calloc(n, sizeof(double)), *b = (double *)calloc(n, sizeof(double));
+  double *c = (double *)calloc(n, sizeof(double)), *d = (double *)calloc(n, sizeof(double));
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    if (g->ctop[i] < g->Nk[i] - 1) {
+      for (k = g->ctop[i] + 1; k < g->Nk[i] - 1; k++) {
+        a[k] = X3(coef, i, k);
+        b[k] = -X3(coef, i, k) - X3(coef, i, k + 1);
+        c[k] = X3(coef, i, k + 1);
+        d[k] = X3(x, i, k);
+      }
+      k = g->ctop[i];
+      b[k] = -2 * X3(coef, i, k) - X3(coef, i, k + 1);
+      c[k] = X3(coef, i, k + 1);
+      d[k] = X3(x, i, k);
+      k = g->Nk[i] - 1;
+      a[k] = X3(coef, i, k);
+      b[k] = -X3(coef, i, k);
+      d[k] = X3(x, i, k);
+      trisolve(&a[g->ctop[i]], &b[g->ctop[i]], &c[g->ctop[i]], &d[g->ctop[i]], &X3(xc, i, g->ctop[i]),
+               g->Nk[i] - g->ctop[i]);
+    } else
+      X3(xc, i, g->ctop[i]) = -0.5 * X3(x, i, g->ctop[i]) / X3(coef, i, g->ctop[i]);
+  }
+  free(a); free(b); free(c); free(d);
+}
+
+/* CGSolveQ: main/phys.c:2411-2550 (x = q, p = src, z, r, rtmp as scratch). */
+void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
+                  const sgo_prop *pr, sgo_result *res) {
+  layout_t Lv, *L = &Lv;
+  int iptr, i, k, n, niters, executed = 0;
+  double mu, nu, alpha, alpha0, eps, eps0;
+  double *x = q, *p = src, *z, *r, *rtmp, *coef, *fcoef;
+  layout_make(g, L);
+  z = (double *)calloc(L->n3 + 1, sizeof(double));
+  r = (double *)calloc(L->n3 + 1, sizeof(double));
+  rtmp = (double *)calloc(L->n3 + 1, sizeof(double));
+  coef = (double *)calloc(L->n3 + 1, sizeof(double));
+  fcoef = (double *)calloc((size_t)g->maxfaces * L->n3 + 1, sizeof(double));
+
+  if (pr->qprecond == 1) {
+    condq_impl(g, L, D, c);
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) {
+        X3(p, i, k) /= X3(c, i, k);
+        X3(x, i, k) *= X3(c, i, k);
+      }
+    }
+  }
+  niters = pr->qmaxiters;
+  qcoef_impl(g, L, D, c, pr->qprecond, coef, fcoef);
+
+  if (pr->qprecond == 1) opqc_impl(g, L, coef, fcoef, x, z);
+  else opq_impl(g, L, D, coef, x, z);
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(r, i, k) = X3(p, i, k) - X3(z, i, k);
+  }
+  if (pr->qprecond == 2) {
+    precond_impl(g, L, coef, r, rtmp);
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(p, i, k) = X3(rtmp, i, k);
+    }
+    alpha = alpha0 = inner3(g, L, r, rtmp);
+  } else {
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(p, i, k) = X3(r, i, k);
+    }
+    alpha = alpha0 = inner3(g, L, r, r);
+  }
+  if (!pr->resnorm) alpha0 = 1;
+  if (pr->qprecond == 2) eps = eps0 = inner3(g, L, r, r);
+  else eps = eps0 = alpha0;
+
+  for (n = 0; n < niters && eps != 0; n++) {
+    executed++;
+    if (pr->qprecond == 1) opqc_impl(g, L, coef, fcoef, p, z);
+    else opq_impl(g, L, D, coef, p, z);
+    mu = 1 / alpha;
+    nu = alpha / inner3(g, L, p, z);
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) {
+        X3(x, i, k) += nu * X3(p, i, k);
+        X3(r, i, k) -= nu * X3(z, i, k);
+      }
+    }
+    if (pr->qprecond == 2) {
+      precond_impl(g, L, coef, r, rtmp);
+      alpha = inner3(g, L, r, rtmp);
+      mu *= alpha;
+      for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+        i = g->cellp[iptr];
+        for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(p, i, k) = X3(rtmp, i, k) + mu * X3(p, i, k);
+      }
+    } else {
+      alpha = inner3(g, L, r, r);
+      mu *= alpha;
+      for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+        i = g->cellp[iptr];
+        for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(p, i, k) = X3(r, i, k) + mu * X3(p, i, k);
+      }
+    }
+    if (pr->qprecond == 2) eps = inner3(g, L, r, r);
+    else eps = alpha;
+    if (sqrt(eps / eps0) < pr->qepsilon) break;
+  }
+  if (pr->qprecond == 1) {
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(x, i, k) /= X3(c, i, k);
+    }
+  }
+  if (res) { res->niters = executed; res->eps = eps; res->eps0 = eps0; }
+  free(z); free(r); free(rtmp); free(coef); free(fcoef);
+  layout_free(L);
+}
+
+/* HCoefficients: main/phys.c:3252-3269 */
+static void hcoef_impl(const sgo_grid *g, const double *D, const sgo_prop *pr, double *coef, double *fcoef) {
+  int iptr, i, nf, ne;
+  double tmp = pr->grav * pow(pr->theta * pr->dt, 2);
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    coef[i] = g->Ac[i];
+    for (nf = 0; nf < g->nfaces[i]; nf++)
+      if (g->neigh[i * g->maxfaces + nf] != -1) {
+        ne = g->face[i * g->maxfaces + nf];
+        fcoef[i * g->maxfaces + nf] = tmp * D[ne] * g->df[ne] / g->dg[ne];
+        coef[i] += fcoef[i * g->maxfaces + nf];
+      }
+  }
+}
+
+/* OperatorH: main/phys.c:3335-3349 */
+static void oph_impl(const sgo_grid *g, const double *x, double *y, const double *coef, const double *fcoef) {
+  int iptr, i, nf;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    y[i] = coef[i] * x[i];
+    for (nf = 0; nf < g->nfaces[i]; nf++)
+      if (g->neigh[i * g->maxfaces + nf] != -1)
+        y[i] -= fcoef[i * g->maxfaces + nf] * x[g->neigh[i * g->maxfaces + nf]];
+  }
+}
+
+/* CGSolve: main/phys.c:3086-3217 (x = h, p = htmp; r, rtmp, z scratch). */
+void sgo_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp, const sgo_prop *pr,
+                 sgo_result *res) {
+  int iptr, i, n, niters, executed = 0;
+  double mu, nu, eps, eps0, alpha, alpha0;
+  double *x = h, *p = htmp, *r, *rtmp, *z, *hcoef, *hfcoef;
+  r = (double *)calloc(g->Nc + 1, sizeof(double));
+  rtmp = (double *)calloc(g->Nc + 1, sizeof(double));
+  z = (double *)calloc(g->Nc + 1, sizeof(double));
+  hcoef = (double *)calloc(g->Nc + 1, sizeof(double));
+  hfcoef = (double *)calloc((size_t)g->maxfaces * g->Nc + 1, sizeof(double));
+  niters = pr->maxiters;
+  hcoef_impl(g, D, pr, hcoef, hfcoef);
+
+  /* type-3 boundary lift, main/phys.c:3102-3134 */
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) x[g->cellp[iptr]] = 0;
+  oph_impl(g, x, z, hcoef, hfcoef);
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    p[i] = p[i] - z[i];
+    r[i] = p[i];
+    x[i] = 0;
+  }
+  for (iptr = g->celldist[1]; iptr < g->celldist[2]; iptr++) p[g->cellp[iptr]] = 0;
+
+  if (pr->hprecond == 1) {
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) { /* HPreconditioner 3227-3235 */
+      i = g->cellp[iptr];
+      rtmp[i] = r[i] / hcoef[i];
+    }
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      p[i] = rtmp[i];
+    }
+    alpha = alpha0 = inner2(g, r, rtmp);
+  } else {
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      p[i] = r[i];
+    }
+    alpha = alpha0 = inner2(g, r, r);
+  }
+  if (!pr->resnorm) alpha0 = 1;
+  if (pr->hprecond == 1) eps = eps0 = inner2(g, r, r);
+  else eps = eps0 = alpha0;
+
+  for (n = 0; n < niters && eps != 0 && alpha != 0; n++) {
+    executed++;
+    oph_impl(g, p, z, hcoef, hfcoef);
+    mu = 1 / alpha;
+    nu = alpha / inner2(g, p, z);
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      x[i] += nu * p[i];
+      r[i] -= nu * z[i];
+    }
+    if (pr->hprecond == 1) {
+      for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+        i = g->cellp[iptr];
+        rtmp[i] = r[i] / hcoef[i];
+      }
+      alpha = inner2(g, r, rtmp);
+      mu *= alpha;
+      for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+        i = g->cellp[iptr];
+        p[i] = rtmp[i] + mu * p[i];
+      }
+    } else {
+      alpha = inner2(g, r, r);
+      mu *= alpha;
+      for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+        i = g->cellp[iptr];
+        p[i] = r[i] + mu * p[i];
+      }
+    }
+    if (pr->hprecond == 1) eps = inner2(g, r, r);
+    else eps = alpha;
+    if (sqrt(eps / eps0) < pr->epsilon) break;
+  }
+  if (res) { res->niters = executed; res->eps = eps; res->eps0 = eps0; }
+  free(r); free(rtmp); free(z); free(hcoef); free(hfcoef);
+}
+
+/* ---- single-operator entry points (kernel-level parity) ---- */
+void sgo_qcoefficients(const sgo_grid *g, const double *D, const double *c, int qprecond, double *coef,
+                       double *fcoef) {
+  layout_t Lv; layout_make(g, &Lv);
+  qcoef_impl(g, &Lv, D, c, qprecond, coef, fcoef);
+  layout_free(&Lv);
+}
+void sgo_operator_q(const sgo_grid *g, const double *D, const double *coef, const double *x, double *y) {
+  layout_t Lv; layout_make(g, &Lv);
+  opq_impl(g, &Lv, D, coef, x, y);
+  layout_free(&Lv);
+}
+void sgo_operator_qc(const sgo_grid *g, const double *coef, const double *fcoef, const double *x, double *y) {
+  layout_t Lv; layout_make(g, &Lv);
+  opqc_impl(g, &Lv, coef, fcoef, x, y);
+  layout_free(&Lv);
+}
+void sgo_condition_q(const sgo_grid *g, const double *D, double *c) {
+  layout_t Lv; layout_make(g, &Lv);
+  condq_impl(g, &Lv, D, c);
+  layout_free(&Lv);
+}
+void sgo_preconditioner(const sgo_grid *g, const double *coef, const double *x, double *xc) {
+  layout_t Lv; layout_make(g, &Lv);
+  precond_impl(g, &Lv, coef, x, xc);
+  layout_free(&Lv);
+}
+void sgo_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p, double *hcoef, double *hfcoef) {
+  hcoef_impl(g, D, p, hcoef, hfcoef);
+}
+void sgo_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef, const double *x, double *y) {
+  oph_impl(g, x, y, hcoef, hfcoef);
+}

@@ -1,0 +1,107 @@
+/*
+ * cg_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Flat-array description of a SUNTANS grid and the two elliptic solves, shared
+ * by the two CPU oracles of this repository:
+ *
+ *   cg_oracle.c   a plain-C restatement of the reference algorithm (the "port"),
+ *                 compiled on any host with -ffp-contract=off so that its
+ *                 floating-point results are the same bits on x86 and Arm;
+ *   ref_harness.c a thin wrapper that #includes the reference's own
+ *                 main/phys.c and calls its static CGSolveQ / CGSolve
+ *                 (built only where the reference sources are present).
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+ * these functions, and only as the checker or the timed CPU baseline.  The
+ * product (suntans_gb300/) never calls them.
+ *
+ * Ragged 3-D fields are flat arrays: cell i occupies [coff[i], coff[i]+Nk[i])
+ * with coff the exclusive prefix sum of Nk over cell index i (natural cell
+ * order, not cellp order); edge j of dzf occupies [eoff[j], eoff[j]+Nke[j]).
+ * This is the reference's jagged REAL** (main/phys.c:247-282) laid end to end.
+ */
+#ifndef SUNTANS_CG_ORACLE_H
+#define SUNTANS_CG_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sgo_grid {
+  int Nc;              /* cells (computational + type-3 boundary), gridT.Nc      */
+  int Ne;              /* edges, gridT.Ne                                         */
+  int maxfaces;        /* gridT.maxfaces                                          */
+  int Nkmax;           /* gridT.Nkmax                                             */
+  const int *nfaces;   /* [Nc]                                                    */
+  const int *neigh;    /* [Nc*maxfaces], -1 = no neighbour                        */
+  const int *face;     /* [Nc*maxfaces], edge index                               */
+  const int *Nk;       /* [Nc]                                                    */
+  const int *Nke;      /* [Ne]                                                    */
+  const int *ctop;     /* [Nc]                                                    */
+  const int *cellp;    /* [celldist[2]]                                           */
+  const int *celldist; /* [3]: computational [0,1), type-3 boundary [1,2)         */
+  const double *Ac;    /* [Nc]                                                    */
+  const double *df;    /* [Ne]                                                    */
+  const double *dg;    /* [Ne]                                                    */
+  const double *dzz;   /* ragged per cell, sum(Nk)                               */
+  const double *dzf;   /* ragged per edge, sum(Nke)                              */
+} sgo_grid;
+
+typedef struct sgo_prop {
+  int qprecond;        /* 0 none, 1 diagonal scaling, 2 column tridiagonal        */
+  int qmaxiters;
+  double qepsilon;
+  int hprecond;        /* 0 none, 1 Jacobi                                        */
+  int maxiters;
+  double epsilon;
+  double resnorm;      /* propT.resnorm is a REAL in the reference (phys.h:185)  */
+  double grav, theta, dt;
+} sgo_prop;
+
+typedef struct sgo_result {
+  int niters;          /* solver iterations executed (operator applications in   
+                          the loop; the reference's n, plus one when it broke)   */
+  double eps, eps0;    /* last eps and the normaliser eps0                        */
+} sgo_result;
+
+/* ---- the restatement (cg_oracle.c) ---- */
+void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
+                  const sgo_prop *p, sgo_result *res);
+void sgo_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp,
+                 const sgo_prop *p, sgo_result *res);
+/* single operator pieces, for kernel-level parity */
+void sgo_qcoefficients(const sgo_grid *g, const double *D, const double *c, int qprecond,
+                       double *coef, double *fcoef);
+void sgo_operator_q(const sgo_grid *g, const double *D, const double *coef,
+                    const double *x, double *y);
+void sgo_operator_qc(const sgo_grid *g, const double *coef, const double *fcoef,
+                     const double *x, double *y);
+void sgo_condition_q(const sgo_grid *g, const double *D, double *c);
+void sgo_preconditioner(const sgo_grid *g, const double *coef, const double *x, double *xc);
+void sgo_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p,
+                       double *hcoef, double *hfcoef);
+void sgo_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef,
+                    const double *x, double *y);
+
+/* ---- the reference itself (ref_harness.c, oracle/_ref only) ---- */
+void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
+                  const sgo_prop *p, sgo_result *res);
+void ref_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp,
+                 const sgo_prop *p, sgo_result *res);
+void ref_qcoefficients(const sgo_grid *g, const double *D, const double *c, int qprecond,
+                       double *coef, double *fcoef);
+void ref_operator_q(const sgo_grid *g, const double *D, const double *coef,
+                    const double *x, double *y);
+void ref_operator_qc(const sgo_grid *g, const double *coef, const double *fcoef,
+                     const double *x, double *y);
+void ref_condition_q(const sgo_grid *g, const double *D, double *c);
+void ref_preconditioner(const sgo_grid *g, const double *coef, const double *x, double *xc);
+void ref_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p,
+                       double *hcoef, double *hfcoef);
+void ref_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef,
+                    const double *x, double *y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

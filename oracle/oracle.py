@@ -1,0 +1,187 @@
+"""ctypes bindings to the CPU oracles -- TEST INFRASTRUCTURE ONLY.
+
+Two libraries share one flat-array interface (cg_oracle.h):
+
+* ``port``  oracle/_build/libsgo_port.so, the plain-C restatement of the
+  reference algorithm (cg_oracle.c); built on any host by ``make -C oracle port``.
+* ``ref``   oracle/_ref/libsuntans_ref.so, the reference's own main/phys.c
+  compiled from its sources (ref_harness.c); exists only where the reference
+  tree was present at build time.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  The product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libsgo_port.so")
+REF_SO = os.path.join(HERE, "_ref", "libsuntans_ref.so")
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+
+
+class SgoGrid(C.Structure):
+    _fields_ = [("Nc", C.c_int), ("Ne", C.c_int), ("maxfaces", C.c_int), ("Nkmax", C.c_int),
+                ("nfaces", _ip), ("neigh", _ip), ("face", _ip), ("Nk", _ip), ("Nke", _ip),
+                ("ctop", _ip), ("cellp", _ip), ("celldist", _ip),
+                ("Ac", _dp), ("df", _dp), ("dg", _dp), ("dzz", _dp), ("dzf", _dp)]
+
+
+class SgoProp(C.Structure):
+    _fields_ = [("qprecond", C.c_int), ("qmaxiters", C.c_int), ("qepsilon", C.c_double),
+                ("hprecond", C.c_int), ("maxiters", C.c_int), ("epsilon", C.c_double),
+                ("resnorm", C.c_double), ("grav", C.c_double), ("theta", C.c_double),
+                ("dt", C.c_double)]
+
+
+class SgoResult(C.Structure):
+    _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double)]
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_SO
+
+
+def build_ref() -> Optional[str]:
+    refdir = os.environ.get("SUNTANS_REFDIR", "/root/reference/main")
+    if not os.path.isfile(os.path.join(refdir, "phys.c")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True)
+    return REF_SO
+
+
+class Oracle:
+    """One of the two oracle libraries, with numpy-level wrappers."""
+
+    def __init__(self, which: str = "port"):
+        path = PORT_SO if which == "port" else REF_SO
+        if which == "port" and not os.path.exists(path):
+            build_port()
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        self.prefix = "sgo_" if which == "port" else "ref_"
+        self.which = which
+
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    @staticmethod
+    def _grid(g):
+        keep = [np.ascontiguousarray(x) for x in
+                (g.nfaces, g.neigh, g.face, g.Nk, g.Nke, g.ctop, g.cellp, g.celldist,
+                 g.Ac, g.df, g.dg, g.dzz, g.dzf)]
+        s = SgoGrid(g.Nc, g.Ne, g.maxfaces, g.Nkmax,
+                    *[_ptr(x, _ip) for x in keep[:8]], *[_ptr(x, _dp) for x in keep[8:]])
+        return s, keep
+
+    @staticmethod
+    def _prop(p):
+        return SgoProp(p.qprecond, p.qmaxiters, p.qepsilon, p.hprecond, p.maxiters, p.epsilon,
+                       float(p.resnorm), p.grav, p.theta, p.dt)
+
+    def cgsolveq(self, prob, props):
+        """Runs CGSolveQ on copies of prob.q / prob.src / prob.c; returns (q, niters)."""
+        g = prob.grid
+        s, keep = self._grid(g)
+        q = np.array(prob.q, dtype=np.float64, copy=True)
+        src = np.array(prob.src, dtype=np.float64, copy=True)
+        c = np.array(prob.c, dtype=np.float64, copy=True)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        pr = self._prop(props)
+        res = SgoResult()
+        self._fn("cgsolveq")(C.byref(s), _ptr(D, _dp), _ptr(q, _dp), _ptr(src, _dp), _ptr(c, _dp),
+                             C.byref(pr), C.byref(res))
+        return q, int(res.niters)
+
+    def cgsolve(self, prob, props):
+        """Runs CGSolve on copies of prob.h / prob.htmp; returns (h, niters)."""
+        g = prob.grid
+        s, keep = self._grid(g)
+        h = np.array(prob.h, dtype=np.float64, copy=True)
+        htmp = np.array(prob.htmp, dtype=np.float64, copy=True)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        pr = self._prop(props)
+        res = SgoResult()
+        self._fn("cgsolve")(C.byref(s), _ptr(D, _dp), _ptr(h, _dp), _ptr(htmp, _dp), C.byref(pr),
+                            C.byref(res))
+        return h, int(res.niters)
+
+    # ---- operator pieces ----
+    def qcoefficients(self, g, D, c, qprecond):
+        s, keep = self._grid(g)
+        coef = np.zeros(g.n3)
+        fcoef = np.zeros(g.n3 * g.maxfaces)
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        self._fn("qcoefficients")(C.byref(s), _ptr(D, _dp), _ptr(c, _dp), C.c_int(qprecond),
+                                  _ptr(coef, _dp), _ptr(fcoef, _dp))
+        return coef, fcoef
+
+    def operator_q(self, g, D, coef, x, y0=None):
+        s, keep = self._grid(g)
+        y = np.zeros(g.n3) if y0 is None else np.array(y0, copy=True)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._fn("operator_q")(C.byref(s), _ptr(D, _dp), _ptr(coef, _dp), _ptr(x, _dp), _ptr(y, _dp))
+        return y
+
+    def operator_qc(self, g, coef, fcoef, x, y0=None):
+        s, keep = self._grid(g)
+        y = np.zeros(g.n3) if y0 is None else np.array(y0, copy=True)
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        fcoef = np.ascontiguousarray(fcoef, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._fn("operator_qc")(C.byref(s), _ptr(coef, _dp), _ptr(fcoef, _dp), _ptr(x, _dp), _ptr(y, _dp))
+        return y
+
+    def condition_q(self, g, D, c0=None):
+        s, keep = self._grid(g)
+        c = np.ones(g.n3) if c0 is None else np.array(c0, copy=True)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        self._fn("condition_q")(C.byref(s), _ptr(D, _dp), _ptr(c, _dp))
+        return c
+
+    def preconditioner(self, g, coef, x, xc0=None):
+        s, keep = self._grid(g)
+        xc = np.zeros(g.n3) if xc0 is None else np.array(xc0, copy=True)
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._fn("preconditioner")(C.byref(s), _ptr(coef, _dp), _ptr(x, _dp), _ptr(xc, _dp))
+        return xc
+
+    def hcoefficients(self, g, D, props):
+        s, keep = self._grid(g)
+        hcoef = np.zeros(g.Nc)
+        hfcoef = np.zeros(g.Nc * g.maxfaces)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        pr = self._prop(props)
+        self._fn("hcoefficients")(C.byref(s), _ptr(D, _dp), C.byref(pr), _ptr(hcoef, _dp), _ptr(hfcoef, _dp))
+        return hcoef, hfcoef
+
+    def operator_h(self, g, hcoef, hfcoef, x, y0=None):
+        s, keep = self._grid(g)
+        y = np.zeros(g.Nc) if y0 is None else np.array(y0, copy=True)
+        hcoef = np.ascontiguousarray(hcoef, dtype=np.float64)
+        hfcoef = np.ascontiguousarray(hfcoef, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._fn("operator_h")(C.byref(s), _ptr(hcoef, _dp), _ptr(hfcoef, _dp), _ptr(x, _dp), _ptr(y, _dp))
+        return y
+
+
+def available(which: str) -> bool:
+    return os.path.exists(PORT_SO if which == "port" else REF_SO)

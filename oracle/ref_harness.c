@@ -1,0 +1,267 @@
+/*
+ * ref_harness.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Calls the reference's own static CGSolveQ / CGSolve and their helpers by
+ * compiling the reference's main/phys.c into this translation unit (the
+ * functions are static, main/phys.c:45-52, so they cannot be linked to from
+ * outside).  The include path points at the reference sources where they lie;
+ * nothing is copied.  Built by oracle/Makefile into oracle/_ref/ only where the
+ * reference tree is present.
+ *
+ * The harness builds gridT / physT / propT whose jagged REAL** rows point into
+ * the caller's flat arrays (layout in cg_oracle.h), so the solvers read and
+ * write the caller's buffers in place, exactly as they do phys->qc and
+ * phys->stmp in the model.
+ *
+ * Iteration counts: CGSolveQ / CGSolve return nothing.  Each solver iteration
+ * calls the halo exchange on p exactly once (main/phys.c:2480, 3163), and the
+ * prologue/epilogue call it a fixed number of times, so the harness counts
+ * calls through -Wl,--wrap of ISendRecvCellData3D/2D.  With one partition the
+ * exchange is a no-op (main/sendrecv.c:134-217 with Nneighs=0).
+ */
+#include "phys.c"
+#include "cg_oracle.h"
+
+static int g_calls3d, g_calls2d;
+void __real_ISendRecvCellData3D(REAL **celldata, gridT *grid, int myproc, MPI_Comm comm);
+void __real_ISendRecvCellData2D(REAL *celldata, gridT *grid, int myproc, MPI_Comm comm);
+void __wrap_ISendRecvCellData3D(REAL **celldata, gridT *grid, int myproc, MPI_Comm comm) {
+  g_calls3d++;
+  __real_ISendRecvCellData3D(celldata, grid, myproc, comm);
+}
+void __wrap_ISendRecvCellData2D(REAL *celldata, gridT *grid, int myproc, MPI_Comm comm) {
+  g_calls2d++;
+  __real_ISendRecvCellData2D(celldata, grid, myproc, comm);
+}
+
+typedef struct {
+  gridT grid;
+  physT phys;
+  propT prop;
+  long *coff, *eoff;
+  REAL **rows_free[16];
+  int nrows_free;
+  void *blk_free[32];
+  int nblk_free;
+} harness_t;
+
+static REAL **jag_view(harness_t *H, const double *flat, const long *off, int n) {
+  int i;
+  REAL **rows = (REAL **)malloc(sizeof(REAL *) * (n > 0 ? n : 1));
+  for (i = 0; i < n; i++) rows[i] = (REAL *)(flat + off[i]);
+  H->rows_free[H->nrows_free++] = rows;
+  return rows;
+}
+static REAL **jag_new(harness_t *H, int n, const int *len, int extra) {
+  long tot = 0;
+  int i;
+  double *blk;
+  for (i = 0; i < n; i++) tot += len[i] + extra;
+  blk = (double *)calloc(tot + 1, sizeof(double));
+  H->blk_free[H->nblk_free++] = blk;
+  REAL **rows = (REAL **)malloc(sizeof(REAL *) * (n > 0 ? n : 1));
+  tot = 0;
+  for (i = 0; i < n; i++) { rows[i] = blk + tot; tot += len[i] + extra; }
+  H->rows_free[H->nrows_free++] = rows;
+  return rows;
+}
+static void *blk_new(harness_t *H, size_t bytes) {
+  void *p = calloc(1, bytes + 16);
+  H->blk_free[H->nblk_free++] = p;
+  return p;
+}
+
+static void harness_init(harness_t *H, const sgo_grid *g, const double *D, const sgo_prop *pr) {
+  int i, nf;
+  memset(H, 0, sizeof(*H));
+  H->coff = (long *)malloc(sizeof(long) * (g->Nc + 1));
+  H->eoff = (long *)malloc(sizeof(long) * (g->Ne + 1));
+  H->coff[0] = 0;
+  for (i = 0; i < g->Nc; i++) H->coff[i + 1] = H->coff[i] + g->Nk[i];
+  H->eoff[0] = 0;
+  for (i = 0; i < g->Ne; i++) H->eoff[i + 1] = H->eoff[i] + g->Nke[i];
+
+  gridT *G = &H->grid;
+  G->Nc = g->Nc;
+  G->Ne = g->Ne;
+  G->maxfaces = g->maxfaces;
+  G->Nkmax = g->Nkmax;
+  G->nfaces = (int *)g->nfaces;
+  G->neigh = (int *)g->neigh;
+  G->face = (int *)g->face;
+  G->Nk = (int *)g->Nk;
+  G->Nke = (int *)g->Nke;
+  G->ctop = (int *)g->ctop;
+  G->cellp = (int *)g->cellp;
+  G->celldist = (int *)g->celldist;
+  G->Ac = (REAL *)g->Ac;
+  G->df = (REAL *)g->df;
+  G->dg = (REAL *)g->dg;
+  G->Nneighs = 0;
+  if (g->dzz) G->dzz = jag_view(H, g->dzz, H->coff, g->Nc);
+  if (g->dzf) G->dzf = jag_view(H, g->dzf, H->eoff, g->Ne);
+
+  physT *P = &H->phys;
+  P->D = (REAL *)D;
+  P->stmp2 = jag_new(H, g->Nc, g->Nk, 0);
+  P->stmp3 = jag_new(H, g->Nc, g->Nk, 0);
+  P->uold = jag_new(H, g->Nc, g->Nk, 0);
+  P->wtmp = jag_new(H, g->Nc, g->Nk, 1);
+  {
+    int *qlen = (int *)malloc(sizeof(int) * g->maxfaces * g->Nc + 1);
+    for (i = 0; i < g->Nc; i++)
+      for (nf = 0; nf < g->maxfaces; nf++) qlen[i * g->maxfaces + nf] = g->Nk[i];
+    P->qtmp = jag_new(H, g->maxfaces * g->Nc, qlen, 0);
+    free(qlen);
+  }
+  P->a = (REAL *)blk_new(H, sizeof(REAL) * (g->Nkmax + 1));
+  P->b = (REAL *)blk_new(H, sizeof(REAL) * (g->Nkmax + 1));
+  P->c = (REAL *)blk_new(H, sizeof(REAL) * (g->Nkmax + 1));
+  P->d = (REAL *)blk_new(H, sizeof(REAL) * (g->Nkmax + 1));
+  P->hold = (REAL *)blk_new(H, sizeof(REAL) * g->Nc);
+  P->htmp2 = (REAL *)blk_new(H, sizeof(REAL) * g->Nc);
+  P->htmp3 = (REAL *)blk_new(H, sizeof(REAL) * g->Nc);
+  P->hcoef = (REAL *)blk_new(H, sizeof(REAL) * g->Nc);
+  P->hfcoef = (REAL *)blk_new(H, sizeof(REAL) * g->maxfaces * g->Nc);
+
+  propT *Q = &H->prop;
+  if (pr) {
+    Q->qprecond = pr->qprecond;
+    Q->qmaxiters = pr->qmaxiters;
+    Q->qepsilon = pr->qepsilon;
+    Q->hprecond = pr->hprecond;
+    Q->maxiters = pr->maxiters;
+    Q->epsilon = pr->epsilon;
+    Q->resnorm = pr->resnorm;
+    Q->grav = pr->grav;
+    Q->theta = pr->theta;
+    Q->dt = pr->dt;
+  }
+  VERBOSE = 0;
+  WARNING = 0;
+}
+
+static void harness_free(harness_t *H) {
+  int i;
+  for (i = 0; i < H->nrows_free; i++) free(H->rows_free[i]);
+  for (i = 0; i < H->nblk_free; i++) free(H->blk_free[i]);
+  free(H->coff);
+  free(H->eoff);
+}
+
+/* copy a harness jagged array (row length Nk[i]) out to a flat ragged array */
+static void jag_out(const harness_t *H, const sgo_grid *g, REAL **src, double *dst) {
+  int i;
+  for (i = 0; i < g->Nc; i++) memcpy(dst + H->coff[i], src[i], sizeof(double) * g->Nk[i]);
+}
+
+void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c, const sgo_prop *pr,
+                  sgo_result *res) {
+  harness_t H;
+  harness_init(&H, g, D, pr);
+  REAL **Q = jag_view(&H, q, H.coff, g->Nc);
+  REAL **S = jag_view(&H, src, H.coff, g->Nc);
+  REAL **C = jag_view(&H, c, H.coff, g->Nc);
+  g_calls3d = 0;
+  CGSolveQ(Q, S, C, &H.grid, &H.phys, &H.prop, 0, 1, 0);
+  if (res) {
+    /* x before, p per iteration, x after; ConditionQ adds one for qprecond=1 */
+    res->niters = g_calls3d - 2 - (pr->qprecond == 1 ? 1 : 0);
+    res->eps = -1;
+    res->eps0 = -1;
+  }
+  harness_free(&H);
+}
+
+void ref_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp, const sgo_prop *pr,
+                 sgo_result *res) {
+  harness_t H;
+  harness_init(&H, g, D, pr);
+  H.phys.h = h;
+  H.phys.htmp = htmp;
+  g_calls2d = 0;
+  CGSolve(&H.grid, &H.phys, &H.prop, 0, 1, 0);
+  if (res) {
+    /* x for the lift, p per iteration, x at the end */
+    res->niters = g_calls2d - 2;
+    res->eps = -1;
+    res->eps0 = -1;
+  }
+  harness_free(&H);
+}
+
+void ref_qcoefficients(const sgo_grid *g, const double *D, const double *c, int qprecond, double *coef,
+                       double *fcoef) {
+  harness_t H;
+  sgo_prop pr;
+  int i, nf;
+  memset(&pr, 0, sizeof(pr));
+  pr.qprecond = qprecond;
+  harness_init(&H, g, D, &pr);
+  REAL **C = jag_view(&H, c, H.coff, g->Nc);
+  QCoefficients(H.phys.wtmp, H.phys.qtmp, C, &H.grid, &H.phys, &H.prop);
+  jag_out(&H, g, H.phys.wtmp, coef);
+  for (i = 0; i < g->Nc; i++)
+    for (nf = 0; nf < g->maxfaces; nf++)
+      memcpy(fcoef + (long)g->maxfaces * H.coff[i] + (long)nf * g->Nk[i], H.phys.qtmp[i * g->maxfaces + nf],
+             sizeof(double) * g->Nk[i]);
+  harness_free(&H);
+}
+
+void ref_operator_q(const sgo_grid *g, const double *D, const double *coef, const double *x, double *y) {
+  harness_t H;
+  harness_init(&H, g, D, NULL);
+  REAL **CO = jag_view(&H, coef, H.coff, g->Nc);
+  REAL **X = jag_view(&H, x, H.coff, g->Nc);
+  REAL **Y = jag_view(&H, y, H.coff, g->Nc);
+  OperatorQ(CO, X, Y, NULL, &H.grid, &H.phys, &H.prop);
+  harness_free(&H);
+}
+
+void ref_operator_qc(const sgo_grid *g, const double *coef, const double *fcoef, const double *x, double *y) {
+  harness_t H;
+  int i, nf;
+  harness_init(&H, g, NULL, NULL);
+  REAL **CO = jag_view(&H, coef, H.coff, g->Nc);
+  REAL **FC = (REAL **)malloc(sizeof(REAL *) * (g->maxfaces * g->Nc + 1));
+  for (i = 0; i < g->Nc; i++)
+    for (nf = 0; nf < g->maxfaces; nf++)
+      FC[i * g->maxfaces + nf] = (REAL *)(fcoef + (long)g->maxfaces * H.coff[i] + (long)nf * g->Nk[i]);
+  REAL **X = jag_view(&H, x, H.coff, g->Nc);
+  REAL **Y = jag_view(&H, y, H.coff, g->Nc);
+  OperatorQC(CO, FC, X, Y, NULL, &H.grid, &H.phys, &H.prop);
+  free(FC);
+  harness_free(&H);
+}
+
+void ref_condition_q(const sgo_grid *g, const double *D, double *c) {
+  harness_t H;
+  harness_init(&H, g, D, NULL);
+  REAL **C = jag_view(&H, c, H.coff, g->Nc);
+  ConditionQ(C, &H.grid, &H.phys, &H.prop, 0, 0);
+  harness_free(&H);
+}
+
+void ref_preconditioner(const sgo_grid *g, const double *coef, const double *x, double *xc) {
+  harness_t H;
+  harness_init(&H, g, NULL, NULL);
+  REAL **CO = jag_view(&H, coef, H.coff, g->Nc);
+  REAL **X = jag_view(&H, x, H.coff, g->Nc);
+  REAL **XC = jag_view(&H, xc, H.coff, g->Nc);
+  Preconditioner(X, XC, CO, &H.grid, &H.phys, &H.prop);
+  harness_free(&H);
+}
+
+void ref_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p, double *hcoef, double *hfcoef) {
+  harness_t H;
+  harness_init(&H, g, D, p);
+  HCoefficients(hcoef, hfcoef, &H.grid, &H.phys, &H.prop);
+  harness_free(&H);
+}
+
+void ref_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef, const double *x, double *y) {
+  harness_t H;
+  harness_init(&H, g, NULL, NULL);
+  OperatorH((REAL *)x, y, (REAL *)hcoef, (REAL *)hfcoef, &H.grid, &H.phys, &H.prop);
+  harness_free(&H);
+}

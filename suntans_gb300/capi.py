@@ -1,0 +1,239 @@
+"""ctypes binding of the C ABI in include/suntans_gb300.h.
+
+The library is the in-tree build suntans_gb300/_lib/libsuntans_gb300.so.
+Loading fails loudly (ImportError) when it is missing; there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .grid import SunGrid, SolverProps
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libsuntans_gb300.so")
+
+# status codes, include/suntans_gb300.h
+OK, MAXITER, BREAKDOWN, TIMEOUT, OOM, BAD_GRID, BAD_ARG, CUDA_ERROR, NO_DEVICE = range(9)
+
+# every symbol the header declares
+EXPORTS = [
+    "sgpu_create", "sgpu_destroy", "sgpu_last_error", "sgpu_status_string",
+    "sgpu_cgsolveq", "sgpu_cgsolve",
+    "sgpu_q_upload", "sgpu_q_solve", "sgpu_q_download",
+    "sgpu_h_upload", "sgpu_h_solve", "sgpu_h_download",
+    "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream",
+]
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_dpp = C.POINTER(C.c_void_p)
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("Nc", C.c_int), ("Ne", C.c_int), ("maxfaces", C.c_int), ("Nkmax", C.c_int),
+                ("nfaces", _ip), ("neigh", _ip), ("face", _ip), ("Nk", _ip), ("Nke", _ip),
+                ("cellp", _ip), ("celldist", _ip), ("Ac", _dp), ("df", _dp), ("dg", _dp)]
+
+
+class Props(C.Structure):
+    _fields_ = [("qprecond", C.c_int), ("qmaxiters", C.c_int), ("qepsilon", C.c_double),
+                ("hprecond", C.c_int), ("maxiters", C.c_int), ("epsilon", C.c_double),
+                ("resnorm", C.c_double), ("grav", C.c_double), ("theta", C.c_double),
+                ("dt", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("status", C.c_int), ("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double),
+                ("ms_solve", C.c_double), ("ms_total", C.c_double), ("unknowns", C.c_longlong)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the CUDA library (raises ImportError if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (or python -m suntans_gb300.build)")
+    lib = C.CDLL(LIB_PATH)
+    lib.sgpu_create.argtypes = [C.POINTER(GridDesc), C.c_int, C.POINTER(C.c_void_p)]
+    lib.sgpu_destroy.argtypes = [C.c_void_p]
+    lib.sgpu_last_error.argtypes = [C.c_void_p]
+    lib.sgpu_last_error.restype = C.c_char_p
+    lib.sgpu_status_string.argtypes = [C.c_int]
+    lib.sgpu_status_string.restype = C.c_char_p
+    lib.sgpu_cgsolveq.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dp, _dpp, _dpp, _dpp, C.POINTER(Props),
+                                  C.POINTER(Stats)]
+    lib.sgpu_cgsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, C.POINTER(Props), C.POINTER(Stats)]
+    lib.sgpu_q_upload.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dp, _dpp, _dpp, _dpp]
+    lib.sgpu_q_solve.argtypes = [C.c_void_p, C.POINTER(Props), C.POINTER(Stats)]
+    lib.sgpu_q_download.argtypes = [C.c_void_p, _dpp]
+    lib.sgpu_h_upload.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    lib.sgpu_h_solve.argtypes = [C.c_void_p, C.POINTER(Props), C.POINTER(Stats)]
+    lib.sgpu_h_download.argtypes = [C.c_void_p, _dp]
+    lib.sgpu_set_timeout_ns.argtypes = [C.c_void_p, C.c_longlong]
+    lib.sgpu_set_grid.argtypes = [C.c_void_p, C.c_int]
+    lib.sgpu_stream.argtypes = [C.c_void_p]
+    lib.sgpu_stream.restype = C.c_void_p
+    _lib = lib
+    return lib
+
+
+def props_struct(p: SolverProps) -> Props:
+    return Props(int(p.qprecond), int(p.qmaxiters), float(p.qepsilon), int(p.hprecond), int(p.maxiters),
+                 float(p.epsilon), float(p.resnorm), float(p.grav), float(p.theta), float(p.dt))
+
+
+def jagged(flat: np.ndarray, offsets: np.ndarray) -> np.ndarray:
+    """Array of row pointers into a flat float64 buffer (the reference's REAL**)."""
+    assert flat.dtype == np.float64 and flat.flags.c_contiguous
+    return (flat.ctypes.data + 8 * offsets[:-1].astype(np.uint64)).astype(np.uint64)
+
+
+def _vp(a: np.ndarray):
+    return a.ctypes.data_as(_dpp)
+
+
+class SolverError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{msg} (status {code})")
+        self.code = code
+
+
+class Context:
+    """One grid resident on one GPU (sgpu_create / sgpu_destroy)."""
+
+    def __init__(self, g: SunGrid, device: int = 0):
+        self.lib = load()
+        self.grid = g
+        self._keep = [g.nfaces, g.neigh, g.face, g.Nk, g.Nke, g.cellp, g.celldist, g.Ac, g.df, g.dg]
+        d = GridDesc(g.Nc, g.Ne, g.maxfaces, g.Nkmax,
+                     *[a.ctypes.data_as(_ip) for a in self._keep[:7]],
+                     *[a.ctypes.data_as(_dp) for a in self._keep[7:]])
+        h = C.c_void_p()
+        rc = self.lib.sgpu_create(C.byref(d), device, C.byref(h))
+        self.h = h
+        if rc != OK:
+            msg = self.lib.sgpu_last_error(h).decode() if h.value else self.lib.sgpu_status_string(rc).decode()
+            if h.value:
+                self.lib.sgpu_destroy(h)
+            self.h = C.c_void_p()
+            raise SolverError(rc, f"sgpu_create: {msg}")
+        self.coff = g.coff
+        self.eoff = g.eoff
+
+    def close(self):
+        if self.h and self.h.value:
+            self.lib.sgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self) -> str:
+        return self.lib.sgpu_last_error(self.h).decode()
+
+    def _check(self, rc, what, allow=(OK, MAXITER, BREAKDOWN)):
+        if rc not in allow:
+            raise SolverError(rc, f"{what}: {self.lib.sgpu_status_string(rc).decode()}: {self.error()}")
+        return rc
+
+    def set_timeout_ns(self, ns: int):
+        self._check(self.lib.sgpu_set_timeout_ns(self.h, int(ns)), "sgpu_set_timeout_ns")
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(self.lib.sgpu_stream(self.h) or 0)
+
+    def set_grid(self, ctas: int):
+        self._check(self.lib.sgpu_set_grid(self.h, int(ctas)), "sgpu_set_grid")
+
+    # ---- pressure ----
+    def _q_ptrs(self, prob, q):
+        g = self.grid
+        dzz = np.ascontiguousarray(g.dzz)
+        dzf = np.ascontiguousarray(g.dzf)
+        src = np.ascontiguousarray(prob.src, dtype=np.float64)
+        c = np.ascontiguousarray(prob.c, dtype=np.float64)
+        keep = [dzz, dzf, src, c, q]
+        ptrs = dict(dzz=jagged(dzz, self.coff), dzf=jagged(dzf, self.eoff) if g.Ne else np.zeros(1, np.uint64),
+                    src=jagged(src, self.coff), c=jagged(c, self.coff), q=jagged(q, self.coff))
+        return keep, ptrs
+
+    def cgsolveq(self, prob, props: SolverProps):
+        """The drop-in call: returns (q, Stats) with q a new ragged array."""
+        g = self.grid
+        q = np.array(prob.q, dtype=np.float64, copy=True)
+        keep, P = self._q_ptrs(prob, q)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        st = Stats()
+        pr = props_struct(props)
+        rc = self.lib.sgpu_cgsolveq(self.h, ctop.ctypes.data_as(_ip), _vp(P["dzz"]), _vp(P["dzf"]),
+                                    D.ctypes.data_as(_dp), _vp(P["q"]), _vp(P["src"]), _vp(P["c"]),
+                                    C.byref(pr), C.byref(st))
+        self._check(rc, "sgpu_cgsolveq")
+        return q, st
+
+    def q_upload(self, prob):
+        g = self.grid
+        q = np.ascontiguousarray(prob.q, dtype=np.float64)
+        keep, P = self._q_ptrs(prob, q)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        rc = self.lib.sgpu_q_upload(self.h, ctop.ctypes.data_as(_ip), _vp(P["dzz"]), _vp(P["dzf"]),
+                                    D.ctypes.data_as(_dp), _vp(P["q"]), _vp(P["src"]), _vp(P["c"]))
+        self._check(rc, "sgpu_q_upload", allow=(OK,))
+
+    def q_solve(self, props: SolverProps) -> Stats:
+        st = Stats()
+        pr = props_struct(props)
+        self._check(self.lib.sgpu_q_solve(self.h, C.byref(pr), C.byref(st)), "sgpu_q_solve")
+        return st
+
+    def q_download(self, q0: np.ndarray) -> np.ndarray:
+        q = np.array(q0, dtype=np.float64, copy=True)
+        ptr = jagged(q, self.coff)
+        self._check(self.lib.sgpu_q_download(self.h, _vp(ptr)), "sgpu_q_download", allow=(OK,))
+        return q
+
+    # ---- free surface ----
+    def cgsolve(self, prob, props: SolverProps):
+        h = np.array(prob.h, dtype=np.float64, copy=True)
+        htmp = np.ascontiguousarray(prob.htmp, dtype=np.float64)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        st = Stats()
+        pr = props_struct(props)
+        rc = self.lib.sgpu_cgsolve(self.h, D.ctypes.data_as(_dp), h.ctypes.data_as(_dp),
+                                   htmp.ctypes.data_as(_dp), C.byref(pr), C.byref(st))
+        self._check(rc, "sgpu_cgsolve")
+        return h, st
+
+    def h_upload(self, prob):
+        h = np.ascontiguousarray(prob.h, dtype=np.float64)
+        htmp = np.ascontiguousarray(prob.htmp, dtype=np.float64)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        self._check(self.lib.sgpu_h_upload(self.h, D.ctypes.data_as(_dp), h.ctypes.data_as(_dp),
+                                           htmp.ctypes.data_as(_dp)), "sgpu_h_upload", allow=(OK,))
+
+    def h_solve(self, props: SolverProps) -> Stats:
+        st = Stats()
+        pr = props_struct(props)
+        self._check(self.lib.sgpu_h_solve(self.h, C.byref(pr), C.byref(st)), "sgpu_h_solve")
+        return st
+
+    def h_download(self, h0: np.ndarray) -> np.ndarray:
+        h = np.array(h0, dtype=np.float64, copy=True)
+        self._check(self.lib.sgpu_h_download(self.h, h.ctypes.data_as(_dp)), "sgpu_h_download", allow=(OK,))
+        return h

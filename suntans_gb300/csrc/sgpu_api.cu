@@ -1,0 +1,677 @@
+// sgpu_api.cu -- the C ABI (include/suntans_gb300.h): grid contexts, host <->
+// HBM staging of the reference's jagged arrays, and the solve launches.
+//
+// Host staging: the jagged rows of q, src, c, dzz (cell order) are gathered
+// into pinned buffers in device column order (computational cells in cellp
+// order, then type-3 cells, then the rest) with several host threads, then
+// copied with one cudaMemcpyAsync per array on the context's stream.  The
+// solution is copied back the same way and scattered into the caller's rows for
+// computational cells and levels k in [ctop, Nk) only.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/suntans_gb300.h"
+#include "sgpu_common.cuh"
+#include "sgpu_q.h"
+
+using namespace sgpu;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct sgpu_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  long long timeout_ns = 2000000000LL;
+  int grid_override = 0;
+
+  // host copies of the static grid
+  int Nc = 0, Ne = 0, F = 0, Nkmax = 0, ncomp = 0, nbdy = 0;
+  std::vector<int> Nk, Nke, dev2cell, cell2dev, dcoff, eoff, tile_col, nbr, fedge;
+  long long n3 = 0, n3c = 0, ne3 = 0;
+  int ntiles = 0;
+
+  // device memory (static grid)
+  std::vector<void*> allocs;
+  int *d_dcoff = nullptr, *d_tile = nullptr, *d_nk = nullptr, *d_nbr = nullptr, *d_fedge = nullptr,
+      *d_nke = nullptr, *d_eoff = nullptr;
+  double *d_Ac = nullptr, *d_df = nullptr, *d_dg = nullptr;
+
+  // pressure solve buffers
+  bool q_ready = false;
+  int *d_ctop = nullptr, *d_fmeta = nullptr, *d_fnoff = nullptr;
+  double *d_dzz = nullptr, *d_dzf = nullptr, *d_Dq = nullptr, *d_qin = nullptr, *d_srcin = nullptr,
+         *d_cin = nullptr, *d_coef = nullptr, *d_fc = nullptr, *d_c = nullptr, *d_tw = nullptr,
+         *d_tib = nullptr, *d_x = nullptr, *d_p = nullptr, *d_r = nullptr, *d_z = nullptr, *d_rt = nullptr;
+  std::vector<int> h_ctop;  // last uploaded ctop (cell order), for the download scatter
+  bool q_uploaded = false, q_solved = false;
+
+  // free-surface buffers
+  bool h_ready = false;
+  double *d_Dh = nullptr, *d_hin = nullptr, *d_bin = nullptr, *d_hcoef = nullptr, *d_hf = nullptr,
+         *d_hx = nullptr, *d_hp = nullptr, *d_hr = nullptr, *d_hz = nullptr, *d_hrt = nullptr;
+  int* d_hn = nullptr;
+  bool h_uploaded = false, h_solved = false;
+
+  // control
+  SolveCtl* d_ctl = nullptr;
+  double* d_partials = nullptr;
+  int partials_cap = 0;
+  SolveCtl* h_ctl = nullptr;  // pinned
+
+  // pinned staging
+  double* pin = nullptr;
+  size_t pin_elems = 0;
+};
+
+static int fail(sgpu_context* c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? SGPU_OOM : SGPU_CUDA_ERROR, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                        \
+  } while (0)
+
+template <class T>
+static int dalloc(sgpu_context* ctx, T** p, size_t n) {
+  void* v = nullptr;
+  CK(cudaMalloc(&v, std::max<size_t>(n, 1) * sizeof(T)));
+  ctx->allocs.push_back(v);
+  *p = (T*)v;
+  return SGPU_OK;
+}
+
+template <class T>
+static int upload(sgpu_context* ctx, T** p, const T* host, size_t n) {
+  int rc = dalloc(ctx, p, n);
+  if (rc) return rc;
+  if (n) CK(cudaMemcpyAsync(*p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  return SGPU_OK;
+}
+
+static int ensure_pinned(sgpu_context* ctx, size_t elems) {
+  if (ctx->pin_elems >= elems) return SGPU_OK;
+  if (ctx->pin) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFreeHost(ctx->pin);
+    ctx->pin = nullptr;
+    ctx->pin_elems = 0;
+  }
+  CK(cudaMallocHost((void**)&ctx->pin, elems * sizeof(double)));
+  ctx->pin_elems = elems;
+  return SGPU_OK;
+}
+
+// parallel host loop over [0, n)
+template <class Fn>
+static void host_parallel(long long n, Fn&& fn) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int nt = (int)std::min<long long>(std::max(1u, std::min(hw, 16u)), std::max(1LL, n / 65536));
+  if (nt <= 1) {
+    fn(0LL, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  long long chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    long long b = t * chunk, e = std::min(n, b + chunk);
+    if (b < e) th.emplace_back([&fn, b, e] { fn(b, e); });
+  }
+  for (auto& x : th) x.join();
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+extern "C" {
+
+const char* sgpu_status_string(int s) {
+  switch (s) {
+    case SGPU_OK: return "ok";
+    case SGPU_MAXITER: return "maxiter";
+    case SGPU_BREAKDOWN: return "breakdown";
+    case SGPU_TIMEOUT: return "timeout";
+    case SGPU_OOM: return "out of memory";
+    case SGPU_BAD_GRID: return "bad grid";
+    case SGPU_BAD_ARG: return "bad argument";
+    case SGPU_CUDA_ERROR: return "cuda error";
+    case SGPU_NO_DEVICE: return "no cuda device";
+  }
+  return "unknown";
+}
+
+const char* sgpu_last_error(const sgpu_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int sgpu_destroy(sgpu_context* ctx) {
+  if (!ctx) return SGPU_BAD_ARG;
+  {
+    DeviceGuard g(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void* p : ctx->allocs) cudaFree(p);
+    if (ctx->pin) cudaFreeHost(ctx->pin);
+    if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return SGPU_OK;
+}
+
+static int build_layout(sgpu_context* ctx, const sgpu_grid_desc* g) {
+  const int Nc = g->Nc, Ne = g->Ne, mf = g->maxfaces;
+  if (Nc <= 0 || Ne < 0 || mf <= 0 || g->Nkmax <= 0) return fail(ctx, SGPU_BAD_GRID, "empty or negative sizes");
+  if (!g->nfaces || !g->neigh || !g->face || !g->Nk || !g->Nke || !g->cellp || !g->celldist || !g->Ac || !g->df ||
+      !g->dg)
+    return fail(ctx, SGPU_BAD_ARG, "null array in grid description");
+  const int* cd = g->celldist;
+  if (!(cd[0] == 0 && cd[0] <= cd[1] && cd[1] <= cd[2] && cd[2] <= Nc))
+    return fail(ctx, SGPU_BAD_GRID, "celldist must satisfy 0 = c0 <= c1 <= c2 <= Nc");
+  if (g->Nkmax > kTileCap) return fail(ctx, SGPU_BAD_GRID, "Nkmax %d exceeds %d", g->Nkmax, kTileCap);
+  ctx->Nc = Nc;
+  ctx->Ne = Ne;
+  ctx->F = mf;
+  ctx->Nkmax = g->Nkmax;
+  ctx->ncomp = cd[1];
+  ctx->nbdy = cd[2] - cd[1];
+  ctx->Nk.assign(g->Nk, g->Nk + Nc);
+  ctx->Nke.assign(g->Nke, g->Nke + Ne);
+  for (int i = 0; i < Nc; ++i) {
+    if (g->Nk[i] < 1 || g->Nk[i] > g->Nkmax) return fail(ctx, SGPU_BAD_GRID, "Nk[%d]=%d out of [1,Nkmax]", i, g->Nk[i]);
+    if (g->nfaces[i] < 1 || g->nfaces[i] > mf)
+      return fail(ctx, SGPU_BAD_GRID, "nfaces[%d]=%d out of [1,maxfaces]", i, g->nfaces[i]);
+  }
+  // device order
+  ctx->cell2dev.assign(Nc, -1);
+  ctx->dev2cell.clear();
+  ctx->dev2cell.reserve(Nc);
+  for (int t = 0; t < cd[2]; ++t) {
+    const int i = g->cellp[t];
+    if (i < 0 || i >= Nc || ctx->cell2dev[i] >= 0) return fail(ctx, SGPU_BAD_GRID, "cellp[%d]=%d invalid or repeated", t, i);
+    ctx->cell2dev[i] = (int)ctx->dev2cell.size();
+    ctx->dev2cell.push_back(i);
+  }
+  for (int i = 0; i < Nc; ++i)
+    if (ctx->cell2dev[i] < 0) {
+      ctx->cell2dev[i] = (int)ctx->dev2cell.size();
+      ctx->dev2cell.push_back(i);
+    }
+  ctx->dcoff.assign(Nc + 1, 0);
+  long long acc = 0;
+  for (int j = 0; j < Nc; ++j) {
+    ctx->dcoff[j] = (int)acc;
+    acc += g->Nk[ctx->dev2cell[j]];
+    if (acc > 0x7fffff00LL) return fail(ctx, SGPU_BAD_GRID, "more than 2^31 storage slots");
+  }
+  ctx->dcoff[Nc] = (int)acc;
+  ctx->n3 = acc;
+  ctx->n3c = ctx->dcoff[ctx->ncomp];
+  ctx->eoff.assign(Ne + 1, 0);
+  acc = 0;
+  for (int e = 0; e < Ne; ++e) {
+    ctx->eoff[e] = (int)acc;
+    acc += g->Nke[e];
+  }
+  ctx->eoff[Ne] = (int)acc;
+  ctx->ne3 = acc;
+  if (acc > 0x7fffff00LL) return fail(ctx, SGPU_BAD_GRID, "more than 2^31 edge slots");
+  // neighbours of computational columns
+  const int ncomp = ctx->ncomp;
+  ctx->nbr.assign((size_t)std::max(ncomp, 1) * mf, -1);
+  ctx->fedge.assign((size_t)std::max(ncomp, 1) * mf, 0);
+  for (int j = 0; j < ncomp; ++j) {
+    const int i = ctx->dev2cell[j];
+    for (int f = 0; f < g->nfaces[i]; ++f) {
+      const int nc = g->neigh[i * mf + f], e = g->face[i * mf + f];
+      if (e < 0 || e >= Ne) return fail(ctx, SGPU_BAD_GRID, "face[%d]=%d out of range", i * mf + f, e);
+      ctx->fedge[(size_t)j * mf + f] = e;
+      if (nc < -1 || nc >= Nc) return fail(ctx, SGPU_BAD_GRID, "neigh[%d]=%d out of range", i * mf + f, nc);
+      if (nc >= 0) {
+        if (g->Nke[e] > g->Nk[i] || g->Nke[e] > g->Nk[nc])
+          return fail(ctx, SGPU_BAD_GRID, "Nke[%d]=%d exceeds Nk of cell %d or %d", e, g->Nke[e], i, nc);
+        ctx->nbr[(size_t)j * mf + f] = ctx->cell2dev[nc];
+      }
+    }
+  }
+  // tiles of whole computational columns, <= kTileCap slots each
+  ctx->tile_col.clear();
+  ctx->tile_col.push_back(0);
+  int cur = 0;
+  for (int j = 0; j < ncomp; ++j) {
+    const int len = g->Nk[ctx->dev2cell[j]];
+    if (cur + len > kTileCap) {
+      ctx->tile_col.push_back(j);
+      cur = 0;
+    }
+    cur += len;
+  }
+  if (ncomp > 0) ctx->tile_col.push_back(ncomp);
+  ctx->ntiles = (int)ctx->tile_col.size() - 1;
+  return SGPU_OK;
+}
+
+int sgpu_create(const sgpu_grid_desc* g, int device, sgpu_context** out) {
+  if (!g || !out) return SGPU_BAD_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return SGPU_NO_DEVICE;
+  if (device < 0 || device >= ndev) return SGPU_BAD_ARG;
+  sgpu_context* ctx = new sgpu_context();
+  ctx->device = device;
+  int rc = build_layout(ctx, g);
+  if (rc) {
+    // keep the message reachable through a context with no device memory
+    *out = ctx;
+    return rc;
+  }
+  DeviceGuard dg(device);
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ctx->ev0));
+  CK(cudaEventCreate(&ctx->ev1));
+  CK(cudaMallocHost((void**)&ctx->h_ctl, sizeof(SolveCtl)));
+  std::vector<double> Acd(ctx->Nc);
+  for (int j = 0; j < ctx->Nc; ++j) Acd[j] = g->Ac[ctx->dev2cell[j]];
+  std::vector<int> nkd(ctx->Nc);
+  for (int j = 0; j < ctx->Nc; ++j) nkd[j] = g->Nk[ctx->dev2cell[j]];
+  if ((rc = upload(ctx, &ctx->d_dcoff, ctx->dcoff.data(), ctx->dcoff.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_tile, ctx->tile_col.data(), ctx->tile_col.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_nk, nkd.data(), nkd.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_nbr, ctx->nbr.data(), ctx->nbr.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_fedge, ctx->fedge.data(), ctx->fedge.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_nke, ctx->Nke.data(), ctx->Nke.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_eoff, ctx->eoff.data(), ctx->eoff.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_Ac, Acd.data(), Acd.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_df, g->df, (size_t)ctx->Ne))) return rc;
+  if ((rc = upload(ctx, &ctx->d_dg, g->dg, (size_t)ctx->Ne))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_ctl, 1))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  *out = ctx;
+  return SGPU_OK;
+}
+
+int sgpu_set_timeout_ns(sgpu_context* ctx, long long ns) {
+  if (!ctx || ns <= 0) return SGPU_BAD_ARG;
+  ctx->timeout_ns = ns;
+  return SGPU_OK;
+}
+
+int sgpu_set_grid(sgpu_context* ctx, int ctas) {
+  if (!ctx || ctas < 0) return SGPU_BAD_ARG;
+  ctx->grid_override = ctas;
+  return SGPU_OK;
+}
+
+void* sgpu_stream(sgpu_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+static int ensure_partials(sgpu_context* ctx, int grid) {
+  if (ctx->partials_cap >= grid) return SGPU_OK;
+  int rc = dalloc(ctx, &ctx->d_partials, (size_t)4 * grid);
+  if (rc) return rc;
+  ctx->partials_cap = grid;
+  return SGPU_OK;
+}
+
+static int alloc_q(sgpu_context* ctx) {
+  if (ctx->q_ready) return SGPU_OK;
+  const size_t n3 = ctx->n3 + 1, n3c = ctx->n3c + 1, ncf = (size_t)std::max(ctx->ncomp, 1) * ctx->F;
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_ctop, ctx->Nc))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_fmeta, ncf))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_fnoff, ncf))) return rc;
+  double** v[] = {&ctx->d_dzz, &ctx->d_qin, &ctx->d_srcin, &ctx->d_cin, &ctx->d_coef, &ctx->d_c,
+                  &ctx->d_x,   &ctx->d_p,   &ctx->d_r,     &ctx->d_z,   &ctx->d_rt};
+  for (auto pp : v)
+    if ((rc = dalloc(ctx, pp, n3))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_tw, n3c))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_tib, n3c))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_fc, n3c * ctx->F))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_dzf, ctx->ne3 + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_Dq, ctx->Ne + 1))) return rc;
+  CK(cudaMemsetAsync(ctx->d_coef, 0, n3 * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_tw, 0, n3c * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_tib, 0, n3c * sizeof(double), ctx->stream));
+  ctx->q_ready = true;
+  return SGPU_OK;
+}
+
+// gather jagged rows (cell order) into pinned staging in device column order
+static void gather_cells(sgpu_context* ctx, const double* const* rows, double* dst) {
+  host_parallel(ctx->Nc, [&](long long b, long long e) {
+    for (long long j = b; j < e; ++j) {
+      const int i = ctx->dev2cell[j];
+      std::memcpy(dst + ctx->dcoff[j], rows[i], sizeof(double) * ctx->Nk[i]);
+    }
+  });
+}
+
+int sgpu_q_upload(sgpu_context* ctx, const int* ctop, const double* const* dzz, const double* const* dzf,
+                  const double* D, const double* const* q, const double* const* src, const double* const* c) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctop || !dzz || !dzf || !D || !q || !src) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  DeviceGuard dg(ctx->device);
+  int rc = alloc_q(ctx);
+  if (rc) return rc;
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3;
+  for (int i = 0; i < ctx->Nc; ++i)
+    if (ctop[i] < 0 || ctop[i] >= ctx->Nk[i]) return fail(ctx, SGPU_BAD_ARG, "ctop[%d]=%d out of [0,Nk)", i, ctop[i]);
+  // staging: [ctop as int | dzz | q | src | c | dzf | D]
+  const size_t n_ctop = (ctx->Nc + 1) / 2 + 1;
+  const size_t need = n_ctop + 4 * n3 + ne3 + ctx->Ne + 8;
+  if ((rc = ensure_pinned(ctx, need))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));  // staging reuse
+  int* s_ctop = (int*)ctx->pin;
+  double* s_dzz = ctx->pin + n_ctop;
+  double* s_q = s_dzz + n3;
+  double* s_src = s_q + n3;
+  double* s_c = s_src + n3;
+  double* s_dzf = s_c + n3;
+  double* s_D = s_dzf + ne3;
+  for (int j = 0; j < ctx->Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  ctx->h_ctop.assign(ctop, ctop + ctx->Nc);
+  gather_cells(ctx, dzz, s_dzz);
+  gather_cells(ctx, q, s_q);
+  gather_cells(ctx, src, s_src);
+  if (c) gather_cells(ctx, c, s_c);
+  else std::fill(s_c, s_c + n3, 1.0);
+  host_parallel(ctx->Ne, [&](long long b, long long e) {
+    for (long long k = b; k < e; ++k) std::memcpy(s_dzf + ctx->eoff[k], dzf[k], sizeof(double) * ctx->Nke[k]);
+  });
+  std::memcpy(s_D, D, sizeof(double) * ctx->Ne);
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_qin, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_srcin, s_src, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_cin, s_c, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_Dq, s_D, sizeof(double) * ctx->Ne, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->q_uploaded = true;
+  ctx->q_solved = false;
+  return SGPU_OK;
+}
+
+static void reset_ctl(sgpu_context* ctx) {
+  std::memset(ctx->h_ctl, 0, sizeof(SolveCtl));
+  ctx->h_ctl->timeout_ns = ctx->timeout_ns;
+}
+
+static int run_solve_common(sgpu_context* ctx, sgpu_stats* st, long long unknowns, int grid,
+                            cudaError_t (*launch)(sgpu_context*, int, void*), void* arg) {
+  reset_ctl(ctx);
+  CK(cudaMemcpyAsync(ctx->d_ctl, ctx->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  cudaError_t le = launch(ctx, grid, arg);
+  if (le != cudaSuccess)
+    return fail(ctx, SGPU_CUDA_ERROR, "solver launch failed: %s", cudaGetErrorString(le));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  const SolveCtl& h = *ctx->h_ctl;
+  if (st) {
+    st->status = h.status;
+    st->niters = h.n;
+    st->eps = h.eps;
+    st->eps0 = h.eps0;
+    st->ms_solve = ms;
+    st->unknowns = unknowns;
+  }
+  if (h.status == SGPU_TIMEOUT) return fail(ctx, SGPU_TIMEOUT, "device barrier wait timed out in phase %d", h.phase_err);
+  return h.status;
+}
+
+struct QLaunch {
+  QArgs a;
+  int qprecond;
+};
+
+static cudaError_t launch_q_cb2(sgpu_context* ctx, int grid, void* arg) {
+  QLaunch* L = (QLaunch*)arg;
+  return q_launch(L->a, L->qprecond, grid, ctx->stream);
+}
+
+int sgpu_q_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
+  if (!ctx || !prop) return SGPU_BAD_ARG;
+  if (!ctx->q_uploaded) return fail(ctx, SGPU_BAD_ARG, "sgpu_q_solve before sgpu_q_upload");
+  if (prop->qprecond < 0 || prop->qprecond > 2) return fail(ctx, SGPU_BAD_ARG, "qprecond must be 0, 1 or 2");
+  auto t0 = std::chrono::steady_clock::now();
+  DeviceGuard dg(ctx->device);
+  int maxg = q_max_grid(prop->qprecond, ctx->device);
+  if (maxg <= 0) return fail(ctx, SGPU_CUDA_ERROR, "occupancy query failed");
+  int grid = ctx->grid_override > 0 ? std::min(ctx->grid_override, maxg) : maxg;
+  int rc = ensure_partials(ctx, grid);
+  if (rc) return rc;
+  QLaunch L;
+  QArgs& a = L.a;
+  a.F = ctx->F;
+  a.ncomp = ctx->ncomp;
+  a.ncols = ctx->Nc;
+  a.n3c = (int)ctx->n3c;
+  a.n3 = (int)ctx->n3;
+  a.ntiles = ctx->ntiles;
+  a.maxiters = prop->qmaxiters;
+  a.qepsilon = prop->qepsilon;
+  a.resnorm = prop->resnorm;
+  a.dcoff = ctx->d_dcoff;
+  a.tile_col = ctx->d_tile;
+  a.nk = ctx->d_nk;
+  a.nbr = ctx->d_nbr;
+  a.fedge = ctx->d_fedge;
+  a.nke = ctx->d_nke;
+  a.eoff = ctx->d_eoff;
+  a.Ac = ctx->d_Ac;
+  a.ctop = ctx->d_ctop;
+  a.dzz = ctx->d_dzz;
+  a.dzf = ctx->d_dzf;
+  a.D = ctx->d_Dq;
+  a.q_in = ctx->d_qin;
+  a.src_in = ctx->d_srcin;
+  a.c_in = ctx->d_cin;
+  a.fmeta = ctx->d_fmeta;
+  a.fnoff = ctx->d_fnoff;
+  a.coef = ctx->d_coef;
+  a.fc = ctx->d_fc;
+  a.c = ctx->d_c;
+  a.tw = ctx->d_tw;
+  a.tib = ctx->d_tib;
+  a.x = ctx->d_x;
+  a.p = ctx->d_p;
+  a.r = ctx->d_r;
+  a.z = ctx->d_z;
+  a.rt = ctx->d_rt;
+  a.ctl = ctx->d_ctl;
+  a.partials = ctx->d_partials;
+  L.qprecond = prop->qprecond;
+  long long unk = 0;
+  for (int j = 0; j < ctx->ncomp; ++j) unk += ctx->Nk[ctx->dev2cell[j]] - ctx->h_ctop[ctx->dev2cell[j]];
+  rc = run_solve_common(ctx, st, unk, grid, launch_q_cb2, &L);
+  if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (rc == SGPU_OK || rc == SGPU_MAXITER || rc == SGPU_BREAKDOWN) ctx->q_solved = true;
+  return rc;
+}
+
+int sgpu_q_download(sgpu_context* ctx, double* const* q) {
+  if (!ctx || !q) return SGPU_BAD_ARG;
+  if (!ctx->q_solved) return fail(ctx, SGPU_BAD_ARG, "sgpu_q_download before a solve");
+  DeviceGuard dg(ctx->device);
+  int rc = ensure_pinned(ctx, ctx->n3c + 1);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->pin, ctx->d_x, sizeof(double) * ctx->n3c, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const double* s = ctx->pin;
+  host_parallel(ctx->ncomp, [&](long long b, long long e) {
+    for (long long j = b; j < e; ++j) {
+      const int i = ctx->dev2cell[j];
+      const int k0 = ctx->h_ctop[i];
+      std::memcpy(q[i] + k0, s + ctx->dcoff[j] + k0, sizeof(double) * (ctx->Nk[i] - k0));
+    }
+  });
+  return SGPU_OK;
+}
+
+int sgpu_cgsolveq(sgpu_context* ctx, const int* ctop, const double* const* dzz, const double* const* dzf,
+                  const double* D, double* const* q, const double* const* src, const double* const* c,
+                  const sgpu_props* prop, sgpu_stats* st) {
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = sgpu_q_upload(ctx, ctop, dzz, dzf, D, (const double* const*)q, src, c);
+  if (rc) return rc;
+  int src_rc = sgpu_q_solve(ctx, prop, st);
+  if (src_rc != SGPU_OK && src_rc != SGPU_MAXITER && src_rc != SGPU_BREAKDOWN) return src_rc;
+  rc = sgpu_q_download(ctx, q);
+  if (rc) return rc;
+  if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return src_rc;
+}
+
+// ---------------------------------------------------------------------------
+// free surface
+// ---------------------------------------------------------------------------
+static int alloc_h(sgpu_context* ctx) {
+  if (ctx->h_ready) return SGPU_OK;
+  const size_t nc = ctx->Nc + 1, ncf = (size_t)std::max(ctx->ncomp, 1) * ctx->F;
+  int rc;
+  double** v[] = {&ctx->d_hin, &ctx->d_bin, &ctx->d_hcoef, &ctx->d_hx, &ctx->d_hp, &ctx->d_hr, &ctx->d_hz, &ctx->d_hrt};
+  for (auto pp : v)
+    if ((rc = dalloc(ctx, pp, nc))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_hf, ncf))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_hn, ncf))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_Dh, ctx->Ne + 1))) return rc;
+  ctx->h_ready = true;
+  return SGPU_OK;
+}
+
+int sgpu_h_upload(sgpu_context* ctx, const double* D, const double* h, const double* htmp) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!D || !h || !htmp) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  DeviceGuard dg(ctx->device);
+  int rc = alloc_h(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_pinned(ctx, 2 * (size_t)ctx->Nc + ctx->Ne + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  double* s_h = ctx->pin;
+  double* s_b = s_h + ctx->Nc;
+  double* s_D = s_b + ctx->Nc;
+  for (int j = 0; j < ctx->Nc; ++j) {
+    s_h[j] = h[ctx->dev2cell[j]];
+    s_b[j] = htmp[ctx->dev2cell[j]];
+  }
+  std::memcpy(s_D, D, sizeof(double) * ctx->Ne);
+  CK(cudaMemcpyAsync(ctx->d_hin, s_h, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_bin, s_b, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_Dh, s_D, sizeof(double) * ctx->Ne, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->h_uploaded = true;
+  ctx->h_solved = false;
+  return SGPU_OK;
+}
+
+struct HLaunch {
+  HArgs a;
+};
+
+static cudaError_t launch_h_cb(sgpu_context* ctx, int grid, void* arg) {
+  return h_launch(((HLaunch*)arg)->a, grid, ctx->stream);
+}
+
+int sgpu_h_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
+  if (!ctx || !prop) return SGPU_BAD_ARG;
+  if (!ctx->h_uploaded) return fail(ctx, SGPU_BAD_ARG, "sgpu_h_solve before sgpu_h_upload");
+  auto t0 = std::chrono::steady_clock::now();
+  DeviceGuard dg(ctx->device);
+  int maxg = h_max_grid(ctx->device);
+  if (maxg <= 0) return fail(ctx, SGPU_CUDA_ERROR, "occupancy query failed");
+  int grid = ctx->grid_override > 0 ? std::min(ctx->grid_override, maxg) : maxg;
+  // no more CTAs than needed to give every thread a cell
+  grid = std::max(1, std::min(grid, (ctx->ncomp + kBlock - 1) / kBlock));
+  int rc = ensure_partials(ctx, grid);
+  if (rc) return rc;
+  HLaunch L;
+  HArgs& a = L.a;
+  a.F = ctx->F;
+  a.ncomp = ctx->ncomp;
+  a.ncells = ctx->Nc;
+  a.maxiters = prop->maxiters;
+  a.hprecond = prop->hprecond;
+  a.epsilon = prop->epsilon;
+  a.resnorm = prop->resnorm;
+  a.tmp = prop->grav * std::pow(prop->theta * prop->dt, 2);
+  a.nbr = ctx->d_nbr;
+  a.fedge = ctx->d_fedge;
+  a.Ac = ctx->d_Ac;
+  a.df = ctx->d_df;
+  a.dg = ctx->d_dg;
+  a.D = ctx->d_Dh;
+  a.h_in = ctx->d_hin;
+  a.b_in = ctx->d_bin;
+  a.hcoef = ctx->d_hcoef;
+  a.hf = ctx->d_hf;
+  a.hn = ctx->d_hn;
+  a.x = ctx->d_hx;
+  a.p = ctx->d_hp;
+  a.r = ctx->d_hr;
+  a.z = ctx->d_hz;
+  a.rt = ctx->d_hrt;
+  a.ctl = ctx->d_ctl;
+  a.partials = ctx->d_partials;
+  rc = run_solve_common(ctx, st, ctx->ncomp, grid, launch_h_cb, &L);
+  if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (rc == SGPU_OK || rc == SGPU_MAXITER || rc == SGPU_BREAKDOWN) ctx->h_solved = true;
+  return rc;
+}
+
+int sgpu_h_download(sgpu_context* ctx, double* h) {
+  if (!ctx || !h) return SGPU_BAD_ARG;
+  if (!ctx->h_solved) return fail(ctx, SGPU_BAD_ARG, "sgpu_h_download before a solve");
+  DeviceGuard dg(ctx->device);
+  int rc = ensure_pinned(ctx, ctx->Nc + 1);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->pin, ctx->d_hx, sizeof(double) * ctx->ncomp, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int j = 0; j < ctx->ncomp; ++j) h[ctx->dev2cell[j]] = ctx->pin[j];
+  return SGPU_OK;
+}
+
+int sgpu_cgsolve(sgpu_context* ctx, const double* D, double* h, const double* htmp, const sgpu_props* prop,
+                 sgpu_stats* st) {
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = sgpu_h_upload(ctx, D, h, htmp);
+  if (rc) return rc;
+  int s_rc = sgpu_h_solve(ctx, prop, st);
+  if (s_rc != SGPU_OK && s_rc != SGPU_MAXITER && s_rc != SGPU_BREAKDOWN) return s_rc;
+  rc = sgpu_h_download(ctx, h);
+  if (rc) return rc;
+  if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return s_rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// sgpu_common.cuh -- device-side building blocks shared by the solver kernels.
+//
+//  * GridSync: a grid-wide barrier for cooperative (co-resident) launches whose
+//    last-arriving CTA runs a "finaliser" (the deterministic reduction of the
+//    per-CTA partial sums and the CG scalar recurrences) before it releases the
+//    others.  Every wait is bounded by %globaltimer; on time-out the waiter
+//    records SGPU_TIMEOUT in the control block and the kernel returns.
+//  * Block reductions in FP64 with a fixed combination order, so every run of
+//    the same problem on the same launch shape gives the same bits.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define SGPU_OK 0
+#define SGPU_MAXITER 1
+#define SGPU_BREAKDOWN 2
+#define SGPU_TIMEOUT 3
+#define SGPU_OOM 4
+#define SGPU_BAD_GRID 5
+#define SGPU_BAD_ARG 6
+#define SGPU_CUDA_ERROR 7
+#define SGPU_NO_DEVICE 8
+
+namespace sgpu {
+
+constexpr int kBlock = 256;        // threads per CTA of the solver kernels
+constexpr int kTileCap = 512;      // storage slots per tile (2 per thread)
+constexpr int kMaxTileCols = kTileCap;  // a tile may hold up to 512 one-level columns
+
+// Control block of one solve, in device memory.  The barrier words live in
+// their own 128-byte lines.
+struct __align__(128) SolveCtl {
+  // barrier
+  unsigned int count;
+  unsigned int pad0[31];
+  unsigned int gen;
+  unsigned int pad1[31];
+  // scalars published by the finaliser
+  double alpha, alpha0, eps, eps0, mu, nu;
+  double res_true;        // optional diagnostic
+  int n;                  // iterations executed
+  int done;               // 1 = leave the loop
+  int status;             // SGPU_* code
+  int phase_err;          // where a wait gave up
+  long long timeout_ns;   // barrier wait bound
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_volatile_int(const int* p) {
+  return *reinterpret_cast<const volatile int*>(p);
+}
+
+// Deterministic FP64 block sum (blockDim.x == kBlock).  All threads get the result.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* [NV][kBlock/32] */) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double s = v[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) smem[j * (kBlock / 32) + wid] = s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) s += smem[j * (kBlock / 32) + w];
+    v[j] = s;
+  }
+  __syncthreads();
+}
+
+// Sum of partials[j*stride + b] over b in [0, n) in a fixed order, by one CTA.
+template <int NV>
+__device__ __forceinline__ void reduce_partials(const double* partials, int stride, int n, double (&out)[NV],
+                                                double* smem) {
+  double v[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < n; b += kBlock) s += ((volatile const double*)partials)[j * stride + b];
+    v[j] = s;
+  }
+  block_sum<NV>(v, smem);
+#pragma unroll
+  for (int j = 0; j < NV; ++j) out[j] = v[j];
+}
+
+// Grid barrier with a finaliser run by the last CTA to arrive.
+// Returns false if the kernel must stop (time-out or an error status).
+template <class Fin>
+__device__ __forceinline__ bool grid_sync(SolveCtl* ctl, int phase, Fin&& fin) {
+  __shared__ int s_last;
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int my_gen = ld_acquire_u32(&ctl->gen);
+    __threadfence();
+    unsigned int old = atomicAdd(&ctl->count, 1u);
+    s_last = (old == gridDim.x - 1);
+    s_ok = 1;
+    if (!s_last) {
+      const unsigned long long t0 = globaltimer_ns();
+      const unsigned long long lim = (unsigned long long)ctl->timeout_ns;
+      unsigned int spins = 0;
+      while (ld_acquire_u32(&ctl->gen) == my_gen) {
+        if (++spins > 64) __nanosleep(64);
+        if ((spins & 255u) == 0 && globaltimer_ns() - t0 > lim) {
+          atomicCAS(&ctl->status, SGPU_OK, SGPU_TIMEOUT);
+          atomicCAS(&ctl->phase_err, 0, phase);
+          s_ok = 0;
+          break;
+        }
+      }
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    fin();           // whole CTA; must end with its own __syncthreads
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      ctl->count = 0u;
+      __threadfence();
+      atomicAdd(&ctl->gen, 1u);
+    }
+    __syncthreads();
+  }
+  if (!s_ok) return false;
+  return ld_volatile_int(&ctl->status) == SGPU_OK || ld_volatile_int(&ctl->status) == SGPU_MAXITER;
+}
+
+}  // namespace sgpu

@@ -1,0 +1,511 @@
+// sgpu_q.cu -- the nonhydrostatic pressure PCG (CGSolveQ) as one persistent,
+// cooperative kernel per solve, FP64 throughout.
+//
+// Reference semantics followed (main/phys.c of SUNTANS):
+//   CGSolveQ        2411-2550  the solve: setup, initial residual, loop, rescale
+//   OperatorQ       3486-3536  y = A x  (qprecond 0 and 2)
+//   OperatorQC      3364-3409  y = C^-1 A C^-1 x with unit diagonal (qprecond 1)
+//   QCoefficients   3420-3471  vertical coef, and fcoef for qprecond 1
+//   ConditionQ      3629-3687  c = sqrt(|diag A|) (qprecond 1)
+//   Preconditioner  3577-3619  per-column tridiagonal solve (qprecond 2)
+//   TriSolve        util.c:185-203
+//   InnerProduct3   3304-3319  sum over computational cells, k in [ctop, Nk)
+//
+// Data layout (device order): column j = cellp[j] for j < ncomp (computational
+// cells), then the type-3 boundary cells, then any remaining cells.  Column j
+// holds levels [0, Nk) at [dcoff[j], dcoff[j+1]).  Slots k < ctop (dry layers)
+// are kept at 0 in every working vector, so vector phases run over the whole
+// computational storage [0, n3c) without masks.  Face coefficients are F
+// separate arrays fc[f][u] over the computational storage (0 where the face
+// does not couple that level).
+//
+// Work split: computational columns are packed into tiles of at most 512
+// storage slots; a CTA of 256 threads owns tiles b, b+G, b+2G, ... in every
+// phase, 2 slots per thread.  Barriers: 3 per CG iteration, each finalised by
+// the last CTA to arrive (deterministic reduction, scalar recurrences).
+#include "sgpu_common.cuh"
+#include "sgpu_q.h"
+
+namespace sgpu {
+
+struct TileCtx {
+  int base;      // storage offset of the tile's first slot
+  int len;       // slots in the tile
+  int c0;        // first column
+  int ncols;     // columns in the tile
+};
+
+__device__ __forceinline__ void tile_load(const QArgs& a, int t, TileCtx& tc, int* s_start) {
+  const int c0 = a.tile_col[t];
+  const int c1 = a.tile_col[t + 1];
+  const int base = a.dcoff[c0];
+  for (int c = threadIdx.x; c <= c1 - c0; c += kBlock) s_start[c] = a.dcoff[c0 + c] - base;
+  tc.base = base;
+  tc.c0 = c0;
+  tc.ncols = c1 - c0;
+  tc.len = a.dcoff[c1] - base;
+  __syncthreads();
+}
+
+// column (local index) holding local slot s: largest c with s_start[c] <= s
+__device__ __forceinline__ int find_col(const int* s_start, int ncols, int s) {
+  int lo = 0, hi = ncols - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (s_start[mid] <= s) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
+// operator apply for one slot u = (column j, level k), k in [ctop, Nk)
+// ---------------------------------------------------------------------------
+template <int QP>
+__device__ __forceinline__ double apply_slot(const QArgs& a, const double* __restrict__ xin, int u, int j, int k,
+                                             int ctop, int nk) {
+  const int F = a.F;
+  double y;
+  if (QP == 1) {
+    // OperatorQC: y = -x + sum_f fcoef*x[nc] + vertical neighbours (3364-3409)
+    y = -xin[u];
+    for (int f = 0; f < F; ++f) {
+      const int meta = a.fmeta[j * F + f];
+      if (meta < 0) continue;
+      const int kmin = meta & 0xffff, kmax = meta >> 16;
+      if (k >= kmin && k < kmax) y += xin[a.fnoff[j * F + f] + k] * a.fc[(size_t)f * a.n3c + u];
+    }
+    if (k > ctop && k < nk - 1) {
+      y += a.coef[u] * xin[u - 1] + a.coef[u + 1] * xin[u + 1];
+    } else if (ctop < nk - 1) {
+      if (k == ctop) y += a.coef[u + 1] * xin[u + 1];
+      else y += a.coef[u] * xin[u - 1];  // k == nk-1
+    }
+  } else {
+    // OperatorQ: horizontal differences then vertical (3486-3536)
+    const double xu = xin[u];
+    y = 0.0;
+    for (int f = 0; f < F; ++f) {
+      const int meta = a.fmeta[j * F + f];
+      if (meta < 0) continue;
+      const int kmin = meta & 0xffff, kmax = meta >> 16;
+      if (k >= kmin && k < kmax) y += (xin[a.fnoff[j * F + f] + k] - xu) * a.fc[(size_t)f * a.n3c + u];
+    }
+    if (ctop < nk - 1) {
+      if (k == ctop) {
+        const double c0 = a.coef[u], c1 = a.coef[u + 1];
+        y += (-2 * c0 - c1) * xu + c1 * xin[u + 1];
+      } else if (k == nk - 1) {
+        const double c0 = a.coef[u];
+        y += c0 * xin[u - 1] - c0 * xu;
+      } else {
+        const double c0 = a.coef[u], c1 = a.coef[u + 1];
+        y += c0 * xin[u - 1] - (c0 + c1) * xu + c1 * xin[u + 1];
+      }
+    } else {
+      y -= 2.0 * a.coef[u] * xu;
+    }
+  }
+  return y;
+}
+
+// Thomas solve of one column with the factors prepared at setup:
+//   d'[k] = d[k] - w[k] d'[k-1];  u[k] = (d'[k] - cup[k] u[k+1]) * ib[k]
+// cup[k] = coef[k+1] (the reference's c[k], 3589-3597).  Single-level column:
+// u = -0.5 d / coef (3617).
+__device__ __forceinline__ void column_solve(const QArgs& a, const double* rin, double* out, int off, int ctop,
+                                             int nk) {
+  const int b = off + ctop, e = off + nk;
+  if (ctop == nk - 1) {
+    out[b] = -0.5 * rin[b] / a.coef[b];
+    return;
+  }
+  double dprev = rin[b];
+  out[b] = dprev;
+  for (int u = b + 1; u < e; ++u) {
+    dprev = rin[u] - a.tw[u] * dprev;
+    out[u] = dprev;
+  }
+  double unext = out[e - 1] * a.tib[e - 1];
+  out[e - 1] = unext;
+  for (int u = e - 2; u >= b; --u) {
+    unext = (out[u] - a.coef[u + 1] * unext) * a.tib[u];
+    out[u] = unext;
+  }
+}
+
+// Factorisation of one column for column_solve (TriSolve's forward sweep on b,
+// util.c:191-195): b'[0]=b[0], b'[k]=b[k]-a[k]*c[k-1]/b'[k-1]; w[k]=a[k]/b'[k-1]; ib=1/b'.
+__device__ __forceinline__ void column_factor(const QArgs& a, int off, int ctop, int nk) {
+  const int b = off + ctop, e = off + nk;
+  if (ctop == nk - 1) return;
+  double bp = -2 * a.coef[b] - a.coef[b + 1];
+  a.tib[b] = 1.0 / bp;
+  for (int u = b + 1; u < e; ++u) {
+    const double ak = a.coef[u];
+    const double ck1 = a.coef[u];  // c[k-1] = coef[k]
+    const double bk = (u == e - 1) ? -a.coef[u] : (-a.coef[u] - a.coef[u + 1]);
+    const double bnew = bk - ak * ck1 / bp;
+    a.tw[u] = ak / bp;
+    bp = bnew;
+    a.tib[u] = 1.0 / bp;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the persistent kernel
+// ---------------------------------------------------------------------------
+template <int QP>
+__global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
+  __shared__ int s_start[kMaxTileCols + 1];
+  __shared__ double s_red[4 * (kBlock / 32)];
+  SolveCtl* ctl = a.ctl;
+  const int G = gridDim.x;
+  const int F = a.F;
+  const int tid = threadIdx.x;
+
+  // ---- S1: working vectors, face metadata, coefficients / conditioner ----
+  for (int t = blockIdx.x; t < a.ntiles; t += G) {
+    TileCtx tc;
+    tile_load(a, t, tc, s_start);
+    for (int s = tid; s < tc.len; s += kBlock) {
+      const int cl = find_col(s_start, tc.ncols, s);
+      const int j = tc.c0 + cl;
+      const int k = s - s_start[cl];
+      const int u = tc.base + s;
+      const int ctop = a.ctop[j];
+      const int nk = a.nk[j];
+      const bool act = k >= ctop;
+      a.z[u] = 0.0;
+      a.r[u] = 0.0;
+      a.rt[u] = 0.0;
+      double diag = 0.0;
+      for (int f = 0; f < F; ++f) {
+        const int nb = a.nbr[j * F + f];
+        int kmin = 0, kmax = 0, meta = -1;
+        if (nb >= 0) {
+          const int e = a.fedge[j * F + f];
+          kmin = max(ctop, a.ctop[nb]);
+          kmax = a.nke[e];
+          meta = kmin | (kmax << 16);
+          if (k == 0) {
+            a.fmeta[j * F + f] = meta;
+            a.fnoff[j * F + f] = a.dcoff[nb];
+          }
+          const bool on = act && k >= kmin && k < kmax;
+          if (QP != 1) {
+            a.fc[(size_t)f * a.n3c + u] = on ? a.dzf[a.eoff[e] + k] * a.D[e] : 0.0;
+          } else {
+            if (on) diag += a.dzz[u] * a.D[e];
+            a.fc[(size_t)f * a.n3c + u] = 0.0;
+          }
+        } else {
+          if (k == 0) {
+            a.fmeta[j * F + f] = -1;
+            a.fnoff[j * F + f] = 0;
+          }
+          a.fc[(size_t)f * a.n3c + u] = 0.0;
+        }
+      }
+      const double Ac = a.Ac[j];
+      if (QP != 1) {
+        // QCoefficients, qprecond != 1 branch (3459-3468)
+        double cf = 0.0;
+        if (k == ctop) cf = Ac / a.dzz[u];
+        else if (k > ctop) cf = 2 * Ac / (a.dzz[u] + a.dzz[u - 1]);
+        a.coef[u] = cf;
+        a.x[u] = act ? a.q_in[u] : 0.0;
+        a.p[u] = act ? a.src_in[u] : 0.0;
+      } else {
+        // ConditionQ vertical part (3660-3675) and sqrt (3678-3685)
+        if (act) {
+          const double ak = (k == ctop) ? Ac / a.dzz[u] : 2 * Ac / (a.dzz[u] + a.dzz[u - 1]);
+          if (ctop < nk - 1) {
+            if (k == ctop) {
+              const double ak1 = 2 * Ac / (a.dzz[u + 1] + a.dzz[u]);
+              diag += 2 * ak + ak1;
+            } else if (k == nk - 1) {
+              diag += ak;
+            } else {
+              const double ak1 = 2 * Ac / (a.dzz[u + 1] + a.dzz[u]);
+              diag += (ak + ak1);
+            }
+          }
+          if (diag <= 0) diag = 1;
+          const double cu = sqrt(diag);
+          a.c[u] = cu;
+          a.p[u] = a.src_in[u] / cu;
+          a.x[u] = a.q_in[u] * cu;
+        } else {
+          a.c[u] = 1.0;
+          a.p[u] = 0.0;
+          a.x[u] = 0.0;
+        }
+        a.coef[u] = 0.0;
+      }
+    }
+    if (QP == 2) {
+      __syncthreads();
+      for (int cl = tid; cl < tc.ncols; cl += kBlock) {
+        const int j = tc.c0 + cl;
+        column_factor(a, tc.base + s_start[cl], a.ctop[j], a.nk[j]);
+      }
+    }
+    __syncthreads();
+  }
+  // boundary / remaining columns: given values, never updated (read as neighbours)
+  for (int u = a.n3c + blockIdx.x * kBlock + tid; u < a.n3; u += G * kBlock) {
+    a.x[u] = a.q_in[u];
+    a.p[u] = a.src_in[u];
+    if (QP == 1) a.c[u] = a.c_in[u];
+  }
+  if (!grid_sync(ctl, 1, [] {})) return;
+
+  // ---- S2 (qprecond 1): scaled coefficients (QCoefficients 3427-3452) ----
+  if (QP == 1) {
+    for (int t = blockIdx.x; t < a.ntiles; t += G) {
+      TileCtx tc;
+      tile_load(a, t, tc, s_start);
+      for (int s = tid; s < tc.len; s += kBlock) {
+        const int cl = find_col(s_start, tc.ncols, s);
+        const int j = tc.c0 + cl;
+        const int k = s - s_start[cl];
+        const int u = tc.base + s;
+        const int ctop = a.ctop[j];
+        if (k < ctop) continue;
+        const double Ac = a.Ac[j];
+        if (k == ctop) a.coef[u] = Ac / a.dzz[u] / a.c[u];
+        else a.coef[u] = 2 * Ac / (a.dzz[u] + a.dzz[u - 1]) / (a.c[u] * a.c[u - 1]);
+        for (int f = 0; f < F; ++f) {
+          const int meta = a.fmeta[j * F + f];
+          if (meta < 0) continue;
+          const int kmin = meta & 0xffff, kmax = meta >> 16;
+          if (k >= kmin && k < kmax) {
+            const int e = a.fedge[j * F + f];
+            a.fc[(size_t)f * a.n3c + u] = a.dzz[u] * a.D[e] / (a.c[u] * a.c[a.fnoff[j * F + f] + k]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (!grid_sync(ctl, 2, [] {})) return;
+  }
+
+  // ---- S3: z = A x; r = p - z; p = r or M^-1 r; alpha0, eps0 (2444-2475) ----
+  {
+    double part[2] = {0.0, 0.0};
+    for (int t = blockIdx.x; t < a.ntiles; t += G) {
+      TileCtx tc;
+      tile_load(a, t, tc, s_start);
+      for (int s = tid; s < tc.len; s += kBlock) {
+        const int cl = find_col(s_start, tc.ncols, s);
+        const int j = tc.c0 + cl;
+        const int k = s - s_start[cl];
+        const int u = tc.base + s;
+        const int ctop = a.ctop[j];
+        if (k < ctop) continue;
+        const double zu = apply_slot<QP>(a, a.x, u, j, k, ctop, a.nk[j]);
+        a.z[u] = zu;
+        const double ru = a.p[u] - zu;
+        a.r[u] = ru;
+        if (QP != 2) {
+          a.p[u] = ru;
+          part[0] += ru * ru;
+        }
+      }
+      if (QP == 2) {
+        __syncthreads();
+        for (int cl = tid; cl < tc.ncols; cl += kBlock) {
+          const int j = tc.c0 + cl;
+          column_solve(a, a.r, a.rt, tc.base + s_start[cl], a.ctop[j], a.nk[j]);
+        }
+        __syncthreads();
+        for (int s = tid; s < tc.len; s += kBlock) {
+          const int u = tc.base + s;
+          const double ru = a.r[u], rtu = a.rt[u];
+          a.p[u] = rtu;
+          part[0] += ru * rtu;
+          part[1] += ru * ru;
+        }
+      }
+      __syncthreads();
+    }
+    block_sum<2>(part, s_red);
+    if (tid == 0) {
+      a.partials[blockIdx.x] = part[0];
+      a.partials[G + blockIdx.x] = part[1];
+    }
+    const double resnorm = a.resnorm;
+    if (!grid_sync(ctl, 3, [&] {
+          double tot[2];
+          reduce_partials<2>(a.partials, G, G, tot, s_red);
+          if (tid == 0) {
+            double alpha = tot[0], alpha0 = tot[0];
+            if (!resnorm) alpha0 = 1;
+            double eps, eps0;
+            if (QP == 2) eps = eps0 = tot[1];
+            else eps = eps0 = alpha0;
+            ctl->alpha = alpha;
+            ctl->alpha0 = alpha0;
+            ctl->eps = eps;
+            ctl->eps0 = eps0;
+            ctl->n = 0;
+            ctl->done = (a.maxiters <= 0 || eps == 0) ? 1 : 0;
+            __threadfence();
+          }
+        }))
+      return;
+  }
+
+  // ---- the CG loop (2478-2525) ----
+  for (;;) {
+    if (ld_volatile_int(&ctl->done)) break;
+    // A: z = A p, p.z
+    {
+      double part[1] = {0.0};
+      for (int t = blockIdx.x; t < a.ntiles; t += G) {
+        TileCtx tc;
+        tile_load(a, t, tc, s_start);
+        for (int s = tid; s < tc.len; s += kBlock) {
+          const int cl = find_col(s_start, tc.ncols, s);
+          const int j = tc.c0 + cl;
+          const int k = s - s_start[cl];
+          const int u = tc.base + s;
+          const int ctop = a.ctop[j];
+          if (k < ctop) continue;
+          const double zu = apply_slot<QP>(a, a.p, u, j, k, ctop, a.nk[j]);
+          a.z[u] = zu;
+          part[0] += a.p[u] * zu;
+        }
+        __syncthreads();
+      }
+      block_sum<1>(part, s_red);
+      if (tid == 0) a.partials[blockIdx.x] = part[0];
+      if (!grid_sync(ctl, 4, [&] {
+            double tot[1];
+            reduce_partials<1>(a.partials, G, G, tot, s_red);
+            if (tid == 0) {
+              const double alpha = *(volatile double*)&ctl->alpha;
+              ctl->mu = 1 / alpha;
+              const double nu = alpha / tot[0];
+              ctl->nu = nu;
+              if (!isfinite(nu)) {
+                ctl->status = SGPU_BREAKDOWN;
+                ctl->done = 1;
+              }
+              __threadfence();
+            }
+          }))
+        return;
+      if (ld_volatile_int(&ctl->done)) break;
+    }
+    // B: x += nu p; r -= nu z; [rt = M^-1 r]; alpha, eps
+    {
+      const double nu = *(volatile double*)&ctl->nu;
+      double part[2] = {0.0, 0.0};
+      for (int t = blockIdx.x; t < a.ntiles; t += G) {
+        const int c0 = a.tile_col[t], c1 = a.tile_col[t + 1];
+        const int base = a.dcoff[c0], end = a.dcoff[c1];
+        for (int u = base + tid; u < end; u += kBlock) {
+          a.x[u] += nu * a.p[u];
+          const double ru = a.r[u] - nu * a.z[u];
+          a.r[u] = ru;
+          if (QP != 2) part[0] += ru * ru;
+        }
+        if (QP == 2) {
+          __syncthreads();
+          for (int c = c0 + tid; c < c1; c += kBlock)
+            column_solve(a, a.r, a.rt, a.dcoff[c], a.ctop[c], a.nk[c]);
+          __syncthreads();
+          for (int u = base + tid; u < end; u += kBlock) {
+            const double ru = a.r[u];
+            part[0] += ru * a.rt[u];
+            part[1] += ru * ru;
+          }
+        }
+      }
+      block_sum<2>(part, s_red);
+      if (tid == 0) {
+        a.partials[blockIdx.x] = part[0];
+        a.partials[G + blockIdx.x] = part[1];
+      }
+      const double qeps = a.qepsilon;
+      const int maxit = a.maxiters;
+      if (!grid_sync(ctl, 5, [&] {
+            double tot[2];
+            reduce_partials<2>(a.partials, G, G, tot, s_red);
+            if (tid == 0) {
+              const double alpha = tot[0];
+              double mu = *(volatile double*)&ctl->mu;
+              mu *= alpha;
+              ctl->mu = mu;
+              ctl->alpha = alpha;
+              const double eps = (QP == 2) ? tot[1] : alpha;
+              ctl->eps = eps;
+              const int n = ctl->n + 1;
+              ctl->n = n;
+              const double eps0 = ctl->eps0;
+              int done = 0;
+              if (sqrt(eps / eps0) < qeps) done = 1;
+              else if (n >= maxit || eps == 0) done = 1;
+              if (!isfinite(alpha)) {
+                ctl->status = SGPU_BREAKDOWN;
+                done = 1;
+              }
+              if (done && n >= maxit && !(sqrt(eps / eps0) < qeps) && ctl->status == SGPU_OK)
+                ctl->status = SGPU_MAXITER;
+              ctl->done = done;
+              __threadfence();
+            }
+          }))
+        return;
+      if (ld_volatile_int(&ctl->done)) break;
+    }
+    // C: p = r + mu p  (or rt + mu p)
+    {
+      const double mu = *(volatile double*)&ctl->mu;
+      const double* src = (QP == 2) ? a.rt : a.r;
+      for (int t = blockIdx.x; t < a.ntiles; t += G) {
+        const int base = a.dcoff[a.tile_col[t]], end = a.dcoff[a.tile_col[t + 1]];
+        for (int u = base + tid; u < end; u += kBlock) a.p[u] = src[u] + mu * a.p[u];
+      }
+      if (!grid_sync(ctl, 6, [] {})) return;
+    }
+  }
+
+  // ---- rescale (2539-2546) ----
+  if (QP == 1) {
+    for (int t = blockIdx.x; t < a.ntiles; t += G) {
+      const int base = a.dcoff[a.tile_col[t]], end = a.dcoff[a.tile_col[t + 1]];
+      for (int u = base + tid; u < end; u += kBlock) a.x[u] /= a.c[u];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host launcher
+// ---------------------------------------------------------------------------
+template <int QP>
+static cudaError_t launch_q(const QArgs& a, int grid, cudaStream_t st) {
+  void* args[] = {(void*)&a};
+  return cudaLaunchCooperativeKernel((const void*)cgsolveq_kernel<QP>, dim3(grid), dim3(kBlock), args, 0, st);
+}
+
+int q_max_grid(int qprecond, int device) {
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const void* fn = qprecond == 1 ? (const void*)cgsolveq_kernel<1>
+                 : qprecond == 2 ? (const void*)cgsolveq_kernel<2> : (const void*)cgsolveq_kernel<0>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kBlock, 0) != cudaSuccess) return 0;
+  return sms * per;
+}
+
+cudaError_t q_launch(const QArgs& a, int qprecond, int grid, cudaStream_t st) {
+  switch (qprecond) {
+    case 0: return launch_q<0>(a, grid, st);
+    case 1: return launch_q<1>(a, grid, st);
+    case 2: return launch_q<2>(a, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace sgpu

@@ -1,0 +1,317 @@
+"""Seeded synthetic SUNTANS grids and right-hand sides.
+
+No dataset is involved anywhere: every grid here is built from a seed, with
+the shapes, sizes and value distributions of the workloads the elliptic solves
+are measured on.
+
+* `quad_channel`      structured quadrilateral channel (maxfaces 4), flat bottom.
+* `delaunay_seamount` Delaunay triangulation of uniform random points in a
+                      rectangle, depth ``H0 - A*exp(-r^2/(2 sigma^2))`` with
+                      partial-cell z-levels stretched downward.
+* `make_q_problem`    pressure right-hand side = the discrete divergence of a
+                      seeded face-normal velocity, as ComputeQSource forms it
+                      (main/phys.c:2364-2394; w = 0), with ``D = df/dg``.
+* `make_h_problem`    free-surface right-hand side ``Ac * eta`` from a seeded
+                      perturbation, ``D = sum_k dzf`` (UPredictor with E = 1,
+                      main/phys.c:2935-2937).
+
+Cells are ordered along a Morton (Z-order) curve of their centres so that
+neighbouring columns sit close together in memory.  Voronoi points are cell
+centroids (the reference's CorrectVoronoi with VoronoiRatio = 1,
+main/grid.c:3735-3821, applied to every edge), which keeps ``dg`` away from zero
+on random triangulations.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .grid import SunGrid, QProblem, HProblem, F64, I32
+
+
+# ----------------------------------------------------------------------------
+# vertical grid
+# ----------------------------------------------------------------------------
+def layer_thicknesses(maxdepth: float, Nkmax: int, rstretch: float) -> np.ndarray:
+    """z-level thicknesses growing downward by ``rstretch`` and summing to ``maxdepth``."""
+    if rstretch == 1.0:
+        return np.full(Nkmax, maxdepth / Nkmax, dtype=F64)
+    r = float(rstretch)
+    dz0 = maxdepth * (r - 1.0) / (r ** Nkmax - 1.0)
+    return dz0 * r ** np.arange(Nkmax, dtype=F64)
+
+
+def vertical_columns(depth: np.ndarray, dz: np.ndarray, stairstep: bool, dzsmall: float = 0.1):
+    """Nk per cell and the bottom-cell thickness (partial cells unless stairstep)."""
+    zb = np.cumsum(dz)                     # bottom of each layer
+    Nkmax = dz.size
+    Nk = np.searchsorted(zb, depth * (1 - 1e-12), side="left") + 1
+    Nk = np.clip(Nk, 1, Nkmax).astype(I32)
+    top_of_bottom = np.where(Nk > 1, zb[np.maximum(Nk - 2, 0)], 0.0)
+    if stairstep:
+        dbot = dz[Nk - 1].copy()
+    else:
+        dbot = depth - top_of_bottom
+        dbot = np.maximum(dbot, dzsmall * dz[Nk - 1])
+    return Nk, dbot
+
+
+def build_dzz(Nk, dz, dbot, ctop, h):
+    """Ragged dzz: full layers, partial bottom, free surface in the top wet cell.
+
+    Layers above ctop are dry (thickness 0).  The top wet cell's thickness is
+    its nominal thickness plus ``h``, the free-surface height above that
+    layer's top (clipped to 40% of the layer), as UpdateDZ leaves it
+    (main/phys.c:816-900)."""
+    Nc = Nk.size
+    coff = np.zeros(Nc + 1, dtype=np.int64)
+    np.cumsum(Nk, out=coff[1:])
+    n3 = int(coff[-1])
+    cell = np.repeat(np.arange(Nc), Nk)
+    k = np.arange(n3) - coff[cell]
+    dzz = dz[k].copy()
+    last = coff[1:] - 1
+    dzz[last] = dbot
+    dzz[k < ctop[cell]] = 0.0
+    top_idx = coff[:-1] + ctop
+    t = dzz[top_idx]
+    dzz[top_idx] = t + np.clip(h, -0.4 * t, 0.4 * t)
+    return dzz
+
+
+# ----------------------------------------------------------------------------
+# horizontal connectivity
+# ----------------------------------------------------------------------------
+def _edges_from_cells(cells: np.ndarray, nfaces: np.ndarray, maxfaces: int):
+    """Unique edges, grad, face/neigh/normal arrays from per-cell node lists."""
+    Nc = cells.shape[0]
+    fidx = np.arange(maxfaces)[None, :]
+    valid = fidx < nfaces[:, None]
+    a = cells
+    b = np.take_along_axis(cells, (fidx + 1) % nfaces[:, None], axis=1)
+    lo = np.minimum(a, b)[valid].astype(np.int64)
+    hi = np.maximum(a, b)[valid].astype(np.int64)
+    key = lo * (int(cells.max()) + 1) + hi
+    cellof = np.repeat(np.arange(Nc), nfaces)
+    slot = np.nonzero(valid.ravel())[0]
+    uniq, inv = np.unique(key, return_inverse=True)
+    Ne = uniq.size
+    order = np.argsort(inv, kind="stable")
+    inv_sorted = inv[order]
+    first = np.ones(order.size, dtype=bool)
+    first[1:] = inv_sorted[1:] != inv_sorted[:-1]
+    grad = -np.ones((Ne, 2), dtype=I32)
+    grad[inv_sorted[first], 0] = cellof[order[first]]
+    second = ~first
+    grad[inv_sorted[second], 1] = cellof[order[second]]
+    enodes = np.zeros((Ne, 2), dtype=np.int64)
+    enodes[inv, 0] = lo
+    enodes[inv, 1] = hi
+    face = -np.ones(Nc * maxfaces, dtype=I32)
+    face[slot] = inv
+    neigh = -np.ones(Nc * maxfaces, dtype=I32)
+    normal = np.zeros(Nc * maxfaces, dtype=I32)
+    g0 = grad[inv, 0]
+    g1 = grad[inv, 1]
+    other = np.where(g0 == cellof, g1, g0)
+    neigh[slot] = other
+    normal[slot] = np.where(g0 == cellof, 1, -1)
+    return Ne, grad, enodes, face, neigh, normal
+
+
+def _morton_order(x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    def spread(v):
+        v = v.astype(np.uint64) & np.uint64(0xFFFF)
+        v = (v | (v << np.uint64(8))) & np.uint64(0x00FF00FF)
+        v = (v | (v << np.uint64(4))) & np.uint64(0x0F0F0F0F)
+        v = (v | (v << np.uint64(2))) & np.uint64(0x33333333)
+        v = (v | (v << np.uint64(1))) & np.uint64(0x55555555)
+        return v
+    xs = (x - x.min()) / max(np.ptp(x), 1e-30) * 65535
+    ys = (y - y.min()) / max(np.ptp(y), 1e-30) * 65535
+    code = spread(xs) | (spread(ys) << np.uint64(1))
+    return np.argsort(code, kind="stable")
+
+
+def _assemble(points, cells, nfaces, maxfaces, depth_fn, Nkmax, rstretch, stairstep,
+              rng, name, h_sigma=0.0, ctop_frac=0.0, ctop_max=3, open_x0=False, maxdepth=None):
+    Nc = cells.shape[0]
+    # cell centroids (Voronoi points, VoronoiRatio = 1) and areas
+    px = points[:, 0][cells]
+    py = points[:, 1][cells]
+    m = np.arange(maxfaces)[None, :] < nfaces[:, None]
+    px = np.where(m, px, 0.0)
+    py = np.where(m, py, 0.0)
+    nxt = (np.arange(maxfaces)[None, :] + 1) % nfaces[:, None]
+    qx = np.take_along_axis(points[:, 0][cells], nxt, 1)
+    qy = np.take_along_axis(points[:, 1][cells], nxt, 1)
+    cross = np.where(m, px * qy - qx * py, 0.0)
+    Ac = 0.5 * cross.sum(1)
+    if np.any(Ac <= 0):
+        raise ValueError("cells must be counter-clockwise with positive area")
+    xv = px.sum(1) / nfaces
+    yv = py.sum(1) / nfaces
+
+    # spatial ordering of cells
+    perm = _morton_order(xv, yv)
+    cells, nfaces, Ac, xv, yv = cells[perm], nfaces[perm], Ac[perm], xv[perm], yv[perm]
+
+    Ne, grad, enodes, face, neigh, normal = _edges_from_cells(cells, nfaces, maxfaces)
+    # order edges by the Morton rank of their first cell, for locality of dzf
+    eorder = np.lexsort((grad[:, 1], grad[:, 0]))
+    einv = np.empty(Ne, dtype=np.int64)
+    einv[eorder] = np.arange(Ne)
+    grad, enodes = grad[eorder], enodes[eorder]
+    face = np.where(face >= 0, einv[np.maximum(face, 0)], -1).astype(I32)
+
+    e0, e1 = enodes[:, 0], enodes[:, 1]
+    df = np.hypot(points[e0, 0] - points[e1, 0], points[e0, 1] - points[e1, 1])
+    interior = grad[:, 1] >= 0
+    g0, g1 = grad[:, 0], np.maximum(grad[:, 1], 0)
+    dg = np.hypot(xv[g0] - xv[g1], yv[g0] - yv[g1])
+    mx = 0.5 * (points[e0, 0] + points[e1, 0])
+    my = 0.5 * (points[e0, 1] + points[e1, 1])
+    dgb = 2.0 * np.hypot(xv[g0] - mx, yv[g0] - my)
+    dg = np.where(interior, dg, dgb)
+
+    # vertical structure
+    depth = depth_fn(xv, yv)
+    md = float(depth.max()) if maxdepth is None else float(maxdepth)
+    dz = layer_thicknesses(md, Nkmax, rstretch)
+    Nk, dbot = vertical_columns(depth, dz, stairstep)
+    ctop = np.zeros(Nc, dtype=I32)
+    if ctop_frac > 0:
+        sel = rng.random(Nc) < ctop_frac
+        ctop[sel] = rng.integers(0, ctop_max + 1, size=int(sel.sum()))
+        ctop = np.minimum(ctop, Nk - 1).astype(I32)
+    h = rng.normal(0.0, h_sigma, size=Nc) if h_sigma > 0 else np.zeros(Nc)
+    dzz = build_dzz(Nk, dz, dbot, ctop, h)
+
+    Nke = np.where(interior, np.minimum(Nk[g0], Nk[g1]), Nk[g0]).astype(I32)
+    coff = np.zeros(Nc + 1, dtype=np.int64)
+    np.cumsum(Nk, out=coff[1:])
+    eoff = np.zeros(Ne + 1, dtype=np.int64)
+    np.cumsum(Nke, out=eoff[1:])
+    edge = np.repeat(np.arange(Ne), Nke)
+    k = np.arange(int(eoff[-1])) - eoff[edge]
+    z0 = dzz[coff[g0[edge]] + k]
+    z1 = np.where(interior[edge], dzz[coff[g1[edge]] + np.minimum(k, Nk[g1[edge]] - 1)], z0)
+    bottom = k == Nke[edge] - 1
+    # SetFluxHeight with u = 0: UpWind -> Max(dz1,dz2); bottom face -> Min (util.c:219-232)
+    dzf = np.where(bottom, np.minimum(z0, z1), np.maximum(z0, z1))
+
+    # computational cells first, then type-3 (open) boundary cells
+    celltype = np.zeros(Nc, dtype=I32)
+    if open_x0:
+        xmin = points[:, 0].min()
+        on_left = (np.abs(points[e0, 0] - xmin) < 1e-9) & (np.abs(points[e1, 0] - xmin) < 1e-9) & ~interior
+        celltype[g0[on_left]] = 1
+    comp = np.nonzero(celltype == 0)[0]
+    bdy = np.nonzero(celltype == 1)[0]
+    cellp = np.concatenate([comp, bdy]).astype(I32)
+    celldist = np.array([0, comp.size, Nc], dtype=I32)
+
+    g = SunGrid(Nc=Nc, Ne=Ne, maxfaces=maxfaces, Nkmax=Nkmax, nfaces=nfaces, neigh=neigh, face=face,
+                Nk=Nk, Nke=Nke, ctop=ctop, cellp=cellp, celldist=celldist, Ac=Ac, df=df, dg=dg,
+                dzz=dzz, dzf=dzf, normal=normal, grad=grad.ravel(), xv=xv, yv=yv, name=name)
+    return g
+
+
+def quad_channel(nx=64, ny=16, dx=10.0, dy=10.0, depth=20.0, Nkmax=32, rstretch=1.0, seed=0,
+                 h_sigma=0.0, ctop_frac=0.0, open_x0=False, depth_fn=None, stairstep=True):
+    """Structured quad channel (maxfaces 4), cells (ix, iy) counter-clockwise."""
+    rng = np.random.default_rng(seed)
+    X, Y = np.meshgrid(np.arange(nx + 1) * dx, np.arange(ny + 1) * dy, indexing="xy")
+    points = np.stack([X.ravel(), Y.ravel()], 1)
+    pid = lambda ix, iy: iy * (nx + 1) + ix
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    ix, iy = ix.ravel(), iy.ravel()
+    cells = np.stack([pid(ix, iy), pid(ix + 1, iy), pid(ix + 1, iy + 1), pid(ix, iy + 1)], 1)
+    nfaces = np.full(cells.shape[0], 4, dtype=I32)
+    dfn = depth_fn if depth_fn is not None else (lambda x, y: np.full_like(x, depth))
+    return _assemble(points, cells, nfaces, 4, dfn, Nkmax, rstretch, stairstep, rng,
+                     name=f"quad{nx}x{ny}x{Nkmax}", h_sigma=h_sigma, ctop_frac=ctop_frac,
+                     open_x0=open_x0, maxdepth=None if depth_fn is None else None)
+
+
+def seamount_depth(Lx, Ly, H0=50.0, amp=30.0, sigma=2000.0):
+    def f(x, y):
+        r2 = (x - 0.5 * Lx) ** 2 + (y - 0.5 * Ly) ** 2
+        return H0 - amp * np.exp(-r2 / (2.0 * sigma ** 2))
+    return f
+
+
+def delaunay_seamount(npoints=200_000, Lx=20_000.0, Ly=10_000.0, Nkmax=50, rstretch=1.02, seed=1,
+                      H0=50.0, amp=30.0, sigma=2000.0, h_sigma=0.0, ctop_frac=0.0,
+                      open_x0=False, stairstep=False, corners=True):
+    """Delaunay triangulation of seeded uniform random points with a Gaussian seamount."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    pts = rng.random((npoints, 2)) * np.array([Lx, Ly])
+    if corners:
+        pts = np.concatenate([pts, np.array([[0, 0], [Lx, 0], [Lx, Ly], [0, Ly]], dtype=F64)])
+    tri = Delaunay(pts)
+    cells = tri.simplices.astype(np.int64)
+    # counter-clockwise orientation
+    p = pts[cells]
+    cr = (p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])
+    flip = cr < 0
+    cells[flip] = cells[flip][:, [0, 2, 1]]
+    # drop degenerate slivers (zero area) that qhull can emit on hull corners
+    p = pts[cells]
+    cr = (p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])
+    cells = cells[cr > 1e-9 * Lx * Ly / max(npoints, 1)]
+    nfaces = np.full(cells.shape[0], 3, dtype=I32)
+    return _assemble(pts, cells, nfaces, 3, seamount_depth(Lx, Ly, H0, amp, sigma), Nkmax, rstretch,
+                     stairstep, rng, name=f"delaunay{npoints}x{Nkmax}", h_sigma=h_sigma,
+                     ctop_frac=ctop_frac, open_x0=open_x0, maxdepth=H0)
+
+
+# ----------------------------------------------------------------------------
+# right-hand sides
+# ----------------------------------------------------------------------------
+def make_q_problem(g: SunGrid, seed=0, sigma_u=0.05, dt=1.0, q0_sigma=0.0) -> QProblem:
+    """Divergence right-hand side (ComputeQSource, main/phys.c:2364-2394, w = 0)."""
+    rng = np.random.default_rng(seed)
+    eoff = g.eoff
+    coff = g.coff
+    interior = g.grad.reshape(-1, 2)[:, 1] >= 0
+    u = rng.normal(0.0, sigma_u, size=int(eoff[-1]))
+    u[np.repeat(~interior, g.Nke)] = 0.0            # closed walls carry no flux
+    src = np.zeros(g.n3, dtype=F64)
+    mf = g.maxfaces
+    for nf in range(mf):
+        cells = np.nonzero(g.nfaces > nf)[0]
+        ne = g.face[cells * mf + nf]
+        nrm = g.normal[cells * mf + nf].astype(F64)
+        for_cells_k0 = g.ctop[cells]
+        nk = g.Nke[ne] - for_cells_k0
+        ok = nk > 0
+        cells, ne, nrm, for_cells_k0, nk = cells[ok], ne[ok], nrm[ok], for_cells_k0[ok], nk[ok]
+        rep = np.repeat(np.arange(cells.size), nk)
+        kk = np.arange(int(nk.sum())) - np.repeat(np.cumsum(nk) - nk, nk) + for_cells_k0[rep]
+        eidx = eoff[ne[rep]] + kk
+        contrib = u[eidx] * g.dzf[eidx] * nrm[rep] * g.df[ne[rep]]
+        np.add.at(src, coff[cells[rep]] + kk, contrib)
+    src /= dt
+    # only computational cells carry a source (ComputeQSource zeroes all, fills computational)
+    mask = g.active_mask()
+    src[~mask] = 0.0
+    D = g.df / g.dg
+    q = np.zeros(g.n3, dtype=F64)
+    if q0_sigma > 0:
+        q[mask] = rng.normal(0.0, q0_sigma, size=int(mask.sum()))
+    c = np.ones(g.n3, dtype=F64)
+    return QProblem(grid=g, D=D, src=src, q=q, c=c)
+
+
+def make_h_problem(g: SunGrid, seed=0, sigma_eta=0.01, bdy_sigma=0.01) -> HProblem:
+    """Free-surface right-hand side Ac*eta with D = sum_k dzf (E = 1)."""
+    rng = np.random.default_rng(seed)
+    eta = rng.normal(0.0, sigma_eta, size=g.Nc)
+    htmp = g.Ac * eta
+    h = np.zeros(g.Nc, dtype=F64)
+    bdy = g.cellp[g.celldist[1]:g.celldist[2]]
+    h[bdy] = rng.normal(0.0, bdy_sigma, size=bdy.size)
+    htmp[bdy] = 0.0
+    D = np.add.reduceat(g.dzf, g.eoff[:-1]) if g.Ne > 0 else np.zeros(0)
+    return HProblem(grid=g, D=np.ascontiguousarray(D, dtype=F64), htmp=htmp, h=h)

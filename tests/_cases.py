@@ -1,0 +1,44 @@
+"""Seeded grids and problems shared by the parity tests (small enough for the oracle)."""
+from __future__ import annotations
+
+import numpy as np
+
+from suntans_gb300 import gridgen as gg
+from suntans_gb300.grid import SolverProps
+
+
+def grid_cases():
+    """(name, builder) pairs; builders are cheap and deterministic."""
+    return [
+        ("quad16x8", lambda: gg.quad_channel(16, 8, Nkmax=12, h_sigma=0.05, ctop_frac=0.3, seed=2)),
+        ("tri600_open", lambda: gg.delaunay_seamount(600, 2000, 1000, Nkmax=15, sigma=300, ctop_frac=0.2,
+                                                    h_sigma=0.05, open_x0=True, seed=5)),
+        ("quad64x16x32", lambda: gg.quad_channel(64, 16, Nkmax=32, h_sigma=0.01, seed=3)),
+        ("tri3000_partial", lambda: gg.delaunay_seamount(3000, 4000, 2000, Nkmax=30, sigma=500,
+                                                        rstretch=1.05, ctop_frac=0.05, h_sigma=0.02, seed=7)),
+        ("tri400_shallow", lambda: gg.delaunay_seamount(400, 1000, 500, Nkmax=6, H0=6.0, amp=5.5, sigma=150,
+                                                       ctop_frac=0.5, h_sigma=0.05, seed=11)),
+    ]
+
+
+def active_mask(g):
+    return g.active_mask()
+
+
+def rel_l2(a, b, mask=None):
+    if mask is not None:
+        a, b = a[mask], b[mask]
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+def q_props(qprecond, **kw):
+    d = dict(qprecond=qprecond, qmaxiters=4000, qepsilon=1e-10, resnorm=1.0, dt=10.0)
+    d.update(kw)
+    return SolverProps(**d)
+
+
+def h_props(hprecond, **kw):
+    d = dict(hprecond=hprecond, maxiters=4000, epsilon=1e-10, resnorm=1.0, dt=30.0, theta=0.55)
+    d.update(kw)
+    return SolverProps(**d)

@@ -1,0 +1,140 @@
+"""CUDA solves through the C ABI against the CPU oracle (the reference algorithm).
+
+Tolerance: relative L2 of the solution over computational cells / active levels
+<= 1e-9 at equal tolerance (1e-10 relative residual), and iteration counts
+within 2 of the oracle's (the GPU sums in a different order).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from suntans_gb300 import gridgen as gg
+from suntans_gb300.capi import Context, MAXITER, OK
+from tests._cases import grid_cases, h_props, q_props, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+_GRIDS = {}
+
+
+def grid(name):
+    if name not in _GRIDS:
+        _GRIDS[name] = dict(grid_cases())[name]()
+    return _GRIDS[name]
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return Oracle("port")
+
+
+@pytest.mark.parametrize("gname", [n for n, _ in grid_cases()])
+@pytest.mark.parametrize("qprecond", [0, 1, 2])
+def test_cgsolveq_parity(gpu_lib, oracle, gname, qprecond):
+    g = grid(gname)
+    prob = gg.make_q_problem(g, seed=1, q0_sigma=0.01)
+    pr = q_props(qprecond)
+    q_ref, n_ref = oracle.cgsolveq(prob, pr)
+    ctx = Context(g)
+    q_gpu, st = ctx.cgsolveq(prob, pr)
+    m = g.active_mask()
+    assert st.status == OK
+    assert abs(st.niters - n_ref) <= 2, (st.niters, n_ref)
+    err = rel_l2(q_gpu, q_ref, m)
+    assert err <= TOL, err
+    # entries outside the active set are returned untouched
+    assert np.array_equal(q_gpu[~m], prob.q[~m])
+    ctx.close()
+
+
+@pytest.mark.parametrize("gname", [n for n, _ in grid_cases()])
+@pytest.mark.parametrize("hprecond", [0, 1])
+def test_cgsolve_parity(gpu_lib, oracle, gname, hprecond):
+    g = grid(gname)
+    prob = gg.make_h_problem(g, seed=2)
+    pr = h_props(hprecond)
+    h_ref, n_ref = oracle.cgsolve(prob, pr)
+    ctx = Context(g)
+    h_gpu, st = ctx.cgsolve(prob, pr)
+    comp = g.comp_cells()
+    assert st.status == OK
+    assert abs(st.niters - n_ref) <= 2, (st.niters, n_ref)
+    assert rel_l2(h_gpu[comp], h_ref[comp]) <= TOL
+    bdy = g.cellp[g.celldist[1]:g.celldist[2]]
+    assert np.array_equal(h_gpu[bdy], prob.h[bdy])
+    ctx.close()
+
+
+@pytest.mark.parametrize("qprecond", [0, 1, 2])
+def test_cgsolveq_maxiter_matches_truncated_oracle(gpu_lib, oracle, qprecond):
+    """Stopping at qmaxiters returns the same iterate as the oracle after that many steps."""
+    g = grid("tri600_open")
+    prob = gg.make_q_problem(g, seed=4)
+    pr = q_props(qprecond, qmaxiters=7)
+    q_ref, n_ref = oracle.cgsolveq(prob, pr)
+    ctx = Context(g)
+    q_gpu, st = ctx.cgsolveq(prob, pr)
+    assert n_ref == 7 and st.niters == 7 and st.status == MAXITER
+    assert rel_l2(q_gpu, q_ref, g.active_mask()) <= 1e-11
+
+
+def test_cgsolveq_zero_rhs(gpu_lib, oracle):
+    """Zero source and zero warm start: eps0 = 0, no iterations, q stays 0 (phys.c:2478)."""
+    g = grid("quad16x8")
+    prob = gg.make_q_problem(g, seed=1)
+    prob.src[:] = 0.0
+    for qp in (0, 1, 2):
+        q_ref, n_ref = oracle.cgsolveq(prob, q_props(qp))
+        ctx = Context(g)
+        q_gpu, st = ctx.cgsolveq(prob, q_props(qp))
+        assert n_ref == 0 and st.niters == 0 and st.status == OK
+        assert np.array_equal(q_gpu, q_ref)
+
+
+@pytest.mark.parametrize("qprecond", [0, 1])
+def test_cgsolveq_absolute_norm(gpu_lib, oracle, qprecond):
+    """resnorm = 0: qprecond 0/1 stop on sqrt(r.r) < qepsilon (phys.c:2470-2475)."""
+    g = grid("quad16x8")
+    prob = gg.make_q_problem(g, seed=5, sigma_u=1e-3)
+    pr = q_props(qprecond, resnorm=0.0, qepsilon=1e-9)
+    q_ref, n_ref = oracle.cgsolveq(prob, pr)
+    ctx = Context(g)
+    q_gpu, st = ctx.cgsolveq(prob, pr)
+    assert abs(st.niters - n_ref) <= 2
+    assert rel_l2(q_gpu, q_ref, g.active_mask()) <= 1e-8
+
+
+def test_repeat_is_bitwise_deterministic(gpu_lib):
+    g = grid("tri3000_partial")
+    prob = gg.make_q_problem(g, seed=9)
+    ctx = Context(g)
+    a, sa = ctx.cgsolveq(prob, q_props(1))
+    b, sb = ctx.cgsolveq(prob, q_props(1))
+    assert sa.niters == sb.niters and np.array_equal(a, b)
+
+
+def test_staged_solve_repeatable(gpu_lib, oracle):
+    """upload once, solve twice on the resident inputs, download: same answer as the drop-in."""
+    g = grid("quad64x16x32")
+    prob = gg.make_q_problem(g, seed=3, q0_sigma=0.01)
+    ctx = Context(g)
+    ctx.q_upload(prob)
+    s1 = ctx.q_solve(q_props(2))
+    s2 = ctx.q_solve(q_props(2))
+    q = ctx.q_download(prob.q)
+    q_ref, n_ref = oracle.cgsolveq(prob, q_props(2))
+    assert s1.niters == s2.niters
+    assert rel_l2(q, q_ref, g.active_mask()) <= TOL
+
+
+def test_small_grid_count(gpu_lib, oracle):
+    """A launch with fewer CTAs gives the same answer within tolerance."""
+    g = grid("tri3000_partial")
+    prob = gg.make_q_problem(g, seed=9)
+    ctx = Context(g)
+    ctx.set_grid(3)
+    q_gpu, st = ctx.cgsolveq(prob, q_props(0))
+    q_ref, n_ref = oracle.cgsolveq(prob, q_props(0))
+    assert abs(st.niters - n_ref) <= 2
+    assert rel_l2(q_gpu, q_ref, g.active_mask()) <= TOL
