@@ -138,6 +138,60 @@ int sgpu_set_grid(sgpu_context *ctx, int ctas);
  * caller can order its own work or record timing events around the solves. */
 void *sgpu_stream(sgpu_context *ctx);
 
+/* ---------------------------------------------------------------------------
+ * Batched mixed-precision pressure solves.
+ *
+ * Many independent CGSolveQ problems (grids of any size and depth, one
+ * qprecond for the batch) share one device arena and advance together in one
+ * persistent cooperative kernel; each keeps its own scalars, tolerance and
+ * iteration count.  Inner CG arithmetic is FP32; inner products, the solution
+ * and the residual used for the stopping test are FP64 ("reliable updates":
+ * the FP64 true residual b - A x replaces the FP32 one whenever the iterated
+ * residual has fallen by `delta`, and convergence is declared only on it).
+ * Same stopping rule as CGSolveQ (main/phys.c:2470-2475, 2516-2524).
+ * Type-3 boundary cells are fixed (Dirichlet) values: the CG direction is 0
+ * there, so a nonzero src at those cells is not propagated as the reference's
+ * p = src does (ComputeQSource never produces one, main/phys.c:2353-2357).
+ * No counterpart in the reference (it solves one partition per process).
+ * ------------------------------------------------------------------------- */
+typedef struct sgpu_batch sgpu_batch;
+
+/* Reserves device memory for up to max_slots cell levels, max_cols
+ * computational columns, max_edge_slots edge levels and max_instances
+ * problems (sgpu_batch_bytes_per_request gives the bytes one problem needs). */
+int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slots, long long max_cols,
+                      long long max_edge_slots, int max_instances, sgpu_batch **out);
+int sgpu_batch_destroy(sgpu_batch *b);
+const char *sgpu_batch_last_error(const sgpu_batch *b);
+long long sgpu_batch_bytes_per_request(int qprecond, int maxfaces, long long n3, long long ncols,
+                                       long long nedge_slots);
+
+/* Adds one problem (same arrays as sgpu_cgsolveq); uploads it and returns its
+ * id.  SGPU_OOM when the arena or the instance table is full (admission). */
+int sgpu_batch_add(sgpu_batch *b, const sgpu_grid_desc *grid, const int *ctop, const double *const *dzz,
+                   const double *const *dzf, const double *D, const double *const *q, const double *const *src,
+                   const double *const *c, double qepsilon, int qmaxiters, double resnorm, int *id);
+
+/* One persistent launch: sets up problems added since the last run, then runs
+ * up to max_iters global iterations (<= 0: until every problem is done).
+ * Reports the problems still running, the device time and the unknown-
+ * iterations done in this launch. */
+int sgpu_batch_run(sgpu_batch *b, int max_iters, int *running, double *ms, long long *unknown_iters);
+
+/* State of problem `id` (1 set-up pending, 2 running, 3 done; -1 unknown id). */
+int sgpu_batch_state(const sgpu_batch *b, int id);
+
+/* Result and report of a finished problem, scattered into the caller's jagged
+ * q (computational cells, levels [ctop, Nk)); q may be NULL for the report
+ * only.  release != 0 frees its device memory and id. */
+int sgpu_batch_result(sgpu_batch *b, int id, double *const *q, sgpu_stats *stats, int release);
+
+/* Tuning: reliable-update factor delta (default 0.01), CTA count (0 = full
+ * wave), barrier wait limit; pass <= 0 / < 0 to keep a value. */
+int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);
+void *sgpu_batch_stream(sgpu_batch *b);
+
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,9 @@ EXPORTS = [
     "sgpu_q_upload", "sgpu_q_solve", "sgpu_q_download",
     "sgpu_h_upload", "sgpu_h_solve", "sgpu_h_download",
     "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream",
+    "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
+    "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set",
+    "sgpu_batch_stream",
 ]
 
 _ip = C.POINTER(C.c_int)
@@ -83,6 +86,22 @@ def load() -> C.CDLL:
     lib.sgpu_set_grid.argtypes = [C.c_void_p, C.c_int]
     lib.sgpu_stream.argtypes = [C.c_void_p]
     lib.sgpu_stream.restype = C.c_void_p
+    lib.sgpu_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_longlong,
+                                      C.c_int, C.POINTER(C.c_void_p)]
+    lib.sgpu_batch_destroy.argtypes = [C.c_void_p]
+    lib.sgpu_batch_last_error.argtypes = [C.c_void_p]
+    lib.sgpu_batch_last_error.restype = C.c_char_p
+    lib.sgpu_batch_bytes_per_request.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_longlong]
+    lib.sgpu_batch_bytes_per_request.restype = C.c_longlong
+    lib.sgpu_batch_add.argtypes = [C.c_void_p, C.POINTER(GridDesc), _ip, _dpp, _dpp, _dp, _dpp, _dpp, _dpp,
+                                   C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int)]
+    lib.sgpu_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_longlong)]
+    lib.sgpu_batch_state.argtypes = [C.c_void_p, C.c_int]
+    lib.sgpu_batch_result.argtypes = [C.c_void_p, C.c_int, _dpp, C.POINTER(Stats), C.c_int]
+    lib.sgpu_batch_set.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_longlong]
+    lib.sgpu_batch_stream.argtypes = [C.c_void_p]
+    lib.sgpu_batch_stream.restype = C.c_void_p
     _lib = lib
     return lib
 

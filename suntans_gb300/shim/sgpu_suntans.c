@@ -1,0 +1,124 @@
+/*
+ * sgpu_suntans.c -- drop-in adapter compiled INSIDE a SUNTANS source tree.
+ *
+ * Provides sgpu_CGSolveQ and sgpu_CGSolve with exactly the parameter lists of
+ * the reference's static CGSolveQ (main/phys.c:50-52, defined 2411) and
+ * CGSolve (main/phys.c:45-46, defined 3086).  patch_phys.sh redirects the two
+ * call sites (main/phys.c:1280 in Solve and main/phys.c:2989 in UPredictor) to
+ * them; nothing else in the model changes.  The adapter reads gridT / physT /
+ * propT through the model's own headers and calls the C ABI of
+ * include/suntans_gb300.h with the model's jagged arrays, so there is no
+ * packing copy in the model.
+ *
+ * Behaviour kept from the reference:
+ *   - the solution goes to q (phys->qc) and phys->h in place;
+ *   - the same convergence messages at VERBOSE > 2 (phys.c:2527-2536,
+ *     3204-3213);
+ *   - a run with more than one process is refused (one GPU, one partition).
+ * Differences: src/htmp and the scratch fields are left untouched (no caller
+ * reads them after the solve); a solver failure prints the library's message
+ * and returns instead of continuing silently.  There is no CPU fallback: a
+ * missing GPU stops the run with an error.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+
+#include "grid.h"
+#include "phys.h"
+#include "suntans_gb300.h"
+
+static sgpu_context *g_ctx = NULL;
+static gridT *g_ctx_grid = NULL;
+
+static void sgpu_die(const char *what, int rc) {
+  fprintf(stderr, "sgpu: %s failed: %s (%s)\n", what, sgpu_status_string(rc),
+          g_ctx ? sgpu_last_error(g_ctx) : "");
+  exit(EXIT_FAILURE);
+}
+
+static void sgpu_ensure_context(gridT *grid, int numprocs) {
+  sgpu_grid_desc d;
+  int rc;
+  if (numprocs > 1) {
+    fprintf(stderr, "sgpu: the GPU solvers run one partition; start SUNTANS with one process\n");
+    exit(EXIT_FAILURE);
+  }
+  if (g_ctx && g_ctx_grid == grid) return;
+  if (g_ctx) sgpu_destroy(g_ctx);
+  d.Nc = grid->Nc;
+  d.Ne = grid->Ne;
+  d.maxfaces = grid->maxfaces;
+  d.Nkmax = grid->Nkmax;
+  d.nfaces = grid->nfaces;
+  d.neigh = grid->neigh;
+  d.face = grid->face;
+  d.Nk = grid->Nk;
+  d.Nke = grid->Nke;
+  d.cellp = grid->cellp;
+  d.celldist = grid->celldist;
+  d.Ac = grid->Ac;
+  d.df = grid->df;
+  d.dg = grid->dg;
+  rc = sgpu_create(&d, 0, &g_ctx);
+  if (rc != SGPU_OK) sgpu_die("sgpu_create", rc);
+  g_ctx_grid = grid;
+}
+
+static void sgpu_props_from(const propT *prop, sgpu_props *p) {
+  p->qprecond = prop->qprecond;
+  p->qmaxiters = prop->qmaxiters;
+  p->qepsilon = prop->qepsilon;
+  p->hprecond = prop->hprecond;
+  p->maxiters = prop->maxiters;
+  p->epsilon = prop->epsilon;
+  p->resnorm = prop->resnorm;
+  p->grav = prop->grav;
+  p->theta = prop->theta;
+  p->dt = prop->dt;
+}
+
+void sgpu_CGSolveQ(REAL **q, REAL **src, REAL **c, gridT *grid, physT *phys, propT *prop, int myproc,
+                   int numprocs, MPI_Comm comm) {
+  sgpu_props p;
+  sgpu_stats st;
+  int rc;
+  (void)comm;
+  sgpu_ensure_context(grid, numprocs);
+  sgpu_props_from(prop, &p);
+  rc = sgpu_cgsolveq(g_ctx, grid->ctop, (const double *const *)grid->dzz, (const double *const *)grid->dzf,
+                     phys->D, q, (const double *const *)src, (const double *const *)c, &p, &st);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER) sgpu_die("sgpu_cgsolveq", rc);
+  if (myproc == 0 && VERBOSE > 2) {
+    double res = st.eps0 != 0 ? sqrt(st.eps / st.eps0) : 0;
+    if (st.eps == 0)
+      printf("Warning...Time step %d, norm of pressure source is 0.\n", prop->n);
+    else if (rc == SGPU_MAXITER)
+      printf("Warning... Time step %d, Pressure iteration not converging after %d steps! RES=%e > %.2e\n",
+             prop->n, st.niters, res, prop->qepsilon);
+    else
+      printf("Time step %d, CGSolve pressure converged after %d iterations, res=%e < %.2e\n", prop->n,
+             st.niters, res, prop->qepsilon);
+  }
+}
+
+void sgpu_CGSolve(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm) {
+  sgpu_props p;
+  sgpu_stats st;
+  int rc;
+  (void)comm;
+  sgpu_ensure_context(grid, numprocs);
+  sgpu_props_from(prop, &p);
+  rc = sgpu_cgsolve(g_ctx, phys->D, phys->h, phys->htmp, &p, &st);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER) sgpu_die("sgpu_cgsolve", rc);
+  if (myproc == 0 && VERBOSE > 2) {
+    double res = st.eps0 != 0 ? sqrt(st.eps / st.eps0) : 0;
+    if (st.eps == 0)
+      printf("Warning...Time step %d, norm of free-surface source is 0.\n", prop->n);
+    else if (rc == SGPU_MAXITER)
+      printf("Warning... Time step %d, Free-surface iteration not converging after %d steps! RES=%e > %.2e\n",
+             prop->n, st.niters, res, prop->qepsilon);
+    else
+      printf("Time step %d, CGSolve free-surface converged after %d iterations, res=%e < %.2e\n", prop->n,
+             st.niters, res, prop->epsilon);
+  }
+}

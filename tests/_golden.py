@@ -1,0 +1,31 @@
+"""Loads the golden fixtures (tests/golden/*.npz) written by make_golden.py."""
+import glob
+import os
+
+import numpy as np
+
+from suntans_gb300.grid import HProblem, QProblem, SolverProps, SunGrid
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def fixture_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz")))
+
+
+def load(name):
+    d = dict(np.load(os.path.join(HERE, name + ".npz")))
+    Nc, Ne, mf, Nkmax = (int(v) for v in d["sizes"])
+    g = SunGrid(Nc=Nc, Ne=Ne, maxfaces=mf, Nkmax=Nkmax,
+                **{k: d[k] for k in ("nfaces", "neigh", "face", "Nk", "Nke", "ctop", "cellp", "celldist",
+                                     "Ac", "df", "dg", "dzz", "dzf")}, name=name)
+    qp = QProblem(grid=g, D=d["qD"], src=d["src"], q=d["q0"], c=d["c0"])
+    hp = HProblem(grid=g, D=d["hD"], htmp=d["htmp"], h=d["h0"])
+    pv = d["props"]
+    props = dict(qmaxiters=int(pv[0]), qepsilon=float(pv[1]), resnorm=float(pv[2]), dt=float(pv[3]),
+                 theta=float(pv[4]), grav=float(pv[5]), maxiters=int(pv[6]), epsilon=float(pv[7]))
+    return g, qp, hp, props, d
+
+
+def props_for(props, **kw):
+    return SolverProps(**{**props, **kw})

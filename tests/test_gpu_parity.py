@@ -2,7 +2,8 @@
 
 Tolerance: relative L2 of the solution over computational cells / active levels
 <= 1e-9 at equal tolerance (1e-10 relative residual), and iteration counts
-within 2 of the oracle's (the GPU sums in a different order).
+within max(2, 2%) of the oracle's (the GPU sums in a different order, which
+shifts the stopping iteration of long unpreconditioned solves slightly).
 """
 import numpy as np
 import pytest
@@ -14,6 +15,10 @@ from tests._cases import grid_cases, h_props, q_props, rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-9
+
+
+def iters_close(n_gpu, n_ref):
+    return abs(n_gpu - n_ref) <= max(2, int(0.02 * n_ref))
 
 _GRIDS = {}
 
@@ -40,7 +45,7 @@ def test_cgsolveq_parity(gpu_lib, oracle, gname, qprecond):
     q_gpu, st = ctx.cgsolveq(prob, pr)
     m = g.active_mask()
     assert st.status == OK
-    assert abs(st.niters - n_ref) <= 2, (st.niters, n_ref)
+    assert iters_close(st.niters, n_ref), (st.niters, n_ref)
     err = rel_l2(q_gpu, q_ref, m)
     assert err <= TOL, err
     # entries outside the active set are returned untouched
@@ -59,7 +64,7 @@ def test_cgsolve_parity(gpu_lib, oracle, gname, hprecond):
     h_gpu, st = ctx.cgsolve(prob, pr)
     comp = g.comp_cells()
     assert st.status == OK
-    assert abs(st.niters - n_ref) <= 2, (st.niters, n_ref)
+    assert iters_close(st.niters, n_ref), (st.niters, n_ref)
     assert rel_l2(h_gpu[comp], h_ref[comp]) <= TOL
     bdy = g.cellp[g.celldist[1]:g.celldist[2]]
     assert np.array_equal(h_gpu[bdy], prob.h[bdy])
@@ -101,7 +106,7 @@ def test_cgsolveq_absolute_norm(gpu_lib, oracle, qprecond):
     q_ref, n_ref = oracle.cgsolveq(prob, pr)
     ctx = Context(g)
     q_gpu, st = ctx.cgsolveq(prob, pr)
-    assert abs(st.niters - n_ref) <= 2
+    assert iters_close(st.niters, n_ref)
     assert rel_l2(q_gpu, q_ref, g.active_mask()) <= 1e-8
 
 
@@ -136,5 +141,5 @@ def test_small_grid_count(gpu_lib, oracle):
     ctx.set_grid(3)
     q_gpu, st = ctx.cgsolveq(prob, q_props(0))
     q_ref, n_ref = oracle.cgsolveq(prob, q_props(0))
-    assert abs(st.niters - n_ref) <= 2
+    assert iters_close(st.niters, n_ref)
     assert rel_l2(q_gpu, q_ref, g.active_mask()) <= TOL

@@ -1,0 +1,94 @@
+"""The C restatement of the reference algorithm (oracle/cg_oracle.c) is pinned
+bit-for-bit against the reference's own outputs: the golden vectors made by
+tests/golden/make_golden.py from the reference's compiled main/phys.c, and --
+where the reference tree is present -- the reference library itself on larger
+seeded grids."""
+import numpy as np
+import pytest
+
+from oracle import oracle as om
+from oracle.oracle import Oracle
+from suntans_gb300 import gridgen as gg
+from tests._cases import grid_cases, h_props, q_props
+from tests._golden import fixture_names, load, props_for
+
+
+@pytest.fixture(scope="module")
+def port():
+    om.build_port()
+    return Oracle("port")
+
+
+def test_fixtures_present():
+    assert len(fixture_names()) >= 3
+
+
+@pytest.mark.parametrize("name", fixture_names())
+@pytest.mark.parametrize("qprecond", [0, 1, 2])
+def test_port_cgsolveq_matches_golden_bitwise(port, name, qprecond):
+    g, qp, hp, props, d = load(name)
+    q, n = port.cgsolveq(qp, props_for(props, qprecond=qprecond))
+    assert n == int(d[f"n_qp{qprecond}"])
+    assert np.array_equal(q, d[f"q_qp{qprecond}"])
+
+
+@pytest.mark.parametrize("name", fixture_names())
+@pytest.mark.parametrize("hprecond", [0, 1])
+def test_port_cgsolve_matches_golden_bitwise(port, name, hprecond):
+    g, qp, hp, props, d = load(name)
+    h, n = port.cgsolve(hp, props_for(props, hprecond=hprecond))
+    assert n == int(d[f"n_hp{hprecond}"])
+    assert np.array_equal(h, d[f"h_hp{hprecond}"])
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_port_operators_match_golden_bitwise(port, name):
+    g, qp, hp, props, d = load(name)
+    x = d["x"]
+    c = port.condition_q(g, qp.D, np.ones(g.n3))
+    assert np.array_equal(c, d["condq"])
+    coef0, _ = port.qcoefficients(g, qp.D, c, 0)
+    coef1, fcoef1 = port.qcoefficients(g, qp.D, c, 1)
+    assert np.array_equal(coef0, d["coef0"])
+    assert np.array_equal(coef1, d["coef1"]) and np.array_equal(fcoef1, d["fcoef1"])
+    assert np.array_equal(port.operator_q(g, qp.D, coef0, x), d["opq"])
+    assert np.array_equal(port.operator_qc(g, coef1, fcoef1, x), d["opqc"])
+    assert np.array_equal(port.preconditioner(g, coef0, x), d["precond"])
+    hcoef, hfcoef = port.hcoefficients(g, hp.D, props_for(props))
+    assert np.array_equal(hcoef, d["hcoef"]) and np.array_equal(hfcoef, d["hfcoef"])
+    assert np.array_equal(port.operator_h(g, hcoef, hfcoef, x[:g.Nc]), d["oph"])
+
+
+def test_golden_cover_edge_cases():
+    """The fixtures hold the cases the solvers special-case: dry top layers
+    (ctop > 0), single-level wet columns (ctop = Nk-1), type-3 boundary cells,
+    walls, quads and triangles."""
+    seen = dict(ctop=False, single=False, bdy=False, quad=False, tri=False)
+    for name in fixture_names():
+        g, *_ = load(name)
+        seen["ctop"] |= bool((g.ctop > 0).any())
+        seen["single"] |= bool((g.ctop == g.Nk - 1).any())
+        seen["bdy"] |= bool(g.celldist[2] > g.celldist[1])
+        seen["quad"] |= g.maxfaces == 4
+        seen["tri"] |= g.maxfaces == 3
+    assert all(seen.values()), seen
+
+
+ref_present = om.build_ref() is not None if not om.available("ref") else True
+
+
+@pytest.mark.skipif(not ref_present, reason="reference sources not present on this host")
+@pytest.mark.parametrize("gname", [n for n, _ in grid_cases()[:2]] + ["tri400_shallow"])
+def test_port_matches_reference_library(port, gname):
+    ref = Oracle("ref")
+    g = dict(grid_cases())[gname]()
+    qp = gg.make_q_problem(g, seed=8, q0_sigma=0.02)
+    for qpc in (0, 1, 2):
+        a, na = port.cgsolveq(qp, q_props(qpc))
+        b, nb = ref.cgsolveq(qp, q_props(qpc))
+        assert na == nb and np.array_equal(a, b)
+    hp = gg.make_h_problem(g, seed=9)
+    for hpc in (0, 1):
+        a, na = port.cgsolve(hp, h_props(hpc))
+        b, nb = ref.cgsolve(hp, h_props(hpc))
+        assert na == nb and np.array_equal(a, b)

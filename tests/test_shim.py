@@ -1,0 +1,39 @@
+"""The SUNTANS-side adapter: patch_phys.sh redirects exactly the two solver
+call sites of a copy of main/phys.c, and the patched file plus
+sgpu_suntans.c compile against the model's own headers.  Needs the SUNTANS
+sources (skipped where they are absent); runs on CPU only."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("SUNTANS_REFDIR", "/root/reference/main")
+SHIM = os.path.join(ROOT, "suntans_gb300", "shim")
+
+pytestmark = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "phys.c")),
+                                reason="SUNTANS sources not present on this host")
+
+
+def test_patch_and_compile(tmp_path):
+    phys = tmp_path / "phys.c"
+    shutil.copy(os.path.join(REF, "phys.c"), phys)
+    r = subprocess.run(["sh", os.path.join(SHIM, "patch_phys.sh"), str(phys)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    new = phys.read_text()
+    old = open(os.path.join(REF, "phys.c")).read()
+    assert new.count("sgpu_CGSolveQ(phys->qc,phys->stmp,phys->stmp3,grid,phys,prop,myproc,numprocs,comm);") == 1
+    assert new.count("sgpu_CGSolve(grid,phys,prop,myproc,numprocs,comm);") == 1
+    # nothing else changed: same lines apart from the 2 declarations and the 2 calls
+    diff = [a for a in new.splitlines() if "sgpu_" not in a]
+    assert diff == [a for a in old.splitlines() if not a.strip().startswith(("CGSolveQ(phys->qc", "CGSolve(grid"))]
+    cc = ["gcc", "-fcommon", "-DNOMPI", "-DNONETCDF", "-w", f"-I{REF}", f"-I{ROOT}/include", "-c"]
+    r = subprocess.run(cc + [str(phys), "-o", str(tmp_path / "phys.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(cc + [os.path.join(SHIM, "sgpu_suntans.c"), "-o", str(tmp_path / "shim.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    syms = subprocess.run(["nm", str(tmp_path / "shim.o")], capture_output=True, text=True).stdout
+    for s in ("sgpu_CGSolveQ", "sgpu_CGSolve", "sgpu_cgsolveq", "sgpu_cgsolve", "sgpu_create"):
+        assert s in syms
