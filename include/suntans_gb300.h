@@ -40,6 +40,7 @@ extern "C" {
 #define SGPU_BAD_ARG 6     /* null pointer or out-of-range parameter */
 #define SGPU_CUDA_ERROR 7  /* a CUDA call failed (message: sgpu_last_error) */
 #define SGPU_NO_DEVICE 8   /* no CUDA device, or the library was built without one */
+#define SGPU_TOO_LARGE 9   /* grid exceeds the fixed scratch of sgpu_cgsolve_noalloc */
 
 /* The part of gridT (main/grid.h:32-149) the two solves read and that does not
  * change between time steps.  Arrays are copied at sgpu_create; the caller
@@ -191,6 +192,42 @@ int sgpu_batch_result(sgpu_batch *b, int id, double *const *q, sgpu_stats *stats
 int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);
 void *sgpu_batch_stream(sgpu_batch *b);
 
+/* Grid of sgpu_cgsolve_noalloc: the same gridT fields as sgpu_grid_desc, but
+ * every pointer is DEVICE memory owned by the caller, in the caller's cell
+ * order (no reordering, no copies). */
+typedef struct sgpu_noalloc_grid {
+  int Nc, Ne, maxfaces;
+  int ncomp;           /* celldist[1]: cellp[0..ncomp) are the computational cells */
+  const int *cellp;    /* device [ncomp]                                          */
+  const int *nfaces;   /* device [Nc]                                              */
+  const int *neigh;    /* device [Nc*maxfaces], -1 = no neighbour                  */
+  const int *face;     /* device [Nc*maxfaces]                                     */
+  const double *Ac;    /* device [Nc]                                              */
+  const double *df;    /* device [Ne]                                              */
+  const double *dg;    /* device [Ne]                                              */
+} sgpu_noalloc_grid;
+
+/* Free-surface solve (the CGSolve semantics above) that allocates nothing.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- a host program whose device memory is owned entirely by its own
+ * pool allocator (a coupled model that hands each component slices of one
+ * arena and forbids other allocations), or a time-critical loop that cannot
+ * pay for cudaMalloc/cudaFree, which synchronise the whole device.
+ *   D, htmp   device inputs [Ne], [Nc];  h  device [Nc], type-3 values in,
+ *             solution out at computational cells (in place, as CGSolve does);
+ *   stream    the cudaStream_t to run on (0 = legacy default stream).
+ * The solver's scratch is one static device array of 32 MiB in this library:
+ * 512 + 16*2048 + 8*Nc*(5+maxfaces) bytes must fit, i.e. up to about 466,000
+ * quadrilateral or 524,000 triangular cells; larger grids return
+ * SGPU_TOO_LARGE before any device work.  Every call shares that array and
+ * leaves its contents behind (the control words are cleared at the start of
+ * each call), so calls that overlap on the GPU race and must not be issued.
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress, with that device current); make it before any stream
+ * capture.  Runs on the current device; blocks until the solve has finished.
+ * stats->ms_solve is -1 (no timing events are created). */
+int sgpu_cgsolve_noalloc(const sgpu_noalloc_grid *grid, const double *D, double *h, const double *htmp,
+                         const sgpu_props *prop, sgpu_stats *stats, void *stream);
 
 #ifdef __cplusplus
 }

@@ -25,10 +25,12 @@ EXPORTS = [
     "sgpu_q_upload", "sgpu_q_solve", "sgpu_q_download",
     "sgpu_h_upload", "sgpu_h_solve", "sgpu_h_download",
     "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream",
+    "sgpu_cgsolve_noalloc",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
     "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set",
     "sgpu_batch_stream",
 ]
+TOO_LARGE = 9
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -46,6 +48,13 @@ class Props(C.Structure):
                 ("hprecond", C.c_int), ("maxiters", C.c_int), ("epsilon", C.c_double),
                 ("resnorm", C.c_double), ("grav", C.c_double), ("theta", C.c_double),
                 ("dt", C.c_double)]
+
+
+class NoallocGrid(C.Structure):
+    """sgpu_noalloc_grid: sizes plus DEVICE pointers (integers) owned by the caller."""
+    _fields_ = [("Nc", C.c_int), ("Ne", C.c_int), ("maxfaces", C.c_int), ("ncomp", C.c_int),
+                ("cellp", C.c_void_p), ("nfaces", C.c_void_p), ("neigh", C.c_void_p), ("face", C.c_void_p),
+                ("Ac", C.c_void_p), ("df", C.c_void_p), ("dg", C.c_void_p)]
 
 
 class Stats(C.Structure):
@@ -86,6 +95,8 @@ def load() -> C.CDLL:
     lib.sgpu_set_grid.argtypes = [C.c_void_p, C.c_int]
     lib.sgpu_stream.argtypes = [C.c_void_p]
     lib.sgpu_stream.restype = C.c_void_p
+    lib.sgpu_cgsolve_noalloc.argtypes = [C.POINTER(NoallocGrid), C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.POINTER(Props), C.POINTER(Stats), C.c_void_p]
     lib.sgpu_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_longlong,
                                       C.c_int, C.POINTER(C.c_void_p)]
     lib.sgpu_batch_destroy.argtypes = [C.c_void_p]

@@ -167,6 +167,7 @@ const char* sgpu_status_string(int s) {
     case SGPU_BAD_ARG: return "bad argument";
     case SGPU_CUDA_ERROR: return "cuda error";
     case SGPU_NO_DEVICE: return "no cuda device";
+    case SGPU_TOO_LARGE: return "grid exceeds the fixed scratch of the allocation-free solve";
   }
   return "unknown";
 }
