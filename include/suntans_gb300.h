@@ -192,6 +192,11 @@ int sgpu_batch_result(sgpu_batch *b, int id, double *const *q, sgpu_stats *stats
 int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);
 void *sgpu_batch_stream(sgpu_batch *b);
 
+/* Device time of the last launch per phase (ns): [1] operator apply, [2]
+ * vector update, [3] FP64 merge, [4] FP64 true residual, [5..7] set-up.
+ * Zero unless the library was built with -DSGPU_PHASE_TIMING. */
+int sgpu_batch_phase_times(const sgpu_batch *b, long long *ns8);
+
 /* Grid of sgpu_cgsolve_noalloc: the same gridT fields as sgpu_grid_desc, but
  * every pointer is DEVICE memory owned by the caller, in the caller's cell
  * order (no reordering, no copies). */

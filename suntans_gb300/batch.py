@@ -118,6 +118,13 @@ class Batch:
             self.grids.pop(i, None)
         return q, st
 
+    def phase_times_ms(self):
+        """Per-phase device time of the last launch (zero unless built with -DSGPU_PHASE_TIMING)."""
+        arr = (C.c_longlong * 8)()
+        self.lib.sgpu_batch_phase_times(self.h, arr)
+        names = ["-", "apply", "update", "merge64", "residual64", "setup1", "setup2", "setup3"]
+        return {n: arr[k] / 1e6 for k, n in enumerate(names) if k}
+
     def stats(self, i):
         st = Stats()
         rc = self.lib.sgpu_batch_result(self.h, int(i), None, C.byref(st), 0)

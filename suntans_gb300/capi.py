@@ -28,7 +28,7 @@ EXPORTS = [
     "sgpu_cgsolve_noalloc",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
     "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set",
-    "sgpu_batch_stream",
+    "sgpu_batch_stream", "sgpu_batch_phase_times",
 ]
 TOO_LARGE = 9
 
@@ -113,6 +113,7 @@ def load() -> C.CDLL:
     lib.sgpu_batch_set.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_longlong]
     lib.sgpu_batch_stream.argtypes = [C.c_void_p]
     lib.sgpu_batch_stream.restype = C.c_void_p
+    lib.sgpu_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     _lib = lib
     return lib
 

@@ -6,8 +6,9 @@
 //   * the CG iteration runs on FP32 vectors: operator apply, preconditioner
 //     (Jacobi through the scaling of qprecond 1, the column tridiagonal solve of
 //     qprecond 2), and the vector updates;
-//   * every inner product (p.Ap, r.r, r.M^-1 r) is accumulated in FP64 from
-//     exact products of FP32 values (a product of two floats is exact in FP64);
+//   * every inner product (p.Ap, r.r, r.M^-1 r) is accumulated from exact
+//     products of FP32 values with FP64-class accuracy: double-float per thread
+//     (error-free transformations on the FP32 pipe), FP64 across threads;
 //   * the solution is accumulated in FP64: the FP32 increments collected since
 //     the last update are added into the FP64 iterate whenever the iterated
 //     residual norm has fallen by delta (default 0.01) since the last update, and
@@ -21,21 +22,27 @@
 // coefficients of QCoefficients/ConditionQ (3420-3471, 3629-3687) for
 // qprecond 1, OperatorQ (3486-3536) for qprecond 0 and 2, Preconditioner +
 // TriSolve (3577-3619, util.c:185-203) for qprecond 2.  In the FP32 apply the
-// qprecond 1 face and vertical coefficients are formed on the fly from dzz and
-// 1/c (2 floats per level instead of F+1), and the qprecond 0/2 face
-// coefficients dzf*D are read from edge storage (each edge level serves both
-// of its cells).
+// qprecond 1 face coefficients are formed on the fly as (dzz_u/c_u) D (1/c_n),
+// and the qprecond 0/2 face coefficients dzf*D are read from edge storage (each
+// edge level serves both of its cells).
 //
-// Per global iteration: phase A (p_new = s + mu p_old formed on the fly for the
-// cell and its neighbours, z = A p_new, p.z), phase B (x += nu p, r -= nu z,
-// preconditioner, r.s and r.r), and, only when some instance asked for it, the
-// reliable-update phases R1 (x64 += x32) and R2 (FP64 true residual).  Each
-// phase ends at a grid barrier; the per-instance reductions finish before it
-// in the CTA that completes the instance's last tile.
+// Work: computational columns are packed into tiles (<= 1024 slots,
+// <= 128 columns); every tile starts on a 16-byte boundary.  A CTA is 8
+// compute warps plus 1 producer warp.  In the two phases of every CG
+// iteration -- A (p_new = s + mu p_old formed on the fly for the cell and its
+// neighbours, z = A p_new, p.z) and B (x += nu p, r -= nu z, preconditioner,
+// r.s, r.r) -- the producer streams each tile's header and its contiguous FP32
+// streams into a two-stage shared-memory ring with bulk asynchronous copies
+// (cp.async.bulk + mbarrier), so the compute warps never wait on metadata
+// chains.  Only when some problem asks for it run the reliable-update phases
+// R1 (x64 += x32) and R2 (FP64 true residual).  Each phase ends at a grid
+// barrier; per-problem reductions finish before it in the CTA that completes
+// the problem's last tile.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -46,99 +53,253 @@
 
 namespace sgpu {
 
+constexpr int kCompute = 256;              // compute threads (8 warps)
+constexpr int kThreads = kCompute + 32;    // + 1 producer warp
+
 // ---------------------------------------------------------------------------
-// device helpers
+// small device helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double f2d(float f) { return (double)f; }
 
-struct TileInfo {
-  int c0, c1;     // global columns [c0, c1)
-  int base, end;  // storage slots [base, end)
-  int inst;
+// Per-thread inner-product accumulator in double-float: the product of two
+// floats is split exactly into p + e (TwoProduct with one FMA), p is added to
+// the high word with an error-free TwoSum, and e plus the rounding error go to
+// the low word.  The pair carries ~48 significant bits, so a thread's partial
+// sum is as accurate as FP64 accumulation, while every operation stays on the
+// FP32 pipe (GB300's FP64 pipe, which also performs f32->f64 conversions, runs
+// at ~1/70 of the FP32 rate).  The intrinsics are never contracted or
+// reassociated.  Thread partials are combined in FP64.
+struct DF {
+  float hi, lo;
 };
-
-__device__ __forceinline__ void load_tile(const BatchArgs& a, int t, TileInfo& ti, int* s_start, int* s_ctop,
-                                          int* s_nk) {
-  const int c0 = a.tile_c0[2 * t], c1 = a.tile_c0[2 * t + 1];
-  ti.c0 = c0;
-  ti.c1 = c1;
-  ti.inst = a.tile_inst[t];
-  const int base = a.col[c0].s;
-  ti.base = base;
-  for (int c = threadIdx.x; c < c1 - c0; c += blockDim.x) {
-    const BCol cc = a.col[c0 + c];
-    s_start[c] = cc.s - base;
-    s_ctop[c] = cc.ctop;
-    s_nk[c] = cc.nk;
-  }
-  if (threadIdx.x == 0) {
-    const BCol cl = a.col[c1 - 1];
-    s_start[c1 - c0] = cl.s + cl.nk - base;
-  }
-  __syncthreads();
-  ti.end = base + s_start[c1 - c0];
+__device__ __forceinline__ void df_zero(DF& s) { s.hi = 0.f; s.lo = 0.f; }
+__device__ __forceinline__ void df_addprod(DF& s, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  const float t = __fadd_rn(s.hi, p);
+  const float bp = __fsub_rn(t, s.hi);
+  const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  s.hi = t;
+  s.lo = __fadd_rn(s.lo, __fadd_rn(err, e));
 }
+__device__ __forceinline__ double df_value(const DF& s) { return (double)s.hi + (double)s.lo; }
 
-__device__ __forceinline__ int find_col_b(const int* s_start, int ncols, int s) {
-  int lo = 0, hi = ncols - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (s_start[mid] <= s) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void csync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }  // compute warps only
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after limit_ns and reports false (the caller records
+// SGPU_TIMEOUT and carries on to the next grid barrier, which ends the kernel).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity))
+    if ((long long)(globaltimer_ns() - t0) > limit_ns) return false;
+  return true;
+}
+// 1-D bulk copy global -> shared, completion counted on `bar`; 16-byte
+// aligned addresses and a size that is a multiple of 16 (asserted by layout).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Deterministic per-instance reduction: the CTA that finishes the last tile of
-// instance `i` in this phase sums the tiles' partials in tile order and runs
-// `fin(tot)` on thread 0.  Must be called by the whole CTA after block_sum.
-template <int NV, class Fin>
-__device__ __forceinline__ void tile_done(const BatchArgs& a, int t, int i, const double (&part)[NV], double* s_red,
-                                          Fin&& fin) {
-  __shared__ int s_last;
-  BInst* I = a.inst + i;
-  if (threadIdx.x == 0) {
+// FP64 sum over the 256 compute threads, fixed order; every compute thread gets it.
+template <int NV>
+__device__ __forceinline__ void csum(double (&v)[NV], double* s_red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int v = 0; v < NV; ++v) a.tpart[2 * t + v] = part[v];
-    __threadfence();
-    const int old = atomicAdd(&I->cnt, 1);
-    s_last = (old == I->t1 - I->t0 - 1);
+  for (int j = 0; j < NV; ++j) {
+    double s = v[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) s_red[j * 8 + wid] = s;
   }
-  __syncthreads();
-  if (s_last) {
+  csync();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) s += s_red[j * 8 + w];
+    v[j] = s;
+  }
+  csync();
+}
+
+__device__ __forceinline__ int inst_state(const BatchArgs& a, int i) { return ld_volatile_int(&a.inst[i].state); }
+__device__ __forceinline__ int inst_flags(const BatchArgs& a, int i) { return ld_volatile_int(&a.inst[i].flags); }
+
+// ---------------------------------------------------------------------------
+// per-instance reduction (two levels, deterministic, composition independent)
+//
+// A CTA accumulates its partial over all of its tiles of one instance (they
+// are consecutive in its tile list) and then flushes it to slot t0 + l with
+// l = (b - t0) mod G, the local index of the CTA's first tile of that instance:
+// the slots used are exactly [t0, t0 + min(G, ntiles)) and their contents do not
+// depend on where the instance sits in the launch's tile list.  The flush that
+// completes the instance's tile count sums those slots in order and runs
+// fin(I, tot) on thread 0.  Compute warps only.
+// ---------------------------------------------------------------------------
+template <int NV, class Fin>
+__device__ __forceinline__ void flush(const BatchArgs& a, int i, int ntiles_done, double (&acc)[NV], double* s_red,
+                                      int* s_flag, Fin&& fin) {
+  csum<NV>(acc, s_red);
+  BInst* I = a.inst + i;
+  const int G = gridDim.x;
+  if (threadIdx.x == 0) {
+    const int t0 = I->t0, n = I->t1 - I->t0;
+    const int l = ((int)blockIdx.x - t0 % G + G) % G;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.tpart[2 * (t0 + l) + v] = acc[v];
     __threadfence();
+    const int old = atomicAdd(&I->cnt, ntiles_done);
+    *s_flag = (old + ntiles_done == n);
+  }
+  csync();
+  if (*s_flag) {
+    __threadfence();
+    const int t0 = I->t0, n = I->t1 - I->t0;
+    const int m = n < G ? n : G;
     double v[NV];
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
       double s = 0.0;
-      for (int tt = I->t0 + (int)threadIdx.x; tt < I->t1; tt += blockDim.x)
-        s += ((volatile double*)a.tpart)[2 * tt + j];
+      for (int l = threadIdx.x; l < m; l += kCompute) s += ((volatile double*)a.tpart)[2 * (t0 + l) + j];
       v[j] = s;
     }
-    block_sum<NV>(v, s_red);
+    csum<NV>(v, s_red);
     if (threadIdx.x == 0) {
       fin(I, v);
       I->cnt = 0;
       __threadfence();
     }
   }
-  __syncthreads();
+  csync();
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
 }
 
-__device__ __forceinline__ int inst_state(const BatchArgs& a, int i) { return ld_volatile_int(&a.inst[i].state); }
-__device__ __forceinline__ int inst_flags(const BatchArgs& a, int i) { return ld_volatile_int(&a.inst[i].flags); }
+// ---------------------------------------------------------------------------
+// simple (non-pipelined) tile access for the rare phases: set-up and the FP64
+// true residual.  Metadata from BCol/BFace staged into shared memory.
+// ---------------------------------------------------------------------------
+struct TileSmem {
+  int start[kBTCols + 1];
+  int ctop[kBTCols];
+  int nk[kBTCols];
+  int fns[kBTFaces];
+  int fkk[kBTFaces];
+  int fes[kBTFaces];
+  int ncols;
+};
+static_assert(sizeof(TileSmem) <= kBufBytes, "simple-path metadata must fit a pipeline stage");
+
+struct TileInfo {
+  int c0, c1, base, end;
+};
+
+__device__ __forceinline__ void load_tile(const BatchArgs& a, int t, TileInfo& ti, TileSmem& sm) {
+  const TileDesc d = a.tiles[t];
+  ti.c0 = d.c0;
+  ti.c1 = d.c1;
+  ti.base = d.base;
+  ti.end = d.base + d.nslots;
+  const int ncols = ti.c1 - ti.c0, F = a.F;
+  for (int c = threadIdx.x; c < ncols; c += kCompute) {
+    const BCol cc = a.col[ti.c0 + c];
+    sm.start[c] = cc.s - ti.base;
+    sm.ctop[c] = cc.ctop;
+    sm.nk[c] = cc.nk;
+  }
+  for (int e = threadIdx.x; e < ncols * F; e += kCompute) {
+    const BFace fc = a.face[(size_t)ti.c0 * F + e];
+    sm.fns[e] = fc.ns;
+    sm.fkk[e] = fc.ns < 0 ? 0 : ((int)fc.kmin | ((int)fc.kmax << 16));
+    sm.fes[e] = fc.es;
+  }
+  if (threadIdx.x == 0) {
+    sm.start[ncols] = d.nslots;
+    sm.ncols = ncols;
+  }
+  csync();
+}
+
+__device__ __forceinline__ int col_of(const int* start, int ncols, int s) {
+  int lo = 0, hi = ncols - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= s) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Walks the CTA's tiles b, b+G, ... of instances for which want(i) holds
+// (compute warps), calling body(t, i, acc) per tile and flushing per instance.
+template <int NV, class Want, class Body, class Fin>
+__device__ __forceinline__ void for_tiles_reduce(const BatchArgs& a, double* s_red, int* s_flag, Want&& want,
+                                                 Body&& body, Fin&& fin) {
+  const int G = gridDim.x;
+  int cur = -1, cnt = 0;
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
+  for (int t = blockIdx.x; t < a.ntiles; t += G) {
+    const int i = a.tile_inst[t];
+    // uniform across the CTA: an instance's state/flags change only in its
+    // finaliser, which runs after every CTA has flushed all its tiles of it
+    if (!want(i)) continue;
+    if (i != cur) {
+      if (cur >= 0) flush<NV>(a, cur, cnt, acc, s_red, s_flag, fin);
+      cur = i;
+      cnt = 0;
+    }
+    body(t, i, acc);
+    ++cnt;
+  }
+  if (cur >= 0) flush<NV>(a, cur, cnt, acc, s_red, s_flag, fin);
+}
+
+template <class Want, class Body>
+__device__ __forceinline__ void for_tiles(const BatchArgs& a, Want&& want, Body&& body) {
+  for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+    const int i = a.tile_inst[t];
+    if (want(i)) body(t, i);
+  }
+}
 
 // ---- FP64 operator (true residual), one active slot ----
 template <int QP>
-__device__ __forceinline__ double apply64(const BatchArgs& a, int u, int j, int k, int ctop, int nk, const double* x) {
+__device__ __forceinline__ double apply64(const BatchArgs& a, const TileSmem& sm, int c, int u, int k, int ctop,
+                                          int nk, const double* x) {
   const int F = a.F;
   double y;
   if (QP == 1) {
     y = -x[u];
     for (int f = 0; f < F; ++f) {
-      const BFace fc = a.face[(size_t)j * F + f];
-      if (fc.ns < 0 || k < fc.kmin || k >= fc.kmax) continue;
-      y += x[fc.ns + k] * a.fc64[(size_t)F * u + f];
+      const int kk = sm.fkk[c * F + f];
+      if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
+      y += x[sm.fns[c * F + f] + k] * a.fc64[(size_t)F * u + f];
     }
     if (k > ctop) y += a.coef64[u] * x[u - 1];
     if (k < nk - 1) y += a.coef64[u + 1] * x[u + 1];
@@ -146,9 +307,9 @@ __device__ __forceinline__ double apply64(const BatchArgs& a, int u, int j, int 
     const double xu = x[u];
     y = 0.0;
     for (int f = 0; f < F; ++f) {
-      const BFace fc = a.face[(size_t)j * F + f];
-      if (fc.ns < 0 || k < fc.kmin || k >= fc.kmax) continue;
-      y += (x[fc.ns + k] - xu) * a.dzfD64[fc.es + k];
+      const int kk = sm.fkk[c * F + f];
+      if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
+      y += (x[sm.fns[c * F + f] + k] - xu) * a.dzfD64[sm.fes[c * F + f] + k];
     }
     if (ctop < nk - 1) {
       if (k == ctop) {
@@ -168,17 +329,19 @@ __device__ __forceinline__ double apply64(const BatchArgs& a, int u, int j, int 
   return y;
 }
 
-// FP32 Thomas solve of one column with FP32 factors (qprecond 2).
-__device__ __forceinline__ void column_solve32(const BatchArgs& a, int off, int ctop, int nk) {
+// FP32 Thomas solve of one column with FP32 factors (qprecond 2); r read from
+// `rin` indexed from `rbase` (global arrays: rbase 0; a staged tile: its base).
+__device__ __forceinline__ void column_solve32(const BatchArgs& a, const float* rin, int rbase, int off, int ctop,
+                                               int nk) {
   const int b = off + ctop, e = off + nk;
   if (ctop == nk - 1) {
-    a.s32[b] = -0.5f * a.r32[b] / a.coef32[b];
+    a.s32[b] = -0.5f * rin[b - rbase] / a.coef32[b];
     return;
   }
-  float dprev = a.r32[b];
+  float dprev = rin[b - rbase];
   a.s32[b] = dprev;
   for (int u = b + 1; u < e; ++u) {
-    dprev = __fmaf_rn(-a.tw32[u], dprev, a.r32[u]);
+    dprev = __fmaf_rn(-a.tw32[u], dprev, rin[u - rbase]);
     a.s32[u] = dprev;
   }
   float un = a.s32[e - 1] * a.tib32[e - 1];
@@ -206,182 +369,769 @@ __device__ __forceinline__ void column_factor64(const BatchArgs& a, int off, int
 }
 
 // ---------------------------------------------------------------------------
+// the pipelined phases
+// ---------------------------------------------------------------------------
+// One pipeline stage in shared memory: a 16-byte descriptor written by the
+// producer, the tile header (capacity kHdrCap - 16), and up to 4 FP32 streams.
+struct StageDesc {
+  int base, nslots, inst, par;
+};
+__device__ __forceinline__ StageDesc* stage_desc(unsigned char* stage) { return (StageDesc*)(stage); }
+__device__ __forceinline__ unsigned char* stage_hdr(unsigned char* stage) { return stage + 16; }
+__device__ __forceinline__ float* stage_stream(unsigned char* stage, int k) {
+  return (float*)(stage + kHdrCap + k * kStreamBytes);
+}
+
+struct Pipe {
+  unsigned char* stage[2];
+  uint64_t* full;    // [2]
+  uint64_t* empty;   // [2]
+  int* list;         // tiles of this CTA for the current phase
+  int* count;
+  uint32_t seq;      // tiles consumed (compute warps) or filled (producer) so far, all phases
+};
+
+// Builds the CTA's ordered list of tiles t = b, b+G, ... with want(inst(t)).
+// All 288 threads take part (it ends with __syncthreads).
+template <class Want>
+__device__ __forceinline__ void build_list(const BatchArgs& a, Pipe& P, Want&& want, int* s_wsum) {
+  const int G = gridDim.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) *P.count = 0;
+  __syncthreads();
+  const int per = (a.ntiles - (int)blockIdx.x + G - 1) / G;  // candidate tiles of this CTA
+  for (int j0 = 0; j0 < per; j0 += kCompute) {
+    bool ok = false;
+    int t = 0;
+    if (warp < 8) {
+      const int j = j0 + (int)threadIdx.x;
+      t = (int)blockIdx.x + j * G;
+      ok = (j < per) && want(a.tile_inst[t]);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0 && warp < 8) s_wsum[warp] = __popc(m);
+    __syncthreads();
+    if (ok) {
+      int off = *P.count;
+      for (int w = 0; w < warp; ++w) off += s_wsum[w];
+      off += __popc(m & ((1u << lane) - 1u));
+      if (off < kListCap) P.list[off] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < 8; ++w) tot += s_wsum[w];
+      *P.count += tot;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && *P.count > kListCap) *P.count = kListCap;  // the host guarantees this never binds
+  __syncthreads();
+}
+
+// Producer: fill stage seq&1 with tile t.  PH 0 = apply, 1 = update.
+template <int QP, int PH>
+__device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, int t, long long lim, int* err) {
+  const uint32_t q = P.seq;
+  const int b = q & 1;
+  if (q >= 2 && !mbar_wait(&P.empty[b], ((q >> 1) - 1) & 1, lim)) *err = 1;
+  const TileDesc d = a.tiles[t];
+  const int par = ld_volatile_int(&a.inst[d.inst].par);
+  const int n4 = (d.nslots + 3) & ~3;
+  unsigned char* st = P.stage[b];
+  StageDesc* sd = stage_desc(st);
+  sd->base = d.base;
+  sd->nslots = d.nslots;
+  sd->inst = d.inst;
+  sd->par = par;
+  const bool hdr = (PH == 0) || (QP == 2);
+  uint32_t bytes = 0;
+  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + (QP == 1 ? 4 * n4 : 0);
+  else bytes = (hdr ? d.hdr_bytes : 0) + 4 * 4 * n4;
+  fence_proxy_async();
+  mbar_arrive_expect_tx(&P.full[b], bytes);
+  if (hdr) bulk_g2s(stage_hdr(st), a.hdrs + d.hdr, d.hdr_bytes, &P.full[b]);
+  if (PH == 0) {
+    const float* pold = par ? a.pb32 : a.pa32;
+    const float* S = (QP == 2) ? a.s32 : a.r32;
+    bulk_g2s(stage_stream(st, 0), pold + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, 1), S + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
+    if (QP == 1) bulk_g2s(stage_stream(st, 3), a.fz32 + d.base, 4 * n4, &P.full[b]);
+  } else {
+    const float* p = par ? a.pb32 : a.pa32;  // the direction written by phase A
+    bulk_g2s(stage_stream(st, 0), p + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, 1), a.x32 + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, 2), a.z32 + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, 3), a.r32 + d.base, 4 * n4, &P.full[b]);
+  }
+  P.seq = q + 1;
+}
+
+// FP32 apply of one active slot from a staged tile (own data in shared
+// memory, neighbours from global).  p_new = S + mu p_old on the fly.
+template <int QP>
+__device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char* hd, const HdrLayout& L, int c,
+                                         int s, int k, int ctop, int nk, float mu, const float* sp, const float* sS,
+                                         const float* sc, const float* sf, const float* __restrict__ pold,
+                                         const float* __restrict__ S, float& pu_out) {
+  const int F = a.F;
+  const int* fns = (const int*)(hd + L.o_fns);
+  const int* fkk = (const int*)(hd + L.o_fkk);
+  const float* fD = (const float*)(hd + L.o_fD);
+  const int* fes = (const int*)(hd + L.o_fes);
+  const float pu = __fmaf_rn(mu, sp[s], sS[s]);
+  pu_out = pu;
+  float y;
+  if (QP == 1) {
+    const float fz = sf[s];
+    y = -pu;
+    for (int f = 0; f < F; ++f) {
+      const int kk = fkk[c * F + f];
+      if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
+      const int n = fns[c * F + f] + k;
+      const float pn = __fmaf_rn(mu, pold[n], S[n]);
+      y = __fmaf_rn(fz * fD[c * F + f] * a.cinv32[n], pn, y);
+    }
+    if (k > ctop) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
+    if (k < nk - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
+  } else {
+    y = 0.f;
+    for (int f = 0; f < F; ++f) {
+      const int kk = fkk[c * F + f];
+      if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
+      const int n = fns[c * F + f] + k;
+      const float pn = __fmaf_rn(mu, pold[n], S[n]);
+      y = __fmaf_rn(pn - pu, a.dzfD32[fes[c * F + f] + k], y);
+    }
+    const float c0 = sc[s];
+    if (ctop < nk - 1) {
+      if (k == ctop) {
+        const float c1 = sc[s + 1];
+        const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+        y += (-2.f * c0 - c1) * pu + c1 * pp;
+      } else if (k == nk - 1) {
+        const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
+        y += c0 * pm - c0 * pu;
+      } else {
+        const float c1 = sc[s + 1];
+        const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
+        const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+        y += c0 * pm - (c0 + c1) * pu + c1 * pp;
+      }
+    } else {
+      y -= 2.f * c0 * pu;
+    }
+  }
+  return y;
+}
+
+__device__ __forceinline__ int hcol_of(const unsigned short* start, int ncols, int s) {
+  int lo = 0, hi = ncols - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((int)start[mid] <= s) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// FP32 apply of the 4 CONSECUTIVE slots 4t..4t+3 of a staged tile owned by
+// thread t, compile-time face count.  Consecutive slots mostly lie in one
+// column: then the column lookup, the face metadata and the address
+// arithmetic are shared, own data comes as float4 from shared memory, the
+// neighbour gathers of the 4 levels are consecutive addresses, and the
+// results leave as float4 stores.  pu/y hold the slot values (0 at inactive
+// slots).
+template <int QP, int FF>
+__device__ __forceinline__ void apply_quad32(const BatchArgs& a, const unsigned char* hd, const HdrLayout& L,
+                                             int ncols, int len, int base, float mu, const float* sp, const float* sS,
+                                             const float* sc, const float* sf, const float* __restrict__ pold,
+                                             const float* __restrict__ S, float (&pu)[4], float (&y)[4]) {
+  const unsigned short* start = (const unsigned short*)(hd + L.o_start);
+  const int* cn = (const int*)(hd + L.o_cn);
+  const int* fns = (const int*)(hd + L.o_fns);
+  const int* fkk = (const int*)(hd + L.o_fkk);
+  const float* fD = (const float*)(hd + L.o_fD);
+  const int* fes = (const int*)(hd + L.o_fes);
+  const int s0 = 4 * (int)threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) pu[j] = y[j] = 0.f;
+  if (s0 >= len) return;
+  const float4 P4 = *(const float4*)(sp + s0);
+  const float4 R4 = *(const float4*)(sS + s0);
+  const float4 C4 = *(const float4*)(sc + s0);
+  const float Pv[4] = {P4.x, P4.y, P4.z, P4.w};
+  const float Rv[4] = {R4.x, R4.y, R4.z, R4.w};
+  const float Cv[5] = {C4.x, C4.y, C4.z, C4.w, sc[s0 + 4]};
+  float Zv[4] = {0.f, 0.f, 0.f, 0.f};
+  if (QP == 1) {
+    const float4 Z4 = *(const float4*)(sf + s0);
+    Zv[0] = Z4.x; Zv[1] = Z4.y; Zv[2] = Z4.z; Zv[3] = Z4.w;
+  }
+  // p_new at the 4 slots and their vertical neighbours below/above the group
+  float pw[6];
+  pw[0] = s0 > 0 ? __fmaf_rn(mu, sp[s0 - 1], sS[s0 - 1]) : 0.f;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) pw[j + 1] = __fmaf_rn(mu, Pv[j], Rv[j]);
+  pw[5] = (s0 + 4 < len) ? __fmaf_rn(mu, sp[s0 + 4], sS[s0 + 4]) : 0.f;
+  // columns of the 4 slots
+  int c = hcol_of(start, ncols, s0);
+  int cj[4], kj[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int s = s0 + j;
+    if (c + 1 < ncols && (int)start[c + 1] <= s) ++c;
+    cj[j] = c;
+    kj[j] = s - start[c];
+  }
+  bool onj[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int w = cn[cj[j]];
+    const int ctop = w & 0xffff, nk = w >> 16;
+    const bool on = (s0 + j < len) && kj[j] >= ctop;
+    onj[j] = on;
+    const float p = pw[j + 1];
+    float acc = (QP == 1) ? -p : 0.f;
+    if (on) {
+      if (QP == 1) {
+        if (kj[j] > ctop) acc = __fmaf_rn(Cv[j], pw[j], acc);
+        if (kj[j] < nk - 1) acc = __fmaf_rn(Cv[j + 1], pw[j + 2], acc);
+      } else {
+        const float c0 = Cv[j];
+        if (ctop < nk - 1) {
+          if (kj[j] == ctop) acc += (-2.f * c0 - Cv[j + 1]) * p + Cv[j + 1] * pw[j + 2];
+          else if (kj[j] == nk - 1) acc += c0 * pw[j] - c0 * p;
+          else acc += c0 * pw[j] - (c0 + Cv[j + 1]) * p + Cv[j + 1] * pw[j + 2];
+        } else {
+          acc -= 2.f * c0 * p;
+        }
+      }
+    }
+    pu[j] = on ? p : 0.f;
+    y[j] = acc;
+  }
+  // faces: gathers of the 4 levels (consecutive neighbour slots when the
+  // group lies in one column)
+#pragma unroll
+  for (int f = 0; f < FF; ++f) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int e = cj[j] * FF + f;
+      const int kk = fkk[e];
+      const bool ok = onj[j] && kj[j] >= (kk & 0xffff) && kj[j] < (kk >> 16);
+      const int n = ok ? fns[e] + kj[j] : base + s0 + j;
+      const float pn = __fmaf_rn(mu, pold[n], S[n]);
+      if (QP == 1) {
+        const float wgt = ok ? Zv[j] * fD[e] * a.cinv32[n] : 0.f;
+        y[j] = __fmaf_rn(wgt, pn, y[j]);
+      } else {
+        const float wgt = ok ? a.dzfD32[fes[e] + kj[j]] : 0.f;
+        y[j] = __fmaf_rn(pn - pw[j + 1], wgt, y[j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (!onj[j]) y[j] = 0.f;
+}
+
+// Branch-free FP32 apply of a thread's 4 slots of a staged tile with a
+// compile-time face count: every neighbour gather of the 4 slots is
+// independent of the others, so all of them are in flight together.  A face
+// that does not couple a level gathers the slot itself (a valid address) with
+// a zero weight.
+template <int QP, int FF>
+__device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned char* hd, const HdrLayout& L,
+                                             int ncols, int len, int base, float mu, const float* sp, const float* sS,
+                                             const float* sc, const float* sf, const float* __restrict__ pold,
+                                             const float* __restrict__ S, float (&yv)[kBTSlots / kCompute],
+                                             float (&pv)[kBTSlots / kCompute], bool (&on)[kBTSlots / kCompute]) {
+  constexpr int Q = kBTSlots / kCompute;
+  const unsigned short* start = (const unsigned short*)(hd + L.o_start);
+  const int* cn = (const int*)(hd + L.o_cn);
+  const int* fns = (const int*)(hd + L.o_fns);
+  const int* fkk = (const int*)(hd + L.o_fkk);
+  const float* fD = (const float*)(hd + L.o_fD);
+  const int* fes = (const int*)(hd + L.o_fes);
+  int cc[Q], kv[Q], ctop[Q], nk[Q], sv[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int s0 = threadIdx.x + q * kCompute;
+    const bool in = s0 < len;
+    const int s = in ? s0 : 0;
+    sv[q] = s;
+    cc[q] = hcol_of(start, ncols, s);
+    kv[q] = s - start[cc[q]];
+    const int w = cn[cc[q]];
+    ctop[q] = w & 0xffff;
+    nk[q] = w >> 16;
+    on[q] = in && kv[q] >= ctop[q];
+  }
+  // gathers
+  float pn[Q][FF], wn[Q][FF];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+#pragma unroll
+    for (int f = 0; f < FF; ++f) {
+      const int e = cc[q] * FF + f;
+      const int kk = fkk[e];
+      const bool ok = on[q] && kv[q] >= (kk & 0xffff) && kv[q] < (kk >> 16);
+      const int n = ok ? fns[e] + kv[q] : base + sv[q];
+      pn[q][f] = __fmaf_rn(mu, pold[n], S[n]);
+      if (QP == 1) {
+        wn[q][f] = ok ? fD[e] * a.cinv32[n] : 0.f;
+      } else {
+        const int es = ok ? fes[e] + kv[q] : 0;
+        wn[q][f] = ok ? a.dzfD32[es] : 0.f;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int s = sv[q], k = kv[q];
+    const float pu = __fmaf_rn(mu, sp[s], sS[s]);
+    pv[q] = pu;
+    float y;
+    if (QP == 1) {
+      const float fz = sf[s];
+      y = -pu;
+#pragma unroll
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(fz * wn[q][f], pn[q][f], y);
+      if (k > ctop[q]) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
+      if (k < nk[q] - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
+    } else {
+      y = 0.f;
+#pragma unroll
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(pn[q][f] - pu, wn[q][f], y);
+      const float c0 = sc[s];
+      if (ctop[q] < nk[q] - 1) {
+        if (k == ctop[q]) {
+          const float c1 = sc[s + 1];
+          const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+          y += (-2.f * c0 - c1) * pu + c1 * pp;
+        } else if (k == nk[q] - 1) {
+          const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
+          y += c0 * pm - c0 * pu;
+        } else {
+          const float c1 = sc[s + 1];
+          const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
+          const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+          y += c0 * pm - (c0 + c1) * pu + c1 * pp;
+        }
+      } else {
+        y -= 2.f * c0 * pu;
+      }
+    }
+    yv[q] = on[q] ? y : 0.f;
+  }
+}
+
+// One pipelined phase over the CTA's list.  PH 0: apply; PH 1: update.
+template <int QP, int PH, class Fin>
+__device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, double* s_red, int* s_flag,
+                                                long long lim, Fin&& fin) {
+  const int n = *P.count;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int err = 0;
+  if (warp == 8) {
+    // producer warp: lane 0 issues every fill of this phase in list order
+    if (lane == 0)
+      for (int j = 0; j < n; ++j) produce<QP, PH>(a, P, P.list[j], lim, &err);
+    P.seq = __shfl_sync(0xffffffffu, P.seq, 0);
+    err = __shfl_sync(0xffffffffu, err, 0);
+    if (lane == 0 && err) atomicCAS(&a.ctl->status, SGPU_OK, SGPU_TIMEOUT);
+    return;
+  }
+  constexpr int NV = (PH == 1 && QP == 2) ? 2 : 1;
+  DF dacc[NV];
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) df_zero(dacc[v]);
+  auto do_flush = [&](int inst, int ntl) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      acc[v] = df_value(dacc[v]);
+      df_zero(dacc[v]);
+    }
+    flush<NV>(a, inst, ntl, acc, s_red, s_flag, fin);
+  };
+  int cur = -1, cnt = 0;
+  float mu = 0.f, nu = 0.f;
+  for (int j = 0; j < n; ++j) {
+    const uint32_t q = P.seq;
+    const int b = q & 1;
+    if (!mbar_wait(&P.full[b], (q >> 1) & 1, lim)) err = 1;
+    unsigned char* st = P.stage[b];
+    const StageDesc sd = *stage_desc(st);
+    if (sd.inst != cur) {
+      if (cur >= 0) do_flush(cur, cnt);
+      cur = sd.inst;
+      cnt = 0;
+      const BInst& I = a.inst[cur];
+      mu = (float)(*(volatile double*)&I.mu);
+      nu = (float)(*(volatile double*)&I.nu);
+    }
+    const int len = sd.nslots;
+    const int base = sd.base;
+    constexpr int Q = kBTSlots / kCompute;
+    if (PH == 0) {
+      const unsigned char* hd = stage_hdr(st);
+      const int ncols = ((const int*)hd)[0];
+      const HdrLayout L = hdr_layout(ncols, a.F);
+      const unsigned short* start = (const unsigned short*)(hd + L.o_start);
+      const int* cn = (const int*)(hd + L.o_cn);
+      const float* sp = stage_stream(st, 0);
+      const float* sS = stage_stream(st, 1);
+      const float* sc = stage_stream(st, 2);
+      const float* sf = stage_stream(st, 3);
+      const float* pold = sd.par ? a.pb32 : a.pa32;
+      float* pnew = sd.par ? a.pa32 : a.pb32;
+      const float* S = (QP == 2) ? a.s32 : a.r32;
+      float yv[Q], pv[Q];
+      bool on[Q];
+      if (a.F == 3 || a.F == 4) {
+        float pu4[4], y4[4];
+        if (a.F == 3) apply_quad32<QP, 3>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, pu4, y4);
+        else apply_quad32<QP, 4>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, pu4, y4);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&P.empty[b]);
+        const int s0 = 4 * (int)threadIdx.x;
+        if (s0 < len) {
+          *(float4*)(a.z32 + base + s0) = make_float4(y4[0], y4[1], y4[2], y4[3]);
+          *(float4*)(pnew + base + s0) = make_float4(pu4[0], pu4[1], pu4[2], pu4[3]);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) df_addprod(dacc[0], pu4[j], y4[j]);
+        }
+        P.seq = q + 1;
+        ++cnt;
+        continue;
+      } else {
+#pragma unroll
+        for (int qq = 0; qq < Q; ++qq) {
+          const int s = threadIdx.x + qq * kCompute;
+          on[qq] = false;
+          yv[qq] = 0.f;
+          pv[qq] = 0.f;
+          if (s < len) {
+            const int c = hcol_of(start, ncols, s);
+            const int k = s - start[c];
+            const int ctop = cn[c] & 0xffff, nk = cn[c] >> 16;
+            if (k >= ctop) {
+              on[qq] = true;
+              yv[qq] = apply32<QP>(a, hd, L, c, s, k, ctop, nk, mu, sp, sS, sc, sf, pold, S, pv[qq]);
+            }
+          }
+        }
+      }
+      // the stage is no longer read: hand it back to the producer
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&P.empty[b]);
+#pragma unroll
+      for (int qq = 0; qq < Q; ++qq) {
+        if (!on[qq]) continue;
+        const int u = base + threadIdx.x + qq * kCompute;
+        a.z32[u] = yv[qq];
+        pnew[u] = pv[qq];
+        df_addprod(dacc[0], pv[qq], yv[qq]);
+      }
+    } else {
+      const float* sp = stage_stream(st, 0);
+      const float* sx = stage_stream(st, 1);
+      const float* sz = stage_stream(st, 2);
+      float* sr = stage_stream(st, 3);
+      {
+        // 4 consecutive slots per thread: float4 in shared memory and global
+        // (padding slots hold zeros in every stream and stay zero)
+        const int s0 = 4 * (int)threadIdx.x;
+        if (s0 < len) {
+          const float4 p4 = *(const float4*)(sp + s0);
+          const float4 x4 = *(const float4*)(sx + s0);
+          const float4 z4 = *(const float4*)(sz + s0);
+          const float4 r4 = *(const float4*)(sr + s0);
+          const float4 xo = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y), __fmaf_rn(nu, p4.z, x4.z),
+                                        __fmaf_rn(nu, p4.w, x4.w));
+          const float4 ro = make_float4(__fmaf_rn(-nu, z4.x, r4.x), __fmaf_rn(-nu, z4.y, r4.y),
+                                        __fmaf_rn(-nu, z4.z, r4.z), __fmaf_rn(-nu, z4.w, r4.w));
+          *(float4*)(a.x32 + base + s0) = xo;
+          *(float4*)(a.r32 + base + s0) = ro;
+          if (QP == 2) {
+            *(float4*)(sr + s0) = ro;
+          } else {
+            df_addprod(dacc[0], ro.x, ro.x);
+            df_addprod(dacc[0], ro.y, ro.y);
+            df_addprod(dacc[0], ro.z, ro.z);
+            df_addprod(dacc[0], ro.w, ro.w);
+          }
+        }
+      }
+      if (QP == 2) {
+        // Column tridiagonal solves entirely in shared memory: the p, x and z
+        // streams of the stage are no longer needed, so they are refilled
+        // (coalesced) with the Thomas factors tw, tib and the coefficients.
+        csync();
+        float* stw = stage_stream(st, 0);
+        float* stib = stage_stream(st, 1);
+        float* scf = stage_stream(st, 2);
+        const int n4 = (len + 3) & ~3;
+        for (int s = threadIdx.x; s < n4 + 4; s += kCompute) {
+          if (s < n4) {
+            stw[s] = a.tw32[base + s];
+            stib[s] = a.tib32[base + s];
+          }
+          scf[s] = a.coef32[base + s];
+        }
+        csync();
+        const unsigned char* hd = stage_hdr(st);
+        const int ncols = ((const int*)hd)[0];
+        const HdrLayout L = hdr_layout(ncols, a.F);
+        const unsigned short* start = (const unsigned short*)(hd + L.o_start);
+        const int* cn = (const int*)(hd + L.o_cn);
+        for (int c = threadIdx.x; c < ncols; c += kCompute) {
+          const int ctop = cn[c] & 0xffff, nk = cn[c] >> 16;
+          const int b0 = start[c] + ctop, e0 = start[c] + nk;
+          if (ctop == nk - 1) {
+            stib[b0] = -0.5f * sr[b0] / scf[b0];
+            continue;
+          }
+          // forward sweep: d'[k] = r[k] - w[k] d'[k-1], stored over w
+          float d = sr[b0];
+          stw[b0] = d;
+          for (int s = b0 + 1; s < e0; ++s) {
+            d = __fmaf_rn(-stw[s], d, sr[s]);
+            stw[s] = d;
+          }
+          // backward sweep: u[k] = (d'[k] - coef[k+1] u[k+1]) / b'[k], stored over 1/b'
+          float un = stw[e0 - 1] * stib[e0 - 1];
+          stib[e0 - 1] = un;
+          for (int s = e0 - 2; s >= b0; --s) {
+            un = __fmaf_rn(-scf[s + 1], un, stw[s]) * stib[s];
+            stib[s] = un;
+          }
+        }
+        csync();
+        // M^-1 r now in stib at wet levels; dry levels hold 0 in s32
+        for (int s = threadIdx.x; s < len; s += kCompute) {
+          const int c = hcol_of(start, ncols, s);
+          const int k = s - start[c];
+          const float sv = (k >= (cn[c] & 0xffff)) ? stib[s] : 0.f;
+          a.s32[base + s] = sv;
+          const float r = sr[s];
+          df_addprod(dacc[0], r, sv);
+          df_addprod(dacc[NV - 1], r, r);
+        }
+        csync();
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&P.empty[b]);
+    }
+    P.seq = q + 1;
+    ++cnt;
+  }
+  if (cur >= 0) do_flush(cur, cnt);
+  if (err && threadIdx.x == 0) atomicCAS(&a.ctl->status, SGPU_OK, SGPU_TIMEOUT);
+}
+
+// ---------------------------------------------------------------------------
 // the persistent kernel
 // ---------------------------------------------------------------------------
+#ifndef SGPU_BATCH_MINB
+#define SGPU_BATCH_MINB 3
+#endif
 template <int QP>
-__global__ void __launch_bounds__(kBlock) batch_kernel(BatchArgs a, int do_setup) {
-  __shared__ int s_start[kTileCap + 1];
-  __shared__ int s_ctop[kTileCap];
-  __shared__ int s_nk[kTileCap];
-  __shared__ double s_red[4 * (kBlock / 32)];
-  const int G = gridDim.x, tid = threadIdx.x, F = a.F;
+__global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchArgs a, int do_setup) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  __shared__ double s_red[4 * 8];
+  __shared__ int s_flag;
+  __shared__ int s_count;
+  __shared__ int s_wsum[8];
+  const int tid = threadIdx.x, F = a.F;
+  const bool compute = tid < kCompute;
   SolveCtl* ctl = a.ctl;
+  const long long lim = ctl->timeout_ns;
+
+  Pipe P;
+  P.stage[0] = dyn;
+  P.stage[1] = dyn + kBufBytes;
+  P.full = (uint64_t*)(dyn + 2 * kBufBytes);
+  P.empty = P.full + 2;
+  P.list = (int*)(dyn + 2 * kBufBytes + 32);
+  P.count = &s_count;
+  P.seq = 0;
+  if (tid == 0) {
+    mbar_init(&P.full[0], 1);
+    mbar_init(&P.full[1], 1);
+    mbar_init(&P.empty[0], 8);
+    mbar_init(&P.empty[1], 8);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  TileSmem& sm = *(TileSmem*)P.stage[0];  // simple phases reuse stage 0 (no copies in flight then)
 
   // ======================= setup of new instances =======================
   if (do_setup) {
-    // S1: FP32 copies, conditioner, unscaled coefficients, zero vectors
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int i = a.tile_inst[t];
-      if (inst_state(a, i) != INST_SETUP) continue;
-      TileInfo ti;
-      load_tile(a, t, ti, s_start, s_ctop, s_nk);
-      const int ncols = ti.c1 - ti.c0;
-      const int len = ti.end - ti.base;
-      for (int s = tid; s < len; s += kBlock) {
-        const int cl = find_col_b(s_start, ncols, s);
-        const int j = ti.c0 + cl;
-        const int k = s - s_start[cl];
-        const int u = ti.base + s;
-        const int ctop = s_ctop[cl], nk = s_nk[cl];
-        const bool act = k >= ctop;
-        const double dz = a.dzz64[u];
-        const double Ac = a.colAc[j];
-        a.dzz32[u] = (float)dz;
-        a.r32[u] = 0.f;
-        a.pa32[u] = 0.f;
-        a.pb32[u] = 0.f;
-        a.x32[u] = 0.f;
-        a.z32[u] = 0.f;
-        if (QP == 2) a.s32[u] = 0.f;
-        if (QP == 1) {
-          double c = 1.0;
-          if (act) {
-            double diag = 0.0;
-            for (int f = 0; f < F; ++f) {
-              const BFace fc = a.face[(size_t)j * F + f];
-              if (fc.ns < 0 || k < fc.kmin || k >= fc.kmax) continue;
-              diag += dz * fc.D64;
-            }
-            const double ak = (k == ctop) ? Ac / dz : 2 * Ac / (dz + a.dzz64[u - 1]);
-            if (ctop < nk - 1) {
-              if (k == ctop) diag += 2 * ak + 2 * Ac / (a.dzz64[u + 1] + dz);
-              else if (k == nk - 1) diag += ak;
-              else diag += ak + 2 * Ac / (a.dzz64[u + 1] + dz);
-            }
-            if (diag <= 0) diag = 1;
-            c = sqrt(diag);
-          }
-          a.c64[u] = c;
-          a.cinv32[u] = (float)(1.0 / c);
-          a.x64[u] = act ? a.q64[u] * c : 0.0;
-          a.b64[u] = act ? a.src64[u] / c : 0.0;
-        } else {
-          double cf = 0.0;
-          if (k == ctop) cf = Ac / dz;
-          else if (k > ctop) cf = 2 * Ac / (dz + a.dzz64[u - 1]);
-          a.coef64[u] = cf;
-          a.coef32[u] = (float)cf;
-          a.x64[u] = act ? a.q64[u] : 0.0;
-          a.b64[u] = act ? a.src64[u] : 0.0;
-        }
-      }
-      if (QP == 2) {
-        __syncthreads();
-        for (int c = tid; c < ncols; c += kBlock) column_factor64(a, ti.base + s_start[c], s_ctop[c], s_nk[c]);
-      }
-      __syncthreads();
-    }
-    // boundary (non-computational) slots of new instances: fixed values
-    for (int i = 0; i < a.ninst; ++i) {
-      const BInst& I = a.inst[i];
-      if (ld_volatile_int(&I.state) != INST_SETUP) continue;
-      for (int u = I.s1 + blockIdx.x * kBlock + tid; u < I.s2; u += G * kBlock) {
-        a.x64[u] = a.q64[u];
-        a.b64[u] = 0.0;
-        a.r32[u] = 0.f;
-        a.pa32[u] = 0.f;
-        a.pb32[u] = 0.f;
-        if (QP == 2) a.s32[u] = 0.f;
-        if (QP == 1) {
-          a.c64[u] = a.cin64[u];
-          a.cinv32[u] = (float)(1.0 / a.cin64[u]);
-        }
-      }
-    }
-    if (!grid_sync(ctl, 11, [] {})) return;
-
-    // S2 (qprecond 1): FP64 scaled coefficients (QCoefficients 3427-3452)
-    if (QP == 1) {
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        const int i = a.tile_inst[t];
-        if (inst_state(a, i) != INST_SETUP) continue;
+    auto is_setup = [&](int i) { return inst_state(a, i) == INST_SETUP; };
+    if (compute) {
+      // S1: conditioner / unscaled coefficients, FP32 copies, zero vectors
+      for_tiles(a, is_setup, [&](int t, int i) {
         TileInfo ti;
-        load_tile(a, t, ti, s_start, s_ctop, s_nk);
-        const int ncols = ti.c1 - ti.c0;
+        load_tile(a, t, ti, sm);
         const int len = ti.end - ti.base;
-        for (int s = tid; s < len; s += kBlock) {
-          const int cl = find_col_b(s_start, ncols, s);
-          const int j = ti.c0 + cl;
-          const int k = s - s_start[cl];
+        for (int s = tid; s < len; s += kCompute) {
+          const int c = col_of(sm.start, sm.ncols, s);
+          const int k = s - sm.start[c];
           const int u = ti.base + s;
-          const int ctop = s_ctop[cl];
-          const double Ac = a.colAc[j];
+          const int ctop = sm.ctop[c], nk = sm.nk[c];
+          const bool act = k >= ctop;
           const double dz = a.dzz64[u];
-          const double cu = a.c64[u];
-          double cf = 0.0;
-          if (k == ctop) cf = Ac / dz / cu;
-          else if (k > ctop) cf = 2 * Ac / (dz + a.dzz64[u - 1]) / (cu * a.c64[u - 1]);
-          a.coef64[u] = cf;
-          for (int f = 0; f < F; ++f) {
-            const BFace fc = a.face[(size_t)j * F + f];
-            double v = 0.0;
-            if (fc.ns >= 0 && k >= ctop && k >= fc.kmin && k < fc.kmax) v = dz * fc.D64 / (cu * a.c64[fc.ns + k]);
-            a.fc64[(size_t)F * u + f] = v;
+          const double Ac = a.colAc[ti.c0 + c];
+          a.r32[u] = 0.f;
+          a.pa32[u] = 0.f;
+          a.pb32[u] = 0.f;
+          a.x32[u] = 0.f;
+          a.z32[u] = 0.f;
+          if (QP == 2) a.s32[u] = 0.f;
+          if (QP == 1) {
+            double cc = 1.0;
+            if (act) {
+              double diag = 0.0;
+              for (int f = 0; f < F; ++f) {
+                const int kk = sm.fkk[c * F + f];
+                if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
+                diag += dz * a.face[(size_t)(ti.c0 + c) * F + f].D64;
+              }
+              const double ak = (k == ctop) ? Ac / dz : 2 * Ac / (dz + a.dzz64[u - 1]);
+              if (ctop < nk - 1) {
+                if (k == ctop) diag += 2 * ak + 2 * Ac / (a.dzz64[u + 1] + dz);
+                else if (k == nk - 1) diag += ak;
+                else diag += ak + 2 * Ac / (a.dzz64[u + 1] + dz);
+              }
+              if (diag <= 0) diag = 1;
+              cc = sqrt(diag);
+            }
+            a.c64[u] = cc;
+            a.cinv32[u] = (float)(1.0 / cc);
+            a.fz32[u] = (float)(dz / cc);
+            a.x64[u] = act ? a.q64[u] * cc : 0.0;
+            a.b64[u] = act ? a.src64[u] / cc : 0.0;
+          } else {
+            double cf = 0.0;
+            if (k == ctop) cf = Ac / dz;
+            else if (k > ctop) cf = 2 * Ac / (dz + a.dzz64[u - 1]);
+            a.coef64[u] = cf;
+            a.coef32[u] = (float)cf;
+            a.x64[u] = act ? a.q64[u] : 0.0;
+            a.b64[u] = act ? a.src64[u] : 0.0;
           }
         }
-        __syncthreads();
+        if (QP == 2) {
+          csync();
+          for (int c = tid; c < ti.c1 - ti.c0; c += kCompute)
+            column_factor64(a, ti.base + sm.start[c], sm.ctop[c], sm.nk[c]);
+        }
+        csync();
+      });
+      // boundary (non-computational) slots of new instances: fixed values
+      for (int i = 0; i < a.ninst; ++i) {
+        const BInst& I = a.inst[i];
+        if (ld_volatile_int(&I.state) != INST_SETUP) continue;
+        for (int u = I.s1 + blockIdx.x * kCompute + tid; u < I.s2; u += gridDim.x * kCompute) {
+          a.x64[u] = a.q64[u];
+          a.b64[u] = 0.0;
+          a.r32[u] = 0.f;
+          a.pa32[u] = 0.f;
+          a.pb32[u] = 0.f;
+          if (QP == 2) a.s32[u] = 0.f;
+          if (QP == 1) {
+            a.c64[u] = a.cin64[u];
+            a.cinv32[u] = (float)(1.0 / a.cin64[u]);
+          }
+        }
       }
-      if (!grid_sync(ctl, 12, [] {})) return;
+    }
+    if (!grid_sync(ctl, 5, [] {})) return;
+
+    // S2 (qprecond 1): FP64 scaled coefficients (QCoefficients 3427-3452) and
+    // their FP32 vertical copy
+    if (QP == 1) {
+      if (compute)
+        for_tiles(a, is_setup, [&](int t, int i) {
+          TileInfo ti;
+          load_tile(a, t, ti, sm);
+          const int len = ti.end - ti.base;
+          for (int s = tid; s < len; s += kCompute) {
+            const int c = col_of(sm.start, sm.ncols, s);
+            const int k = s - sm.start[c];
+            const int u = ti.base + s;
+            const int ctop = sm.ctop[c];
+            const double Ac = a.colAc[ti.c0 + c];
+            const double dz = a.dzz64[u];
+            const double cu = a.c64[u];
+            double cf = 0.0;
+            if (k == ctop) cf = Ac / dz / cu;
+            else if (k > ctop) cf = 2 * Ac / (dz + a.dzz64[u - 1]) / (cu * a.c64[u - 1]);
+            a.coef64[u] = cf;
+            a.coef32[u] = (float)cf;
+            for (int f = 0; f < F; ++f) {
+              const int kk = sm.fkk[c * F + f];
+              double v = 0.0;
+              if (k >= ctop && k >= (kk & 0xffff) && k < (kk >> 16))
+                v = dz * a.face[(size_t)(ti.c0 + c) * F + f].D64 / (cu * a.c64[sm.fns[c * F + f] + k]);
+              a.fc64[(size_t)F * u + f] = v;
+            }
+          }
+          csync();
+        });
+      if (!grid_sync(ctl, 6, [] {})) return;
     }
 
     // S3: initial FP64 residual, first preconditioned residual, alpha0, eps0
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int i = a.tile_inst[t];
-      if (inst_state(a, i) != INST_SETUP) continue;
-      TileInfo ti;
-      load_tile(a, t, ti, s_start, s_ctop, s_nk);
-      const int ncols = ti.c1 - ti.c0;
-      const int len = ti.end - ti.base;
-      double part[2] = {0.0, 0.0};
-      for (int s = tid; s < len; s += kBlock) {
-        const int cl = find_col_b(s_start, ncols, s);
-        const int j = ti.c0 + cl;
-        const int k = s - s_start[cl];
-        const int u = ti.base + s;
-        const int ctop = s_ctop[cl], nk = s_nk[cl];
-        if (k < ctop) continue;
-        const double r = a.b64[u] - apply64<QP>(a, u, j, k, ctop, nk, a.x64);
-        const float rf = (float)r;
-        a.r32[u] = rf;
-        if (QP == 2) part[1] += r * r;
-        else part[0] += f2d(rf) * f2d(rf);
-      }
-      if (QP == 2) {
-        __syncthreads();
-        for (int c = tid; c < ncols; c += kBlock) column_solve32(a, ti.base + s_start[c], s_ctop[c], s_nk[c]);
-        __syncthreads();
-        for (int u = ti.base + tid; u < ti.end; u += kBlock) part[0] += f2d(a.r32[u]) * f2d(a.s32[u]);
-      }
-      block_sum<2>(part, s_red);
-      tile_done<2>(a, t, i, part, s_red, [&](BInst* I, const double* tot) {
-        double alpha = tot[0], alpha0 = tot[0];
-        if (!I->resnorm) alpha0 = 1;
-        const double eps0 = (QP == 2) ? tot[1] : alpha0;
-        I->alpha = alpha;
-        I->eps0 = eps0;
-        I->eps = eps0;
-        I->eps_ref = eps0;
-        I->mu = 0.0;
-        I->nu = 0.0;
-        I->n = 0;
-        I->nrel = 0;
-        I->flags = 0;
-        I->par = 0;
-        I->status = SGPU_OK;
-        I->state = (I->maxiters <= 0 || eps0 == 0) ? INST_DONE : INST_RUN;
-      });
-    }
-    if (!grid_sync(ctl, 13, [&] {
+    if (compute)
+      for_tiles_reduce<2>(a, s_red, &s_flag, is_setup,
+          [&](int t, int i, double (&acc)[2]) {
+            TileInfo ti;
+            load_tile(a, t, ti, sm);
+            const int len = ti.end - ti.base;
+            for (int s = tid; s < len; s += kCompute) {
+              const int c = col_of(sm.start, sm.ncols, s);
+              const int k = s - sm.start[c];
+              const int u = ti.base + s;
+              const int ctop = sm.ctop[c], nk = sm.nk[c];
+              if (k < ctop) continue;
+              const double r = a.b64[u] - apply64<QP>(a, sm, c, u, k, ctop, nk, a.x64);
+              const float rf = (float)r;
+              a.r32[u] = rf;
+              if (QP == 2) acc[1] += r * r;
+              else acc[0] += f2d(rf) * f2d(rf);
+            }
+            if (QP == 2) {
+              csync();
+              for (int c = tid; c < ti.c1 - ti.c0; c += kCompute)
+                column_solve32(a, a.r32, 0, ti.base + sm.start[c], sm.ctop[c], sm.nk[c]);
+              csync();
+              for (int u = ti.base + tid; u < ti.end; u += kCompute) acc[0] += f2d(a.r32[u]) * f2d(a.s32[u]);
+            }
+            csync();
+          },
+          [&](BInst* I, const double* tot) {
+            double alpha0 = tot[0];
+            if (!I->resnorm) alpha0 = 1;
+            const double eps0 = (QP == 2) ? tot[1] : alpha0;
+            I->alpha = tot[0];
+            I->eps0 = eps0;
+            I->eps = eps0;
+            I->eps_ref = eps0;
+            I->mu = 0.0;
+            I->nu = 0.0;
+            I->n = 0;
+            I->nrel = 0;
+            I->flags = 0;
+            I->par = 0;
+            I->status = SGPU_OK;
+            I->state = (I->maxiters <= 0 || eps0 == 0) ? INST_DONE : INST_RUN;
+          });
+    if (!grid_sync(ctl, 7, [&] {
           if (tid == 0) {
             int any = 0;
             for (int i = 0; i < a.ninst; ++i) any |= (a.inst[i].state == INST_RUN);
@@ -393,168 +1143,59 @@ __global__ void __launch_bounds__(kBlock) batch_kernel(BatchArgs a, int do_setup
   }
 
   // ============================ iterations ==============================
+  auto is_run = [&](int i) { return inst_state(a, i) == INST_RUN; };
   for (int it = 0; it < a.max_iters_chunk; ++it) {
     if (!ld_volatile_int(&a.gflags[3])) break;
 
-    // ---- A: p_new = s + mu p_old (on the fly), z = A p_new, p.z ----
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int i = a.tile_inst[t];
-      if (inst_state(a, i) != INST_RUN) continue;
-      TileInfo ti;
-      load_tile(a, t, ti, s_start, s_ctop, s_nk);
-      const BInst& I = a.inst[i];
-      const float mu = (float)(*(volatile double*)&I.mu);
-      const int par = ld_volatile_int(&I.par);
-      const float* pold = par ? a.pb32 : a.pa32;
-      float* pnew = par ? a.pa32 : a.pb32;
-      const float* S = (QP == 2) ? a.s32 : a.r32;
-      const int ncols = ti.c1 - ti.c0;
-      const int len = ti.end - ti.base;
-      double part[1] = {0.0};
-      for (int s = tid; s < len; s += kBlock) {
-        const int cl = find_col_b(s_start, ncols, s);
-        const int j = ti.c0 + cl;
-        const int k = s - s_start[cl];
-        const int u = ti.base + s;
-        const int ctop = s_ctop[cl], nk = s_nk[cl];
-        if (k < ctop) continue;
-        const float pu = __fmaf_rn(mu, pold[u], S[u]);
-        float y;
-        if (QP == 1) {
-          const float dz = a.dzz32[u], cu = a.cinv32[u];
-          const float Ac = (float)a.colAc[j];
-          y = -pu;
-          for (int f = 0; f < F; ++f) {
-            const BFace fc = a.face[(size_t)j * F + f];
-            if (fc.ns < 0 || k < fc.kmin || k >= fc.kmax) continue;
-            const int n = fc.ns + k;
-            const float pn = __fmaf_rn(mu, pold[n], S[n]);
-            y = __fmaf_rn(dz * fc.D * cu * a.cinv32[n], pn, y);
-          }
-          if (k > ctop) {
-            const float pm = __fmaf_rn(mu, pold[u - 1], S[u - 1]);
-            const float cf = (2.f * Ac / (dz + a.dzz32[u - 1])) * (cu * a.cinv32[u - 1]);
-            y = __fmaf_rn(cf, pm, y);
-          }
-          if (k < nk - 1) {
-            const float pp = __fmaf_rn(mu, pold[u + 1], S[u + 1]);
-            const float cf = (2.f * Ac / (a.dzz32[u + 1] + dz)) * (a.cinv32[u + 1] * cu);
-            y = __fmaf_rn(cf, pp, y);
-          }
-        } else {
-          y = 0.f;
-          for (int f = 0; f < F; ++f) {
-            const BFace fc = a.face[(size_t)j * F + f];
-            if (fc.ns < 0 || k < fc.kmin || k >= fc.kmax) continue;
-            const int n = fc.ns + k;
-            const float pn = __fmaf_rn(mu, pold[n], S[n]);
-            y = __fmaf_rn(pn - pu, a.dzfD32[fc.es + k], y);
-          }
-          if (ctop < nk - 1) {
-            const float c0 = a.coef32[u];
-            if (k == ctop) {
-              const float c1 = a.coef32[u + 1];
-              const float pp = __fmaf_rn(mu, pold[u + 1], S[u + 1]);
-              y += (-2.f * c0 - c1) * pu + c1 * pp;
-            } else if (k == nk - 1) {
-              const float pm = __fmaf_rn(mu, pold[u - 1], S[u - 1]);
-              y += c0 * pm - c0 * pu;
-            } else {
-              const float c1 = a.coef32[u + 1];
-              const float pm = __fmaf_rn(mu, pold[u - 1], S[u - 1]);
-              const float pp = __fmaf_rn(mu, pold[u + 1], S[u + 1]);
-              y += c0 * pm - (c0 + c1) * pu + c1 * pp;
-            }
-          } else {
-            y -= 2.f * a.coef32[u] * pu;
-          }
-        }
-        a.z32[u] = y;
-        pnew[u] = pu;
-        part[0] += f2d(pu) * f2d(y);
+    // ---- A: p_new = S + mu p_old (on the fly), z = A p_new, p.z ----
+    build_list(a, P, is_run, s_wsum);
+    pipelined_phase<QP, 0>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
+      const double alpha = In->alpha;
+      In->alpha_prev = alpha;
+      In->mu = 1 / alpha;  // mu = 1/alpha before nu (2484-2485)
+      const double nu = alpha / tot[0];
+      In->nu = nu;
+      In->par ^= 1;
+      if (!isfinite(nu)) {
+        In->status = SGPU_BREAKDOWN;
+        In->flags = 2;  // final merge
+        In->state = INST_DONE;
+        atomicOr(&a.gflags[0], 1);
       }
-      block_sum<1>(part, s_red);
-      tile_done<1>(a, t, i, part, s_red, [&](BInst* In, const double* tot) {
-        const double alpha = In->alpha;
-        In->alpha_prev = alpha;
-        In->mu = 1 / alpha;  // mu = 1/alpha before nu (2484-2485)
-        const double nu = alpha / tot[0];
-        In->nu = nu;
-        In->par ^= 1;
-        if (!isfinite(nu)) {
-          In->status = SGPU_BREAKDOWN;
-          In->flags = 2;  // final merge
-          In->state = INST_DONE;
-          atomicOr(&a.gflags[0], 1);
-        }
-      });
-    }
-    if (!grid_sync(ctl, 21, [] {})) return;
+    });
+    if (!grid_sync(ctl, 1, [] {})) return;
 
     // ---- B: x32 += nu p, r -= nu z, preconditioner, r.s, r.r ----
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int i = a.tile_inst[t];
-      if (inst_state(a, i) != INST_RUN) continue;
-      TileInfo ti;
-      const BInst& I = a.inst[i];
-      const float nu = (float)(*(volatile double*)&I.nu);
-      const float* p = ld_volatile_int(&I.par) ? a.pb32 : a.pa32;
-      double part[2] = {0.0, 0.0};
-      if (QP == 2) {
-        load_tile(a, t, ti, s_start, s_ctop, s_nk);
-      } else {
-        ti.base = a.col[a.tile_c0[2 * t]].s;
-        const BCol cl = a.col[a.tile_c0[2 * t + 1] - 1];
-        ti.end = cl.s + cl.nk;
+    build_list(a, P, is_run, s_wsum);
+    pipelined_phase<QP, 1>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
+      const double alpha = tot[0];
+      const double mu = In->mu * alpha;  // mu *= alpha (2498/2509)
+      In->mu = mu;
+      In->alpha = alpha;
+      const double eps = (QP == 2) ? tot[1] : alpha;
+      In->eps = eps;
+      const int n = In->n + 1;
+      In->n = n;
+      int flags = 0;
+      if (!isfinite(alpha) || !isfinite(mu)) {
+        In->status = SGPU_BREAKDOWN;
+        In->state = INST_DONE;
+        flags = 2;
+      } else if (eps == 0) {
+        In->state = INST_DONE;
+        flags = 2;
+      } else if (eps < In->tol2 * In->eps0 || eps < a.delta2 * In->eps_ref) {
+        flags = 1;  // verify / refresh with the FP64 true residual
+      } else if (n >= In->maxiters) {
+        In->status = SGPU_MAXITER;
+        In->state = INST_DONE;
+        flags = 2;
       }
-      for (int u = ti.base + tid; u < ti.end; u += kBlock) {
-        a.x32[u] = __fmaf_rn(nu, p[u], a.x32[u]);
-        const float r = __fmaf_rn(-nu, a.z32[u], a.r32[u]);
-        a.r32[u] = r;
-        if (QP != 2) part[0] += f2d(r) * f2d(r);
-      }
-      if (QP == 2) {
-        __syncthreads();
-        const int ncols = a.tile_c0[2 * t + 1] - a.tile_c0[2 * t];
-        for (int c = tid; c < ncols; c += kBlock) column_solve32(a, ti.base + s_start[c], s_ctop[c], s_nk[c]);
-        __syncthreads();
-        for (int u = ti.base + tid; u < ti.end; u += kBlock) {
-          const float r = a.r32[u];
-          part[0] += f2d(r) * f2d(a.s32[u]);
-          part[1] += f2d(r) * f2d(r);
-        }
-      }
-      block_sum<2>(part, s_red);
-      tile_done<2>(a, t, i, part, s_red, [&](BInst* In, const double* tot) {
-        const double alpha = tot[0];
-        const double mu = In->mu * alpha;  // mu *= alpha (2498/2509)
-        In->mu = mu;
-        In->alpha = alpha;
-        const double eps = (QP == 2) ? tot[1] : alpha;
-        In->eps = eps;
-        const int n = In->n + 1;
-        In->n = n;
-        int flags = 0;
-        if (!isfinite(alpha) || !isfinite(mu)) {
-          In->status = SGPU_BREAKDOWN;
-          In->state = INST_DONE;
-          flags = 2;
-        } else if (eps == 0) {
-          In->state = INST_DONE;
-          flags = 2;
-        } else if (eps < In->tol2 * In->eps0 || eps < a.delta2 * In->eps_ref) {
-          flags = 1;  // verify / refresh with the FP64 true residual
-        } else if (n >= In->maxiters) {
-          In->status = SGPU_MAXITER;
-          In->state = INST_DONE;
-          flags = 2;
-        }
-        if (flags == 1 && n >= In->maxiters) flags = 1 | 4;  // last chance: verify, else stop
-        In->flags = flags;
-        if (flags) atomicOr(&a.gflags[0], 1);
-      });
-    }
-    if (!grid_sync(ctl, 22, [&] {
+      if (flags == 1 && n >= In->maxiters) flags = 1 | 4;  // last chance: verify, else stop
+      In->flags = flags;
+      if (flags) atomicOr(&a.gflags[0], 1);
+    });
+    if (!grid_sync(ctl, 2, [&] {
           if (tid == 0) {
             a.gflags[2] = a.gflags[0];
             a.gflags[0] = 0;
@@ -564,74 +1205,67 @@ __global__ void __launch_bounds__(kBlock) batch_kernel(BatchArgs a, int do_setup
       return;
 
     if (ld_volatile_int(&a.gflags[2])) {
+      auto flagged = [&](int i) { return inst_flags(a, i) != 0; };
       // ---- R1: x64 += x32, x32 = 0 for flagged instances ----
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        const int i = a.tile_inst[t];
-        if (!inst_flags(a, i)) continue;
-        const int base = a.col[a.tile_c0[2 * t]].s;
-        const BCol cl = a.col[a.tile_c0[2 * t + 1] - 1];
-        const int end = cl.s + cl.nk;
-        for (int u = base + tid; u < end; u += kBlock) {
-          a.x64[u] += f2d(a.x32[u]);
-          a.x32[u] = 0.f;
-        }
-      }
-      if (!grid_sync(ctl, 23, [] {})) return;
-      // ---- R2: FP64 true residual for instances that verify / refresh ----
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        const int i = a.tile_inst[t];
-        const int fl = inst_flags(a, i);
-        if (!fl) continue;
-        if (!(fl & 1)) {
-          // final merge only: finish the tile count so the flags get cleared
-          double part[2] = {0.0, 0.0};
-          tile_done<2>(a, t, i, part, s_red, [&](BInst* In, const double*) { In->flags = 0; });
-          continue;
-        }
-        TileInfo ti;
-        load_tile(a, t, ti, s_start, s_ctop, s_nk);
-        const int ncols = ti.c1 - ti.c0;
-        const int len = ti.end - ti.base;
-        double part[2] = {0.0, 0.0};
-        for (int s = tid; s < len; s += kBlock) {
-          const int cl = find_col_b(s_start, ncols, s);
-          const int j = ti.c0 + cl;
-          const int k = s - s_start[cl];
-          const int u = ti.base + s;
-          const int ctop = s_ctop[cl], nk = s_nk[cl];
-          if (k < ctop) continue;
-          const double r = a.b64[u] - apply64<QP>(a, u, j, k, ctop, nk, a.x64);
-          const float rf = (float)r;
-          a.r32[u] = rf;
-          if (QP == 2) part[1] += r * r;
-          else part[0] += r * r;
-        }
-        if (QP == 2) {
-          __syncthreads();
-          for (int c = tid; c < ncols; c += kBlock) column_solve32(a, ti.base + s_start[c], s_ctop[c], s_nk[c]);
-          __syncthreads();
-          for (int u = ti.base + tid; u < ti.end; u += kBlock) part[0] += f2d(a.r32[u]) * f2d(a.s32[u]);
-        }
-        block_sum<2>(part, s_red);
-        tile_done<2>(a, t, i, part, s_red, [&](BInst* In, const double* tot) {
-          const double alpha = tot[0];
-          const double eps = (QP == 2) ? tot[1] : alpha;
-          In->nrel += 1;
-          In->eps = eps;
-          In->eps_ref = eps;
-          if (eps < In->tol2 * In->eps0 || eps == 0) {
-            In->state = INST_DONE;
-          } else if (In->flags & 4) {
-            In->status = SGPU_MAXITER;
-            In->state = INST_DONE;
-          } else {
-            In->mu = alpha / In->alpha_prev;  // beta from the true residual
-            In->alpha = alpha;
+      if (compute)
+        for_tiles(a, flagged, [&](int t, int i) {
+          const TileDesc d = a.tiles[t];
+          for (int u = d.base + tid; u < d.base + d.nslots; u += kCompute) {
+            a.x64[u] += f2d(a.x32[u]);
+            a.x32[u] = 0.f;
           }
-          In->flags = 0;
         });
-      }
-      if (!grid_sync(ctl, 24, [&] {
+      if (!grid_sync(ctl, 3, [] {})) return;
+      // ---- R2: FP64 true residual for instances that verify / refresh ----
+      if (compute)
+        for_tiles_reduce<2>(a, s_red, &s_flag, flagged,
+            [&](int t, int i, double (&acc)[2]) {
+              if (!(inst_flags(a, i) & 1)) return;  // final merge only: counted, nothing to compute
+              TileInfo ti;
+              load_tile(a, t, ti, sm);
+              const int len = ti.end - ti.base;
+              for (int s = tid; s < len; s += kCompute) {
+                const int c = col_of(sm.start, sm.ncols, s);
+                const int k = s - sm.start[c];
+                const int u = ti.base + s;
+                const int ctop = sm.ctop[c], nk = sm.nk[c];
+                if (k < ctop) continue;
+                const double r = a.b64[u] - apply64<QP>(a, sm, c, u, k, ctop, nk, a.x64);
+                a.r32[u] = (float)r;
+                if (QP == 2) acc[1] += r * r;
+                else acc[0] += r * r;
+              }
+              if (QP == 2) {
+                csync();
+                for (int c = tid; c < ti.c1 - ti.c0; c += kCompute)
+                  column_solve32(a, a.r32, 0, ti.base + sm.start[c], sm.ctop[c], sm.nk[c]);
+                csync();
+                for (int u = ti.base + tid; u < ti.end; u += kCompute) acc[0] += f2d(a.r32[u]) * f2d(a.s32[u]);
+              }
+              csync();
+            },
+            [&](BInst* In, const double* tot) {
+              if (!(In->flags & 1)) {
+                In->flags = 0;
+                return;
+              }
+              const double alpha = tot[0];
+              const double eps = (QP == 2) ? tot[1] : alpha;
+              In->nrel += 1;
+              In->eps = eps;
+              In->eps_ref = eps;
+              if (eps < In->tol2 * In->eps0 || eps == 0) {
+                In->state = INST_DONE;
+              } else if (In->flags & 4) {
+                In->status = SGPU_MAXITER;
+                In->state = INST_DONE;
+              } else {
+                In->mu = alpha / In->alpha_prev;  // beta from the true residual
+                In->alpha = alpha;
+              }
+              In->flags = 0;
+            });
+      if (!grid_sync(ctl, 4, [&] {
             if (tid == 0) {
               int any = 0;
               for (int i = 0; i < a.ninst; ++i) any |= (a.inst[i].state == INST_RUN);
@@ -644,6 +1278,9 @@ __global__ void __launch_bounds__(kBlock) batch_kernel(BatchArgs a, int do_setup
   }
 }
 
+}  // namespace sgpu
+
+namespace sgpu {
 // ---------------------------------------------------------------------------
 // host side: the batch engine
 // ---------------------------------------------------------------------------
@@ -651,16 +1288,18 @@ struct Range {
   long long off = 0, len = 0;
 };
 
-// first-fit allocator over [0, cap)
+// first-fit allocator over [0, cap) in units of `unit`
 struct Arena {
-  long long cap = 0;
+  long long cap = 0, unit = 1;
   std::vector<Range> freel;
-  void init(long long c) {
-    cap = c;
-    freel.assign(1, Range{0, c});
+  void init(long long c, long long u = 1) {
+    unit = u;
+    cap = c / u * u;
+    freel.assign(1, Range{0, cap});
   }
+  long long round(long long n) const { return (n + unit - 1) / unit * unit; }
   long long alloc(long long n) {
-    if (n <= 0) return 0;
+    n = round(std::max(n, 1LL));
     for (size_t i = 0; i < freel.size(); ++i)
       if (freel[i].len >= n) {
         long long o = freel[i].off;
@@ -672,7 +1311,7 @@ struct Arena {
     return -1;
   }
   void release(long long off, long long n) {
-    if (n <= 0) return;
+    n = round(std::max(n, 1LL));
     freel.push_back(Range{off, n});
     std::sort(freel.begin(), freel.end(), [](const Range& x, const Range& y) { return x.off < y.off; });
     std::vector<Range> m;
@@ -689,20 +1328,22 @@ struct Arena {
   }
 };
 
+struct HostTile {
+  int c0, c1;          // relative computational columns
+  int base, nslots;    // relative slots
+  int hdr, hdr_bytes;  // relative header bytes
+};
+
 struct HostInst {
   bool live = false;
   int id = -1;
-  long long s_off = 0, n3 = 0, n3c = 0;  // slots
+  long long s_off = 0, n3 = 0, n3c = 0;  // slots (n3 includes tile padding)
   long long c_off = 0, ncomp = 0;        // columns
   long long e_off = 0, ne3 = 0;          // edge slots
+  long long h_off = 0, h_bytes = 0;      // header bytes
   int Nc = 0;
-  std::vector<int> dev2cell, Nk, ctop, coff;  // device column -> cell, per cell Nk/ctop, device column offsets
-  std::vector<int> tiles_rel;                  // tile boundaries (relative column index), size ntiles+1
-  int qprecond = 1;
-  double tol = 1e-10;
-  int maxiters = 1000;
-  double resnorm = 1.0;
-  bool done_reported = false;
+  std::vector<int> dev2cell, Nk, ctop, coff;  // device column -> cell; per cell Nk/ctop; device column -> relative slot
+  std::vector<HostTile> tiles;
 };
 
 }  // namespace sgpu
@@ -719,17 +1360,18 @@ struct sgpu_batch {
   long long timeout_ns = 2000000000LL;
   int grid_override = 0;
   double delta = 0.01;
-  long long max_slots = 0, max_cols = 0, max_eslots = 0;
+  long long max_slots = 0, max_cols = 0, max_eslots = 0, max_hdr = 0;
   int max_inst = 0, max_tiles = 0;
-  Arena slots, cols, eslots;
+  Arena slots, cols, eslots, hdrs;
   std::vector<HostInst> inst;
   std::vector<BInst> h_inst;
   bool pending_setup = false;
   // device
   std::vector<void*> allocs;
   BatchArgs a{};
-  int* d_tile_c0 = nullptr;
+  TileDesc* d_tiles = nullptr;
   int* d_tile_inst = nullptr;
+  unsigned char* d_hdrs = nullptr;
   BCol* d_col = nullptr;
   BFace* d_face = nullptr;
   double* d_colAc = nullptr;
@@ -739,9 +1381,9 @@ struct sgpu_batch {
   int* d_gflags = nullptr;
   SolveCtl* h_ctl = nullptr;
   int ntiles = 0;
-  std::vector<int> h_tile_c0, h_tile_inst;
   double last_ms = 0.0;
   long long last_work = 0;
+  bool attr_set[3] = {false, false, false};
 };
 
 static int bfail(sgpu_batch* b, int code, const char* fmt, ...) {
@@ -782,14 +1424,21 @@ struct Guard {
     if (prev >= 0) cudaSetDevice(prev);
   }
 };
+
+const void* kernel_of(int qp) {
+  return qp == 1 ? (const void*)batch_kernel<1> : qp == 2 ? (const void*)batch_kernel<2> : (const void*)batch_kernel<0>;
+}
 }  // namespace
 
-static int batch_max_grid(int qp, int dev) {
+static int batch_max_grid(sgpu_batch* b) {
+  const void* fn = kernel_of(b->qprecond);
+  if (!b->attr_set[b->qprecond]) {
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem) != cudaSuccess) return 0;
+    b->attr_set[b->qprecond] = true;
+  }
   int sms = 0, per = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const void* fn = qp == 1 ? (const void*)batch_kernel<1> : qp == 2 ? (const void*)batch_kernel<2>
-                                                                      : (const void*)batch_kernel<0>;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kBlock, 0) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kThreads, kDynSmem) != cudaSuccess) return 0;
   return sms * per;
 }
 
@@ -809,14 +1458,20 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   b->device = device;
   b->qprecond = qprecond;
   b->F = maxfaces;
-  b->max_slots = max_slots;
+  // tiles are 4-slot aligned: reserve room for the padding (< 4 slots per tile)
+  const long long tiles_est = max_cols + max_slots / kBTSlots + 2LL * max_instances + 2;
+  b->max_slots = std::min(0x7ffffff0LL, max_slots + 4 * std::min(tiles_est, max_slots) + 8LL * max_instances + 16);
   b->max_cols = max_cols;
   b->max_eslots = std::max(1LL, max_edge_slots);
   b->max_inst = max_instances;
-  b->max_tiles = (int)std::min<long long>(0x7fffffff, max_cols + max_slots / kTileCap + 2);
-  b->slots.init(max_slots);
+  b->max_tiles = (int)std::min<long long>(0x7fffffff, tiles_est);
+  // header bytes: per tile 16 + 3 x 16 padding, per column 2 + 4, per column-face 16
+  b->max_hdr = 80LL * (b->max_tiles + 1) + (long long)max_cols * (8 + 16LL * maxfaces) + 16;
+  if (b->max_hdr > 0x7ffffff0LL) return bfail(b, SGPU_BAD_ARG, "header arena too large");
+  b->slots.init(b->max_slots, 4);
   b->cols.init(max_cols);
   b->eslots.init(b->max_eslots);
+  b->hdrs.init(b->max_hdr, 16);
   b->inst.resize(max_instances);
   b->h_inst.assign(max_instances, BInst{});
   Guard g(device);
@@ -824,12 +1479,13 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   BCK(cudaEventCreate(&b->ev0));
   BCK(cudaEventCreate(&b->ev1));
   BCK(cudaMallocHost((void**)&b->h_ctl, sizeof(SolveCtl)));
-  const size_t S = (size_t)max_slots + 1, E = (size_t)b->max_eslots + 1, Cn = (size_t)max_cols + 1;
+  const size_t S = (size_t)b->max_slots + 8, E = (size_t)b->max_eslots + 8, Cn = (size_t)max_cols + 1;
   int rc;
   BatchArgs& a = b->a;
   a.F = maxfaces;
-  if ((rc = balloc(b, &b->d_tile_c0, 2 * ((size_t)b->max_tiles + 1)))) return rc;
+  if ((rc = balloc(b, &b->d_tiles, (size_t)b->max_tiles + 1))) return rc;
   if ((rc = balloc(b, &b->d_tile_inst, (size_t)b->max_tiles + 1))) return rc;
+  if ((rc = balloc(b, &b->d_hdrs, (size_t)b->max_hdr))) return rc;
   if ((rc = balloc(b, &b->d_col, Cn))) return rc;
   if ((rc = balloc(b, &b->d_face, Cn * maxfaces))) return rc;
   if ((rc = balloc(b, &b->d_colAc, Cn))) return rc;
@@ -843,7 +1499,7 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if (qprecond == 1 && (rc = balloc(b, &a.fc64, S * maxfaces))) return rc;
   if ((rc = balloc(b, &a.x64, S))) return rc;
   if ((rc = balloc(b, &a.b64, S))) return rc;
-  if ((rc = balloc(b, &a.dzz32, S))) return rc;
+  if ((rc = balloc(b, &a.fz32, S))) return rc;
   if ((rc = balloc(b, &a.cinv32, S))) return rc;
   if ((rc = balloc(b, &a.coef32, S))) return rc;
   if ((rc = balloc(b, &a.dzfD32, E))) return rc;
@@ -861,12 +1517,17 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if ((rc = balloc(b, &b->d_inst, (size_t)max_instances))) return rc;
   if ((rc = balloc(b, &b->d_ctl, 1))) return rc;
   if ((rc = balloc(b, &b->d_gflags, 4))) return rc;
+  // padding slots are copied by the bulk copies but never used: keep them finite
+  float* f32s[] = {a.fz32, a.cinv32, a.coef32, a.r32, a.pa32, a.pb32, a.x32, a.z32, a.s32, a.tw32, a.tib32};
+  for (float* p : f32s)
+    if (p) BCK(cudaMemsetAsync(p, 0, S * sizeof(float), b->stream));
   BCK(cudaMemsetAsync(a.coef64, 0, S * sizeof(double), b->stream));
   BCK(cudaMemsetAsync(b->d_cin64, 0, S * sizeof(double), b->stream));
   BCK(cudaMemsetAsync(b->d_inst, 0, sizeof(BInst) * max_instances, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
-  a.tile_c0 = b->d_tile_c0;
+  a.tiles = b->d_tiles;
   a.tile_inst = b->d_tile_inst;
+  a.hdrs = b->d_hdrs;
   a.col = b->d_col;
   a.face = b->d_face;
   a.colAc = b->d_colAc;
@@ -901,10 +1562,11 @@ const char* sgpu_batch_last_error(const sgpu_batch* b) { return b ? b->err.c_str
 long long sgpu_batch_bytes_per_request(int qprecond, int maxfaces, long long n3, long long ncols,
                                        long long nedge_slots) {
   // device bytes an instance occupies (layout of sgpu_batch_create's arrays)
-  long long per_slot = 8 * 7 + 4 * 8 + (qprecond == 1 ? 8LL * maxfaces : 0) + (qprecond == 2 ? 12 : 0);
-  long long per_col = (long long)sizeof(BCol) + (long long)sizeof(BFace) * maxfaces + 8;
+  long long per_slot = 8 * 8 + 4 * 8 + (qprecond == 1 ? 8LL * maxfaces : 0) + (qprecond == 2 ? 12 : 0);
+  long long per_col = (long long)sizeof(BCol) + (long long)sizeof(BFace) * maxfaces + 8 + 8 + 16LL * maxfaces;
   long long per_eslot = 12;
-  return per_slot * n3 + per_col * ncols + per_eslot * nedge_slots + 16 * (ncols + n3 / kTileCap + 2);
+  const long long tiles = ncols / 16 + n3 / kBTSlots + 2;
+  return per_slot * (n3 + 4 * tiles) + per_col * ncols + per_eslot * nedge_slots + 96 * tiles;
 }
 
 int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, const double* const* dzz,
@@ -943,52 +1605,71 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
       c2d[i] = (int)H.dev2cell.size();
       H.dev2cell.push_back(i);
     }
-  H.coff.assign(Nc + 1, 0);
-  long long acc = 0;
   for (int j = 0; j < Nc; ++j) {
     const int i = H.dev2cell[j];
     if (g->Nk[i] < 1 || g->Nk[i] > g->Nkmax || ctop[i] < 0 || ctop[i] >= g->Nk[i])
       return bfail(b, SGPU_BAD_GRID, "Nk/ctop out of range at cell %d", i);
+    if (g->nfaces[i] < 1 || g->nfaces[i] > F) return bfail(b, SGPU_BAD_GRID, "nfaces out of range at cell %d", i);
+  }
+  // tiles over the computational columns: <= kBTSlots slots, <= kBTCols columns,
+  // <= kBTFaces column-faces; every tile starts on a 4-slot boundary
+  const int maxc = std::min(kBTCols, kBTFaces / F);
+  H.coff.assign(Nc + 1, 0);
+  long long acc = 0, hacc = 0;
+  {
+    int j = 0;
+    while (j < cd[1]) {
+      HostTile T;
+      T.c0 = j;
+      T.base = (int)acc;
+      int len = 0;
+      while (j < cd[1] && j - T.c0 < maxc && len + g->Nk[H.dev2cell[j]] <= kBTSlots) {
+        H.coff[j] = (int)(acc + len);
+        len += g->Nk[H.dev2cell[j]];
+        ++j;
+      }
+      T.c1 = j;
+      T.nslots = len;
+      const HdrLayout L = hdr_layout(T.c1 - T.c0, F);
+      T.hdr = (int)hacc;
+      T.hdr_bytes = L.bytes;
+      hacc += L.bytes;
+      H.tiles.push_back(T);
+      acc += (len + 3) & ~3;
+    }
+  }
+  H.n3c = acc;
+  for (int j = cd[1]; j < Nc; ++j) {
     H.coff[j] = (int)acc;
-    acc += g->Nk[i];
+    acc += g->Nk[H.dev2cell[j]];
   }
   H.coff[Nc] = (int)acc;
   H.n3 = acc;
   H.ncomp = cd[1];
-  H.n3c = H.coff[cd[1]];
+  H.h_bytes = hacc;
   std::vector<long long> eoff(Ne + 1, 0);
   for (int e = 0; e < Ne; ++e) eoff[e + 1] = eoff[e] + g->Nke[e];
   H.ne3 = eoff[Ne];
-  H.qprecond = b->qprecond;
-  H.tol = qepsilon;
-  H.maxiters = qmaxiters;
-  H.resnorm = resnorm;
-  // tiles over the computational columns (relative)
-  H.tiles_rel.push_back(0);
-  int cur = 0;
-  for (int j = 0; j < cd[1]; ++j) {
-    const int len = g->Nk[H.dev2cell[j]];
-    if (cur + len > kTileCap) {
-      H.tiles_rel.push_back(j);
-      cur = 0;
-    }
-    cur += len;
-  }
-  H.tiles_rel.push_back(cd[1]);
-  // reserve device ranges
-  H.s_off = b->slots.alloc(H.n3);
+  // reserve device ranges (+4 slots: the coefficient stream of a tile reads one group past it)
+  H.s_off = b->slots.alloc(H.n3 + 4);
   H.c_off = b->cols.alloc(H.ncomp);
   H.e_off = b->eslots.alloc(std::max(1LL, H.ne3));
-  if (H.s_off < 0 || H.c_off < 0 || H.e_off < 0) {
-    if (H.s_off >= 0) b->slots.release(H.s_off, H.n3);
+  H.h_off = b->hdrs.alloc(H.h_bytes);
+  long long ntl = 0;
+  for (int i = 0; i < b->max_inst; ++i)
+    if (b->inst[i].live) ntl += (long long)b->inst[i].tiles.size();
+  if (H.s_off < 0 || H.c_off < 0 || H.e_off < 0 || H.h_off < 0 || ntl + (long long)H.tiles.size() > b->max_tiles) {
+    if (H.s_off >= 0) b->slots.release(H.s_off, H.n3 + 4);
     if (H.c_off >= 0) b->cols.release(H.c_off, H.ncomp);
     if (H.e_off >= 0) b->eslots.release(H.e_off, std::max(1LL, H.ne3));
+    if (H.h_off >= 0) b->hdrs.release(H.h_off, H.h_bytes);
     return bfail(b, SGPU_OOM, "batch capacity exhausted (slots %lld free of %lld)", b->slots.free_total(),
                  b->max_slots);
   }
   // stage host data (pageable copies; the upload is synchronous per instance)
   Guard gd(b->device);
-  std::vector<double> v_dzz(H.n3), v_src(H.n3), v_q(H.n3), v_c(H.n3, 1.0), v_dzfD(std::max(1LL, H.ne3));
+  std::vector<double> v_dzz(H.n3, 1.0), v_src(H.n3, 0.0), v_q(H.n3, 0.0), v_c(H.n3, 1.0),
+      v_dzfD(std::max(1LL, H.ne3));
   for (int j = 0; j < Nc; ++j) {
     const int i = H.dev2cell[j];
     std::memcpy(&v_dzz[H.coff[j]], dzz[i], sizeof(double) * g->Nk[i]);
@@ -1028,6 +1709,37 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
       fc.D64 = D[e];
     }
   }
+  // tile headers
+  std::vector<unsigned char> v_hdr(std::max(16LL, H.h_bytes), 0);
+  for (const HostTile& T : H.tiles) {
+    const int ncols = T.c1 - T.c0;
+    const HdrLayout L = hdr_layout(ncols, F);
+    unsigned char* h = v_hdr.data() + T.hdr;
+    int* h0 = (int*)h;
+    h0[0] = ncols;
+    h0[1] = T.nslots;
+    h0[2] = (int)(H.s_off + T.base);
+    h0[3] = id;
+    unsigned short* st = (unsigned short*)(h + L.o_start);
+    int* cn = (int*)(h + L.o_cn);
+    int* fns = (int*)(h + L.o_fns);
+    int* fkk = (int*)(h + L.o_fkk);
+    float* fD = (float*)(h + L.o_fD);
+    int* fes = (int*)(h + L.o_fes);
+    for (int cc = 0; cc < ncols; ++cc) {
+      const int j = T.c0 + cc;
+      st[cc] = (unsigned short)(H.coff[j] - T.base);
+      cn[cc] = v_col[j].ctop | (v_col[j].nk << 16);
+      for (int f = 0; f < F; ++f) {
+        const BFace& fc = v_face[(size_t)j * F + f];
+        fns[cc * F + f] = fc.ns;
+        fkk[cc * F + f] = fc.ns < 0 ? 0 : ((int)fc.kmin | ((int)fc.kmax << 16));
+        fD[cc * F + f] = fc.D;
+        fes[cc * F + f] = fc.es;
+      }
+    }
+    st[ncols] = (unsigned short)T.nslots;
+  }
   std::vector<float> v_dzfD32(v_dzfD.size());
   for (size_t k = 0; k < v_dzfD.size(); ++k) v_dzfD32[k] = (float)v_dzfD[k];
   cudaStream_t s = b->stream;
@@ -1042,6 +1754,11 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   BCK(cudaMemcpyAsync(b->d_col + H.c_off, v_col.data(), sizeof(BCol) * H.ncomp, cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->d_face + H.c_off * F, v_face.data(), sizeof(BFace) * H.ncomp * F, cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->d_colAc + H.c_off, v_Ac.data(), 8 * H.ncomp, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->d_hdrs + H.h_off, v_hdr.data(), H.h_bytes, cudaMemcpyHostToDevice, s));
+  // padding slots of the instance must be finite in every FP32 stream (they are copied, never used)
+  float* f32s[] = {b->a.fz32, b->a.cinv32, b->a.coef32, b->a.r32, b->a.pa32, b->a.pb32, b->a.x32, b->a.z32};
+  for (float* p : f32s) BCK(cudaMemsetAsync(p + H.s_off, 0, 4 * (H.n3 + 4), s));
+  if (b->qprecond == 2) BCK(cudaMemsetAsync(b->a.s32 + H.s_off, 0, 4 * (H.n3 + 4), s));
   BCK(cudaStreamSynchronize(s));
   BInst& I = b->h_inst[id];
   std::memset(&I, 0, sizeof(BInst));
@@ -1065,9 +1782,8 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
 int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long long* unknown_iters) {
   if (!b) return SGPU_BAD_ARG;
   Guard gd(b->device);
-  // tile table of live, unfinished instances
-  b->h_tile_c0.clear();
-  b->h_tile_inst.clear();
+  std::vector<TileDesc> tiles;
+  std::vector<int> tinst;
   int ninst = 0;
   std::vector<int> n_before(b->max_inst, 0);
   for (int i = 0; i < b->max_inst; ++i) {
@@ -1080,15 +1796,24 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
       continue;
     }
     n_before[i] = I.state == INST_RUN ? I.n : 0;
-    I.t0 = (int)b->h_tile_c0.size();
-    for (size_t k = 0; k + 1 < H.tiles_rel.size(); ++k) {
-      b->h_tile_c0.push_back((int)(H.c_off + H.tiles_rel[k]));
-      b->h_tile_inst.push_back(i);
+    I.t0 = (int)tiles.size();
+    for (const HostTile& T : H.tiles) {
+      TileDesc d;
+      d.hdr = (int)(H.h_off + T.hdr);
+      d.hdr_bytes = T.hdr_bytes;
+      d.base = (int)(H.s_off + T.base);
+      d.nslots = T.nslots;
+      d.inst = i;
+      d.c0 = (int)(H.c_off + T.c0);
+      d.c1 = (int)(H.c_off + T.c1);
+      d.pad = 0;
+      tiles.push_back(d);
+      tinst.push_back(i);
     }
-    I.t1 = (int)b->h_tile_c0.size();
+    I.t1 = (int)tiles.size();
     I.cnt = 0;
   }
-  const int ntiles = (int)b->h_tile_c0.size();
+  const int ntiles = (int)tiles.size();
   if (ntiles > b->max_tiles) return bfail(b, SGPU_OOM, "too many tiles");
   if (ntiles == 0) {
     if (running) *running = 0;
@@ -1096,17 +1821,14 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     if (unknown_iters) *unknown_iters = 0;
     return SGPU_OK;
   }
-  // tiles as (first column, end column) pairs: an instance's last tile ends at its last column
-  std::vector<int> table(2 * ntiles), tinst(ntiles);
-  for (int t = 0; t < ntiles; ++t) {
-    const int i = b->h_tile_inst[t];
-    tinst[t] = i;
-    const bool same = t + 1 < ntiles && b->h_tile_inst[t + 1] == i;
-    table[2 * t] = b->h_tile_c0[t];
-    table[2 * t + 1] = same ? b->h_tile_c0[t + 1] : (int)(b->inst[i].c_off + b->inst[i].ncomp);
-  }
+  int maxg = batch_max_grid(b);
+  if (maxg <= 0) return bfail(b, SGPU_CUDA_ERROR, "occupancy query failed");
+  int grid = b->grid_override > 0 ? std::min(b->grid_override, maxg) : maxg;
+  grid = std::max(1, std::min(grid, ntiles));
+  if ((ntiles + grid - 1) / grid > kListCap)
+    return bfail(b, SGPU_OOM, "%d tiles exceed %d per CTA at %d CTAs", ntiles, kListCap, grid);
   b->ntiles = ntiles;
-  BCK(cudaMemcpyAsync(b->d_tile_c0, table.data(), sizeof(int) * 2 * ntiles, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaMemcpyAsync(b->d_tile_inst, tinst.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaMemcpyAsync(b->d_inst, b->h_inst.data(), sizeof(BInst) * ninst, cudaMemcpyHostToDevice, b->stream));
   std::memset(b->h_ctl, 0, sizeof(SolveCtl));
@@ -1122,16 +1844,10 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
   a.ninst = ninst;
   a.max_iters_chunk = max_iters > 0 ? max_iters : 0x7fffffff;
   a.delta2 = b->delta * b->delta;
-  int maxg = batch_max_grid(b->qprecond, b->device);
-  if (maxg <= 0) return bfail(b, SGPU_CUDA_ERROR, "occupancy query failed");
-  int grid = b->grid_override > 0 ? std::min(b->grid_override, maxg) : maxg;
-  grid = std::max(1, std::min(grid, ntiles));
   int do_setup = b->pending_setup ? 1 : 0;
   void* args[] = {(void*)&a, (void*)&do_setup};
-  const void* fn = b->qprecond == 1 ? (const void*)batch_kernel<1>
-                 : b->qprecond == 2 ? (const void*)batch_kernel<2> : (const void*)batch_kernel<0>;
   BCK(cudaEventRecord(b->ev0, b->stream));
-  BCK(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0, b->stream));
+  BCK(cudaLaunchCooperativeKernel(kernel_of(b->qprecond), dim3(grid), dim3(kThreads), args, kDynSmem, b->stream));
   BCK(cudaEventRecord(b->ev1, b->stream));
   BCK(cudaMemcpyAsync(b->h_inst.data(), b->d_inst, sizeof(BInst) * ninst, cudaMemcpyDeviceToHost, b->stream));
   BCK(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, b->stream));
@@ -1141,7 +1857,7 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
   cudaEventElapsedTime(&fms, b->ev0, b->ev1);
   b->last_ms = fms;
   if (b->h_ctl->status == SGPU_TIMEOUT)
-    return bfail(b, SGPU_TIMEOUT, "device barrier wait timed out in phase %d", b->h_ctl->phase_err);
+    return bfail(b, SGPU_TIMEOUT, "device wait timed out (phase %d)", b->h_ctl->phase_err);
   int run = 0;
   long long work = 0;
   for (int i = 0; i < ninst; ++i) {
@@ -1194,9 +1910,10 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
     }
   }
   if (release) {
-    b->slots.release(H.s_off, H.n3);
+    b->slots.release(H.s_off, H.n3 + 4);
     b->cols.release(H.c_off, H.ncomp);
     b->eslots.release(H.e_off, std::max(1LL, H.ne3));
+    b->hdrs.release(H.h_off, H.h_bytes);
     H = HostInst();
     std::memset(&b->h_inst[id], 0, sizeof(BInst));
   }
@@ -1217,5 +1934,11 @@ int sgpu_batch_set(sgpu_batch* b, double delta, int grid, long long timeout_ns) 
 }
 
 void* sgpu_batch_stream(sgpu_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int sgpu_batch_phase_times(const sgpu_batch* b, long long* ns8) {
+  if (!b || !ns8) return SGPU_BAD_ARG;
+  for (int k = 0; k < 8; ++k) ns8[k] = b->h_ctl ? b->h_ctl->phase_ns[k] : 0;
+  return SGPU_OK;
+}
 
 }  // extern "C"

@@ -2,17 +2,65 @@
 //
 // Many independent grids ("instances") share one set of device arrays: every
 // instance owns a contiguous range of storage slots (one slot per cell level,
-// columns z-contiguous), of columns, of edge slots and of tiles.  One
-// persistent cooperative kernel advances every active instance by one CG
-// iteration per global iteration; each instance keeps its own scalars,
-// tolerance, iteration count and status.
+// columns z-contiguous, every tile starting on a 4-slot = 16-byte boundary so
+// that tiles can be moved with bulk copies), of columns, of edge slots and of
+// tile headers.  One persistent cooperative kernel advances every active
+// instance by one CG iteration per global iteration; each instance keeps its
+// own scalars, tolerance, iteration count and status.
 #pragma once
 #include <cuda_runtime.h>
 #include "sgpu_common.cuh"
 
 namespace sgpu {
 
-constexpr int kMaxF = 8;        // faces per cell supported by the batched engine
+constexpr int kMaxF = 8;         // faces per cell supported by the batched engine
+constexpr int kBTSlots = 1024;   // storage slots per tile (4 per thread of a 256-thread CTA)
+constexpr int kBTCols = 128;     // columns per tile
+constexpr int kBTFaces = 512;    // column-faces per tile (ncols * F)
+constexpr int kHdrCap = 9216;    // bytes of a tile header (see tile header layout below)
+constexpr int kStreamFloats = kBTSlots + 4;                 // one FP32 stream of a tile (+1 group)
+constexpr int kStreamBytes = kStreamFloats * 4;             // 4112, a multiple of 16
+constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // one pipeline stage
+constexpr int kListCap = 512;    // tiles per CTA per phase
+// dynamic shared memory of the kernel: 2 stages, 4 mbarriers (32 B), the tile list
+constexpr int kDynSmem = 2 * kBufBytes + 32 + 4 * kListCap;
+
+// Tile header (global, built on the host when an instance is added; all
+// offsets are multiples of 16 bytes):
+//   [0]       int ncols, nslots, base, inst
+//   o_start   unsigned short start[ncols+1]   slot offset of each column in the tile
+//   o_cn      int cn[ncols]                   ctop | nk << 16
+//   o_fns     int fns[ncols*F]                neighbour's first slot (-1: none)
+//   o_fkk     int fkk[ncols*F]                kmin | kmax << 16 (empty when no neighbour)
+//   o_fD      float fD[ncols*F]               D of the edge
+//   o_fes     int fes[ncols*F]                edge's first slot (dzf*D storage)
+__host__ __device__ __forceinline__ int pad16(int b) { return (b + 15) & ~15; }
+struct HdrLayout {
+  int o_start, o_cn, o_fns, o_fkk, o_fD, o_fes, bytes;
+};
+__host__ __device__ __forceinline__ HdrLayout hdr_layout(int ncols, int F) {
+  HdrLayout L;
+  L.o_start = 16;
+  L.o_cn = L.o_start + pad16(2 * (ncols + 1));
+  const int sf = pad16(4 * ncols * F);
+  L.o_fns = L.o_cn + pad16(4 * ncols);
+  L.o_fkk = L.o_fns + sf;
+  L.o_fD = L.o_fkk + sf;
+  L.o_fes = L.o_fD + sf;
+  L.bytes = L.o_fes + sf;
+  return L;
+}
+
+// Per-launch tile descriptor.
+struct TileDesc {
+  int hdr;      // byte offset of the header in the header arena
+  int hdr_bytes;
+  int base;     // first storage slot (multiple of 4)
+  int nslots;
+  int inst;
+  int c0, c1;   // global computational columns [c0, c1)
+  int pad;
+};
 
 // Instance lifecycle inside the persistent kernel.
 enum InstState : int { INST_EMPTY = 0, INST_SETUP = 1, INST_RUN = 2, INST_DONE = 3 };
@@ -20,7 +68,7 @@ enum InstState : int { INST_EMPTY = 0, INST_SETUP = 1, INST_RUN = 2, INST_DONE =
 // Per-instance scalars and bookkeeping (device memory, one per instance slot).
 struct __align__(64) BInst {
   // static description
-  int t0, t1;          // tile range [t0, t1)
+  int t0, t1;          // tile range [t0, t1) in this launch's tile list
   int s0, s1;          // computational storage range [s0, s1) (tiles cover it)
   int maxiters;
   int qprecond;
@@ -30,8 +78,8 @@ struct __align__(64) BInst {
   int state;           // InstState
   int n;               // iterations executed
   int status;          // SGPU_* code
-  int flags;           // bit0: reliable update now; bit1: final merge (no verification)
-  int cnt;             // tiles finished in the current phase (last one reduces)
+  int flags;           // bit0: reliable update now; bit1: final merge; bit2: last chance at maxiters
+  int cnt;             // tiles finished in the current phase (the last flush reduces)
   int par;             // which p buffer holds the current direction
   int nrel;            // reliable updates done
   int s2;              // end of the instance's storage (boundary columns in [s1, s2))
@@ -40,7 +88,8 @@ struct __align__(64) BInst {
   double alpha_prev;
 };
 
-// Column metadata (one entry per computational column, global column index).
+// Column metadata (one entry per computational column, global column index),
+// used by the set-up and FP64 residual phases.
 struct BCol {
   int s;               // first storage slot of the column
   int nk;              // levels stored
@@ -64,8 +113,9 @@ struct BatchArgs {
   int max_iters_chunk; // global iterations allowed in this launch
   double delta2;       // reliable-update trigger: eps < delta2 * eps_ref
   // tiles
-  const int* tile_c0;    // [2*ntiles] (first, end) global column of each tile
-  const int* tile_inst;  // [ntiles]
+  const TileDesc* tiles;       // [ntiles]
+  const int* tile_inst;        // [ntiles]
+  const unsigned char* hdrs;   // header arena
   // columns (global, computational only) and faces
   const BCol* col;       // [ncols]
   const BFace* face;     // [ncols*F]
@@ -77,14 +127,14 @@ struct BatchArgs {
   const double* cin64;   // [nslots] c at boundary columns (qprecond 1)
   const double* dzfD64;  // [nedge_slots] dzf*D per edge level (qprecond 0/2)
   double* c64;           // [nslots] sqrt|diag| (qprecond 1), 1 elsewhere
-  double* coef64;        // [nslots+1] vertical coefficient (scaled for qprecond 1)
-  double* fc64;          // [F*nslots] face coefficients of the FP64 operator
+  double* coef64;        // [nslots+4] vertical coefficient (scaled for qprecond 1)
+  double* fc64;          // [F*nslots] face coefficients of the FP64 operator (qprecond 1)
   double* x64;           // [nslots] FP64 iterate (scaled variables for qprecond 1)
   double* b64;           // [nslots] FP64 right-hand side (scaled for qprecond 1)
   // FP32 inner data
-  float* dzz32;          // [nslots]
+  float* fz32;           // [nslots] dzz/c (qprecond 1 face coefficients)
   float* cinv32;         // [nslots] 1/c (qprecond 1)
-  float* coef32;         // [nslots+1] vertical coefficient (qprecond 0/2)
+  float* coef32;         // [nslots+4] vertical coefficient (scaled for qprecond 1)
   float* dzfD32;         // [nedge_slots]
   float* tw32;           // [nslots] Thomas factors (qprecond 2)
   float* tib32;          // [nslots]
@@ -97,8 +147,8 @@ struct BatchArgs {
   // per-tile partial sums [ntiles*2] and instance table
   double* tpart;
   BInst* inst;
-  SolveCtl* ctl;         // grid barrier + global flags
-  int* gflags;           // [4]: 0 any reliable flag, 1 any active, 2 snapshot reliable, 3 snapshot active
+  SolveCtl* ctl;         // grid barrier
+  int* gflags;           // [4]: 0 any reliable flag, 2 its snapshot, 3 any instance running
 };
 
 }  // namespace sgpu

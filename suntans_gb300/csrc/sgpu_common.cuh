@@ -43,6 +43,9 @@ struct __align__(128) SolveCtl {
   int status;             // SGPU_* code
   int phase_err;          // where a wait gave up
   long long timeout_ns;   // barrier wait bound
+  // per-phase device time, filled only in builds with SGPU_PHASE_TIMING
+  long long phase_ns[8];  // indexed by (phase id & 7)
+  long long last_ts;
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -140,6 +143,13 @@ __device__ __forceinline__ bool grid_sync(SolveCtl* ctl, int phase, Fin&& fin) {
     }
     __syncthreads();
   }
+#ifdef SGPU_PHASE_TIMING
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const long long now = (long long)globaltimer_ns();
+    if (ctl->last_ts) ctl->phase_ns[phase & 7] += now - ctl->last_ts;
+    ctl->last_ts = now;
+  }
+#endif
   if (!s_ok) return false;
   return ld_volatile_int(&ctl->status) == SGPU_OK || ld_volatile_int(&ctl->status) == SGPU_MAXITER;
 }

@@ -42,3 +42,26 @@ def h_props(hprecond, **kw):
     d = dict(hprecond=hprecond, maxiters=4000, epsilon=1e-10, resnorm=1.0, dt=30.0, theta=0.55)
     d.update(kw)
     return SolverProps(**d)
+
+
+def stopping_ratio(oracle, prob, q, qprecond):
+    """sqrt(eps/eps0) of CGSolveQ's stopping rule (main/phys.c:2470-2524) for the
+    solution q, evaluated on the CPU with the oracle's own operators: the
+    scaled residual for qprecond 1, the plain residual for 0 and 2."""
+    import numpy as np
+    g = prob.grid
+    m = g.active_mask()
+    if qprecond == 1:
+        c = oracle.condition_q(g, prob.D, np.ones(g.n3))
+        coef, fcoef = oracle.qcoefficients(g, prob.D, c, 1)
+        b = np.where(m, prob.src / c, 0.0)
+
+        def res(x):
+            return b - oracle.operator_qc(g, coef, fcoef, np.where(m, x * c, 0.0))
+    else:
+        coef, _ = oracle.qcoefficients(g, prob.D, np.ones(g.n3), 0)
+
+        def res(x):
+            return prob.src - oracle.operator_q(g, prob.D, coef, np.where(m, x, 0.0) + np.where(m, 0.0, prob.q))
+    r, r0 = res(q)[m], res(prob.q)[m]
+    return float(np.linalg.norm(r) / np.linalg.norm(r0))
