@@ -187,6 +187,21 @@ int sgpu_batch_state(const sgpu_batch *b, int id);
  * only.  release != 0 frees its device memory and id. */
 int sgpu_batch_result(sgpu_batch *b, int id, double *const *q, sgpu_stats *stats, int release);
 
+/* Re-submits finished problem `id`.  src (jagged, cell order, as
+ * sgpu_batch_add) replaces the right-hand side, or NULL keeps the resident one.
+ * warm != 0: the last solution is the initial guess, as phys->qc is for the
+ * next CGSolveQ in the model; warm == 0: the initial guess uploaded by
+ * sgpu_batch_add is used again.  Grid and coefficients stay resident on the
+ * device; only src is uploaded. */
+int sgpu_batch_resubmit(sgpu_batch *b, int id, const double *const *src, double qepsilon, int qmaxiters, int warm);
+
+/* Capture each launch sequence (tables in, persistent kernel, report out) in a
+ * CUDA graph and replay it while the set of problems is unchanged.  Returns 1
+ * when graph launches are in use, 0 when capture is unavailable (direct
+ * launches continue).  sgpu_batch_graph_launches counts graph replays. */
+int sgpu_batch_use_graph(sgpu_batch *b, int on);
+long long sgpu_batch_graph_launches(const sgpu_batch *b);
+
 /* Tuning: reliable-update factor delta (default 0.01), CTA count (0 = full
  * wave), barrier wait limit; pass <= 0 / < 0 to keep a value. */
 int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);

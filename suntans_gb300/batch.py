@@ -118,6 +118,26 @@ class Batch:
             self.grids.pop(i, None)
         return q, st
 
+    def resubmit(self, i, src=None, tol=1e-10, maxiters=5000, warm=True):
+        """Re-run finished problem i: new right-hand side (None keeps the resident
+        one); warm=True starts from its last solution, False from the original guess."""
+        g = self.grids[i]
+        if src is None:
+            p = None
+        else:
+            src = np.ascontiguousarray(src, dtype=np.float64)
+            ptr = jagged(src, g.coff)
+            p = ptr.ctypes.data_as(_dpp)
+        rc = self.lib.sgpu_batch_resubmit(self.h, int(i), p, float(tol), int(maxiters), int(bool(warm)))
+        if rc != OK:
+            raise SolverError(rc, f"sgpu_batch_resubmit: {self.error()}")
+
+    def use_graph(self, on=True) -> bool:
+        return bool(self.lib.sgpu_batch_use_graph(self.h, int(on)))
+
+    def graph_launches(self) -> int:
+        return int(self.lib.sgpu_batch_graph_launches(self.h))
+
     def phase_times_ms(self):
         """Per-phase device time of the last launch (zero unless built with -DSGPU_PHASE_TIMING)."""
         arr = (C.c_longlong * 8)()

@@ -940,7 +940,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
 #define SGPU_BATCH_MINB 3
 #endif
 template <int QP>
-__global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchArgs a, int do_setup) {
+__global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchArgs a) {
   extern __shared__ __align__(128) unsigned char dyn[];
   __shared__ double s_red[4 * 8];
   __shared__ int s_flag;
@@ -970,7 +970,8 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   TileSmem& sm = *(TileSmem*)P.stage[0];  // simple phases reuse stage 0 (no copies in flight then)
 
   // ======================= setup of new instances =======================
-  if (do_setup) {
+  // gflags[1]: some instance needs its set-up phases (written by the host)
+  if (ld_volatile_int(&a.gflags[1])) {
     auto is_setup = [&](int i) { return inst_state(a, i) == INST_SETUP; };
     if (compute) {
       // S1: conditioner / unscaled coefficients, FP32 copies, zero vectors
@@ -1278,6 +1279,14 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   }
 }
 
+// q64 := the solution of an instance's computational slots (warm start for a
+// re-submission, and the unscaled result for download)
+__global__ void finalize_q_kernel(const double* __restrict__ x64, const double* __restrict__ c64,
+                                  double* __restrict__ q64, int s0, int n, int scaled) {
+  for (int u = s0 + blockIdx.x * blockDim.x + threadIdx.x; u < s0 + n; u += gridDim.x * blockDim.x)
+    q64[u] = scaled ? x64[u] / c64[u] : x64[u];
+}
+
 }  // namespace sgpu
 
 namespace sgpu {
@@ -1344,6 +1353,7 @@ struct HostInst {
   int Nc = 0;
   std::vector<int> dev2cell, Nk, ctop, coff;  // device column -> cell; per cell Nk/ctop; device column -> relative slot
   std::vector<HostTile> tiles;
+  long long unk = 0;                          // pressure unknowns: sum of Nk - ctop over computational cells
 };
 
 }  // namespace sgpu
@@ -1364,8 +1374,18 @@ struct sgpu_batch {
   int max_inst = 0, max_tiles = 0;
   Arena slots, cols, eslots, hdrs;
   std::vector<HostInst> inst;
-  std::vector<BInst> h_inst;
-  bool pending_setup = false;
+  BInst* h_inst = nullptr;         // pinned, max_inst entries
+  TileDesc* h_tiles = nullptr;     // pinned, max_tiles entries
+  int* h_tinst = nullptr;          // pinned
+  int* h_gflags = nullptr;         // pinned [4]
+  double* h_stage = nullptr;       // pinned staging for re-submitted right-hand sides
+  long long h_stage_n = 0;
+  std::vector<int> n_before;
+  // CUDA graph of the launch sequence (tables in, kernel, instance table out)
+  bool use_graph = false, graph_failed = false;
+  cudaGraphExec_t gexec = nullptr;
+  int g_ntiles = -1, g_ninst = -1, g_grid = -1, g_chunk = -1;
+  long long graph_launches = 0;
   // device
   std::vector<void*> allocs;
   BatchArgs a{};
@@ -1473,8 +1493,14 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   b->eslots.init(b->max_eslots);
   b->hdrs.init(b->max_hdr, 16);
   b->inst.resize(max_instances);
-  b->h_inst.assign(max_instances, BInst{});
+  b->n_before.assign(max_instances, 0);
   Guard g(device);
+  BCK(cudaMallocHost((void**)&b->h_inst, sizeof(BInst) * max_instances));
+  std::memset(b->h_inst, 0, sizeof(BInst) * max_instances);
+  BCK(cudaMallocHost((void**)&b->h_tiles, sizeof(TileDesc) * ((size_t)b->max_tiles + 1)));
+  std::memset(b->h_tiles, 0xff, sizeof(TileDesc) * ((size_t)b->max_tiles + 1));
+  BCK(cudaMallocHost((void**)&b->h_tinst, sizeof(int) * ((size_t)b->max_tiles + 1)));
+  BCK(cudaMallocHost((void**)&b->h_gflags, 4 * sizeof(int)));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   BCK(cudaEventCreate(&b->ev0));
   BCK(cudaEventCreate(&b->ev1));
@@ -1547,8 +1573,14 @@ int sgpu_batch_destroy(sgpu_batch* b) {
   {
     Guard g(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
     for (void* p : b->allocs) cudaFree(p);
     if (b->h_ctl) cudaFreeHost(b->h_ctl);
+    if (b->h_inst) cudaFreeHost(b->h_inst);
+    if (b->h_tiles) cudaFreeHost(b->h_tiles);
+    if (b->h_tinst) cudaFreeHost(b->h_tinst);
+    if (b->h_gflags) cudaFreeHost(b->h_gflags);
+    if (b->h_stage) cudaFreeHost(b->h_stage);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -1771,8 +1803,8 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   I.resnorm = resnorm;
   I.state = INST_SETUP;
   I.status = SGPU_OK;
+  for (int j = 0; j < cd[1]; ++j) H.unk += g->Nk[H.dev2cell[j]] - ctop[H.dev2cell[j]];
   b->inst[id] = std::move(H);
-  b->pending_setup = true;
   *id_out = id;
   return SGPU_OK;
 }
@@ -1782,39 +1814,40 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
 int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long long* unknown_iters) {
   if (!b) return SGPU_BAD_ARG;
   Guard gd(b->device);
-  std::vector<TileDesc> tiles;
-  std::vector<int> tinst;
+  int ntiles = 0;
   int ninst = 0;
-  std::vector<int> n_before(b->max_inst, 0);
+  bool tiles_changed = false;
   for (int i = 0; i < b->max_inst; ++i) {
     HostInst& H = b->inst[i];
     BInst& I = b->h_inst[i];
     if (!H.live) continue;
     ninst = i + 1;
+    b->n_before[i] = (I.state == INST_RUN) ? I.n : 0;
     if (I.state != INST_SETUP && I.state != INST_RUN) {
       I.t0 = I.t1 = 0;
       continue;
     }
-    n_before[i] = I.state == INST_RUN ? I.n : 0;
-    I.t0 = (int)tiles.size();
+    if (I.t0 != ntiles) tiles_changed = true;
+    I.t0 = ntiles;
     for (const HostTile& T : H.tiles) {
-      TileDesc d;
-      d.hdr = (int)(H.h_off + T.hdr);
+      if (ntiles >= b->max_tiles) return bfail(b, SGPU_OOM, "too many tiles");
+      TileDesc& d = b->h_tiles[ntiles];
+      const int nb = (int)(H.h_off + T.hdr), base = (int)(H.s_off + T.base);
+      if (d.hdr != nb || d.base != base || d.inst != i) tiles_changed = true;
+      d.hdr = nb;
       d.hdr_bytes = T.hdr_bytes;
-      d.base = (int)(H.s_off + T.base);
+      d.base = base;
       d.nslots = T.nslots;
       d.inst = i;
       d.c0 = (int)(H.c_off + T.c0);
       d.c1 = (int)(H.c_off + T.c1);
       d.pad = 0;
-      tiles.push_back(d);
-      tinst.push_back(i);
+      b->h_tinst[ntiles] = i;
+      ++ntiles;
     }
-    I.t1 = (int)tiles.size();
+    I.t1 = ntiles;
     I.cnt = 0;
   }
-  const int ntiles = (int)tiles.size();
-  if (ntiles > b->max_tiles) return bfail(b, SGPU_OOM, "too many tiles");
   if (ntiles == 0) {
     if (running) *running = 0;
     if (ms) *ms = 0;
@@ -1827,32 +1860,88 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
   grid = std::max(1, std::min(grid, ntiles));
   if ((ntiles + grid - 1) / grid > kListCap)
     return bfail(b, SGPU_OOM, "%d tiles exceed %d per CTA at %d CTAs", ntiles, kListCap, grid);
-  b->ntiles = ntiles;
-  BCK(cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice, b->stream));
-  BCK(cudaMemcpyAsync(b->d_tile_inst, tinst.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, b->stream));
-  BCK(cudaMemcpyAsync(b->d_inst, b->h_inst.data(), sizeof(BInst) * ninst, cudaMemcpyHostToDevice, b->stream));
   std::memset(b->h_ctl, 0, sizeof(SolveCtl));
   b->h_ctl->timeout_ns = b->timeout_ns;
-  BCK(cudaMemcpyAsync(b->d_ctl, b->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, b->stream));
-  int any_run = 0;
-  for (int i = 0; i < ninst; ++i) any_run |= (b->inst[i].live && b->h_inst[i].state == INST_RUN);
-  int gfl[4] = {0, 0, 0, any_run};
-  BCK(cudaMemcpyAsync(b->d_gflags, gfl, sizeof gfl, cudaMemcpyHostToDevice, b->stream));
-  BatchArgs a = b->a;
-  a.F = b->F;
-  a.ntiles = ntiles;
-  a.ninst = ninst;
-  a.max_iters_chunk = max_iters > 0 ? max_iters : 0x7fffffff;
-  a.delta2 = b->delta * b->delta;
-  int do_setup = b->pending_setup ? 1 : 0;
-  void* args[] = {(void*)&a, (void*)&do_setup};
-  BCK(cudaEventRecord(b->ev0, b->stream));
-  BCK(cudaLaunchCooperativeKernel(kernel_of(b->qprecond), dim3(grid), dim3(kThreads), args, kDynSmem, b->stream));
-  BCK(cudaEventRecord(b->ev1, b->stream));
-  BCK(cudaMemcpyAsync(b->h_inst.data(), b->d_inst, sizeof(BInst) * ninst, cudaMemcpyDeviceToHost, b->stream));
-  BCK(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, b->stream));
-  BCK(cudaStreamSynchronize(b->stream));
-  b->pending_setup = false;
+  int any_run = 0, any_setup = 0;
+  for (int i = 0; i < ninst; ++i) {
+    if (!b->inst[i].live) continue;
+    any_run |= b->h_inst[i].state == INST_RUN;
+    any_setup |= b->h_inst[i].state == INST_SETUP;
+  }
+  b->h_gflags[0] = 0;
+  b->h_gflags[1] = any_setup;
+  b->h_gflags[2] = 0;
+  b->h_gflags[3] = any_run;
+  const int chunk = max_iters > 0 ? max_iters : 0x7fffffff;
+  const bool key_same = b->g_ntiles == ntiles && b->g_ninst == ninst && b->g_grid == grid && b->g_chunk == chunk &&
+                        !tiles_changed;
+  cudaStream_t st = b->stream;
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(b->d_tiles, b->h_tiles, sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(b->d_tile_inst, b->h_tinst, sizeof(int) * ntiles, cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(b->d_inst, b->h_inst, sizeof(BInst) * ninst, cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(b->d_ctl, b->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(b->d_gflags, b->h_gflags, 4 * sizeof(int), cudaMemcpyHostToDevice, st))) return e;
+    BatchArgs a = b->a;
+    a.F = b->F;
+    a.ntiles = ntiles;
+    a.ninst = ninst;
+    a.max_iters_chunk = chunk;
+    a.delta2 = b->delta * b->delta;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kDynSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {(void*)&a};
+    if ((e = cudaLaunchKernelExC(&cfg, kernel_of(b->qprecond), args))) return e;
+    if ((e = cudaMemcpyAsync(b->h_inst, b->d_inst, sizeof(BInst) * ninst, cudaMemcpyDeviceToHost, st))) return e;
+    return cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, st);
+  };
+  BCK(cudaEventRecord(b->ev0, st));
+  bool launched = false;
+  if (b->use_graph) {
+    if (!(b->gexec && key_same)) {
+      if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+      }
+      cudaGraph_t gph = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = enqueue();
+        e = cudaStreamEndCapture(st, &gph);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, gph, 0);
+      if (gph) cudaGraphDestroy(gph);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        b->gexec = nullptr;
+        b->use_graph = false;  // capture not available: launch directly from now on
+        b->graph_failed = true;
+      } else {
+        b->g_ntiles = ntiles;
+        b->g_ninst = ninst;
+        b->g_grid = grid;
+        b->g_chunk = chunk;
+      }
+    }
+    if (b->gexec) {
+      BCK(cudaGraphLaunch(b->gexec, st));
+      launched = true;
+      ++b->graph_launches;
+    }
+  }
+  if (!launched) BCK(enqueue());
+  BCK(cudaEventRecord(b->ev1, st));
+  BCK(cudaStreamSynchronize(st));
   float fms = 0.f;
   cudaEventElapsedTime(&fms, b->ev0, b->ev1);
   b->last_ms = fms;
@@ -1864,10 +1953,7 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     if (!b->inst[i].live) continue;
     const BInst& I = b->h_inst[i];
     run += I.state == INST_RUN || I.state == INST_SETUP;
-    long long unk = 0;
-    const HostInst& H = b->inst[i];
-    for (int j = 0; j < H.ncomp; ++j) unk += H.Nk[H.dev2cell[j]] - H.ctop[H.dev2cell[j]];
-    work += unk * (long long)(I.n - n_before[i]);
+    work += b->inst[i].unk * (long long)(I.n - b->n_before[i]);
   }
   b->last_work = work;
   if (running) *running = run;
@@ -1889,9 +1975,7 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
     st->eps0 = I.eps0;
     st->ms_solve = b->last_ms;
     st->ms_total = 0;
-    long long unk = 0;
-    for (int j = 0; j < H.ncomp; ++j) unk += H.Nk[H.dev2cell[j]] - H.ctop[H.dev2cell[j]];
-    st->unknowns = unk;
+    st->unknowns = H.unk;
   }
   if (q) {
     if (I.state != INST_DONE) return bfail(b, SGPU_BAD_ARG, "instance %d has not finished", id);
@@ -1919,6 +2003,55 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
   }
   return SGPU_OK;
 }
+
+// Re-submits a finished instance.  src (jagged rows of Nk[i] doubles, cell
+// order) replaces the right-hand side, or NULL keeps the resident one; with
+// warm != 0 the last solution becomes the initial guess (as phys->qc is in the
+// model), otherwise the originally uploaded initial guess is used again.  The
+// grid and coefficients stay resident.
+int sgpu_batch_resubmit(sgpu_batch* b, int id, const double* const* src, double qepsilon, int qmaxiters, int warm) {
+  if (!b || id < 0 || id >= b->max_inst || !b->inst[id].live) return SGPU_BAD_ARG;
+  HostInst& H = b->inst[id];
+  BInst& I = b->h_inst[id];
+  if (I.state != INST_DONE) return bfail(b, SGPU_BAD_ARG, "instance %d is still running", id);
+  Guard gd(b->device);
+  const int n = (int)H.n3c;
+  if (warm) {
+    finalize_q_kernel<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, b->stream>>>(
+        b->a.x64, b->a.c64, b->d_q64, (int)H.s_off, n, b->qprecond == 1);
+    BCK(cudaGetLastError());
+  }
+  if (src) {
+    if (b->h_stage_n < H.n3c) {
+      if (b->h_stage) cudaFreeHost(b->h_stage);
+      b->h_stage = nullptr;
+      BCK(cudaMallocHost((void**)&b->h_stage, sizeof(double) * H.n3c));
+      b->h_stage_n = H.n3c;
+    }
+    std::fill(b->h_stage, b->h_stage + H.n3c, 0.0);
+    for (int j = 0; j < H.ncomp; ++j) {
+      const int i = H.dev2cell[j];
+      std::memcpy(b->h_stage + H.coff[j], src[i], sizeof(double) * H.Nk[i]);
+    }
+    BCK(cudaMemcpyAsync(b->d_src64 + H.s_off, b->h_stage, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
+  }
+  if (warm || src) BCK(cudaStreamSynchronize(b->stream));
+  I.tol2 = qepsilon * qepsilon;
+  I.maxiters = qmaxiters;
+  I.state = INST_SETUP;
+  I.status = SGPU_OK;
+  I.n = 0;
+  I.flags = 0;
+  return SGPU_OK;
+}
+
+int sgpu_batch_use_graph(sgpu_batch* b, int on) {
+  if (!b) return SGPU_BAD_ARG;
+  b->use_graph = on != 0 && !b->graph_failed;
+  return b->use_graph ? 1 : 0;
+}
+
+long long sgpu_batch_graph_launches(const sgpu_batch* b) { return b ? b->graph_launches : -1; }
 
 int sgpu_batch_state(const sgpu_batch* b, int id) {
   if (!b || id < 0 || id >= b->max_inst || !b->inst[id].live) return -1;

@@ -315,3 +315,49 @@ def make_h_problem(g: SunGrid, seed=0, sigma_eta=0.01, bdy_sigma=0.01) -> HProbl
     htmp[bdy] = 0.0
     D = np.add.reduceat(g.dzf, g.eoff[:-1]) if g.Ne > 0 else np.zeros(0)
     return HProblem(grid=g, D=np.ascontiguousarray(D, dtype=F64), htmp=htmp, h=h)
+
+
+# ----------------------------------------------------------------------------
+# families of problems for the batched and serving workloads
+# ----------------------------------------------------------------------------
+CELL_AREA = 500.0   # m^2 per triangle, as in the 200k-point, 20 km x 10 km seamount grid
+
+
+def bump_grid(nc_target: int, Nkmax: int, seed: int, aspect: float = 2.0, H0: float = 60.0, amp: float = 50.0,
+              rstretch: float = 1.02):
+    """Delaunay grid of ~nc_target triangles in an aspect:1 rectangle with a
+    centred Gaussian bump (depth H0 - amp at the top, H0 far away)."""
+    npts = max(8, int(nc_target) // 2)
+    Ly = float(np.sqrt(CELL_AREA * nc_target / aspect))
+    Lx = aspect * Ly
+    return delaunay_seamount(npts, Lx, Ly, Nkmax=Nkmax, rstretch=rstretch, seed=seed, H0=H0, amp=amp,
+                             sigma=Lx / 6.0, h_sigma=0.01)
+
+
+def batch_instances(n=256, seed=4, nc_range=(2000, 50000), nkmax_choices=(10, 20, 40)):
+    """Independent problems with Nc log-uniform in nc_range and Nkmax drawn from
+    nkmax_choices, each with its own seeded divergence right-hand side."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(nc_range[0]), np.log(nc_range[1])
+    out = []
+    for k in range(n):
+        nc = int(np.exp(rng.uniform(lo, hi)))
+        nkmax = int(rng.choice(nkmax_choices))
+        g = bump_grid(nc, nkmax, seed=int(rng.integers(1 << 30)))
+        out.append(make_q_problem(g, seed=int(rng.integers(1 << 30)), sigma_u=0.05, dt=20.0))
+    return out
+
+
+def serving_pool(n=24, seed=5, nc_range=(1000, 200000), nkmax_range=(10, 60), rhs_per_grid=2):
+    """A pool of seeded grids (Nc log-uniform, Nkmax uniform) with a few
+    seeded right-hand sides each; requests draw (grid, rhs) pairs from it."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(nc_range[0]), np.log(nc_range[1])
+    pool = []
+    for k in range(n):
+        nc = int(np.exp(rng.uniform(lo, hi)))
+        nkmax = int(rng.integers(nkmax_range[0], nkmax_range[1] + 1))
+        g = bump_grid(nc, nkmax, seed=int(rng.integers(1 << 30)))
+        rhs = [make_q_problem(g, seed=int(rng.integers(1 << 30)), sigma_u=0.05, dt=20.0) for _ in range(rhs_per_grid)]
+        pool.append(rhs)
+    return pool
