@@ -1,22 +1,40 @@
 """Benchmark of the SUNTANS elliptic hot path on GB300.
 
-Workload (default, the plain FP64 method at scale): Delaunay triangulation of
-200,000 seeded uniform random points in a 20 km x 10 km rectangle (~400k
-triangles), Gaussian seamount (50 m - 30 m exp(-r^2/(2*2000^2))), partial-cell
-z-levels Nkmax = 50 stretched 1.02 downward; pressure right-hand side = the
-divergence of a seeded N(0, 0.05 m/s) face velocity; free-surface right-hand
-side from a seeded N(0, 0.01 m) perturbation.  One step = one CGSolveQ
-(qprecond 1) plus one CGSolve (hprecond 1), each to a 1e-10 relative residual,
-in FP64.
+Workloads (--workload):
+
+  cfg2 (default)  the plain FP64 method at scale: Delaunay triangulation of
+        200,000 seeded uniform random points in a 20 km x 10 km rectangle
+        (~400k triangles), Gaussian seamount (50 m - 30 m exp(-r^2/(2*2000^2))),
+        partial-cell z-levels Nkmax = 50 stretched 1.02 downward; pressure
+        right-hand side = the divergence of a seeded N(0, 0.05 m/s) face
+        velocity; free-surface right-hand side from a seeded N(0, 0.01 m)
+        perturbation.  One step = one CGSolveQ (qprecond 1) plus one CGSolve
+        (hprecond 1), each to a 1e-10 relative residual, in FP64.  The line
+        also carries "mixed_form": the same pressure problem through the
+        mixed-precision batched solver (one instance), against the FP64 solve.
+  cfg1  the 64x16 quad channel (1024 cells, Nkmax 32), FP64.
+  cfg3  mixed precision at 1M triangles (500k points, 50 km x 25 km, Nkmax 40,
+        ~4e7 unknowns): one pressure solve per step; errors against the FP64
+        GPU solve of the same problem (itself matched to the oracle).
+  cfg4  256 independent problems (Nc log-uniform in [2k, 50k], aspect 2,
+        Gaussian bump 10-60 m, Nkmax in {10, 20, 40}) in one persistent launch
+        under a CUDA graph, launch shape from the autotuner; against a loop of
+        the plain FP64 solver over the same problems.
+  cfg5  serving: open-loop Poisson arrivals at 2000 requests/s drawn from a
+        seeded pool of grids (Nc log-uniform in [1k, 200k], Nkmax uniform in
+        [10, 60]), tolerance from {1e-8, 1e-10}, warm starts from the resident
+        previous solution, admission by a 150 GB HBM budget; p50/p99 latency,
+        and again at a rate the measured capacity sustains.
 
 Metric: unknown-iterations per second = sum over the step's solves of
-(unknowns x iterations) / time.  `value` is measured on inputs already
-resident in HBM (sgpu_q_solve / sgpu_h_solve) with CUDA events on the solver
-stream; `e2e` goes through the drop-in C ABI calls with host jagged arrays
-(sgpu_cgsolveq / sgpu_cgsolve), copies included.
+(unknowns x iterations) / time.  For the mixed-precision forms `value` counts
+the FP64 solver's iteration count for the same problem ("equivalent"), and the
+executed inner iterations are reported beside it.  `value` is measured on
+inputs already resident in HBM with CUDA events on the solver stream; `e2e`
+goes through the public C ABI with host arrays, copies included.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg2|cfg1] [--qprecond 0|1|2]
+                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5] [--qprecond 0|1|2]
 """
 from __future__ import annotations
 
@@ -59,7 +77,16 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
+    ap.add_argument("--no-mixed", action="store_true", help="cfg2: skip the mixed_form measurement")
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--drain-seconds", type=float, default=30.0)
+    ap.add_argument("--pool", type=int, default=64)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--chunk", type=int, default=32)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--qprecond", type=int, default=1)
     ap.add_argument("--points", type=int, default=200_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -288,6 +315,17 @@ def run_ours(args):
             "e2e": {"value": e2e_work / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 2 * args.steps, "clocks": clocks}
+    if args.workload == "cfg2" and not args.no_mixed:
+        # the same pressure problem through the mixed-precision batched solver
+        q64 = ctx.q_download(qp.q)
+        it64 = int(np.median(nq))
+        mf, _, _ = mixed_form(qp, props.qprecond, max(2, min(args.steps, 5)), 3, props.qepsilon, props.qmaxiters,
+                              local, q64, it64)
+        plain_q_rate = g.n_q() * it64 / (q_launch_ms / 1e3)
+        mf["plain_fp64_q_unknown_iters_per_s"] = plain_q_rate
+        mf["speedup_vs_plain_fp64"] = mf["equivalent_unknown_iters_per_s"] / plain_q_rate
+        mf["roofline_frac_fp32_inner"] = mf["achieved_gbs_fp32_inner"] / peak
+        line["mixed_form"] = mf
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g, qp, hp, props, args.cpu_seconds)
     if rank == 0:
@@ -296,11 +334,298 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
 
+# ---------------------------------------------------------------------------
+# mixed-precision forms (batched engine)
+# ---------------------------------------------------------------------------
+FP32_BYTES_PER_UNKNOWN_ITER = 4 * (12 + 3)   # s(12+F) with s = 4, triangles, qprecond 0/1
+
+
+def rel_errors(q, q64, g):
+    """Relative L2 and max errors of q against q64 over the active levels."""
+    m = g.active_mask()
+    d = (q - q64)[m]
+    ref = q64[m]
+    return {"rel_l2": float(np.linalg.norm(d) / max(np.linalg.norm(ref), 1e-300)),
+            "max_abs_rel": float(np.abs(d).max() / max(np.abs(ref).max(), 1e-300)) if d.size else 0.0}
+
+
+def batch_timed(b, ids, steps, warmup, tol, maxiters, device):
+    """Cold-start solves of every resident problem (set-up included), W untimed
+    then K timed with CUDA events on the batch stream.  Returns (ms_total, per_step_ms, clocks)."""
+    import torch
+    stream = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", device))
+
+    def step(first):
+        if not first:
+            for i in ids:
+                b.resubmit(i, None, tol=tol, maxiters=maxiters, warm=False)
+        run, ms, _ = b.run()
+        assert run == 0
+        return ms
+
+    for w in range(warmup):
+        step(w == 0)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(device)
+    sampler.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    per = [step(warmup == 0 and k == 0) for k in range(steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    return ev0.elapsed_time(ev1), per, clocks
+
+
+def mixed_form(prob, qprecond, steps, warmup, tol, maxiters, device, q64=None, iters64=None):
+    """One problem through the batched mixed-precision solver: timing, iterations, errors."""
+    from suntans_gb300.batch import Batch, capacity_for
+    g = prob.grid
+    b = Batch(qprecond=qprecond, maxfaces=g.maxfaces, device=device, **capacity_for([g]))
+    try:
+        b.use_graph(True)
+        iid = b.add(prob, tol=tol, maxiters=maxiters)
+        ms_total, per, clocks = batch_timed(b, [iid], steps, max(warmup, 1), tol, maxiters, device)
+        q, st = b.result(iid, prob.q, release=False)
+    finally:
+        b.close()
+    t = ms_total / steps / 1e3
+    N = g.n_q()
+    out = {"ms_per_solve": ms_total / steps, "iters_inner": int(st.niters), "status": int(st.status),
+           "raw_unknown_iters_per_s": N * st.niters / t}
+    if iters64 is not None:
+        out["iters_fp64"] = int(iters64)
+        out["equivalent_unknown_iters_per_s"] = N * iters64 / t
+    if q64 is not None:
+        out.update(rel_errors(q, q64, g))
+    out["achieved_gbs_fp32_inner"] = N * st.niters * FP32_BYTES_PER_UNKNOWN_ITER / t / 1e9
+    return out, clocks, q
+
+
+def _props(qprecond, tol=1e-10, maxiters=20000):
+    from suntans_gb300.grid import SolverProps
+    return SolverProps(qprecond=qprecond, qmaxiters=maxiters, qepsilon=tol, hprecond=1, maxiters=maxiters,
+                       epsilon=tol, resnorm=1.0, dt=20.0, theta=0.55)
+
+
+def bench_cfg3(args):
+    from suntans_gb300 import gridgen as gg
+    from suntans_gb300.batch import Batch, capacity_for
+    from suntans_gb300.capi import Context
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    g = gg.delaunay_seamount(500_000, 50_000.0, 25_000.0, Nkmax=40, rstretch=1.02, seed=3, H0=50.0, amp=30.0,
+                             sigma=2000.0, h_sigma=0.01)
+    qp = gg.make_q_problem(g, seed=13, sigma_u=0.05, dt=20.0)
+    props = _props(args.qprecond)
+    N = g.n_q()
+    # FP64 plain solve of the same problem: iteration count, reference solution, plain rate
+    ctx = Context(g, device=local)
+    ctx.q_upload(qp)
+    ctx.q_solve(props)
+    s64 = ctx.q_solve(props)
+    q64 = ctx.q_download(qp.q)
+    plain_rate = N * s64.niters / (s64.ms_solve / 1e3)
+    ctx.close()
+    mf, clocks, _ = mixed_form(qp, args.qprecond, args.steps, args.warmup, 1e-10, 20000, local, q64, s64.niters)
+    peak, peak_kind = peaks()
+    # end to end through the public API: add (host arrays in), solve, result (host array out)
+    t0 = time.perf_counter()
+    b = Batch(qprecond=args.qprecond, maxfaces=g.maxfaces, device=local, **capacity_for([g]))
+    iid = b.add(qp, tol=1e-10, maxiters=20000)
+    b.run()
+    q, st = b.result(iid, qp.q)
+    e2e_s = time.perf_counter() - t0
+    b.close()
+    h2d = 8 * (4 * g.n3 + int(g.Nke.sum()) + g.Ne) + 4 * g.Nc
+    line = {"metric": "Poisson CG unknown-iters/s (equivalent: FP64 iteration count, 1e-10 relative residual)",
+            "value": mf["equivalent_unknown_iters_per_s"], "unit": "unknown-iters/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": mf["ms_per_solve"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+            "data": "synthetic (seeded grid and right-hand side)",
+            "config": {"workload": "Delaunay seamount, 500000 random points in 50x25 km, Nkmax=40, mixed precision",
+                       "cells": g.Nc, "N_q": N, "qprecond": args.qprecond, "tolerance": 1e-10,
+                       "l2": "not flushed: working set > 129 MB L2"},
+            "mixed": mf, "plain_fp64_unknown_iters_per_s": plain_rate, "iters_fp64": int(s64.niters),
+            "speedup_vs_plain_fp64": mf["equivalent_unknown_iters_per_s"] / plain_rate,
+            "roofline": {"bound": "hbm", "achieved": mf["achieved_gbs_fp32_inner"], "peak": peak, "unit": "GB/s",
+                         "frac": mf["achieved_gbs_fp32_inner"] / peak, "traffic": None,
+                         "kernel": f"batch_kernel<{args.qprecond}>",
+                         "bytes_per_unknown_iter": FP32_BYTES_PER_UNKNOWN_ITER, "peak_kind": peak_kind},
+            "e2e": {"value": N * st.niters / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 8 * N},
+            "gpu_launches": args.steps, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(g, qp, None, props, args.cpu_seconds)
+    return line
+
+
+def bench_cfg4(args):
+    import torch
+    from suntans_gb300 import gridgen as gg
+    from suntans_gb300.autotune import autotune, sm_count
+    from suntans_gb300.batch import Batch, capacity_for
+    from suntans_gb300.capi import Context
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    tol, maxiters = 1e-10, 20000
+    probs = gg.batch_instances(n=args.instances, seed=4, workers=None)
+    grids = [p.grid for p in probs]
+    Ns = np.array([g.n_q() for g in grids], dtype=np.float64)
+    props = _props(args.qprecond, tol, maxiters)
+    # loop of the plain FP64 solver over the problems (inputs resident, one context each)
+    ctxs = []
+    for p in probs:
+        c = Context(p.grid, device=local)
+        c.q_upload(p)
+        ctxs.append(c)
+    for c in ctxs:
+        c.q_solve(props)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    it64, dev_ms = [], 0.0
+    for c in ctxs:
+        s = c.q_solve(props)
+        it64.append(s.niters)
+        dev_ms += s.ms_solve
+    loop_s = time.perf_counter() - t0
+    q64 = [c.q_download(p.q) for c, p in zip(ctxs, probs)]
+    for c in ctxs:
+        c.close()
+    it64 = np.array(it64, dtype=np.float64)
+    plain_rate = float((Ns * it64).sum() / loop_s)
+    # launch shape
+    if args.no_autotune:
+        best, table = {"ctas_per_sm": 3, "tile_slots": 1024}, []
+    else:
+        best, table = autotune(probs, qprecond=args.qprecond, tol=tol, maxiters=maxiters, device=local)
+
+    def make_batch():
+        b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
+        b.set(ctas=best["ctas_per_sm"] * sm_count(local))
+        b.set_tile_slots(best["tile_slots"])
+        return b
+
+    b = make_batch()
+    graph = b.use_graph(True)
+    ids = [b.add(p, tol=tol, maxiters=maxiters) for p in probs]
+    ms_total, per, clocks = batch_timed(b, ids, args.steps, args.warmup, tol, maxiters, local)
+    res = [b.result(i, p.q, release=False) for i, p in zip(ids, probs)]
+    graph_launches = b.graph_launches()
+    b.close()
+    itm = np.array([st.niters for _, st in res], dtype=np.float64)
+    t = ms_total / args.steps / 1e3
+    equiv = float((Ns * it64).sum() / t)
+    raw = float((Ns * itm).sum() / t)
+    errs = [rel_errors(q, r, g) for (q, _), r, g in zip(res, q64, grids)]
+    ach = float((Ns * itm).sum() * FP32_BYTES_PER_UNKNOWN_ITER / t / 1e9)
+    peak, peak_kind = peaks()
+    # end to end: the public API with host arrays (add, one launch, result per problem)
+    t0 = time.perf_counter()
+    b = make_batch()
+    ids = [b.add(p, tol=tol, maxiters=maxiters) for p in probs]
+    b.run()
+    e2e_work = sum(g.n_q() * b.result(i, p.q)[1].niters for i, p, g in zip(ids, probs, grids))
+    e2e_s = time.perf_counter() - t0
+    b.close()
+    h2d = sum(8 * (4 * g.n3 + int(g.Nke.sum()) + g.Ne) + 4 * g.Nc for g in grids)
+    line = {"metric": "Poisson CG unknown-iters/s (equivalent: FP64 iteration count, 1e-10 relative residual)",
+            "value": equiv, "unit": "unknown-iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+            "data": "synthetic (seeded grids and right-hand sides)",
+            "config": {"workload": f"{len(probs)} Delaunay bump grids, Nc log-uniform in [2k, 50k], Nkmax in "
+                                   "{10,20,40}, one persistent launch under a CUDA graph",
+                       "instances": len(probs), "N_q_total": int(Ns.sum()), "qprecond": args.qprecond,
+                       "tolerance": tol, "l2": f"not flushed: working set {(Ns.sum() * 60 / 1e9):.1f} GB > 129 MB L2",
+                       "launch_shape": best, "graph": bool(graph), "graph_launches": int(graph_launches)},
+            "raw_unknown_iters_per_s": raw, "plain_fp64_loop_unknown_iters_per_s": plain_rate,
+            "plain_fp64_loop_device_ms": dev_ms, "plain_fp64_loop_wall_ms": loop_s * 1e3,
+            "speedup_vs_plain_fp64_loop": equiv / plain_rate,
+            "iters_inner_over_fp64": float(itm.sum() / it64.sum()),
+            "errors": {"max_rel_l2": max(e["rel_l2"] for e in errs),
+                       "max_abs_rel": max(e["max_abs_rel"] for e in errs),
+                       "status_ok": int(sum(st.status == 0 for _, st in res))},
+            "autotune": table,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None, "kernel": f"batch_kernel<{args.qprecond}>",
+                         "bytes_per_unknown_iter": FP32_BYTES_PER_UNKNOWN_ITER, "peak_kind": peak_kind},
+            "e2e": {"value": e2e_work / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": int(8 * Ns.sum())},
+            "gpu_launches": args.steps, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        k = int(np.argsort(Ns)[len(Ns) // 2])
+        line["cpu_baseline"] = cpu_baseline(grids[k], probs[k], None, props, args.cpu_seconds)
+        line["cpu_baseline"]["sample"] += " (the median-size problem of the set)"
+    return line
+
+
+def bench_cfg5(args):
+    from suntans_gb300 import gridgen as gg
+    from suntans_gb300.batch import Batch, capacity_for, request_bytes
+    from suntans_gb300.serve import Request, Server, latency_report, poisson_stream
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pool = gg.serving_pool(n=args.pool, seed=5, workers=None)
+    grids = [p[0].grid for p in pool]
+    need = sum(request_bytes(g, args.qprecond) for g in grids)
+    b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
+    b.use_graph(True)
+    srv = Server(pool, b, args.budget_gb * 1e9, lambda g: request_bytes(g, args.qprecond), chunk=args.chunk,
+                 maxiters=5000, keep_q=False)
+    # warm-up: one untimed request per grid (cold starts; every grid resident)
+    srv.run([Request(-1 - k, k, 0, 1e-8, 0.0) for k in range(len(pool))], realtime=False)
+    warm_launches = srv.launches
+
+    def stream(rate, seconds, seed):
+        reqs = poisson_stream(len(pool), len(pool[0]), rate, seconds, seed=seed)
+        l0, ms0 = srv.launches, srv.device_ms
+        sampler = ClockSampler(local)
+        sampler.start()
+        srv.run(reqs, realtime=True, drain_limit=seconds + args.drain_seconds)
+        clocks = sampler.stop()
+        rep = latency_report(reqs, srv.t_end)
+        rep.update(rate=rate, seconds=seconds, launches=srv.launches - l0,
+                   device_busy_frac=(srv.device_ms - ms0) / 1e3 / max(srv.t_end, 1e-9))
+        return rep, clocks, reqs
+
+    rep, clocks, reqs = stream(args.rate, args.serve_seconds, 7)
+    # again at a rate the measured capacity sustains (latency without a growing queue)
+    sus_rate = max(1.0, 0.7 * rep["served_per_s"])
+    rep2, _, _ = stream(sus_rate, max(10.0, 200.0 / sus_rate), 8)
+    b.close()
+    launches = rep["launches"]
+    line = {"metric": "Poisson CG unknown-iters/s under an open-loop request stream; p50/p99 latency",
+            "value": rep["unknown_iters_per_s"], "unit": "unknown-iters/s", "n_gpus": 1, "steps": launches,
+            "warmup": warm_launches, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+            "data": "synthetic (seeded grid pool, Poisson arrivals)",
+            "config": {"workload": f"serving: Poisson arrivals {args.rate:g}/s for {args.serve_seconds:g} s, pool of "
+                                   f"{len(pool)} grids (Nc log-uniform [1k, 200k], Nkmax uniform [10, 60]) x "
+                                   f"{len(pool[0])} right-hand sides mixed per request, tolerance from "
+                                   "{1e-8, 1e-10}, warm starts",
+                       "hbm_budget_gb": args.budget_gb, "pool_resident_gb": need / 1e9, "chunk_iters": args.chunk,
+                       "qprecond": args.qprecond, "step": "one launch of the serving loop",
+                       "drain_limit_s": args.drain_seconds},
+            "latency": rep, "latency_at_sustainable_rate": rep2, "evictions": srv.evictions,
+            "e2e": {"value": rep["unknown_iters_per_s"], "unit": "unknown-iters/s",
+                    "h2d_bytes_per_step": int(sum(8 * pool[r.grid][0].grid.n3 for r in reqs if r.t_admit >= 0)
+                                              / max(launches, 1)),
+                    "d2h_bytes_per_step": int(sum(8 * r.unknowns for r in reqs if r.t_done >= 0) / max(launches, 1))},
+            "gpu_launches": launches + srv.resubmits, "clocks": clocks}
+    return line
+
 
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in ("cfg3", "cfg4", "cfg5"):
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        import __graft_entry__
+        __graft_entry__.build()
+        fn = {"cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5}[args.workload]
+        line = fn(args)
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps(line), flush=True)
     else:
         run_ours(args)
 

@@ -205,6 +205,10 @@ long long sgpu_batch_graph_launches(const sgpu_batch *b);
 /* Tuning: reliable-update factor delta (default 0.01), CTA count (0 = full
  * wave), barrier wait limit; pass <= 0 / < 0 to keep a value. */
 int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);
+/* Tuning: storage slots per tile (4..1024, default 1024) for problems added
+ * from now on; a column longer than this still gets a tile of its own.
+ * Smaller tiles spread small problems over more CTAs. */
+int sgpu_batch_set_tile_slots(sgpu_batch *b, int tile_slots);
 void *sgpu_batch_stream(sgpu_batch *b);
 
 /* Device time of the last launch per phase (ns): [1] operator apply, [2]

@@ -66,6 +66,12 @@ class Batch:
         if rc != OK:
             raise SolverError(rc, "sgpu_batch_set")
 
+    def set_tile_slots(self, n: int):
+        """Storage slots per tile for problems added from now on (4..1024)."""
+        rc = self.lib.sgpu_batch_set_tile_slots(self.h, int(n))
+        if rc != OK:
+            raise SolverError(rc, "sgpu_batch_set_tile_slots")
+
     def add(self, prob, tol=1e-10, maxiters=5000, resnorm=1.0) -> int:
         """Uploads one pressure problem; returns its id (raises SolverError(OOM) when full)."""
         g = prob.grid
@@ -118,6 +124,13 @@ class Batch:
             self.grids.pop(i, None)
         return q, st
 
+    def release(self, i):
+        """Frees problem i's device storage without copying its result."""
+        rc = self.lib.sgpu_batch_result(self.h, int(i), None, None, 1)
+        if rc != OK:
+            raise SolverError(rc, f"sgpu_batch_result: {self.error()}")
+        self.grids.pop(i, None)
+
     def resubmit(self, i, src=None, tol=1e-10, maxiters=5000, warm=True):
         """Re-run finished problem i: new right-hand side (None keeps the resident
         one); warm=True starts from its last solution, False from the original guess."""
@@ -131,6 +144,10 @@ class Batch:
         rc = self.lib.sgpu_batch_resubmit(self.h, int(i), p, float(tol), int(maxiters), int(bool(warm)))
         if rc != OK:
             raise SolverError(rc, f"sgpu_batch_resubmit: {self.error()}")
+
+    def stream(self) -> int:
+        """The batch's cudaStream_t as an integer handle."""
+        return int(self.lib.sgpu_batch_stream(self.h) or 0)
 
     def use_graph(self, on=True) -> bool:
         return bool(self.lib.sgpu_batch_use_graph(self.h, int(on)))

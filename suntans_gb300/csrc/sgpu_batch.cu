@@ -1369,6 +1369,7 @@ struct sgpu_batch {
   std::string err;
   long long timeout_ns = 2000000000LL;
   int grid_override = 0;
+  int tile_slots = kBTSlots;  // storage slots per tile for instances added from now on
   double delta = 0.01;
   long long max_slots = 0, max_cols = 0, max_eslots = 0, max_hdr = 0;
   int max_inst = 0, max_tiles = 0;
@@ -1646,6 +1647,7 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   // tiles over the computational columns: <= kBTSlots slots, <= kBTCols columns,
   // <= kBTFaces column-faces; every tile starts on a 4-slot boundary
   const int maxc = std::min(kBTCols, kBTFaces / F);
+  const int cap = std::max(b->tile_slots, g->Nkmax);  // a column always fits a tile
   H.coff.assign(Nc + 1, 0);
   long long acc = 0, hacc = 0;
   {
@@ -1655,7 +1657,7 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
       T.c0 = j;
       T.base = (int)acc;
       int len = 0;
-      while (j < cd[1] && j - T.c0 < maxc && len + g->Nk[H.dev2cell[j]] <= kBTSlots) {
+      while (j < cd[1] && j - T.c0 < maxc && len + g->Nk[H.dev2cell[j]] <= cap) {
         H.coff[j] = (int)(acc + len);
         len += g->Nk[H.dev2cell[j]];
         ++j;
@@ -2063,6 +2065,12 @@ int sgpu_batch_set(sgpu_batch* b, double delta, int grid, long long timeout_ns) 
   if (delta > 0) b->delta = delta;
   if (grid >= 0) b->grid_override = grid;
   if (timeout_ns > 0) b->timeout_ns = timeout_ns;
+  return SGPU_OK;
+}
+
+int sgpu_batch_set_tile_slots(sgpu_batch* b, int tile_slots) {
+  if (!b || tile_slots < 4 || tile_slots > kBTSlots) return SGPU_BAD_ARG;
+  b->tile_slots = tile_slots;
   return SGPU_OK;
 }
 

@@ -23,6 +23,8 @@ on random triangulations.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from .grid import SunGrid, QProblem, HProblem, F64, I32
@@ -334,30 +336,49 @@ def bump_grid(nc_target: int, Nkmax: int, seed: int, aspect: float = 2.0, H0: fl
                              sigma=Lx / 6.0, h_sigma=0.01)
 
 
-def batch_instances(n=256, seed=4, nc_range=(2000, 50000), nkmax_choices=(10, 20, 40)):
+def _batch_instance(args):
+    nc, nkmax, gseed, qseeds = args
+    g = bump_grid(nc, nkmax, seed=gseed)
+    return [make_q_problem(g, seed=q, sigma_u=0.05, dt=20.0) for q in qseeds]
+
+
+def _build_all(params, workers):
+    """Builds the problems of `params` (in order), in `workers` spawned processes
+    when > 1 (None: one per core, at most 16).  The calling program must be a
+    file (spawned workers re-import it)."""
+    if workers is None:
+        workers = min(16, os.cpu_count() or 1)
+    if workers <= 1 or len(params) <= 1:
+        return [_batch_instance(a) for a in params]
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(min(workers, len(params))) as pool:
+        return pool.map(_batch_instance, params, chunksize=1)
+
+
+def batch_instances(n=256, seed=4, nc_range=(2000, 50000), nkmax_choices=(10, 20, 40), workers=1):
     """Independent problems with Nc log-uniform in nc_range and Nkmax drawn from
-    nkmax_choices, each with its own seeded divergence right-hand side."""
+    nkmax_choices, each with its own seeded divergence right-hand side.  The
+    seeds are drawn in order from `seed`, so the set does not depend on workers."""
     rng = np.random.default_rng(seed)
     lo, hi = np.log(nc_range[0]), np.log(nc_range[1])
-    out = []
+    params = []
     for k in range(n):
         nc = int(np.exp(rng.uniform(lo, hi)))
         nkmax = int(rng.choice(nkmax_choices))
-        g = bump_grid(nc, nkmax, seed=int(rng.integers(1 << 30)))
-        out.append(make_q_problem(g, seed=int(rng.integers(1 << 30)), sigma_u=0.05, dt=20.0))
-    return out
+        gseed = int(rng.integers(1 << 30))
+        params.append((nc, nkmax, gseed, [int(rng.integers(1 << 30))]))
+    return [r[0] for r in _build_all(params, workers)]
 
 
-def serving_pool(n=24, seed=5, nc_range=(1000, 200000), nkmax_range=(10, 60), rhs_per_grid=2):
+def serving_pool(n=24, seed=5, nc_range=(1000, 200000), nkmax_range=(10, 60), rhs_per_grid=2, workers=1):
     """A pool of seeded grids (Nc log-uniform, Nkmax uniform) with a few
     seeded right-hand sides each; requests draw (grid, rhs) pairs from it."""
     rng = np.random.default_rng(seed)
     lo, hi = np.log(nc_range[0]), np.log(nc_range[1])
-    pool = []
+    params = []
     for k in range(n):
         nc = int(np.exp(rng.uniform(lo, hi)))
         nkmax = int(rng.integers(nkmax_range[0], nkmax_range[1] + 1))
-        g = bump_grid(nc, nkmax, seed=int(rng.integers(1 << 30)))
-        rhs = [make_q_problem(g, seed=int(rng.integers(1 << 30)), sigma_u=0.05, dt=20.0) for _ in range(rhs_per_grid)]
-        pool.append(rhs)
-    return pool
+        gseed = int(rng.integers(1 << 30))
+        params.append((nc, nkmax, gseed, [int(rng.integers(1 << 30)) for _ in range(rhs_per_grid)]))
+    return _build_all(params, workers)

@@ -1,0 +1,220 @@
+"""Serving loop for pressure solves: continuous batching over the batched solver.
+
+Requests (grid, right-hand side, tolerance) arrive over time.  Every grid a
+request names becomes a resident problem of one `Batch`: its connectivity,
+coefficients and last solution stay in HBM, and the next request on the same
+grid only uploads its right-hand side and starts from that solution (the warm
+start the model itself uses: CGSolveQ begins from the previous phys->qc,
+main/phys.c:2411-2550).  The device runs one persistent launch of at most
+`chunk` CG iterations over every active problem; between launches the host
+harvests finished problems and admits requests that arrived meanwhile, so new
+work joins the running batch at the next launch instead of waiting for it to
+drain.
+
+Admission is by HBM budget: a grid becomes resident only while the bytes of
+all resident grids (`request_bytes`) stay within the budget and the batch's
+arenas have room; otherwise idle resident grids are evicted least recently
+used first, and when nothing is evictable the request waits.  Requests on one
+grid run one at a time in arrival order, so the warm-start chain of a grid
+does not depend on what else is in flight: a result is the same alone and in
+any mix (the batched kernel is composition-independent bit for bit).
+
+A request's right-hand side is (1 - mix) x rhs_j + mix x rhs_(j+1) of its
+grid's stored right-hand sides.  With the reference's relative stopping rule
+(sqrt(eps/eps0) < tol, eps0 from the initial guess) a warm start from the
+solution of the very same right-hand side would ask for a residual below
+round-off, so streams draw mix per request.
+
+The engine is duck-typed (`Batch` or a host fake with the same methods), so
+the scheduling logic is testable without a GPU.
+"""
+from __future__ import annotations
+
+import collections
+import dataclasses
+import time
+
+import numpy as np
+
+from .capi import OOM, SolverError
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    grid: int            # index into the grid pool
+    rhs: int             # index of the right-hand side among the grid's problems
+    tol: float
+    t_arrival: float     # seconds from the start of the stream
+    mix: float = 0.0     # weight of the next stored right-hand side
+    t_admit: float = -1.0
+    t_done: float = -1.0
+    iters: int = 0
+    status: int = -1
+    unknowns: int = 0
+    launch_done: int = -1  # serving-loop launch after which the result was harvested
+    warm: bool = False     # started from the grid's resident previous solution
+    q: np.ndarray | None = None
+
+
+def poisson_stream(n_grids, rhs_per_grid, rate, seconds, seed=7, tols=(1e-8, 1e-10)):
+    """Open-loop Poisson arrivals: exponential gaps at `rate`/s for `seconds`,
+    each request a uniformly drawn (grid, right-hand side, mix, tolerance)."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        out.append(Request(len(out), int(rng.integers(n_grids)), int(rng.integers(rhs_per_grid)),
+                           float(tols[int(rng.integers(len(tols)))]), t, mix=float(rng.uniform())))
+    return out
+
+
+def request_src(pool, r: Request):
+    probs = pool[r.grid]
+    p = probs[r.rhs]
+    if r.mix == 0.0 or len(probs) < 2:
+        return p.src
+    o = probs[(r.rhs + 1) % len(probs)]
+    return (1.0 - r.mix) * p.src + r.mix * o.src
+
+
+class Server:
+    """pool[g] is a list of QProblem on grid g (its stored right-hand sides)."""
+
+    def __init__(self, pool, engine, budget_bytes, request_bytes, chunk=64, maxiters=20000, keep_q=True,
+                 clock=time.perf_counter):
+        self.pool = pool
+        self.engine = engine
+        self.budget = float(budget_bytes)
+        self.rbytes = [int(request_bytes(p[0].grid)) for p in pool]
+        self.chunk = int(chunk)
+        self.maxiters = int(maxiters)
+        self.keep_q = keep_q
+        self.clock = clock
+        self.resident = collections.OrderedDict()  # grid -> instance id (LRU order)
+        self.busy = {}                             # grid -> Request in flight
+        self.used = 0
+        self.evictions = 0
+        self.launches = 0
+        self.resubmits = 0
+        self.work = 0
+        self.device_ms = 0.0
+        self.t0 = self.clock()
+
+    # -- admission --------------------------------------------------------
+    def _evict_one(self, avoid) -> bool:
+        for g, iid in self.resident.items():
+            if g not in self.busy and g != avoid:
+                self.engine.release(iid)
+                del self.resident[g]
+                self.used -= self.rbytes[g]
+                self.evictions += 1
+                return True
+        return False
+
+    def _admit(self, r: Request) -> bool:
+        g = r.grid
+        if g in self.busy:
+            return False
+        if g in self.resident:
+            iid = self.resident.pop(g)
+            self.resident[g] = iid  # most recently used
+            self.engine.resubmit(iid, request_src(self.pool, r), tol=r.tol, maxiters=self.maxiters, warm=True)
+            self.resubmits += 1
+            r.warm = True
+        else:
+            if self.rbytes[g] > self.budget:
+                raise SolverError(OOM, f"grid {g} needs {self.rbytes[g]} bytes, budget {self.budget:.0f}")
+            while self.used + self.rbytes[g] > self.budget:
+                if not self._evict_one(g):
+                    return False
+            prob = self.pool[g][r.rhs]
+            if r.mix != 0.0:
+                prob = type(prob)(**{**prob.__dict__, "src": request_src(self.pool, r)})
+            while True:
+                try:
+                    iid = self.engine.add(prob, tol=r.tol, maxiters=self.maxiters)
+                    break
+                except SolverError as e:
+                    if e.code != OOM:
+                        raise
+                    if not self._evict_one(g):
+                        return False
+            self.resident[g] = iid
+            self.used += self.rbytes[g]
+        self.busy[g] = r
+        r.t_admit = self.clock() - self.t0
+        return True
+
+    def _harvest(self):
+        for g, r in list(self.busy.items()):
+            iid = self.resident[g]
+            if self.engine.state(iid) == 3:  # INST_DONE
+                q0 = self.pool[g][r.rhs].q if self.keep_q else None
+                q, st = self.engine.result(iid, q0, release=False)
+                r.t_done = self.clock() - self.t0
+                r.launch_done = self.launches
+                r.iters, r.status, r.unknowns = int(st.niters), int(st.status), int(st.unknowns)
+                if self.keep_q:
+                    r.q = q
+                del self.busy[g]
+
+    # -- the loop -----------------------------------------------------------
+    def run(self, requests, realtime=True, drain_limit=None):
+        """Serves `requests` (sorted by t_arrival).  realtime=False admits every
+        request at once (arrival times ignored).  drain_limit (s) stops the loop
+        with requests unfinished.  Returns the requests."""
+        reqs = sorted(requests, key=lambda r: r.t_arrival)
+        pending = collections.deque()
+        self.t0 = self.clock()
+        i = 0
+        while True:
+            now = self.clock() - self.t0
+            while i < len(reqs) and (not realtime or reqs[i].t_arrival <= now):
+                pending.append(reqs[i])
+                i += 1
+            # admit in arrival order; a request whose grid is busy waits without blocking others
+            blocked = set()
+            for _ in range(len(pending)):
+                r = pending.popleft()
+                if r.grid in blocked or not self._admit(r):
+                    blocked.add(r.grid)
+                    pending.append(r)
+            if self.busy:
+                _, ms, work = self.engine.run(max_iters=self.chunk)
+                self.launches += 1
+                self.work += work
+                self.device_ms += ms
+                self._harvest()
+            elif i < len(reqs):
+                if pending:
+                    raise RuntimeError("requests pending with nothing running: budget too small")
+                wait = reqs[i].t_arrival - (self.clock() - self.t0)
+                if wait > 0:
+                    time.sleep(min(wait, 0.001))
+            elif not pending:
+                break
+            if drain_limit is not None and self.clock() - self.t0 > drain_limit:
+                break
+        self.t_end = self.clock() - self.t0
+        return reqs
+
+
+def latency_report(reqs, t_end):
+    """p50/p99 latency (arrival to harvest) over completed requests, throughput over the run."""
+    done = [r for r in reqs if r.t_done >= 0]
+    lat = np.array([r.t_done - r.t_arrival for r in done]) * 1e3
+    out = {"requests": len(reqs), "completed": len(done),
+           "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+           "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+           "mean_ms": float(lat.mean()) if len(lat) else None,
+           "makespan_s": t_end,
+           "unknown_iters": int(sum(r.unknowns * r.iters for r in done)),
+           "status_counts": {int(s): int(sum(r.status == s for r in done)) for s in sorted({r.status for r in done})},
+           "mean_iters": float(np.mean([r.iters for r in done])) if done else None,
+           "mean_unknowns": float(np.mean([r.unknowns for r in done])) if done else None}
+    out["unknown_iters_per_s"] = out["unknown_iters"] / t_end if t_end > 0 else 0.0
+    out["served_per_s"] = len(done) / t_end if t_end > 0 else 0.0
+    return out

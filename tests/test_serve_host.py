@@ -1,0 +1,165 @@
+"""Scheduling logic of the serving loop (suntans_gb300/serve.py) on a host fake
+of the batched engine: arrival order, one request per grid at a time, HBM
+budget admission with least-recently-used eviction, warm starts on resident
+grids, continuous admission between launches."""
+import types
+
+import numpy as np
+import pytest
+
+from suntans_gb300.capi import OOM, SolverError
+from suntans_gb300.serve import Request, Server, latency_report, poisson_stream, request_src
+
+
+class FakeEngine:
+    """Same methods as Batch; a problem needs 40 iterations cold (80 at 1e-10),
+    a quarter of that warm.  Capacity counted in storage slots."""
+
+    def __init__(self, cap):
+        self.cap, self.used, self.inst, self.next = cap, 0, {}, 0
+        self.peak = 0
+
+    @staticmethod
+    def _iters(tol, warm):
+        n = 80 if tol < 1e-9 else 40
+        return n // 4 if warm else n
+
+    def add(self, prob, tol, maxiters):
+        n = prob.grid.n3
+        if self.used + n > self.cap:
+            raise SolverError(OOM, "full")
+        i = self.next
+        self.next += 1
+        self.inst[i] = dict(n=n, left=self._iters(tol, False), state=1, it=0)
+        self.used += n
+        self.peak = max(self.peak, self.used)
+        return i
+
+    def resubmit(self, i, src, tol, maxiters, warm):
+        I = self.inst[i]
+        assert I["state"] == 3
+        I.update(left=self._iters(tol, warm), state=1, it=0)
+
+    def run(self, max_iters=0):
+        work, running = 0, 0
+        for I in self.inst.values():
+            if I["state"] in (1, 2):
+                k = I["left"] if max_iters <= 0 else min(I["left"], max_iters)
+                I["left"] -= k
+                I["it"] += k
+                work += k * I["n"]
+                I["state"] = 3 if I["left"] == 0 else 2
+                running += I["state"] != 3
+        return running, 0.1, work
+
+    def state(self, i):
+        return self.inst[i]["state"]
+
+    def result(self, i, q0, release=False):
+        I = self.inst[i]
+        st = types.SimpleNamespace(niters=I["it"], status=0, unknowns=I["n"])
+        if release:
+            self.release(i)
+        return None, st
+
+    def release(self, i):
+        self.used -= self.inst.pop(i)["n"]
+
+
+def fake_pool(sizes, rhs=2):
+    pool = []
+    for gid, n in enumerate(sizes):
+        g = types.SimpleNamespace(n3=n, gid=gid)
+        pool.append([types.SimpleNamespace(grid=g, src=np.full(3, float(j + 1)), q=None) for j in range(rhs)])
+    return pool
+
+
+def rbytes(g):
+    return 100 * g.n3
+
+
+def requests(seq, tols=(1e-8, 1e-10)):
+    return [Request(k, gid, k % 2, tols[k % 2], 0.0001 * k) for k, gid in enumerate(seq)]
+
+
+def test_every_request_served_and_grid_order_kept():
+    pool = fake_pool([100, 200, 300, 400, 500])
+    eng = FakeEngine(10_000)
+    srv = Server(pool, eng, 1e12, rbytes, chunk=8, keep_q=False)
+    rng = np.random.default_rng(0)
+    reqs = requests(rng.integers(0, 5, 60))
+    srv.run(reqs, realtime=False)
+    assert all(r.t_done >= 0 and r.status == 0 for r in reqs)
+    for gid in range(5):
+        chain = [r for r in reqs if r.grid == gid]
+        for a, b in zip(chain, chain[1:]):
+            assert b.t_admit >= a.t_done  # one in flight per grid, in arrival order
+        # the first request on a grid is cold, later ones warm-start
+        assert not chain[0].warm and chain[0].iters == FakeEngine._iters(chain[0].tol, False)
+        assert all(r.warm and r.iters == FakeEngine._iters(r.tol, True) for r in chain[1:])
+    assert srv.evictions == 0
+    assert srv.work == sum(r.iters * r.unknowns for r in reqs)
+
+
+def test_requests_join_running_launches():
+    """Continuous batching: requests admitted together share their launches."""
+    pool = fake_pool([100, 100, 100])
+    srv = Server(pool, FakeEngine(10_000), 1e12, rbytes, chunk=4, keep_q=False)
+    reqs = requests([0, 1, 2])
+    srv.run(reqs, realtime=False)
+    # 40 iterations at 1e-8 (requests 0, 2) and 80 at 1e-10 (request 1) in chunks of 4
+    assert [r.launch_done for r in reqs] == [10, 20, 10]
+    assert srv.launches == 20
+
+
+def test_budget_admission_and_lru_eviction():
+    pool = fake_pool([1000, 1000, 1000, 1000])
+    eng = FakeEngine(10_000)
+    budget = 2.5 * 100 * 1000  # room for two grids
+    srv = Server(pool, eng, budget, rbytes, chunk=8, keep_q=False)
+    reqs = requests([0, 1, 2, 3, 0, 1, 2, 3, 0])
+    srv.run(reqs, realtime=False)
+    assert all(r.t_done >= 0 for r in reqs)
+    assert eng.peak <= 2000
+    assert srv.evictions >= 5
+    assert srv.used <= budget
+    assert not any(r.warm for r in reqs[4:8])  # each revisit found its grid evicted
+
+
+def test_engine_capacity_triggers_eviction():
+    pool = fake_pool([600, 600, 600])
+    eng = FakeEngine(1300)  # the arena holds two grids although the budget holds all
+    srv = Server(pool, eng, 1e12, rbytes, chunk=8, keep_q=False)
+    reqs = requests([0, 1, 2, 0])
+    srv.run(reqs, realtime=False)
+    assert all(r.t_done >= 0 for r in reqs)
+    assert srv.evictions >= 1 and eng.peak <= 1300
+
+
+def test_grid_over_budget_raises():
+    srv = Server(fake_pool([1000]), FakeEngine(10_000), 1000.0, rbytes, keep_q=False)
+    with pytest.raises(SolverError):
+        srv.run(requests([0]), realtime=False)
+
+
+def test_request_right_hand_side_mix():
+    pool = fake_pool([10], rhs=2)
+    r = Request(0, 0, 1, 1e-8, 0.0, mix=0.25)
+    assert np.allclose(request_src(pool, r), 0.75 * 2.0 + 0.25 * 1.0)
+    assert request_src(pool, Request(1, 0, 0, 1e-8, 0.0)) is pool[0][0].src
+
+
+def test_poisson_stream_and_realtime_loop():
+    reqs = poisson_stream(3, 2, rate=2000.0, seconds=0.05, seed=3)
+    n = len(reqs)
+    assert abs(n - 100) < 5 * np.sqrt(100)
+    t = [r.t_arrival for r in reqs]
+    assert t == sorted(t) and t[-1] < 0.05
+    assert {r.tol for r in reqs} <= {1e-8, 1e-10}
+    assert all(0.0 <= r.mix < 1.0 for r in reqs)
+    srv = Server(fake_pool([100, 100, 100]), FakeEngine(10_000), 1e12, rbytes, chunk=16, keep_q=False)
+    srv.run(reqs, realtime=True)
+    assert all(r.t_done >= r.t_arrival and r.t_admit >= r.t_arrival for r in reqs)
+    rep = latency_report(reqs, srv.t_end)
+    assert rep["completed"] == n and rep["p99_ms"] >= rep["p50_ms"] > 0
+    assert rep["status_counts"] == {0: n}
