@@ -369,15 +369,57 @@ __device__ __forceinline__ void column_factor64(const BatchArgs& a, int off, int
 }
 
 // ---------------------------------------------------------------------------
+// per-warp partial-sum slots of the pipelined phases
+//
+// Slot (t0 + l, w) holds warp w's partial of CTA l of an instance whose tiles
+// start at t0 (l = (b - t0) mod G as for the set-up reductions).  An empty
+// slot holds kEmptyPartial, a NaN bit pattern that no arithmetic produces (a
+// computed NaN is the canonical one), so the value itself signals arrival.
+// ---------------------------------------------------------------------------
+constexpr long long kEmptyPartial = 0x7ff4deadbeef0001LL;
+
+__device__ __forceinline__ void st_partial(double* p, double v) {
+  *(volatile long long*)p = __double_as_longlong(v);
+}
+
+// Waits (bounded) until the slot is written, returns its value and empties it.
+__device__ __forceinline__ bool take_partial(double* p, long long lim, double& out) {
+  volatile long long* q = (volatile long long*)p;
+  long long bits = *q;
+  if (bits == kEmptyPartial) {
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while ((bits = *q) == kEmptyPartial) {
+      if (++spins > 16) __nanosleep(64);
+      if ((spins & 63u) == 0 && (long long)(globaltimer_ns() - t0) > lim) {
+        out = 0.0;
+        return false;
+      }
+    }
+  }
+  *q = kEmptyPartial;
+  out = __longlong_as_double(bits);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // the pipelined phases
 // ---------------------------------------------------------------------------
-// One pipeline stage in shared memory: a 16-byte descriptor written by the
-// producer, the tile header (capacity kHdrCap - 16), and up to 4 FP32 streams.
+// One pipeline stage in shared memory: a 32-byte descriptor written by the
+// producer, the tile header (capacity kHdrCap - 32), and up to 4 FP32 streams.
+// The descriptor carries what the compute warps need of the tile's instance
+// (its scalars and its partial-sum slot), so that they never wait on a global
+// load when the instance changes.
 struct StageDesc {
   int base, nslots, inst, par;
+  int slot;      // partial-sum slot of this CTA for the instance: t0 + ((b - t0) mod G)
+  int owner;     // 1: this CTA holds the instance's first tile and finalises it
+  float mu, nu;  // the instance's scalars for this phase (FP32)
 };
+static_assert(sizeof(StageDesc) == 32, "stage descriptor is 32 bytes");
+constexpr int kStageHdrOff = 32;
 __device__ __forceinline__ StageDesc* stage_desc(unsigned char* stage) { return (StageDesc*)(stage); }
-__device__ __forceinline__ unsigned char* stage_hdr(unsigned char* stage) { return stage + 16; }
+__device__ __forceinline__ unsigned char* stage_hdr(unsigned char* stage) { return stage + kStageHdrOff; }
 __device__ __forceinline__ float* stage_stream(unsigned char* stage, int k) {
   return (float*)(stage + kHdrCap + k * kStreamBytes);
 }
@@ -387,6 +429,8 @@ struct Pipe {
   uint64_t* full;    // [2]
   uint64_t* empty;   // [2]
   int* list;         // tiles of this CTA for the current phase
+  int* own;          // instances this CTA finalises in the current phase
+  int* nown;
   int* count;
   uint32_t seq;      // tiles consumed (compute warps) or filled (producer) so far, all phases
 };
@@ -429,14 +473,34 @@ __device__ __forceinline__ void build_list(const BatchArgs& a, Pipe& P, Want&& w
   __syncthreads();
 }
 
-// Producer: fill stage seq&1 with tile t.  PH 0 = apply, 1 = update.
+// Instance fields the producer hands to the compute warps with each tile.
+struct ProdInst {
+  int inst, par, slot, owner;
+  float mu, nu;
+};
+__device__ __forceinline__ ProdInst prod_inst(const BatchArgs& a, int i) {
+  const BInst& I = a.inst[i];
+  ProdInst r;
+  r.inst = i;
+  r.par = ld_volatile_int(&I.par);
+  const int G = gridDim.x, t0 = ld_volatile_int(&I.t0);
+  const int l = ((int)blockIdx.x - t0 % G + G) % G;
+  r.slot = t0 + l;
+  r.owner = (l == 0);
+  r.mu = (float)(*(volatile const double*)&I.mu);
+  r.nu = (float)(*(volatile const double*)&I.nu);
+  return r;
+}
+
+// Producer: fill stage seq&1 with tile descriptor d of instance fields pi.
+// PH 0 = apply, 1 = update.
 template <int QP, int PH>
-__device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, int t, long long lim, int* err) {
+__device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileDesc& d, const ProdInst& pi,
+                                        long long lim, int* err) {
   const uint32_t q = P.seq;
   const int b = q & 1;
   if (q >= 2 && !mbar_wait(&P.empty[b], ((q >> 1) - 1) & 1, lim)) *err = 1;
-  const TileDesc d = a.tiles[t];
-  const int par = ld_volatile_int(&a.inst[d.inst].par);
+  const int par = pi.par;
   const int n4 = (d.nslots + 3) & ~3;
   unsigned char* st = P.stage[b];
   StageDesc* sd = stage_desc(st);
@@ -444,6 +508,10 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, int t, long
   sd->nslots = d.nslots;
   sd->inst = d.inst;
   sd->par = par;
+  sd->slot = pi.slot;
+  sd->owner = pi.owner;
+  sd->mu = pi.mu;
+  sd->nu = pi.nu;
   const bool hdr = (PH == 0) || (QP == 2);
   uint32_t bytes = 0;
   if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + (QP == 1 ? 4 * n4 : 0);
@@ -736,9 +804,20 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int err = 0;
   if (warp == 8) {
-    // producer warp: lane 0 issues every fill of this phase in list order
-    if (lane == 0)
-      for (int j = 0; j < n; ++j) produce<QP, PH>(a, P, P.list[j], lim, &err);
+    // producer warp: lane 0 issues every fill of this phase in list order.
+    // Tile descriptors are loaded one tile ahead; the instance fields are
+    // re-read only when the instance changes.
+    if (lane == 0 && n > 0) {
+      TileDesc dn = a.tiles[P.list[0]];
+      ProdInst pi;
+      pi.inst = -1;
+      for (int j = 0; j < n; ++j) {
+        const TileDesc d = dn;
+        if (j + 1 < n) dn = a.tiles[P.list[j + 1]];
+        if (d.inst != pi.inst) pi = prod_inst(a, d.inst);
+        produce<QP, PH>(a, P, d, pi, lim, &err);
+      }
+    }
     P.seq = __shfl_sync(0xffffffffu, P.seq, 0);
     err = __shfl_sync(0xffffffffu, err, 0);
     if (lane == 0 && err) atomicCAS(&a.ctl->status, SGPU_OK, SGPU_TIMEOUT);
@@ -749,16 +828,26 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
   double acc[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) df_zero(dacc[v]);
-  auto do_flush = [&](int inst, int ntl) {
+  // Per-warp flush of the instance's partial sums: a fixed shuffle tree, then
+  // lane 0 stores the warp's value into the CTA's slot.  No barrier, fence or
+  // atomic: the owner CTA collects the slots at the end of the phase.
+  // `enc` is the slot, bitwise complemented when this CTA owns the instance.
+  if (threadIdx.x == 0) *P.nown = 0;
+  auto do_flush = [&](int inst, int enc) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       acc[v] = df_value(dacc[v]);
       df_zero(dacc[v]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
     }
-    flush<NV>(a, inst, ntl, acc, s_red, s_flag, fin);
+    const int slot = enc < 0 ? ~enc : enc;
+    if (lane == 0)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) st_partial(a.tpw + ((size_t)slot * 8 + warp) * 2 + v, acc[v]);
+    if (enc < 0 && threadIdx.x == 0) P.own[(*P.nown)++] = inst;
   };
-  int cur = -1, cnt = 0;
-  float mu = 0.f, nu = 0.f;
+  int cur = -1, cur_enc = 0;
   for (int j = 0; j < n; ++j) {
     const uint32_t q = P.seq;
     const int b = q & 1;
@@ -766,13 +855,11 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     unsigned char* st = P.stage[b];
     const StageDesc sd = *stage_desc(st);
     if (sd.inst != cur) {
-      if (cur >= 0) do_flush(cur, cnt);
+      if (cur >= 0) do_flush(cur, cur_enc);
       cur = sd.inst;
-      cnt = 0;
-      const BInst& I = a.inst[cur];
-      mu = (float)(*(volatile double*)&I.mu);
-      nu = (float)(*(volatile double*)&I.nu);
+      cur_enc = sd.owner ? ~sd.slot : sd.slot;
     }
+    const float mu = sd.mu, nu = sd.nu;
     const int len = sd.nslots;
     const int base = sd.base;
     constexpr int Q = kBTSlots / kCompute;
@@ -805,7 +892,6 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
           for (int j = 0; j < 4; ++j) df_addprod(dacc[0], pu4[j], y4[j]);
         }
         P.seq = q + 1;
-        ++cnt;
         continue;
       } else {
 #pragma unroll
@@ -927,9 +1013,52 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       if (lane == 0) mbar_arrive(&P.empty[b]);
     }
     P.seq = q + 1;
-    ++cnt;
   }
-  if (cur >= 0) do_flush(cur, cnt);
+  if (cur >= 0) do_flush(cur, cur_enc);
+  // The owner of each instance (the CTA holding its first tile) sums the
+  // min(G, tiles) x 8 warp slots in a fixed order once every CTA has stored
+  // them, restores the empty marks, and runs the finaliser.  Loads are issued
+  // kPer at a time so that their latencies overlap.
+  csync();
+  const int G = gridDim.x, nown = *P.nown;
+  constexpr int kPer = 8 / NV;
+  for (int o = 0; o < nown; ++o) {
+    const int i = P.own[o];
+    BInst* I = a.inst + i;
+    const int t0 = I->t0, nt = I->t1 - I->t0;
+    const int m8 = 8 * (nt < G ? nt : G);
+    double v[NV];
+#pragma unroll
+    for (int vv = 0; vv < NV; ++vv) v[vv] = 0.0;
+    volatile long long* base = (volatile long long*)(a.tpw + (size_t)t0 * 16);
+    for (int e0 = threadIdx.x; e0 < m8; e0 += kPer * kCompute) {
+      long long bits[kPer][NV];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) {
+        const int e = e0 + k * kCompute;
+#pragma unroll
+        for (int vv = 0; vv < NV; ++vv) bits[k][vv] = e < m8 ? base[2 * e + vv] : 0;
+      }
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) {
+        const int e = e0 + k * kCompute;
+        if (e >= m8) continue;
+#pragma unroll
+        for (int vv = 0; vv < NV; ++vv) {
+          double x;
+          if (bits[k][vv] != kEmptyPartial) {
+            base[2 * e + vv] = kEmptyPartial;
+            x = __longlong_as_double(bits[k][vv]);
+          } else if (!take_partial((double*)(base + 2 * e + vv), lim, x)) {
+            err = 1;
+          }
+          v[vv] += x;
+        }
+      }
+    }
+    csum<NV>(v, s_red);
+    if (threadIdx.x == 0) fin(I, v);
+  }
   if (err && threadIdx.x == 0) atomicCAS(&a.ctl->status, SGPU_OK, SGPU_TIMEOUT);
 }
 
@@ -946,6 +1075,8 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   __shared__ int s_flag;
   __shared__ int s_count;
   __shared__ int s_wsum[8];
+  __shared__ int s_own[kListCap];
+  __shared__ int s_nown;
   const int tid = threadIdx.x, F = a.F;
   const bool compute = tid < kCompute;
   SolveCtl* ctl = a.ctl;
@@ -957,6 +1088,8 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   P.full = (uint64_t*)(dyn + 2 * kBufBytes);
   P.empty = P.full + 2;
   P.list = (int*)(dyn + 2 * kBufBytes + 32);
+  P.own = s_own;
+  P.nown = &s_nown;
   P.count = &s_count;
   P.seq = 0;
   if (tid == 0) {
@@ -968,6 +1101,13 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   }
   __syncthreads();
   TileSmem& sm = *(TileSmem*)P.stage[0];  // simple phases reuse stage 0 (no copies in flight then)
+
+  // every partial-sum slot of this launch starts empty (a grid barrier orders
+  // this before the first flush: in the set-up phases, or just below)
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + tid; e < (size_t)a.ntiles * 16; e += (size_t)gridDim.x * blockDim.x)
+    ((long long*)a.tpw)[e] = kEmptyPartial;
+  if (!ld_volatile_int(&a.gflags[1]))
+    if (!grid_sync(ctl, 5, [] {})) return;
 
   // ======================= setup of new instances =======================
   // gflags[1]: some instance needs its set-up phases (written by the host)
@@ -1541,6 +1681,7 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if ((rc = balloc(b, &a.x32, S))) return rc;
   if ((rc = balloc(b, &a.z32, S))) return rc;
   if ((rc = balloc(b, &a.tpart, 2 * ((size_t)b->max_tiles + 1)))) return rc;
+  if ((rc = balloc(b, &a.tpw, 16 * ((size_t)b->max_tiles + 1)))) return rc;
   if ((rc = balloc(b, &b->d_inst, (size_t)max_instances))) return rc;
   if ((rc = balloc(b, &b->d_ctl, 1))) return rc;
   if ((rc = balloc(b, &b->d_gflags, 4))) return rc;
@@ -1599,7 +1740,7 @@ long long sgpu_batch_bytes_per_request(int qprecond, int maxfaces, long long n3,
   long long per_col = (long long)sizeof(BCol) + (long long)sizeof(BFace) * maxfaces + 8 + 8 + 16LL * maxfaces;
   long long per_eslot = 12;
   const long long tiles = ncols / 16 + n3 / kBTSlots + 2;
-  return per_slot * (n3 + 4 * tiles) + per_col * ncols + per_eslot * nedge_slots + 96 * tiles;
+  return per_slot * (n3 + 4 * tiles) + per_col * ncols + per_eslot * nedge_slots + (96 + 128) * tiles;
 }
 
 int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, const double* const* dzz,
@@ -1665,6 +1806,7 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
       T.c1 = j;
       T.nslots = len;
       const HdrLayout L = hdr_layout(T.c1 - T.c0, F);
+      if (L.bytes > kHdrCap - kStageHdrOff) return bfail(b, SGPU_BAD_GRID, "tile header of %d bytes", L.bytes);
       T.hdr = (int)hacc;
       T.hdr_bytes = L.bytes;
       hacc += L.bytes;

@@ -144,8 +144,9 @@ struct BatchArgs {
   float* pb32;
   float* x32;            // [nslots] FP32 correction accumulated since the last reliable update
   float* z32;            // [nslots]
-  // per-tile partial sums [ntiles*2] and instance table
+  // per-CTA partial sums [ntiles*2] of the simple phases and instance table
   double* tpart;
+  double* tpw;           // [ntiles*8*2] per-warp partial sums of the pipelined phases
   BInst* inst;
   SolveCtl* ctl;         // grid barrier
   int* gflags;           // [4]: 0 any reliable flag, 2 its snapshot, 3 any instance running
