@@ -159,8 +159,8 @@ class Batch:
         """Per-phase device time of the last launch (zero unless built with -DSGPU_PHASE_TIMING)."""
         arr = (C.c_longlong * 8)()
         self.lib.sgpu_batch_phase_times(self.h, arr)
-        names = ["-", "apply", "update", "merge64", "residual64", "setup1", "setup2", "setup3"]
-        return {n: arr[k] / 1e6 for k, n in enumerate(names) if k}
+        names = ["owner_fin_apply", "apply", "update", "merge64", "residual64", "setup1", "setup2", "setup3"]
+        return {n: arr[k] / 1e6 for k, n in enumerate(names)}
 
     def stats(self, i):
         st = Stats()

@@ -723,6 +723,7 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
   const int* fkk = (const int*)(hd + L.o_fkk);
   const float* fD = (const float*)(hd + L.o_fD);
   const int* fes = (const int*)(hd + L.o_fes);
+  const unsigned char* cmap = hd + L.o_cmap;
   int cc[Q], kv[Q], ctop[Q], nk[Q], sv[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -730,7 +731,7 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
     const bool in = s0 < len;
     const int s = in ? s0 : 0;
     sv[q] = s;
-    cc[q] = hcol_of(start, ncols, s);
+    cc[q] = cmap[s];
     kv[q] = s - start[cc[q]];
     const int w = cn[cc[q]];
     ctop[q] = w & 0xffff;
@@ -866,7 +867,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     if (PH == 0) {
       const unsigned char* hd = stage_hdr(st);
       const int ncols = ((const int*)hd)[0];
-      const HdrLayout L = hdr_layout(ncols, a.F);
+      const HdrLayout L = hdr_layout(ncols, a.F, len);
       const unsigned short* start = (const unsigned short*)(hd + L.o_start);
       const int* cn = (const int*)(hd + L.o_cn);
       const float* sp = stage_stream(st, 0);
@@ -878,6 +879,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       const float* S = (QP == 2) ? a.s32 : a.r32;
       float yv[Q], pv[Q];
       bool on[Q];
+#ifdef SGPU_APPLY_QUAD
       if (a.F == 3 || a.F == 4) {
         float pu4[4], y4[4];
         if (a.F == 3) apply_quad32<QP, 3>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, pu4, y4);
@@ -893,6 +895,12 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         }
         P.seq = q + 1;
         continue;
+      } else
+#endif
+      if (a.F == 3) {
+        apply_tile32<QP, 3>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, yv, pv, on);
+      } else if (a.F == 4) {
+        apply_tile32<QP, 4>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, yv, pv, on);
       } else {
 #pragma unroll
         for (int qq = 0; qq < Q; ++qq) {
@@ -971,7 +979,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         csync();
         const unsigned char* hd = stage_hdr(st);
         const int ncols = ((const int*)hd)[0];
-        const HdrLayout L = hdr_layout(ncols, a.F);
+        const HdrLayout L = hdr_layout(ncols, a.F, len);
         const unsigned short* start = (const unsigned short*)(hd + L.o_start);
         const int* cn = (const int*)(hd + L.o_cn);
         for (int c = threadIdx.x; c < ncols; c += kCompute) {
@@ -1020,6 +1028,9 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
   // them, restores the empty marks, and runs the finaliser.  Loads are issued
   // kPer at a time so that their latencies overlap.
   csync();
+#ifdef SGPU_PHASE_TIMING
+  const unsigned long long t_fin0 = globaltimer_ns();
+#endif
   const int G = gridDim.x, nown = *P.nown;
   constexpr int kPer = 8 / NV;
   for (int o = 0; o < nown; ++o) {
@@ -1059,6 +1070,11 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     csum<NV>(v, s_red);
     if (threadIdx.x == 0) fin(I, v);
   }
+#ifdef SGPU_PHASE_TIMING
+  // time the owners spend collecting and finalising (apply phase only)
+  if (PH == 0 && nown > 0 && threadIdx.x == 0)
+    atomicAdd((unsigned long long*)&a.ctl->phase_ns[0], globaltimer_ns() - t_fin0);
+#endif
   if (err && threadIdx.x == 0) atomicCAS(&a.ctl->status, SGPU_OK, SGPU_TIMEOUT);
 }
 
@@ -1805,7 +1821,7 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
       }
       T.c1 = j;
       T.nslots = len;
-      const HdrLayout L = hdr_layout(T.c1 - T.c0, F);
+      const HdrLayout L = hdr_layout(T.c1 - T.c0, F, T.nslots);
       if (L.bytes > kHdrCap - kStageHdrOff) return bfail(b, SGPU_BAD_GRID, "tile header of %d bytes", L.bytes);
       T.hdr = (int)hacc;
       T.hdr_bytes = L.bytes;
@@ -1889,7 +1905,7 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   std::vector<unsigned char> v_hdr(std::max(16LL, H.h_bytes), 0);
   for (const HostTile& T : H.tiles) {
     const int ncols = T.c1 - T.c0;
-    const HdrLayout L = hdr_layout(ncols, F);
+    const HdrLayout L = hdr_layout(ncols, F, T.nslots);
     unsigned char* h = v_hdr.data() + T.hdr;
     int* h0 = (int*)h;
     h0[0] = ncols;
@@ -1902,9 +1918,11 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
     int* fkk = (int*)(h + L.o_fkk);
     float* fD = (float*)(h + L.o_fD);
     int* fes = (int*)(h + L.o_fes);
+    unsigned char* cmap = h + L.o_cmap;
     for (int cc = 0; cc < ncols; ++cc) {
       const int j = T.c0 + cc;
       st[cc] = (unsigned short)(H.coff[j] - T.base);
+      for (int u = H.coff[j] - T.base; u < H.coff[j] - T.base + g->Nk[H.dev2cell[j]]; ++u) cmap[u] = (unsigned char)cc;
       cn[cc] = v_col[j].ctop | (v_col[j].nk << 16);
       for (int f = 0; f < F; ++f) {
         const BFace& fc = v_face[(size_t)j * F + f];

@@ -17,10 +17,11 @@ constexpr int kMaxF = 8;         // faces per cell supported by the batched engi
 constexpr int kBTSlots = 1024;   // storage slots per tile (4 per thread of a 256-thread CTA)
 constexpr int kBTCols = 128;     // columns per tile
 constexpr int kBTFaces = 512;    // column-faces per tile (ncols * F)
-constexpr int kHdrCap = 9216;    // bytes of a tile header (see tile header layout below)
+constexpr int kHdrCap = 10240;   // bytes of a tile header (see tile header layout below)
 constexpr int kStreamFloats = kBTSlots + 4;                 // one FP32 stream of a tile (+1 group)
 constexpr int kStreamBytes = kStreamFloats * 4;             // 4112, a multiple of 16
 constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // one pipeline stage
+static_assert(kBTCols <= 256, "the header's slot-to-column map holds one byte per slot");
 constexpr int kListCap = 512;    // tiles per CTA per phase
 // dynamic shared memory of the kernel: 2 stages, 4 mbarriers (32 B), the tile list
 constexpr int kDynSmem = 2 * kBufBytes + 32 + 4 * kListCap;
@@ -34,11 +35,12 @@ constexpr int kDynSmem = 2 * kBufBytes + 32 + 4 * kListCap;
 //   o_fkk     int fkk[ncols*F]                kmin | kmax << 16 (empty when no neighbour)
 //   o_fD      float fD[ncols*F]               D of the edge
 //   o_fes     int fes[ncols*F]                edge's first slot (dzf*D storage)
+//   o_cmap    unsigned char cmap[nslots]      column of each slot of the tile
 __host__ __device__ __forceinline__ int pad16(int b) { return (b + 15) & ~15; }
 struct HdrLayout {
-  int o_start, o_cn, o_fns, o_fkk, o_fD, o_fes, bytes;
+  int o_start, o_cn, o_fns, o_fkk, o_fD, o_fes, o_cmap, bytes;
 };
-__host__ __device__ __forceinline__ HdrLayout hdr_layout(int ncols, int F) {
+__host__ __device__ __forceinline__ HdrLayout hdr_layout(int ncols, int F, int nslots) {
   HdrLayout L;
   L.o_start = 16;
   L.o_cn = L.o_start + pad16(2 * (ncols + 1));
@@ -47,7 +49,8 @@ __host__ __device__ __forceinline__ HdrLayout hdr_layout(int ncols, int F) {
   L.o_fkk = L.o_fns + sf;
   L.o_fD = L.o_fkk + sf;
   L.o_fes = L.o_fD + sf;
-  L.bytes = L.o_fes + sf;
+  L.o_cmap = L.o_fes + sf;
+  L.bytes = L.o_cmap + pad16(nslots);
   return L;
 }
 
