@@ -80,6 +80,7 @@ def parse():
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
     ap.add_argument("--no-mixed", action="store_true", help="cfg2: skip the mixed_form measurement")
     ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--cfg3-points", type=int, default=500_000, help="cfg3: random points (domain scaled to keep the density)")
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--drain-seconds", type=float, default=30.0)
@@ -413,8 +414,9 @@ def bench_cfg3(args):
     from suntans_gb300.batch import Batch, capacity_for
     from suntans_gb300.capi import Context
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    g = gg.delaunay_seamount(500_000, 50_000.0, 25_000.0, Nkmax=40, rstretch=1.02, seed=3, H0=50.0, amp=30.0,
-                             sigma=2000.0, h_sigma=0.01)
+    scale = (args.cfg3_points / 500_000) ** 0.5
+    g = gg.delaunay_seamount(args.cfg3_points, 50_000.0 * scale, 25_000.0 * scale, Nkmax=40, rstretch=1.02, seed=3,
+                             H0=50.0, amp=30.0, sigma=2000.0, h_sigma=0.01)
     qp = gg.make_q_problem(g, seed=13, sigma_u=0.05, dt=20.0)
     props = _props(args.qprecond)
     N = g.n_q()
@@ -442,7 +444,8 @@ def bench_cfg3(args):
             "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": mf["ms_per_solve"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
             "data": "synthetic (seeded grid and right-hand side)",
-            "config": {"workload": "Delaunay seamount, 500000 random points in 50x25 km, Nkmax=40, mixed precision",
+            "config": {"workload": f"Delaunay seamount, {args.cfg3_points} random points in "
+                                   f"{50 * scale:g}x{25 * scale:g} km, Nkmax=40, mixed precision",
                        "cells": g.Nc, "N_q": N, "qprecond": args.qprecond, "tolerance": 1e-10,
                        "l2": "not flushed: working set > 129 MB L2"},
             "mixed": mf, "plain_fp64_unknown_iters_per_s": plain_rate, "iters_fp64": int(s64.niters),
