@@ -131,6 +131,13 @@ int sgpu_h_download(sgpu_context *ctx, double *h);
  * runs out ends the solve with SGPU_TIMEOUT instead of hanging. */
 int sgpu_set_timeout_ns(sgpu_context *ctx, long long ns);
 
+/* Device time per barrier-separated phase of the last solve (ns), indexed by
+ * phase: pressure solve [1..3] set-up, [4] operator apply, [5] vector update,
+ * [6] direction update; free-surface solve [1..2] set-up, [3] apply,
+ * [4] update, [5] direction update.  Zero unless the library was built with
+ * -DSGPU_PHASE_TIMING. */
+int sgpu_phase_times(const sgpu_context *ctx, long long *ns8);
+
 /* Number of CTAs the persistent kernels are launched with (0 = one full wave,
  * the default).  For experiments and tests of the reduction order. */
 int sgpu_set_grid(sgpu_context *ctx, int ctas);

@@ -24,7 +24,7 @@ EXPORTS = [
     "sgpu_cgsolveq", "sgpu_cgsolve",
     "sgpu_q_upload", "sgpu_q_solve", "sgpu_q_download",
     "sgpu_h_upload", "sgpu_h_solve", "sgpu_h_download",
-    "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream",
+    "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream", "sgpu_phase_times",
     "sgpu_cgsolve_noalloc",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
     "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set", "sgpu_batch_set_tile_slots",
@@ -116,6 +116,7 @@ def load() -> C.CDLL:
     lib.sgpu_batch_stream.argtypes = [C.c_void_p]
     lib.sgpu_batch_stream.restype = C.c_void_p
     lib.sgpu_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+    lib.sgpu_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     lib.sgpu_batch_resubmit.argtypes = [C.c_void_p, C.c_int, _dpp, C.c_double, C.c_int, C.c_int]
     lib.sgpu_batch_use_graph.argtypes = [C.c_void_p, C.c_int]
     lib.sgpu_batch_graph_launches.argtypes = [C.c_void_p]
@@ -192,6 +193,12 @@ class Context:
     def stream(self) -> int:
         """The context's cudaStream_t as an integer handle."""
         return int(self.lib.sgpu_stream(self.h) or 0)
+
+    def phase_times_ms(self):
+        """Device time per phase of the last solve (zero unless built with -DSGPU_PHASE_TIMING)."""
+        arr = (C.c_longlong * 8)()
+        self.lib.sgpu_phase_times(self.h, arr)
+        return [arr[k] / 1e6 for k in range(8)]
 
     def set_grid(self, ctas: int):
         self._check(self.lib.sgpu_set_grid(self.h, int(ctas)), "sgpu_set_grid")

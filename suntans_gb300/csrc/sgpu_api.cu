@@ -53,7 +53,7 @@ struct sgpu_context {
   int *d_ctop = nullptr, *d_fmeta = nullptr, *d_fnoff = nullptr;
   double *d_dzz = nullptr, *d_dzf = nullptr, *d_Dq = nullptr, *d_qin = nullptr, *d_srcin = nullptr,
          *d_cin = nullptr, *d_coef = nullptr, *d_fc = nullptr, *d_c = nullptr, *d_tw = nullptr,
-         *d_tib = nullptr, *d_x = nullptr, *d_p = nullptr, *d_p2 = nullptr, *d_r = nullptr, *d_z = nullptr, *d_rt = nullptr;
+         *d_tib = nullptr, *d_x = nullptr, *d_p = nullptr, *d_r = nullptr, *d_z = nullptr, *d_rt = nullptr;
   std::vector<int> h_ctop;  // last uploaded ctop (cell order), for the download scatter
   bool q_uploaded = false, q_solved = false;
 
@@ -193,7 +193,6 @@ int sgpu_destroy(sgpu_context* ctx) {
 static int build_layout(sgpu_context* ctx, const sgpu_grid_desc* g) {
   const int Nc = g->Nc, Ne = g->Ne, mf = g->maxfaces;
   if (Nc <= 0 || Ne < 0 || mf <= 0 || g->Nkmax <= 0) return fail(ctx, SGPU_BAD_GRID, "empty or negative sizes");
-  if (mf > kQMaxF) return fail(ctx, SGPU_BAD_GRID, "maxfaces %d exceeds %d", mf, kQMaxF);
   if (!g->nfaces || !g->neigh || !g->face || !g->Nk || !g->Nke || !g->cellp || !g->celldist || !g->Ac || !g->df ||
       !g->dg)
     return fail(ctx, SGPU_BAD_ARG, "null array in grid description");
@@ -336,6 +335,12 @@ int sgpu_set_grid(sgpu_context* ctx, int ctas) {
 
 void* sgpu_stream(sgpu_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
+int sgpu_phase_times(const sgpu_context* ctx, long long* ns8) {
+  if (!ctx || !ns8) return SGPU_BAD_ARG;
+  for (int k = 0; k < 8; ++k) ns8[k] = ctx->h_ctl ? ctx->h_ctl->phase_ns[k] : 0;
+  return SGPU_OK;
+}
+
 static int ensure_partials(sgpu_context* ctx, int grid) {
   if (ctx->partials_cap >= grid) return SGPU_OK;
   int rc = dalloc(ctx, &ctx->d_partials, (size_t)4 * grid);
@@ -352,7 +357,7 @@ static int alloc_q(sgpu_context* ctx) {
   if ((rc = dalloc(ctx, &ctx->d_fmeta, ncf))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_fnoff, ncf))) return rc;
   double** v[] = {&ctx->d_dzz, &ctx->d_qin, &ctx->d_srcin, &ctx->d_cin, &ctx->d_coef, &ctx->d_c,
-                  &ctx->d_x,   &ctx->d_p,   &ctx->d_p2,    &ctx->d_r,   &ctx->d_z,   &ctx->d_rt};
+                  &ctx->d_x,   &ctx->d_p,   &ctx->d_r,     &ctx->d_z,   &ctx->d_rt};
   for (auto pp : v)
     if ((rc = dalloc(ctx, pp, n3))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_tw, n3c))) return rc;
@@ -509,7 +514,6 @@ int sgpu_q_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   a.tib = ctx->d_tib;
   a.x = ctx->d_x;
   a.p = ctx->d_p;
-  a.p2 = ctx->d_p2;
   a.r = ctx->d_r;
   a.z = ctx->d_z;
   a.rt = ctx->d_rt;

@@ -21,14 +21,8 @@
 //
 // Work split: computational columns are packed into tiles of at most 512
 // storage slots; a CTA of 256 threads owns tiles b, b+G, b+2G, ... in every
-// phase, 2 slots per thread.  Barriers: 2 per CG iteration, each finalised by
-// the last CTA to arrive (deterministic reduction, scalar recurrences).  The
-// direction update p = r + mu p (2522-2524) is folded into the next operator
-// apply: every slot's new direction, its own and each neighbour's, is formed
-// on the fly from r and the previous direction (two direction buffers), which
-// saves one pass over the vectors and one barrier per iteration.  The apply
-// stages each tile's column metadata and a slot-to-column map in shared
-// memory, so a slot's work starts without a chain of dependent global loads.
+// phase, 2 slots per thread.  Barriers: 3 per CG iteration, each finalised by
+// the last CTA to arrive (deterministic reduction, scalar recurrences).
 #include "sgpu_common.cuh"
 #include "sgpu_q.h"
 
@@ -61,94 +55,6 @@ __device__ __forceinline__ int find_col(const int* s_start, int ncols, int s) {
     if (s_start[mid] <= s) lo = mid; else hi = mid - 1;
   }
   return lo;
-}
-
-// Column metadata of one tile in shared memory for the loop's operator apply.
-struct QTileSmem {
-  int start[kMaxTileCols + 1];             // slot offset of each column in the tile
-  int cn[kMaxTileCols];                    // ctop | nk << 16
-  int fmeta[kMaxTileCols * kQMaxF];        // kmin | kmax << 16, -1 = no neighbour
-  int fnoff[kMaxTileCols * kQMaxF];        // neighbour column's storage offset
-  unsigned short cmap[kTileCap];           // column of each slot
-};
-
-__device__ __forceinline__ void tile_stage(const QArgs& a, int t, TileCtx& tc, QTileSmem& sm) {
-  const int c0 = a.tile_col[t], c1 = a.tile_col[t + 1];
-  const int base = a.dcoff[c0], ncols = c1 - c0, F = a.F;
-  for (int c = threadIdx.x; c <= ncols; c += kBlock) {
-    sm.start[c] = a.dcoff[c0 + c] - base;
-    if (c < ncols) sm.cn[c] = a.ctop[c0 + c] | (a.nk[c0 + c] << 16);
-  }
-  for (int e = threadIdx.x; e < ncols * F; e += kBlock) {
-    sm.fmeta[e] = a.fmeta[c0 * F + e];
-    sm.fnoff[e] = a.fnoff[c0 * F + e];
-  }
-  tc.base = base;
-  tc.c0 = c0;
-  tc.ncols = ncols;
-  __syncthreads();
-  tc.len = sm.start[ncols];
-  for (int c = threadIdx.x; c < ncols; c += kBlock)
-    for (int s = sm.start[c]; s < sm.start[c + 1]; ++s) sm.cmap[s] = (unsigned short)c;
-  __syncthreads();
-}
-
-// New direction at slot n: r (or M^-1 r) + mu p_old; boundary columns keep their
-// fixed values (the reference never updates p outside the computational cells).
-__device__ __forceinline__ double pdir(const QArgs& a, const double* __restrict__ src,
-                                       const double* __restrict__ pold, double mu, int n) {
-  return n < a.n3c ? __fma_rn(mu, pold[n], src[n]) : pold[n];
-}
-
-// Operator apply at slot u = (tile column c, level k) to the new direction
-// formed on the fly; pu receives the slot's own new direction.
-template <int QP>
-__device__ __forceinline__ double apply_fused(const QArgs& a, const QTileSmem& sm, const double* __restrict__ src,
-                                              const double* __restrict__ pold, double mu, int u, int c, int k,
-                                              int ctop, int nk, double& pu_out) {
-  const int F = a.F;
-  const double pu = __fma_rn(mu, pold[u], src[u]);
-  pu_out = pu;
-  double y;
-  if (QP == 1) {
-    y = -pu;
-    for (int f = 0; f < F; ++f) {
-      const int meta = sm.fmeta[c * F + f];
-      if (meta < 0) continue;
-      const int kmin = meta & 0xffff, kmax = meta >> 16;
-      if (k >= kmin && k < kmax) y += pdir(a, src, pold, mu, sm.fnoff[c * F + f] + k) * a.fc[(size_t)f * a.n3c + u];
-    }
-    if (k > ctop && k < nk - 1) {
-      y += a.coef[u] * __fma_rn(mu, pold[u - 1], src[u - 1]) + a.coef[u + 1] * __fma_rn(mu, pold[u + 1], src[u + 1]);
-    } else if (ctop < nk - 1) {
-      if (k == ctop) y += a.coef[u + 1] * __fma_rn(mu, pold[u + 1], src[u + 1]);
-      else y += a.coef[u] * __fma_rn(mu, pold[u - 1], src[u - 1]);  // k == nk-1
-    }
-  } else {
-    y = 0.0;
-    for (int f = 0; f < F; ++f) {
-      const int meta = sm.fmeta[c * F + f];
-      if (meta < 0) continue;
-      const int kmin = meta & 0xffff, kmax = meta >> 16;
-      if (k >= kmin && k < kmax)
-        y += (pdir(a, src, pold, mu, sm.fnoff[c * F + f] + k) - pu) * a.fc[(size_t)f * a.n3c + u];
-    }
-    if (ctop < nk - 1) {
-      if (k == ctop) {
-        const double c0 = a.coef[u], c1 = a.coef[u + 1];
-        y += (-2 * c0 - c1) * pu + c1 * __fma_rn(mu, pold[u + 1], src[u + 1]);
-      } else if (k == nk - 1) {
-        const double c0 = a.coef[u];
-        y += c0 * __fma_rn(mu, pold[u - 1], src[u - 1]) - c0 * pu;
-      } else {
-        const double c0 = a.coef[u], c1 = a.coef[u + 1];
-        y += c0 * __fma_rn(mu, pold[u - 1], src[u - 1]) - (c0 + c1) * pu + c1 * __fma_rn(mu, pold[u + 1], src[u + 1]);
-      }
-    } else {
-      y -= 2.0 * a.coef[u] * pu;
-    }
-  }
-  return y;
 }
 
 // ---------------------------------------------------------------------------
@@ -252,7 +158,6 @@ template <int QP>
 __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
   __shared__ int s_start[kMaxTileCols + 1];
   __shared__ double s_red[4 * (kBlock / 32)];
-  __shared__ QTileSmem s_tile;
   SolveCtl* ctl = a.ctl;
   const int G = gridDim.x;
   const int F = a.F;
@@ -273,7 +178,6 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
       a.z[u] = 0.0;
       a.r[u] = 0.0;
       a.rt[u] = 0.0;
-      a.p2[u] = 0.0;
       double diag = 0.0;
       for (int f = 0; f < F; ++f) {
         const int nb = a.nbr[j * F + f];
@@ -352,7 +256,6 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
   for (int u = a.n3c + blockIdx.x * kBlock + tid; u < a.n3; u += G * kBlock) {
     a.x[u] = a.q_in[u];
     a.p[u] = a.src_in[u];
-    a.p2[u] = a.src_in[u];
     if (QP == 1) a.c[u] = a.c_in[u];
   }
   if (!grid_sync(ctl, 1, [] {})) return;
@@ -446,7 +349,6 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
             ctl->eps = eps;
             ctl->eps0 = eps0;
             ctl->n = 0;
-            ctl->mu = 0.0;  // the first apply takes p as set here (p = r + 0 p)
             ctl->done = (a.maxiters <= 0 || eps == 0) ? 1 : 0;
             __threadfence();
           }
@@ -455,34 +357,24 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
   }
 
   // ---- the CG loop (2478-2525) ----
-  // S3 left the first direction in p; later directions alternate p2, p, ...
-  const double* dsrc = (QP == 2) ? a.rt : a.r;
-  for (int par = 0;; par ^= 1) {
+  for (;;) {
     if (ld_volatile_int(&ctl->done)) break;
-    const double* pold = par ? a.p2 : a.p;
-    double* pnew = par ? a.p : a.p2;
-    // A: p = r + mu p (on the fly, 2522-2524), z = A p, p.z
+    // A: z = A p, p.z
     {
-      const double mu = *(volatile double*)&ctl->mu;
       double part[1] = {0.0};
       for (int t = blockIdx.x; t < a.ntiles; t += G) {
         TileCtx tc;
-        tile_stage(a, t, tc, s_tile);
-#pragma unroll
-        for (int q = 0; q < kTileCap / kBlock; ++q) {
-          const int s = tid + q * kBlock;
-          if (s >= tc.len) continue;
-          const int c = s_tile.cmap[s];
-          const int k = s - s_tile.start[c];
-          const int w = s_tile.cn[c];
-          const int ctop = w & 0xffff, nk = w >> 16;
-          if (k < ctop) continue;
+        tile_load(a, t, tc, s_start);
+        for (int s = tid; s < tc.len; s += kBlock) {
+          const int cl = find_col(s_start, tc.ncols, s);
+          const int j = tc.c0 + cl;
+          const int k = s - s_start[cl];
           const int u = tc.base + s;
-          double pu;
-          const double zu = apply_fused<QP>(a, s_tile, dsrc, pold, mu, u, c, k, ctop, nk, pu);
+          const int ctop = a.ctop[j];
+          if (k < ctop) continue;
+          const double zu = apply_slot<QP>(a, a.p, u, j, k, ctop, a.nk[j]);
           a.z[u] = zu;
-          pnew[u] = pu;
-          part[0] += pu * zu;
+          part[0] += a.p[u] * zu;
         }
         __syncthreads();
       }
@@ -514,7 +406,7 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
         const int c0 = a.tile_col[t], c1 = a.tile_col[t + 1];
         const int base = a.dcoff[c0], end = a.dcoff[c1];
         for (int u = base + tid; u < end; u += kBlock) {
-          a.x[u] += nu * pnew[u];
+          a.x[u] += nu * a.p[u];
           const double ru = a.r[u] - nu * a.z[u];
           a.r[u] = ru;
           if (QP != 2) part[0] += ru * ru;
@@ -566,6 +458,17 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
             }
           }))
         return;
+      if (ld_volatile_int(&ctl->done)) break;
+    }
+    // C: p = r + mu p  (or rt + mu p)
+    {
+      const double mu = *(volatile double*)&ctl->mu;
+      const double* src = (QP == 2) ? a.rt : a.r;
+      for (int t = blockIdx.x; t < a.ntiles; t += G) {
+        const int base = a.dcoff[a.tile_col[t]], end = a.dcoff[a.tile_col[t + 1]];
+        for (int u = base + tid; u < end; u += kBlock) a.p[u] = src[u] + mu * a.p[u];
+      }
+      if (!grid_sync(ctl, 6, [] {})) return;
     }
   }
 

@@ -6,8 +6,6 @@
 namespace sgpu {
 
 // Arguments of the pressure-solve kernel (all pointers are device memory).
-constexpr int kQMaxF = 8;  // faces per cell the pressure kernel's tile staging holds
-
 struct QArgs {
   int F;            // maxfaces
   int ncomp;        // computational columns [0, ncomp)
@@ -46,7 +44,6 @@ struct QArgs {
   // working vectors [n3]
   double* x;
   double* p;
-  double* p2;           // second direction buffer (the loop alternates p and p2)
   double* r;
   double* z;
   double* rt;
