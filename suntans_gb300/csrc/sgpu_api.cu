@@ -38,13 +38,13 @@ struct sgpu_context {
 
   // host copies of the static grid
   int Nc = 0, Ne = 0, F = 0, Nkmax = 0, ncomp = 0, nbdy = 0;
-  std::vector<int> Nk, Nke, dev2cell, cell2dev, dcoff, eoff, tile_col, nbr, fedge;
+  std::vector<int> Nk, Nke, dev2cell, cell2dev, dcoff, eoff, tile_col, nbr, fedge, slotcol;
   long long n3 = 0, n3c = 0, ne3 = 0;
   int ntiles = 0;
 
   // device memory (static grid)
   std::vector<void*> allocs;
-  int *d_dcoff = nullptr, *d_tile = nullptr, *d_nk = nullptr, *d_nbr = nullptr, *d_fedge = nullptr,
+  int *d_dcoff = nullptr, *d_tile = nullptr, *d_slotcol = nullptr, *d_nk = nullptr, *d_nbr = nullptr, *d_fedge = nullptr,
       *d_nke = nullptr, *d_eoff = nullptr;
   double *d_Ac = nullptr, *d_df = nullptr, *d_dg = nullptr;
 
@@ -279,6 +279,9 @@ static int build_layout(sgpu_context* ctx, const sgpu_grid_desc* g) {
   }
   if (ncomp > 0) ctx->tile_col.push_back(ncomp);
   ctx->ntiles = (int)ctx->tile_col.size() - 1;
+  ctx->slotcol.assign((size_t)std::max(1, ctx->dcoff[ncomp]), 0);
+  for (int j = 0; j < ncomp; ++j)
+    for (int u = ctx->dcoff[j]; u < ctx->dcoff[j + 1]; ++u) ctx->slotcol[u] = j;
   return SGPU_OK;
 }
 
@@ -307,6 +310,7 @@ int sgpu_create(const sgpu_grid_desc* g, int device, sgpu_context** out) {
   for (int j = 0; j < ctx->Nc; ++j) nkd[j] = g->Nk[ctx->dev2cell[j]];
   if ((rc = upload(ctx, &ctx->d_dcoff, ctx->dcoff.data(), ctx->dcoff.size()))) return rc;
   if ((rc = upload(ctx, &ctx->d_tile, ctx->tile_col.data(), ctx->tile_col.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->d_slotcol, ctx->slotcol.data(), ctx->slotcol.size()))) return rc;
   if ((rc = upload(ctx, &ctx->d_nk, nkd.data(), nkd.size()))) return rc;
   if ((rc = upload(ctx, &ctx->d_nbr, ctx->nbr.data(), ctx->nbr.size()))) return rc;
   if ((rc = upload(ctx, &ctx->d_fedge, ctx->fedge.data(), ctx->fedge.size()))) return rc;
@@ -492,6 +496,7 @@ int sgpu_q_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   a.resnorm = prop->resnorm;
   a.dcoff = ctx->d_dcoff;
   a.tile_col = ctx->d_tile;
+  a.slotcol = ctx->d_slotcol;
   a.nk = ctx->d_nk;
   a.nbr = ctx->d_nbr;
   a.fedge = ctx->d_fedge;

@@ -108,6 +108,46 @@ __device__ __forceinline__ double apply_slot(const QArgs& a, const double* __res
   return y;
 }
 
+// Branch-free form of apply_slot for the loop's flat apply: every load of a
+// slot is issued unconditionally (a face that does not couple the level reads
+// the slot itself and has coefficient fc = 0; vertical neighbours outside the
+// column get coefficient 0), so the loads of several slots overlap.  The sums
+// are those of apply_slot: terms with a zero coefficient add exactly 0.
+// Dry slots (k < ctop) return 0.  FF: compile-time face count (0 = a.F).
+template <int QP, int FF>
+__device__ __forceinline__ double apply_flat(const QArgs& a, const double* __restrict__ xin, int u) {
+  const int F = FF ? FF : a.F;
+  const int j = a.slotcol[u];
+  const int k = u - a.dcoff[j];
+  const int ctop = a.ctop[j], nk = a.nk[j];
+  const bool act = k >= ctop;
+  const double xu = xin[u];
+  double y = (QP == 1) ? -xu : 0.0;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const int meta = a.fmeta[j * F + f];
+    const bool ok = act && meta >= 0 && k >= (meta & 0xffff) && k < (meta >> 16);
+    const int n = ok ? a.fnoff[j * F + f] + k : u;
+    const double w = a.fc[(size_t)f * a.n3c + u];
+    if (QP == 1) y += xin[n] * w;
+    else y += (xin[n] - xu) * w;
+  }
+  const double xm = xin[u > 0 ? u - 1 : 0], xp = xin[u + 1];
+  const double c0 = a.coef[u], c1 = a.coef[u + 1];
+  if (QP == 1) {
+    const double cm = (act && k > ctop) ? c0 : 0.0;
+    const double cp = (act && k < nk - 1) ? c1 : 0.0;
+    y += cm * xm + cp * xp;
+  } else if (ctop < nk - 1) {
+    if (k == ctop) y += (-2 * c0 - c1) * xu + c1 * xp;
+    else if (k == nk - 1) y += c0 * xm - c0 * xu;
+    else y += c0 * xm - (c0 + c1) * xu + c1 * xp;
+  } else {
+    y -= 2.0 * c0 * xu;
+  }
+  return act ? y : 0.0;
+}
+
 // Thomas solve of one column with the factors prepared at setup:
 //   d'[k] = d[k] - w[k] d'[k-1];  u[k] = (d'[k] - cup[k] u[k+1]) * ib[k]
 // cup[k] = coef[k+1] (the reference's c[k], 3589-3597).  Single-level column:
@@ -359,24 +399,33 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
   // ---- the CG loop (2478-2525) ----
   for (;;) {
     if (ld_volatile_int(&ctl->done)) break;
-    // A: z = A p, p.z
+    // A: z = A p, p.z -- flat over the computational storage: slot u of
+    // thread g is u = g + i*T (T = all threads), its column from the static
+    // slot-to-column index, so no tile barrier or column search stands between
+    // a slot's loads and the next slot's.
     {
       double part[1] = {0.0};
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        TileCtx tc;
-        tile_load(a, t, tc, s_start);
-        for (int s = tid; s < tc.len; s += kBlock) {
-          const int cl = find_col(s_start, tc.ncols, s);
-          const int j = tc.c0 + cl;
-          const int k = s - s_start[cl];
-          const int u = tc.base + s;
-          const int ctop = a.ctop[j];
-          if (k < ctop) continue;
-          const double zu = apply_slot<QP>(a, a.p, u, j, k, ctop, a.nk[j]);
+      const int T = G * kBlock;
+      if (F == 3) {
+#pragma unroll 4
+        for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
+          const double zu = apply_flat<QP, 3>(a, a.p, u);
           a.z[u] = zu;
           part[0] += a.p[u] * zu;
         }
-        __syncthreads();
+      } else if (F == 4) {
+#pragma unroll 4
+        for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
+          const double zu = apply_flat<QP, 4>(a, a.p, u);
+          a.z[u] = zu;
+          part[0] += a.p[u] * zu;
+        }
+      } else {
+        for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
+          const double zu = apply_flat<QP, 0>(a, a.p, u);
+          a.z[u] = zu;
+          part[0] += a.p[u] * zu;
+        }
       }
       block_sum<1>(part, s_red);
       if (tid == 0) a.partials[blockIdx.x] = part[0];
@@ -402,16 +451,25 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
     {
       const double nu = *(volatile double*)&ctl->nu;
       double part[2] = {0.0, 0.0};
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
+      if (QP != 2) {
+        const int T = G * kBlock;
+#pragma unroll 4
+        for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
+          a.x[u] += nu * a.p[u];
+          const double ru = a.r[u] - nu * a.z[u];
+          a.r[u] = ru;
+          part[0] += ru * ru;
+        }
+      }
+      for (int t = blockIdx.x; QP == 2 && t < a.ntiles; t += G) {
         const int c0 = a.tile_col[t], c1 = a.tile_col[t + 1];
         const int base = a.dcoff[c0], end = a.dcoff[c1];
         for (int u = base + tid; u < end; u += kBlock) {
           a.x[u] += nu * a.p[u];
           const double ru = a.r[u] - nu * a.z[u];
           a.r[u] = ru;
-          if (QP != 2) part[0] += ru * ru;
         }
-        if (QP == 2) {
+        {
           __syncthreads();
           for (int c = c0 + tid; c < c1; c += kBlock)
             column_solve(a, a.r, a.rt, a.dcoff[c], a.ctop[c], a.nk[c]);
@@ -464,10 +522,9 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
     {
       const double mu = *(volatile double*)&ctl->mu;
       const double* src = (QP == 2) ? a.rt : a.r;
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        const int base = a.dcoff[a.tile_col[t]], end = a.dcoff[a.tile_col[t + 1]];
-        for (int u = base + tid; u < end; u += kBlock) a.p[u] = src[u] + mu * a.p[u];
-      }
+      const int T = G * kBlock;
+#pragma unroll 4
+      for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) a.p[u] = src[u] + mu * a.p[u];
       if (!grid_sync(ctl, 6, [] {})) return;
     }
   }

@@ -19,6 +19,7 @@ struct QArgs {
   // static grid (device order)
   const int* dcoff;     // [ncols+1]
   const int* tile_col;  // [ntiles+1]
+  const int* slotcol;   // [n3c] column of each computational storage slot
   const int* nk;        // [ncols]
   const int* nbr;       // [ncomp*F] neighbour column or -1
   const int* fedge;     // [ncomp*F] edge index
