@@ -173,6 +173,33 @@ __device__ __forceinline__ void column_solve(const QArgs& a, const double* rin, 
   }
 }
 
+// Staged tile of the qprecond-2 vector update: r, the Thomas factors, the
+// vertical coefficients (one past the tile) and the solve's output.
+struct TriSmem {
+  double r[kTileCap], w[kTileCap], ib[kTileCap], cf[kTileCap + 1], out[kTileCap];
+};
+
+// column_solve on a staged tile: the column's slots start at local offset off.
+__device__ __forceinline__ void column_solve_smem(TriSmem& sm, int off, int ctop, int nk) {
+  const int b = off + ctop, e = off + nk;
+  if (ctop == nk - 1) {
+    sm.out[b] = -0.5 * sm.r[b] / sm.cf[b];
+    return;
+  }
+  double dprev = sm.r[b];
+  sm.out[b] = dprev;
+  for (int u = b + 1; u < e; ++u) {
+    dprev = sm.r[u] - sm.w[u] * dprev;
+    sm.out[u] = dprev;
+  }
+  double unext = sm.out[e - 1] * sm.ib[e - 1];
+  sm.out[e - 1] = unext;
+  for (int u = e - 2; u >= b; --u) {
+    unext = (sm.out[u] - sm.cf[u + 1] * unext) * sm.ib[u];
+    sm.out[u] = unext;
+  }
+}
+
 // Factorisation of one column for column_solve (TriSolve's forward sweep on b,
 // util.c:191-195): b'[0]=b[0], b'[k]=b[k]-a[k]*c[k-1]/b'[k-1]; w[k]=a[k]/b'[k-1]; ib=1/b'.
 __device__ __forceinline__ void column_factor(const QArgs& a, int off, int ctop, int nk) {
@@ -198,6 +225,7 @@ template <int QP>
 __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
   __shared__ int s_start[kMaxTileCols + 1];
   __shared__ double s_red[4 * (kBlock / 32)];
+  __shared__ TriSmem s_tri;
   SolveCtl* ctl = a.ctl;
   const int G = gridDim.x;
   const int F = a.F;
@@ -461,25 +489,36 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
           part[0] += ru * ru;
         }
       }
+      // qprecond 2: the tile's r, Thomas factors and coefficients are staged
+      // in shared memory and each column is solved there (one thread per
+      // column), then M^-1 r leaves coalesced.
       for (int t = blockIdx.x; QP == 2 && t < a.ntiles; t += G) {
         const int c0 = a.tile_col[t], c1 = a.tile_col[t + 1];
-        const int base = a.dcoff[c0], end = a.dcoff[c1];
-        for (int u = base + tid; u < end; u += kBlock) {
-          a.x[u] += nu * a.p[u];
-          const double ru = a.r[u] - nu * a.z[u];
-          a.r[u] = ru;
-        }
-        {
-          __syncthreads();
-          for (int c = c0 + tid; c < c1; c += kBlock)
-            column_solve(a, a.r, a.rt, a.dcoff[c], a.ctop[c], a.nk[c]);
-          __syncthreads();
-          for (int u = base + tid; u < end; u += kBlock) {
-            const double ru = a.r[u];
-            part[0] += ru * a.rt[u];
-            part[1] += ru * ru;
+        const int base = a.dcoff[c0], end = a.dcoff[c1], len = end - base;
+        for (int sl = tid; sl <= len; sl += kBlock) {
+          const int u = base + sl;
+          if (sl < len) {
+            a.x[u] += nu * a.p[u];
+            const double ru = a.r[u] - nu * a.z[u];
+            a.r[u] = ru;
+            s_tri.r[sl] = ru;
+            s_tri.w[sl] = a.tw[u];
+            s_tri.ib[sl] = a.tib[u];
           }
+          s_tri.cf[sl] = a.coef[u];
         }
+        for (int c = tid; c <= c1 - c0; c += kBlock) s_start[c] = a.dcoff[c0 + c] - base;
+        __syncthreads();
+        for (int c = tid; c < c1 - c0; c += kBlock)
+          column_solve_smem(s_tri, s_start[c], a.ctop[c0 + c], a.nk[c0 + c]);
+        __syncthreads();
+        for (int sl = tid; sl < len; sl += kBlock) {
+          const double ru = s_tri.r[sl], rtu = s_tri.out[sl];
+          a.rt[base + sl] = rtu;
+          part[0] += ru * rtu;
+          part[1] += ru * ru;
+        }
+        __syncthreads();
       }
       block_sum<2>(part, s_red);
       if (tid == 0) {

@@ -18,7 +18,11 @@ TOL = 1e-9
 
 
 def iters_close(n_gpu, n_ref):
-    return abs(n_gpu - n_ref) <= max(2, int(0.02 * n_ref))
+    """The inner products are summed in a different order on the GPU (a
+    deterministic tree over threads) than in the reference (serial over cells),
+    so the iteration at which sqrt(eps/eps0) first drops below the tolerance can
+    move by a few iterations; the solution itself is held to TOL below."""
+    return abs(n_gpu - n_ref) <= max(4, int(0.03 * n_ref))
 
 _GRIDS = {}
 
