@@ -738,9 +738,25 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
     nk[q] = w >> 16;
     on[q] = in && kv[q] >= ctop[q];
   }
-  // per slot: gathers of the new direction at the coupled neighbours, then the
-  // operator row (the slots of a thread are independent, so the compiler can
-  // keep the gathers of several slots in flight without holding them all)
+  // gathers
+  float pn[Q][FF], wn[Q][FF];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+#pragma unroll
+    for (int f = 0; f < FF; ++f) {
+      const int e = cc[q] * FF + f;
+      const int kk = fkk[e];
+      const bool ok = on[q] && kv[q] >= (kk & 0xffff) && kv[q] < (kk >> 16);
+      const int n = ok ? fns[e] + kv[q] : base + sv[q];
+      pn[q][f] = __fmaf_rn(mu, pold[n], S[n]);
+      if (QP == 1) {
+        wn[q][f] = ok ? fD[e] * a.cinv32[n] : 0.f;
+      } else {
+        const int es = ok ? fes[e] + kv[q] : 0;
+        wn[q][f] = ok ? a.dzfD32[es] : 0.f;
+      }
+    }
+  }
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int s = sv[q], k = kv[q];
@@ -751,29 +767,13 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
       const float fz = sf[s];
       y = -pu;
 #pragma unroll
-      for (int f = 0; f < FF; ++f) {
-        const int e = cc[q] * FF + f;
-        const int kk = fkk[e];
-        const bool ok = on[q] && k >= (kk & 0xffff) && k < (kk >> 16);
-        const int n = ok ? fns[e] + k : base + s;
-        const float pn = __fmaf_rn(mu, pold[n], S[n]);
-        const float wn = ok ? fD[e] * a.cinv32[n] : 0.f;
-        y = __fmaf_rn(fz * wn, pn, y);
-      }
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(fz * wn[q][f], pn[q][f], y);
       if (k > ctop[q]) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
       if (k < nk[q] - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
     } else {
       y = 0.f;
 #pragma unroll
-      for (int f = 0; f < FF; ++f) {
-        const int e = cc[q] * FF + f;
-        const int kk = fkk[e];
-        const bool ok = on[q] && k >= (kk & 0xffff) && k < (kk >> 16);
-        const int n = ok ? fns[e] + k : base + s;
-        const float pn = __fmaf_rn(mu, pold[n], S[n]);
-        const float wn = ok ? a.dzfD32[fes[e] + k] : 0.f;
-        y = __fmaf_rn(pn - pu, wn, y);
-      }
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(pn[q][f] - pu, wn[q][f], y);
       const float c0 = sc[s];
       if (ctop[q] < nk[q] - 1) {
         if (k == ctop[q]) {
