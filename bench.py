@@ -65,6 +65,14 @@ def q_bytes_per_unknown_iter(qprecond: int, F: int) -> int:
     return S * (12 + F + (3 if qprecond == 2 else 0))
 
 
+# DRAM bytes per unknown-iteration measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch ÷ its unknowns × iterations) on smaller
+# cases of the same constructions; a launch's traffic grows in proportion to
+# unknowns × iterations, so `traffic` below scales these to the launch timed.
+# profiles/cgsolveq_kernel_fp64_seamount50k.md, profiles/batch_kernel_mixed_seamount250k.md
+MEASURED_TRAFFIC_PER_UNKNOWN_ITER = {"cgsolveq_kernel<1>": 118.8, "batch_kernel<1>": 56.6}
+
+
 def h_bytes_per_unknown_iter(F: int) -> int:
     """Free surface: apply s(3+F) + 4F bytes of neighbour indices, update 6s, Jacobi + direction 4s."""
     return S * (13 + F) + 4 * F
@@ -168,6 +176,12 @@ class ClockSampler:
                         reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic(kernel, unknown_iters):
+    """DRAM bytes of one launch from the ncu-measured bytes per unknown-iteration (None if not measured)."""
+    b = MEASURED_TRAFFIC_PER_UNKNOWN_ITER.get(kernel)
+    return None if b is None else b * unknown_iters
 
 
 def peaks():
@@ -310,7 +324,8 @@ def run_ours(args):
                              f"{(13 + g.maxfaces) * 8 * g.n3 / 1e9:.2f} GB > 129 MB L2",
                        "iters_q": int(np.median(nq)), "iters_h": int(np.median(nh))},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": traffic(f"cgsolveq_kernel<{props.qprecond}>",
+                                                                     g.n_q() * float(np.mean(nq))),
                          "kernel": f"cgsolveq_kernel<{props.qprecond}>", "bytes_per_unknown_iter": bpu,
                          "peak_kind": peak_kind},
             "e2e": {"value": e2e_work / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
@@ -451,7 +466,8 @@ def bench_cfg3(args):
             "mixed": mf, "plain_fp64_unknown_iters_per_s": plain_rate, "iters_fp64": int(s64.niters),
             "speedup_vs_plain_fp64": mf["equivalent_unknown_iters_per_s"] / plain_rate,
             "roofline": {"bound": "hbm", "achieved": mf["achieved_gbs_fp32_inner"], "peak": peak, "unit": "GB/s",
-                         "frac": mf["achieved_gbs_fp32_inner"] / peak, "traffic": None,
+                         "frac": mf["achieved_gbs_fp32_inner"] / peak,
+                         "traffic": traffic(f"batch_kernel<{args.qprecond}>", N * mf["iters_inner"]),
                          "kernel": f"batch_kernel<{args.qprecond}>",
                          "bytes_per_unknown_iter": FP32_BYTES_PER_UNKNOWN_ITER, "peak_kind": peak_kind},
             "e2e": {"value": N * st.niters / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
@@ -549,7 +565,8 @@ def bench_cfg4(args):
                        "status_ok": int(sum(st.status == 0 for _, st in res))},
             "autotune": table,
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": None, "kernel": f"batch_kernel<{args.qprecond}>",
+                         "traffic": traffic(f"batch_kernel<{args.qprecond}>", float((Ns * itm).sum())),
+                         "kernel": f"batch_kernel<{args.qprecond}>",
                          "bytes_per_unknown_iter": FP32_BYTES_PER_UNKNOWN_ITER, "peak_kind": peak_kind},
             "e2e": {"value": e2e_work / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(8 * Ns.sum())},
