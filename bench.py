@@ -96,6 +96,7 @@ def parse():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--chunk", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="cfg5: launch directly instead of graph replays")
     ap.add_argument("--qprecond", type=int, default=1)
     ap.add_argument("--points", type=int, default=200_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -581,13 +582,13 @@ def bench_cfg4(args):
 def bench_cfg5(args):
     from suntans_gb300 import gridgen as gg
     from suntans_gb300.batch import Batch, capacity_for, request_bytes
-    from suntans_gb300.serve import Request, Server, latency_report, poisson_stream
+    from suntans_gb300.serve import PrefetchedSources, Request, Server, latency_report, poisson_stream
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pool = gg.serving_pool(n=args.pool, seed=5, workers=None)
     grids = [p[0].grid for p in pool]
     need = sum(request_bytes(g, args.qprecond) for g in grids)
     b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
-    b.use_graph(True)
+    b.use_graph(not args.no_graph)
     srv = Server(pool, b, args.budget_gb * 1e9, lambda g: request_bytes(g, args.qprecond), chunk=args.chunk,
                  maxiters=5000, keep_q=False)
     # warm-up: one untimed request per grid (cold starts; every grid resident)
@@ -596,14 +597,20 @@ def bench_cfg5(args):
 
     def stream(rate, seconds, seed):
         reqs = poisson_stream(len(pool), len(pool[0]), rate, seconds, seed=seed)
+        # the clients prepare each request's right-hand side ahead of its arrival
+        pre = PrefetchedSources(pool, reqs, workers=4, depth=64)
+        srv.sources = pre.get
+        srv.host_s = {k: 0.0 for k in srv.host_s}
         l0, ms0 = srv.launches, srv.device_ms
         sampler = ClockSampler(local)
         sampler.start()
         srv.run(reqs, realtime=True, drain_limit=seconds + args.drain_seconds)
         clocks = sampler.stop()
+        pre.close()
         rep = latency_report(reqs, srv.t_end)
         rep.update(rate=rate, seconds=seconds, launches=srv.launches - l0,
-                   device_busy_frac=(srv.device_ms - ms0) / 1e3 / max(srv.t_end, 1e-9))
+                   device_busy_frac=(srv.device_ms - ms0) / 1e3 / max(srv.t_end, 1e-9),
+                   host_s={k: round(v, 3) for k, v in srv.host_s.items()})
         return rep, clocks, reqs
 
     rep, clocks, reqs = stream(args.rate, args.serve_seconds, 7)
@@ -623,7 +630,7 @@ def bench_cfg5(args):
                                    "{1e-8, 1e-10}, warm starts",
                        "hbm_budget_gb": args.budget_gb, "pool_resident_gb": need / 1e9, "chunk_iters": args.chunk,
                        "qprecond": args.qprecond, "step": "one launch of the serving loop",
-                       "drain_limit_s": args.drain_seconds},
+                       "drain_limit_s": args.drain_seconds, "graph": not args.no_graph},
             "latency": rep, "latency_at_sustainable_rate": rep2, "evictions": srv.evictions,
             "e2e": {"value": rep["unknown_iters_per_s"], "unit": "unknown-iters/s",
                     "h2d_bytes_per_step": int(sum(8 * pool[r.grid][0].grid.n3 for r in reqs if r.t_admit >= 0)

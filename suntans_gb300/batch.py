@@ -109,13 +109,18 @@ class Batch:
     def state(self, i) -> int:
         return self.lib.sgpu_batch_state(self.h, int(i))
 
-    def result(self, i, q0=None, release=True):
-        """(q, Stats) of a finished problem; q starts from q0 (entries outside the active set kept)."""
+    def result(self, i, q0=None, release=True, out=None):
+        """(q, Stats) of a finished problem; q starts from q0 (entries outside the
+        active set kept), or the solution is written into `out` (flat ragged
+        float64 array of the grid, reused by the caller) when given."""
         g = self.grids[i]
         st = Stats()
-        if q0 is None:
-            q0 = np.zeros(g.n3)
-        q = np.array(q0, dtype=np.float64, copy=True)
+        if out is not None:
+            q = out
+        else:
+            if q0 is None:
+                q0 = np.zeros(g.n3)
+            q = np.array(q0, dtype=np.float64, copy=True)
         ptr = jagged(q, g.coff)
         rc = self.lib.sgpu_batch_result(self.h, int(i), ptr.ctypes.data_as(_dpp), C.byref(st), int(release))
         if rc != OK:

@@ -2142,17 +2142,27 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
   if (q) {
     if (I.state != INST_DONE) return bfail(b, SGPU_BAD_ARG, "instance %d has not finished", id);
     Guard gd(b->device);
-    std::vector<double> x(H.n3c), c(H.n3c, 1.0);
-    BCK(cudaMemcpyAsync(x.data(), b->a.x64 + H.s_off, 8 * H.n3c, cudaMemcpyDeviceToHost, b->stream));
-    if (b->qprecond == 1)
-      BCK(cudaMemcpyAsync(c.data(), b->a.c64 + H.s_off, 8 * H.n3c, cudaMemcpyDeviceToHost, b->stream));
+    // x64 (and c64 for qprecond 1) copied once into pinned staging, then
+    // unscaled and scattered row by row
+    const long long n = H.n3c, need = (b->qprecond == 1 ? 2 : 1) * n;
+    if (b->h_stage_n < need) {
+      if (b->h_stage) cudaFreeHost(b->h_stage);
+      b->h_stage = nullptr;
+      BCK(cudaMallocHost((void**)&b->h_stage, sizeof(double) * need));
+      b->h_stage_n = need;
+    }
+    double* x = b->h_stage;
+    double* c = b->h_stage + n;
+    BCK(cudaMemcpyAsync(x, b->a.x64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->stream));
+    if (b->qprecond == 1) BCK(cudaMemcpyAsync(c, b->a.c64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     for (int j = 0; j < H.ncomp; ++j) {
-      const int i = H.dev2cell[j];
-      for (int k = H.ctop[i]; k < H.Nk[i]; ++k) {
-        const int u = H.coff[j] + k;
-        q[i][k] = b->qprecond == 1 ? x[u] / c[u] : x[u];
-      }
+      const int i = H.dev2cell[j], k0 = H.ctop[i];
+      const long long o = H.coff[j];
+      if (b->qprecond == 1)
+        for (int k = k0; k < H.Nk[i]; ++k) q[i][k] = x[o + k] / c[o + k];
+      else
+        std::memcpy(q[i] + k0, x + o + k0, sizeof(double) * (H.Nk[i] - k0));
     }
   }
   if (release) {

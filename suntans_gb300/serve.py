@@ -80,11 +80,43 @@ def request_src(pool, r: Request):
     return (1.0 - r.mix) * p.src + r.mix * o.src
 
 
+class PrefetchedSources:
+    """Right-hand sides of a request stream prepared ahead of arrival by worker
+    threads (the stream's clients), so that producing them is not part of the
+    server's critical path.  `get(r)` returns request r's array; at most
+    `depth` requests beyond the latest one asked for are prepared."""
+
+    def __init__(self, pool, reqs, workers=2, depth=64):
+        import concurrent.futures as cf
+        self.pool, self.depth = pool, depth
+        self.reqs = sorted(reqs, key=lambda r: r.t_arrival)
+        self.pos = {r.rid: k for k, r in enumerate(self.reqs)}
+        self.ex = cf.ThreadPoolExecutor(workers)
+        self.fut = {}
+        self.next = 0
+        self._fill(0)
+
+    def _fill(self, upto):
+        while self.next < len(self.reqs) and self.next <= upto + self.depth:
+            r = self.reqs[self.next]
+            self.fut[r.rid] = self.ex.submit(request_src, self.pool, r)
+            self.next += 1
+
+    def get(self, r):
+        self._fill(self.pos.get(r.rid, 0))
+        f = self.fut.pop(r.rid, None)
+        return f.result() if f is not None else request_src(self.pool, r)
+
+    def close(self):
+        self.ex.shutdown(wait=False, cancel_futures=True)
+
+
 class Server:
-    """pool[g] is a list of QProblem on grid g (its stored right-hand sides)."""
+    """pool[g] is a list of QProblem on grid g (its stored right-hand sides).
+    sources: callable request -> right-hand side (default: request_src)."""
 
     def __init__(self, pool, engine, budget_bytes, request_bytes, chunk=64, maxiters=20000, keep_q=True,
-                 clock=time.perf_counter):
+                 clock=time.perf_counter, sources=None):
         self.pool = pool
         self.engine = engine
         self.budget = float(budget_bytes)
@@ -102,6 +134,9 @@ class Server:
         self.work = 0
         self.device_ms = 0.0
         self.t0 = self.clock()
+        self.sources = sources or (lambda r: request_src(pool, r))
+        self.qbuf = {}  # grid -> reusable result buffer when results are not kept
+        self.host_s = {"admit": 0.0, "launch": 0.0, "harvest": 0.0}  # wall time by loop part
 
     # -- admission --------------------------------------------------------
     def _evict_one(self, avoid) -> bool:
@@ -121,7 +156,7 @@ class Server:
         if g in self.resident:
             iid = self.resident.pop(g)
             self.resident[g] = iid  # most recently used
-            self.engine.resubmit(iid, request_src(self.pool, r), tol=r.tol, maxiters=self.maxiters, warm=True)
+            self.engine.resubmit(iid, self.sources(r), tol=r.tol, maxiters=self.maxiters, warm=True)
             self.resubmits += 1
             r.warm = True
         else:
@@ -132,7 +167,7 @@ class Server:
                     return False
             prob = self.pool[g][r.rhs]
             if r.mix != 0.0:
-                prob = type(prob)(**{**prob.__dict__, "src": request_src(self.pool, r)})
+                prob = type(prob)(**{**prob.__dict__, "src": self.sources(r)})
             while True:
                 try:
                     iid = self.engine.add(prob, tol=r.tol, maxiters=self.maxiters)
@@ -152,8 +187,12 @@ class Server:
         for g, r in list(self.busy.items()):
             iid = self.resident[g]
             if self.engine.state(iid) == 3:  # INST_DONE
-                q0 = self.pool[g][r.rhs].q if self.keep_q else None
-                q, st = self.engine.result(iid, q0, release=False)
+                if self.keep_q:
+                    q, st = self.engine.result(iid, self.pool[g][r.rhs].q, release=False)
+                else:
+                    if g not in self.qbuf:
+                        self.qbuf[g] = np.zeros(self.pool[g][0].grid.n3)
+                    q, st = self.engine.result(iid, None, release=False, out=self.qbuf[g])
                 r.t_done = self.clock() - self.t0
                 r.launch_done = self.launches
                 r.iters, r.status, r.unknowns = int(st.niters), int(st.status), int(st.unknowns)
@@ -177,17 +216,23 @@ class Server:
                 i += 1
             # admit in arrival order; a request whose grid is busy waits without blocking others
             blocked = set()
+            t1 = self.clock()
             for _ in range(len(pending)):
                 r = pending.popleft()
                 if r.grid in blocked or not self._admit(r):
                     blocked.add(r.grid)
                     pending.append(r)
+            t2 = self.clock()
+            self.host_s["admit"] += t2 - t1
             if self.busy:
                 _, ms, work = self.engine.run(max_iters=self.chunk)
+                t3 = self.clock()
                 self.launches += 1
                 self.work += work
                 self.device_ms += ms
                 self._harvest()
+                self.host_s["launch"] += t3 - t2
+                self.host_s["harvest"] += self.clock() - t3
             elif i < len(reqs):
                 if pending:
                     raise RuntimeError("requests pending with nothing running: budget too small")

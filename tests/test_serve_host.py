@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from suntans_gb300.capi import OOM, SolverError
-from suntans_gb300.serve import Request, Server, latency_report, poisson_stream, request_src
+from suntans_gb300.serve import PrefetchedSources, Request, Server, latency_report, poisson_stream, request_src
 
 
 class FakeEngine:
@@ -55,7 +55,7 @@ class FakeEngine:
     def state(self, i):
         return self.inst[i]["state"]
 
-    def result(self, i, q0, release=False):
+    def result(self, i, q0, release=False, out=None):
         I = self.inst[i]
         st = types.SimpleNamespace(niters=I["it"], status=0, unknowns=I["n"])
         if release:
@@ -69,7 +69,7 @@ class FakeEngine:
 def fake_pool(sizes, rhs=2):
     pool = []
     for gid, n in enumerate(sizes):
-        g = types.SimpleNamespace(n3=n, gid=gid)
+        g = types.SimpleNamespace(n3=n, gid=gid)  # n3: storage slots
         pool.append([types.SimpleNamespace(grid=g, src=np.full(3, float(j + 1)), q=None) for j in range(rhs)])
     return pool
 
@@ -163,3 +163,18 @@ def test_poisson_stream_and_realtime_loop():
     rep = latency_report(reqs, srv.t_end)
     assert rep["completed"] == n and rep["p99_ms"] >= rep["p50_ms"] > 0
     assert rep["status_counts"] == {0: n}
+
+
+def test_prefetched_sources_equal_direct():
+    pool = fake_pool([10, 20], rhs=3)
+    reqs = poisson_stream(2, 3, rate=1000.0, seconds=0.2, seed=5)
+    pre = PrefetchedSources(pool, reqs, workers=2, depth=8)
+    try:
+        for r in reqs:
+            assert np.array_equal(pre.get(r), request_src(pool, r))
+    finally:
+        pre.close()
+    srv = Server(pool, FakeEngine(10_000), 1e12, rbytes, chunk=16, keep_q=False,
+                 sources=PrefetchedSources(pool, reqs).get)
+    srv.run(reqs, realtime=False)
+    assert all(r.t_done >= 0 for r in reqs)
