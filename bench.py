@@ -96,7 +96,8 @@ def parse():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--chunk", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--no-graph", action="store_true", help="cfg5: launch directly instead of graph replays")
+    ap.add_argument("--graph", action="store_true",
+                    help="cfg5: replay launches from CUDA graphs (re-captured whenever the set of problems changes)")
     ap.add_argument("--qprecond", type=int, default=1)
     ap.add_argument("--points", type=int, default=200_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -588,7 +589,7 @@ def bench_cfg5(args):
     grids = [p[0].grid for p in pool]
     need = sum(request_bytes(g, args.qprecond) for g in grids)
     b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
-    b.use_graph(not args.no_graph)
+    b.use_graph(args.graph)
     srv = Server(pool, b, args.budget_gb * 1e9, lambda g: request_bytes(g, args.qprecond), chunk=args.chunk,
                  maxiters=5000, keep_q=False)
     # warm-up: one untimed request per grid (cold starts; every grid resident)
@@ -630,7 +631,7 @@ def bench_cfg5(args):
                                    "{1e-8, 1e-10}, warm starts",
                        "hbm_budget_gb": args.budget_gb, "pool_resident_gb": need / 1e9, "chunk_iters": args.chunk,
                        "qprecond": args.qprecond, "step": "one launch of the serving loop",
-                       "drain_limit_s": args.drain_seconds, "graph": not args.no_graph},
+                       "drain_limit_s": args.drain_seconds, "graph": args.graph},
             "latency": rep, "latency_at_sustainable_rate": rep2, "evictions": srv.evictions,
             "e2e": {"value": rep["unknown_iters_per_s"], "unit": "unknown-iters/s",
                     "h2d_bytes_per_step": int(sum(8 * pool[r.grid][0].grid.n3 for r in reqs if r.t_admit >= 0)

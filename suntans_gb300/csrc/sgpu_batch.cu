@@ -46,6 +46,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/suntans_gb300.h"
@@ -1453,6 +1454,25 @@ struct Range {
   long long off = 0, len = 0;
 };
 
+// Runs fn(begin, end) over [0, n) on up to 8 host threads (one per `grain`
+// items), for the per-column copies between caller rows and pinned staging.
+template <class Fn>
+static void host_split(long long n, long long grain, Fn&& fn) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::min<long long>(std::min(hw, 8u), std::max(1LL, n / std::max(1LL, grain)));
+  if (nt <= 1) {
+    fn(0LL, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const long long chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    const long long b = t * chunk, e = std::min(n, b + chunk);
+    if (b < e) th.emplace_back([&fn, b, e] { fn(b, e); });
+  }
+  for (auto& x : th) x.join();
+}
+
 // first-fit allocator over [0, cap) in units of `unit`
 struct Arena {
   long long cap = 0, unit = 1;
@@ -2156,14 +2176,17 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
     BCK(cudaMemcpyAsync(x, b->a.x64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->stream));
     if (b->qprecond == 1) BCK(cudaMemcpyAsync(c, b->a.c64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
-    for (int j = 0; j < H.ncomp; ++j) {
-      const int i = H.dev2cell[j], k0 = H.ctop[i];
-      const long long o = H.coff[j];
-      if (b->qprecond == 1)
-        for (int k = k0; k < H.Nk[i]; ++k) q[i][k] = x[o + k] / c[o + k];
-      else
-        std::memcpy(q[i] + k0, x + o + k0, sizeof(double) * (H.Nk[i] - k0));
-    }
+    const bool scaled = b->qprecond == 1;
+    host_split(H.ncomp, 8192, [&](long long jb, long long je) {
+      for (long long j = jb; j < je; ++j) {
+        const int i = H.dev2cell[j], k0 = H.ctop[i];
+        const long long o = H.coff[j];
+        if (scaled)
+          for (int k = k0; k < H.Nk[i]; ++k) q[i][k] = x[o + k] / c[o + k];
+        else
+          std::memcpy(q[i] + k0, x + o + k0, sizeof(double) * (H.Nk[i] - k0));
+      }
+    });
   }
   if (release) {
     b->slots.release(H.s_off, H.n3 + 4);
@@ -2200,11 +2223,16 @@ int sgpu_batch_resubmit(sgpu_batch* b, int id, const double* const* src, double 
       BCK(cudaMallocHost((void**)&b->h_stage, sizeof(double) * H.n3c));
       b->h_stage_n = H.n3c;
     }
-    std::fill(b->h_stage, b->h_stage + H.n3c, 0.0);
-    for (int j = 0; j < H.ncomp; ++j) {
-      const int i = H.dev2cell[j];
-      std::memcpy(b->h_stage + H.coff[j], src[i], sizeof(double) * H.Nk[i]);
-    }
+    double* stg = b->h_stage;
+    host_split(H.ncomp, 8192, [&](long long jb, long long je) {
+      // this range's columns and the padding after each (up to the next column)
+      for (long long j = jb; j < je; ++j) {
+        const int i = H.dev2cell[j];
+        const long long o = H.coff[j], end = (j + 1 < H.ncomp) ? H.coff[j + 1] : H.n3c;
+        std::memcpy(stg + o, src[i], sizeof(double) * H.Nk[i]);
+        std::fill(stg + o + H.Nk[i], stg + end, 0.0);
+      }
+    });
     BCK(cudaMemcpyAsync(b->d_src64 + H.s_off, b->h_stage, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
   }
   if (warm || src) BCK(cudaStreamSynchronize(b->stream));
