@@ -206,22 +206,26 @@ class Server:
         request at once (arrival times ignored).  drain_limit (s) stops the loop
         with requests unfinished.  Returns the requests."""
         reqs = sorted(requests, key=lambda r: r.t_arrival)
-        pending = collections.deque()
+        queues = collections.OrderedDict()  # grid -> deque of waiting requests, in arrival order
+        npending = 0
         self.t0 = self.clock()
         i = 0
         while True:
             now = self.clock() - self.t0
             while i < len(reqs) and (not realtime or reqs[i].t_arrival <= now):
-                pending.append(reqs[i])
+                queues.setdefault(reqs[i].grid, collections.deque()).append(reqs[i])
+                npending += 1
                 i += 1
-            # admit in arrival order; a request whose grid is busy waits without blocking others
-            blocked = set()
+            # admit the oldest waiting request of every idle grid, oldest first;
+            # a grid's later requests wait for its earlier ones
             t1 = self.clock()
-            for _ in range(len(pending)):
-                r = pending.popleft()
-                if r.grid in blocked or not self._admit(r):
-                    blocked.add(r.grid)
-                    pending.append(r)
+            heads = sorted((q[0].t_arrival, g) for g, q in queues.items() if q and g not in self.busy)
+            for _, g in heads:
+                if self._admit(queues[g][0]):
+                    queues[g].popleft()
+                    npending -= 1
+                    if not queues[g]:
+                        del queues[g]
             t2 = self.clock()
             self.host_s["admit"] += t2 - t1
             if self.busy:
@@ -233,13 +237,13 @@ class Server:
                 self._harvest()
                 self.host_s["launch"] += t3 - t2
                 self.host_s["harvest"] += self.clock() - t3
+            elif npending:
+                raise RuntimeError("requests pending with nothing running: budget too small")
             elif i < len(reqs):
-                if pending:
-                    raise RuntimeError("requests pending with nothing running: budget too small")
                 wait = reqs[i].t_arrival - (self.clock() - self.t0)
                 if wait > 0:
                     time.sleep(min(wait, 0.001))
-            elif not pending:
+            else:
                 break
             if drain_limit is not None and self.clock() - self.t0 > drain_limit:
                 break
