@@ -34,7 +34,7 @@ def stream():
     stopping rule, a warm start from the solution of the very same right-hand
     side would have to push the residual below round-off."""
     tols = (1e-8, 1e-10)
-    reqs = [Request(k, g, (k // 3) % 2, tols[k % 2], 0.0, mix=0.03 * k) for k, g in enumerate(SEQ)]
+    reqs = [Request(k, g, (k // 3) % 2, tols[k % 2], 0.001 * k, mix=0.03 * k) for k, g in enumerate(SEQ)]
     w = [1 - r.mix if r.rhs == 0 else r.mix for r in reqs]  # weight of the first stored right-hand side
     assert min(abs(a - b) for i, a in enumerate(w) for b in w[:i]) > 0.02
     return reqs
