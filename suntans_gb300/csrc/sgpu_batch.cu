@@ -515,7 +515,7 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   sd->nu = pi.nu;
   const bool hdr = (PH == 0) || (QP == 2);
   uint32_t bytes = 0;
-  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + (QP == 1 ? 4 * n4 : 0);
+  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + (QP == 1 ? a.F * 4 * n4 : 0);
   else bytes = (hdr ? d.hdr_bytes : 0) + 4 * 4 * n4;
   fence_proxy_async();
   mbar_arrive_expect_tx(&P.full[b], bytes);
@@ -526,7 +526,9 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
     bulk_g2s(stage_stream(st, 0), pold + d.base, 4 * n4, &P.full[b]);
     bulk_g2s(stage_stream(st, 1), S + d.base, 4 * n4, &P.full[b]);
     bulk_g2s(stage_stream(st, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
-    if (QP == 1) bulk_g2s(stage_stream(st, 3), a.fz32 + d.base, 4 * n4, &P.full[b]);
+    if (QP == 1)
+      for (int f = 0; f < a.F; ++f)
+        bulk_g2s(stage_stream(st, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
   } else {
     const float* p = par ? a.pb32 : a.pa32;  // the direction written by phase A
     bulk_g2s(stage_stream(st, 0), p + d.base, 4 * n4, &P.full[b]);
@@ -553,14 +555,13 @@ __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char
   pu_out = pu;
   float y;
   if (QP == 1) {
-    const float fz = sf[s];
     y = -pu;
     for (int f = 0; f < F; ++f) {
       const int kk = fkk[c * F + f];
       if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
       const int n = fns[c * F + f] + k;
       const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      y = __fmaf_rn(fz * fD[c * F + f] * a.cinv32[n], pn, y);
+      y = __fmaf_rn(sf[f * kStreamFloats + s], pn, y);  // staged face weight stream f
     }
     if (k > ctop) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
     if (k < nk - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
@@ -603,107 +604,6 @@ __device__ __forceinline__ int hcol_of(const unsigned short* start, int ncols, i
     else hi = mid - 1;
   }
   return lo;
-}
-
-// FP32 apply of the 4 CONSECUTIVE slots 4t..4t+3 of a staged tile owned by
-// thread t, compile-time face count.  Consecutive slots mostly lie in one
-// column: then the column lookup, the face metadata and the address
-// arithmetic are shared, own data comes as float4 from shared memory, the
-// neighbour gathers of the 4 levels are consecutive addresses, and the
-// results leave as float4 stores.  pu/y hold the slot values (0 at inactive
-// slots).
-template <int QP, int FF>
-__device__ __forceinline__ void apply_quad32(const BatchArgs& a, const unsigned char* hd, const HdrLayout& L,
-                                             int ncols, int len, int base, float mu, const float* sp, const float* sS,
-                                             const float* sc, const float* sf, const float* __restrict__ pold,
-                                             const float* __restrict__ S, float (&pu)[4], float (&y)[4]) {
-  const unsigned short* start = (const unsigned short*)(hd + L.o_start);
-  const int* cn = (const int*)(hd + L.o_cn);
-  const int* fns = (const int*)(hd + L.o_fns);
-  const int* fkk = (const int*)(hd + L.o_fkk);
-  const float* fD = (const float*)(hd + L.o_fD);
-  const int* fes = (const int*)(hd + L.o_fes);
-  const int s0 = 4 * (int)threadIdx.x;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) pu[j] = y[j] = 0.f;
-  if (s0 >= len) return;
-  const float4 P4 = *(const float4*)(sp + s0);
-  const float4 R4 = *(const float4*)(sS + s0);
-  const float4 C4 = *(const float4*)(sc + s0);
-  const float Pv[4] = {P4.x, P4.y, P4.z, P4.w};
-  const float Rv[4] = {R4.x, R4.y, R4.z, R4.w};
-  const float Cv[5] = {C4.x, C4.y, C4.z, C4.w, sc[s0 + 4]};
-  float Zv[4] = {0.f, 0.f, 0.f, 0.f};
-  if (QP == 1) {
-    const float4 Z4 = *(const float4*)(sf + s0);
-    Zv[0] = Z4.x; Zv[1] = Z4.y; Zv[2] = Z4.z; Zv[3] = Z4.w;
-  }
-  // p_new at the 4 slots and their vertical neighbours below/above the group
-  float pw[6];
-  pw[0] = s0 > 0 ? __fmaf_rn(mu, sp[s0 - 1], sS[s0 - 1]) : 0.f;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) pw[j + 1] = __fmaf_rn(mu, Pv[j], Rv[j]);
-  pw[5] = (s0 + 4 < len) ? __fmaf_rn(mu, sp[s0 + 4], sS[s0 + 4]) : 0.f;
-  // columns of the 4 slots
-  int c = hcol_of(start, ncols, s0);
-  int cj[4], kj[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int s = s0 + j;
-    if (c + 1 < ncols && (int)start[c + 1] <= s) ++c;
-    cj[j] = c;
-    kj[j] = s - start[c];
-  }
-  bool onj[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int w = cn[cj[j]];
-    const int ctop = w & 0xffff, nk = w >> 16;
-    const bool on = (s0 + j < len) && kj[j] >= ctop;
-    onj[j] = on;
-    const float p = pw[j + 1];
-    float acc = (QP == 1) ? -p : 0.f;
-    if (on) {
-      if (QP == 1) {
-        if (kj[j] > ctop) acc = __fmaf_rn(Cv[j], pw[j], acc);
-        if (kj[j] < nk - 1) acc = __fmaf_rn(Cv[j + 1], pw[j + 2], acc);
-      } else {
-        const float c0 = Cv[j];
-        if (ctop < nk - 1) {
-          if (kj[j] == ctop) acc += (-2.f * c0 - Cv[j + 1]) * p + Cv[j + 1] * pw[j + 2];
-          else if (kj[j] == nk - 1) acc += c0 * pw[j] - c0 * p;
-          else acc += c0 * pw[j] - (c0 + Cv[j + 1]) * p + Cv[j + 1] * pw[j + 2];
-        } else {
-          acc -= 2.f * c0 * p;
-        }
-      }
-    }
-    pu[j] = on ? p : 0.f;
-    y[j] = acc;
-  }
-  // faces: gathers of the 4 levels (consecutive neighbour slots when the
-  // group lies in one column)
-#pragma unroll
-  for (int f = 0; f < FF; ++f) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int e = cj[j] * FF + f;
-      const int kk = fkk[e];
-      const bool ok = onj[j] && kj[j] >= (kk & 0xffff) && kj[j] < (kk >> 16);
-      const int n = ok ? fns[e] + kj[j] : base + s0 + j;
-      const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      if (QP == 1) {
-        const float wgt = ok ? Zv[j] * fD[e] * a.cinv32[n] : 0.f;
-        y[j] = __fmaf_rn(wgt, pn, y[j]);
-      } else {
-        const float wgt = ok ? a.dzfD32[fes[e] + kj[j]] : 0.f;
-        y[j] = __fmaf_rn(pn - pw[j + 1], wgt, y[j]);
-      }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j)
-    if (!onj[j]) y[j] = 0.f;
 }
 
 // Branch-free FP32 apply of a thread's 4 slots of a staged tile with a
@@ -751,7 +651,7 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
       const int n = ok ? fns[e] + kv[q] : base + sv[q];
       pn[q][f] = __fmaf_rn(mu, pold[n], S[n]);
       if (QP == 1) {
-        wn[q][f] = ok ? fD[e] * a.cinv32[n] : 0.f;
+        wn[q][f] = sf[f * kStreamFloats + sv[q]];  // staged face weight (0 where the face does not couple)
       } else {
         const int es = ok ? fes[e] + kv[q] : 0;
         wn[q][f] = ok ? a.dzfD32[es] : 0.f;
@@ -765,10 +665,9 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
     pv[q] = pu;
     float y;
     if (QP == 1) {
-      const float fz = sf[s];
       y = -pu;
 #pragma unroll
-      for (int f = 0; f < FF; ++f) y = __fmaf_rn(fz * wn[q][f], pn[q][f], y);
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(wn[q][f], pn[q][f], y);
       if (k > ctop[q]) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
       if (k < nk[q] - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
     } else {
@@ -880,24 +779,6 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       const float* S = (QP == 2) ? a.s32 : a.r32;
       float yv[Q], pv[Q];
       bool on[Q];
-#ifdef SGPU_APPLY_QUAD
-      if (a.F == 3 || a.F == 4) {
-        float pu4[4], y4[4];
-        if (a.F == 3) apply_quad32<QP, 3>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, pu4, y4);
-        else apply_quad32<QP, 4>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, pu4, y4);
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&P.empty[b]);
-        const int s0 = 4 * (int)threadIdx.x;
-        if (s0 < len) {
-          *(float4*)(a.z32 + base + s0) = make_float4(y4[0], y4[1], y4[2], y4[3]);
-          *(float4*)(pnew + base + s0) = make_float4(pu4[0], pu4[1], pu4[2], pu4[3]);
-#pragma unroll
-          for (int j = 0; j < 4; ++j) df_addprod(dacc[0], pu4[j], y4[j]);
-        }
-        P.seq = q + 1;
-        continue;
-      } else
-#endif
       if (a.F == 3) {
         apply_tile32<QP, 3>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, yv, pv, on);
       } else if (a.F == 4) {
@@ -1101,10 +982,10 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
 
   Pipe P;
   P.stage[0] = dyn;
-  P.stage[1] = dyn + kBufBytes;
-  P.full = (uint64_t*)(dyn + 2 * kBufBytes);
+  P.stage[1] = dyn + a.stage_bytes;
+  P.full = (uint64_t*)(dyn + 2 * a.stage_bytes);
   P.empty = P.full + 2;
-  P.list = (int*)(dyn + 2 * kBufBytes + 32);
+  P.list = (int*)(dyn + 2 * a.stage_bytes + 32);
   P.own = s_own;
   P.nown = &s_nown;
   P.count = &s_count;
@@ -1237,6 +1118,12 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
               if (k >= ctop && k >= (kk & 0xffff) && k < (kk >> 16))
                 v = dz * a.face[(size_t)(ti.c0 + c) * F + f].D64 / (cu * a.c64[sm.fns[c * F + f] + k]);
               a.fc64[(size_t)F * u + f] = v;
+              // the FP32 weight the inner apply uses: (dzz/c_u) * (D * (1/c_n)), as formed
+              // from the FP32 copies (0 where the face does not couple the level)
+              float w = 0.f;
+              if (k >= ctop && k >= (kk & 0xffff) && k < (kk >> 16))
+                w = a.fz32[u] * (a.face[(size_t)(ti.c0 + c) * F + f].D * a.cinv32[sm.fns[c * F + f] + k]);
+              a.fw32[(size_t)f * a.fw_stride + u] = w;
             }
           }
           csync();
@@ -1581,6 +1468,8 @@ struct sgpu_batch {
   double last_ms = 0.0;
   long long last_work = 0;
   bool attr_set[3] = {false, false, false};
+  int streams = 4;                    // FP32 streams per pipeline stage
+  int dyn_smem = kDynSmem;            // dynamic shared memory of the kernel
 };
 
 static int bfail(sgpu_batch* b, int code, const char* fmt, ...) {
@@ -1630,12 +1519,16 @@ const void* kernel_of(int qp) {
 static int batch_max_grid(sgpu_batch* b) {
   const void* fn = kernel_of(b->qprecond);
   if (!b->attr_set[b->qprecond]) {
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem) != cudaSuccess) return 0;
+    // the largest stage configuration any batch may use, so that batches of
+    // different face counts sharing the kernel never find the limit too low
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_bytes(3 + kMaxF)) !=
+        cudaSuccess)
+      return 0;
     b->attr_set[b->qprecond] = true;
   }
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kThreads, kDynSmem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kThreads, b->dyn_smem) != cudaSuccess) return 0;
   return sms * per;
 }
 
@@ -1655,6 +1548,8 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   b->device = device;
   b->qprecond = qprecond;
   b->F = maxfaces;
+  b->streams = qprecond == 1 ? 3 + maxfaces : 4;
+  b->dyn_smem = dyn_smem_bytes(b->streams);
   // tiles are 4-slot aligned: reserve room for the padding (< 4 slots per tile)
   const long long tiles_est = max_cols + max_slots / kBTSlots + 2LL * max_instances + 2;
   b->max_slots = std::min(0x7ffffff0LL, max_slots + 4 * std::min(tiles_est, max_slots) + 8LL * max_instances + 16);
@@ -1703,6 +1598,11 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if ((rc = balloc(b, &a.x64, S))) return rc;
   if ((rc = balloc(b, &a.b64, S))) return rc;
   if ((rc = balloc(b, &a.fz32, S))) return rc;
+  if (qprecond == 1) {
+    a.fw_stride = (long long)S;
+    if ((rc = balloc(b, &a.fw32, S * (size_t)maxfaces))) return rc;
+    BCK(cudaMemsetAsync(a.fw32, 0, S * (size_t)maxfaces * sizeof(float), b->stream));
+  }
   if ((rc = balloc(b, &a.cinv32, S))) return rc;
   if ((rc = balloc(b, &a.coef32, S))) return rc;
   if ((rc = balloc(b, &a.dzfD32, E))) return rc;
@@ -1772,7 +1672,7 @@ const char* sgpu_batch_last_error(const sgpu_batch* b) { return b ? b->err.c_str
 long long sgpu_batch_bytes_per_request(int qprecond, int maxfaces, long long n3, long long ncols,
                                        long long nedge_slots) {
   // device bytes an instance occupies (layout of sgpu_batch_create's arrays)
-  long long per_slot = 8 * 8 + 4 * 8 + (qprecond == 1 ? 8LL * maxfaces : 0) + (qprecond == 2 ? 12 : 0);
+  long long per_slot = 8 * 8 + 4 * 8 + (qprecond == 1 ? 12LL * maxfaces : 0) + (qprecond == 2 ? 12 : 0);
   long long per_col = (long long)sizeof(BCol) + (long long)sizeof(BFace) * maxfaces + 8 + 8 + 16LL * maxfaces;
   long long per_eslot = 12;
   const long long tiles = ncols / 16 + n3 / kBTSlots + 2;
@@ -1973,6 +1873,9 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   float* f32s[] = {b->a.fz32, b->a.cinv32, b->a.coef32, b->a.r32, b->a.pa32, b->a.pb32, b->a.x32, b->a.z32};
   for (float* p : f32s) BCK(cudaMemsetAsync(p + H.s_off, 0, 4 * (H.n3 + 4), s));
   if (b->qprecond == 2) BCK(cudaMemsetAsync(b->a.s32 + H.s_off, 0, 4 * (H.n3 + 4), s));
+  if (b->qprecond == 1)
+    for (int f = 0; f < F; ++f)
+      BCK(cudaMemsetAsync(b->a.fw32 + (size_t)f * b->a.fw_stride + H.s_off, 0, 4 * (H.n3 + 4), s));
   BCK(cudaStreamSynchronize(s));
   BInst& I = b->h_inst[id];
   std::memset(&I, 0, sizeof(BInst));
@@ -2067,6 +1970,7 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     if ((e = cudaMemcpyAsync(b->d_gflags, b->h_gflags, 4 * sizeof(int), cudaMemcpyHostToDevice, st))) return e;
     BatchArgs a = b->a;
     a.F = b->F;
+    a.stage_bytes = stage_bytes_for(b->streams);
     a.ntiles = ntiles;
     a.ninst = ninst;
     a.max_iters_chunk = chunk;
@@ -2074,7 +1978,7 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = kDynSmem;
+    cfg.dynamicSmemBytes = b->dyn_smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

@@ -20,11 +20,15 @@ constexpr int kBTFaces = 512;    // column-faces per tile (ncols * F)
 constexpr int kHdrCap = 10240;   // bytes of a tile header (see tile header layout below)
 constexpr int kStreamFloats = kBTSlots + 4;                 // one FP32 stream of a tile (+1 group)
 constexpr int kStreamBytes = kStreamFloats * 4;             // 4112, a multiple of 16
-constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // one pipeline stage
+constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // the smallest pipeline stage (4 streams)
+// A stage holds the header and `streams` FP32 streams: 4, or 3 + F for
+// qprecond 1 (p, s, coef and one face-weight stream per face).
+__host__ __device__ constexpr int stage_bytes_for(int streams) { return kHdrCap + streams * kStreamBytes; }
 static_assert(kBTCols <= 256, "the header's slot-to-column map holds one byte per slot");
 constexpr int kListCap = 512;    // tiles per CTA per phase
 // dynamic shared memory of the kernel: 2 stages, 4 mbarriers (32 B), the tile list
-constexpr int kDynSmem = 2 * kBufBytes + 32 + 4 * kListCap;
+__host__ __device__ constexpr int dyn_smem_bytes(int streams) { return 2 * stage_bytes_for(streams) + 32 + 4 * kListCap; }
+constexpr int kDynSmem = dyn_smem_bytes(4);
 
 // Tile header (global, built on the host when an instance is added; all
 // offsets are multiples of 16 bytes):
@@ -111,6 +115,7 @@ struct BFace {
 
 struct BatchArgs {
   int F;
+  int stage_bytes;     // bytes of one pipeline stage (stage_bytes_for(streams))
   int ntiles;
   int ninst;           // instance slots in use (some may be EMPTY/DONE)
   int max_iters_chunk; // global iterations allowed in this launch
@@ -136,6 +141,8 @@ struct BatchArgs {
   double* b64;           // [nslots] FP64 right-hand side (scaled for qprecond 1)
   // FP32 inner data
   float* fz32;           // [nslots] dzz/c (qprecond 1 face coefficients)
+  float* fw32;           // [F][fw_stride] qprecond 1 face weights (dzz/c_u) D (1/c_n), FP32
+  long long fw_stride;
   float* cinv32;         // [nslots] 1/c (qprecond 1)
   float* coef32;         // [nslots+4] vertical coefficient (scaled for qprecond 1)
   float* dzfD32;         // [nedge_slots]
