@@ -1599,9 +1599,12 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if ((rc = balloc(b, &a.b64, S))) return rc;
   if ((rc = balloc(b, &a.fz32, S))) return rc;
   if (qprecond == 1) {
-    a.fw_stride = (long long)S;
-    if ((rc = balloc(b, &a.fw32, S * (size_t)maxfaces))) return rc;
-    BCK(cudaMemsetAsync(a.fw32, 0, S * (size_t)maxfaces * sizeof(float), b->stream));
+    // one array per face, each starting on a 128-byte boundary: the bulk copies
+    // of a tile's weights need 16-byte aligned sources
+    const size_t FS = (S + 31) & ~(size_t)31;
+    a.fw_stride = (long long)FS;
+    if ((rc = balloc(b, &a.fw32, FS * (size_t)maxfaces))) return rc;
+    BCK(cudaMemsetAsync(a.fw32, 0, FS * (size_t)maxfaces * sizeof(float), b->stream));
   }
   if ((rc = balloc(b, &a.cinv32, S))) return rc;
   if ((rc = balloc(b, &a.coef32, S))) return rc;
