@@ -515,7 +515,7 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   sd->nu = pi.nu;
   const bool hdr = (PH == 0) || (QP == 2);
   uint32_t bytes = 0;
-  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + (QP == 1 ? a.F * 4 * n4 : 0);
+  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + a.F * 4 * n4;
   else bytes = (hdr ? d.hdr_bytes : 0) + 4 * 4 * n4;
   fence_proxy_async();
   mbar_arrive_expect_tx(&P.full[b], bytes);
@@ -526,9 +526,8 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
     bulk_g2s(stage_stream(st, 0), pold + d.base, 4 * n4, &P.full[b]);
     bulk_g2s(stage_stream(st, 1), S + d.base, 4 * n4, &P.full[b]);
     bulk_g2s(stage_stream(st, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
-    if (QP == 1)
-      for (int f = 0; f < a.F; ++f)
-        bulk_g2s(stage_stream(st, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
+    for (int f = 0; f < a.F; ++f)
+      bulk_g2s(stage_stream(st, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
   } else {
     const float* p = par ? a.pb32 : a.pa32;  // the direction written by phase A
     bulk_g2s(stage_stream(st, 0), p + d.base, 4 * n4, &P.full[b]);
@@ -572,7 +571,7 @@ __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char
       if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
       const int n = fns[c * F + f] + k;
       const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      y = __fmaf_rn(pn - pu, a.dzfD32[fes[c * F + f] + k], y);
+      y = __fmaf_rn(pn - pu, sf[f * kStreamFloats + s], y);  // staged dzf*D of the edge level
     }
     const float c0 = sc[s];
     if (ctop < nk - 1) {
@@ -653,8 +652,7 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
       if (QP == 1) {
         wn[q][f] = sf[f * kStreamFloats + sv[q]];  // staged face weight (0 where the face does not couple)
       } else {
-        const int es = ok ? fes[e] + kv[q] : 0;
-        wn[q][f] = ok ? a.dzfD32[es] : 0.f;
+        wn[q][f] = sf[f * kStreamFloats + sv[q]];  // staged dzf*D of the edge level (0 likewise)
       }
     }
   }
@@ -1060,6 +1058,12 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
             else if (k > ctop) cf = 2 * Ac / (dz + a.dzz64[u - 1]);
             a.coef64[u] = cf;
             a.coef32[u] = (float)cf;
+            // per-slot copy of the edge levels' dzf*D that the inner apply streams
+            for (int f = 0; f < F; ++f) {
+              const int kk = sm.fkk[c * F + f];
+              const bool on = act && k >= (kk & 0xffff) && k < (kk >> 16);
+              a.fw32[(size_t)f * a.fw_stride + u] = on ? a.dzfD32[sm.fes[c * F + f] + k] : 0.f;
+            }
             a.x64[u] = act ? a.q64[u] : 0.0;
             a.b64[u] = act ? a.src64[u] : 0.0;
           }
@@ -1548,7 +1552,7 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   b->device = device;
   b->qprecond = qprecond;
   b->F = maxfaces;
-  b->streams = qprecond == 1 ? 3 + maxfaces : 4;
+  b->streams = 3 + maxfaces;
   b->dyn_smem = dyn_smem_bytes(b->streams);
   // tiles are 4-slot aligned: reserve room for the padding (< 4 slots per tile)
   const long long tiles_est = max_cols + max_slots / kBTSlots + 2LL * max_instances + 2;
@@ -1598,7 +1602,7 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if ((rc = balloc(b, &a.x64, S))) return rc;
   if ((rc = balloc(b, &a.b64, S))) return rc;
   if ((rc = balloc(b, &a.fz32, S))) return rc;
-  if (qprecond == 1) {
+  {
     // one array per face, each starting on a 128-byte boundary: the bulk copies
     // of a tile's weights need 16-byte aligned sources
     const size_t FS = (S + 31) & ~(size_t)31;
@@ -1675,7 +1679,7 @@ const char* sgpu_batch_last_error(const sgpu_batch* b) { return b ? b->err.c_str
 long long sgpu_batch_bytes_per_request(int qprecond, int maxfaces, long long n3, long long ncols,
                                        long long nedge_slots) {
   // device bytes an instance occupies (layout of sgpu_batch_create's arrays)
-  long long per_slot = 8 * 8 + 4 * 8 + (qprecond == 1 ? 12LL * maxfaces : 0) + (qprecond == 2 ? 12 : 0);
+  long long per_slot = 8 * 8 + 4 * 8 + 4LL * maxfaces + (qprecond == 1 ? 8LL * maxfaces : 0) + (qprecond == 2 ? 12 : 0);
   long long per_col = (long long)sizeof(BCol) + (long long)sizeof(BFace) * maxfaces + 8 + 8 + 16LL * maxfaces;
   long long per_eslot = 12;
   const long long tiles = ncols / 16 + n3 / kBTSlots + 2;
@@ -1876,9 +1880,8 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   float* f32s[] = {b->a.fz32, b->a.cinv32, b->a.coef32, b->a.r32, b->a.pa32, b->a.pb32, b->a.x32, b->a.z32};
   for (float* p : f32s) BCK(cudaMemsetAsync(p + H.s_off, 0, 4 * (H.n3 + 4), s));
   if (b->qprecond == 2) BCK(cudaMemsetAsync(b->a.s32 + H.s_off, 0, 4 * (H.n3 + 4), s));
-  if (b->qprecond == 1)
-    for (int f = 0; f < F; ++f)
-      BCK(cudaMemsetAsync(b->a.fw32 + (size_t)f * b->a.fw_stride + H.s_off, 0, 4 * (H.n3 + 4), s));
+  for (int f = 0; f < F; ++f)
+    BCK(cudaMemsetAsync(b->a.fw32 + (size_t)f * b->a.fw_stride + H.s_off, 0, 4 * (H.n3 + 4), s));
   BCK(cudaStreamSynchronize(s));
   BInst& I = b->h_inst[id];
   std::memset(&I, 0, sizeof(BInst));

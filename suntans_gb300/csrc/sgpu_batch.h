@@ -21,8 +21,8 @@ constexpr int kHdrCap = 10240;   // bytes of a tile header (see tile header layo
 constexpr int kStreamFloats = kBTSlots + 4;                 // one FP32 stream of a tile (+1 group)
 constexpr int kStreamBytes = kStreamFloats * 4;             // 4112, a multiple of 16
 constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // the smallest pipeline stage (4 streams)
-// A stage holds the header and `streams` FP32 streams: 4, or 3 + F for
-// qprecond 1 (p, s, coef and one face-weight stream per face).
+// A stage holds the header and `streams` = 3 + F FP32 streams (p, s, coef and
+// one face-weight stream per face; the update phase uses 4 of them).
 __host__ __device__ constexpr int stage_bytes_for(int streams) { return kHdrCap + streams * kStreamBytes; }
 static_assert(kBTCols <= 256, "the header's slot-to-column map holds one byte per slot");
 constexpr int kListCap = 512;    // tiles per CTA per phase
@@ -141,7 +141,7 @@ struct BatchArgs {
   double* b64;           // [nslots] FP64 right-hand side (scaled for qprecond 1)
   // FP32 inner data
   float* fz32;           // [nslots] dzz/c (qprecond 1 face coefficients)
-  float* fw32;           // [F][fw_stride] qprecond 1 face weights (dzz/c_u) D (1/c_n), FP32
+  float* fw32;           // [F][fw_stride] face weights, FP32: (dzz/c_u) D (1/c_n) for qprecond 1, dzf*D else
   long long fw_stride;
   float* cinv32;         // [nslots] 1/c (qprecond 1)
   float* coef32;         // [nslots+4] vertical coefficient (scaled for qprecond 1)
