@@ -469,3 +469,72 @@ void sgo_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p, do
 void sgo_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef, const double *x, double *y) {
   oph_impl(g, x, y, hcoef, hfcoef);
 }
+
+/* ------------------------------------------------------------------------
+ * The steps on either side of CGSolveQ in Solve (main/phys.c:1273-1287).
+ * ------------------------------------------------------------------------ */
+
+/* ComputeQSource, main/phys.c:2345-2395: src = div(u*, w*)/dt over the wet
+   levels of the computational cells (zero elsewhere), and D = df/dg. */
+void sgo_compute_qsource(const sgo_grid *g, const sgo_ext *x, const double *u, const double *utmp2,
+                         const double *w, const double *wtmp2, const sgo_prop *p, double *src, double *D) {
+  layout_t Lv, *L = &Lv;
+  int i, iptr, j, k, nf, ne;
+  const double thetafactor = (1 - p->theta) / p->theta;
+  long *woff;
+  layout_make(g, L);
+  woff = (long *)malloc(sizeof(long) * (g->Nc + 1));
+  woff[0] = 0;
+  for (i = 0; i < g->Nc; i++) woff[i + 1] = woff[i] + g->Nk[i] + 1;
+  for (i = 0; i < g->Nc; i++)                                 /* 2357-2360 */
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(src, i, k) = 0;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++)                   /* vertical, 2369-2373 */
+      X3(src, i, k) = g->Ac[i] * (w[woff[i] + k] - w[woff[i] + k + 1]) +
+                      thetafactor * g->Ac[i] * (wtmp2[woff[i] + k] - wtmp2[woff[i] + k + 1]);
+    for (nf = 0; nf < g->nfaces[i]; nf++) {                   /* horizontal, 2377-2386 */
+      ne = g->face[i * g->maxfaces + nf];
+      for (k = g->ctop[i]; k < g->Nke[ne]; k++)
+        X3(src, i, k) += (u[L->eoff[ne] + k] + thetafactor * utmp2[L->eoff[ne] + k]) * DZF(ne, k) *
+                         x->normal[i * g->maxfaces + nf] * g->df[ne];
+    }
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(src, i, k) /= p->dt;   /* 2389-2390 */
+  }
+  for (j = 0; j < g->Ne; j++) D[j] = g->df[j] / g->dg[j];   /* 2392-2394 */
+  free(woff);
+  layout_free(L);
+}
+
+/* Corrector, main/phys.c:2301-2333: u -= dt/dg grad(qc) on the computational
+   edges with D != 0 and more than one wet level, w corrected from the
+   vertical gradient of qc, and q += qc on columns with more than one level. */
+void sgo_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const double *D,
+                   const sgo_prop *p, double *u, double *w, double *q) {
+  layout_t Lv, *L = &Lv;
+  int i, iptr, j, jptr, k;
+  long *woff;
+  layout_make(g, L);
+  woff = (long *)malloc(sizeof(long) * (g->Nc + 1));
+  woff[0] = 0;
+  for (i = 0; i < g->Nc; i++) woff[i + 1] = woff[i] + g->Nk[i] + 1;
+  for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++) {     /* 2306-2312 */
+    j = x->edgep[jptr];
+    if (D[j] != 0 && x->etop[j] < g->Nke[j] - 1)
+      for (k = x->etop[j]; k < g->Nke[j]; k++)
+        u[L->eoff[j] + k] -= p->dt / g->dg[j] * (X3(qc, x->grad[2 * j], k) - X3(qc, x->grad[2 * j + 1], k));
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {    /* 2315-2322 */
+    i = g->cellp[iptr];
+    for (k = g->ctop[i] + 1; k < g->Nk[i]; k++)
+      w[woff[i] + k] -= 2.0 * p->dt / (DZZ(i, k - 1) + DZZ(i, k)) * (X3(qc, i, k - 1) - X3(qc, i, k));
+    w[woff[i] + g->ctop[i]] += 2.0 * p->dt / DZZ(i, g->ctop[i]) * X3(qc, i, g->ctop[i]);
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {    /* 2325-2331 */
+    i = g->cellp[iptr];
+    if (g->ctop[i] < g->Nk[i] - 1)
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(q, i, k) += X3(qc, i, k);
+  }
+  free(woff);
+  layout_free(L);
+}

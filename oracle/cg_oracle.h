@@ -64,6 +64,20 @@ typedef struct sgo_result {
   double eps, eps0;    /* last eps and the normaliser eps0                        */
 } sgo_result;
 
+/* The gridT fields the steps on either side of CGSolveQ read in addition:
+ * ComputeQSource (main/phys.c:2345-2395) and Corrector (main/phys.c:2301-2333). */
+typedef struct sgo_ext {
+  const int *normal;   /* [Nc*maxfaces] gridT.normal (+1 / -1)                   */
+  const int *grad;     /* [2*Ne] gridT.grad, the two cells of each edge           */
+  const int *edgep;    /* gridT.edgep: computational edges [edgedist[0], edgedist[1]) */
+  const int *edgedist; /* [2]                                                     */
+  const int *etop;     /* [Ne] gridT.etop                                          */
+} sgo_ext;
+
+/* Ragged layouts of the step fields: u, utmp2 per edge with Nke[j] levels (as
+ * dzf); w, wtmp2 per cell with Nk[i]+1 levels (offsets the prefix sum of
+ * Nk+1); src, q, qc per cell with Nk[i] levels (as dzz). */
+
 /* ---- the restatement (cg_oracle.c) ---- */
 void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
                   const sgo_prop *p, sgo_result *res);
@@ -82,6 +96,10 @@ void sgo_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p,
                        double *hcoef, double *hfcoef);
 void sgo_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef,
                     const double *x, double *y);
+void sgo_compute_qsource(const sgo_grid *g, const sgo_ext *x, const double *u, const double *utmp2,
+                         const double *w, const double *wtmp2, const sgo_prop *p, double *src, double *D);
+void sgo_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const double *D,
+                   const sgo_prop *p, double *u, double *w, double *q);
 
 /* ---- the reference itself (ref_harness.c, oracle/_ref only) ---- */
 void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
@@ -100,6 +118,10 @@ void ref_hcoefficients(const sgo_grid *g, const double *D, const sgo_prop *p,
                        double *hcoef, double *hfcoef);
 void ref_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef,
                     const double *x, double *y);
+void ref_compute_qsource(const sgo_grid *g, const sgo_ext *x, const double *u, const double *utmp2,
+                         const double *w, const double *wtmp2, const sgo_prop *p, double *src, double *D);
+void ref_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const double *D,
+                   const sgo_prop *p, double *u, double *w, double *q);
 
 #ifdef __cplusplus
 }

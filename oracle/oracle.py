@@ -42,6 +42,10 @@ class SgoProp(C.Structure):
                 ("dt", C.c_double)]
 
 
+class SgoExt(C.Structure):
+    _fields_ = [("normal", _ip), ("grad", _ip), ("edgep", _ip), ("edgedist", _ip), ("etop", _ip)]
+
+
 class SgoResult(C.Structure):
     _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double)]
 
@@ -181,6 +185,42 @@ class Oracle:
         x = np.ascontiguousarray(x, dtype=np.float64)
         self._fn("operator_h")(C.byref(s), _ptr(hcoef, _dp), _ptr(hfcoef, _dp), _ptr(x, _dp), _ptr(y, _dp))
         return y
+
+
+    # ---- the steps around CGSolveQ ----
+    @staticmethod
+    def _ext(st):
+        g = st.grid
+        keep = [np.ascontiguousarray(x, dtype=np.int32) for x in (g.normal, g.grad, st.edgep, st.edgedist, st.etop)]
+        return SgoExt(*[_ptr(x, _ip) for x in keep]), keep
+
+    def compute_qsource(self, st, props):
+        """ComputeQSource on the step fields st; returns (src, D)."""
+        g = st.grid
+        s, keep = self._grid(g)
+        x, keepx = self._ext(st)
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (st.u, st.utmp2, st.w, st.wtmp2)]
+        src = np.zeros(g.n3)
+        D = np.zeros(max(g.Ne, 1))
+        pr = self._prop(props)
+        self._fn("compute_qsource")(C.byref(s), C.byref(x), *[_ptr(a, _dp) for a in arrs], C.byref(pr),
+                                    _ptr(src, _dp), _ptr(D, _dp))
+        return src, D[:g.Ne]
+
+    def corrector(self, st, qc, D, props):
+        """Corrector with the correction qc; returns (u, w, q) updated copies of st's."""
+        g = st.grid
+        s, keep = self._grid(g)
+        x, keepx = self._ext(st)
+        qc = np.ascontiguousarray(qc, dtype=np.float64)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        u = np.array(st.u, dtype=np.float64, copy=True)
+        w = np.array(st.w, dtype=np.float64, copy=True)
+        q = np.array(st.q, dtype=np.float64, copy=True)
+        pr = self._prop(props)
+        self._fn("corrector")(C.byref(s), C.byref(x), _ptr(qc, _dp), _ptr(D, _dp), C.byref(pr), _ptr(u, _dp),
+                              _ptr(w, _dp), _ptr(q, _dp))
+        return u, w, q
 
 
 def available(which: str) -> bool:

@@ -265,3 +265,47 @@ void ref_operator_h(const sgo_grid *g, const double *hcoef, const double *hfcoef
   OperatorH((REAL *)x, y, (REAL *)hcoef, (REAL *)hfcoef, &H.grid, &H.phys, &H.prop);
   harness_free(&H);
 }
+
+/* the gridT fields of the steps around CGSolveQ, and a view of w-like rows
+   (Nk[i]+1 levels per cell) */
+static void harness_ext(harness_t *H, const sgo_grid *g, const sgo_ext *x) {
+  H->grid.normal = (int *)x->normal;
+  H->grid.grad = (int *)x->grad;
+  H->grid.edgep = (int *)x->edgep;
+  H->grid.edgedist = (int *)x->edgedist;
+  H->grid.etop = (int *)x->etop;
+}
+static REAL **wrow_view(harness_t *H, const sgo_grid *g, const double *flat) {
+  long *woff = (long *)blk_new(H, sizeof(long) * (g->Nc + 1));
+  int i;
+  woff[0] = 0;
+  for (i = 0; i < g->Nc; i++) woff[i + 1] = woff[i] + g->Nk[i] + 1;
+  return jag_view(H, flat, woff, g->Nc);
+}
+
+void ref_compute_qsource(const sgo_grid *g, const sgo_ext *x, const double *u, const double *utmp2,
+                         const double *w, const double *wtmp2, const sgo_prop *p, double *src, double *D) {
+  harness_t H;
+  harness_init(&H, g, D, p);
+  harness_ext(&H, g, x);
+  H.phys.u = jag_view(&H, u, H.eoff, g->Ne);
+  H.phys.utmp2 = jag_view(&H, utmp2, H.eoff, g->Ne);
+  H.phys.w = wrow_view(&H, g, w);
+  H.phys.wtmp2 = wrow_view(&H, g, wtmp2);
+  REAL **S = jag_view(&H, src, H.coff, g->Nc);
+  ComputeQSource(S, &H.grid, &H.phys, &H.prop, 0, 1);
+  harness_free(&H);
+}
+
+void ref_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const double *D,
+                   const sgo_prop *p, double *u, double *w, double *q) {
+  harness_t H;
+  harness_init(&H, g, D, p);
+  harness_ext(&H, g, x);
+  H.phys.u = jag_view(&H, u, H.eoff, g->Ne);
+  H.phys.w = wrow_view(&H, g, w);
+  H.phys.q = jag_view(&H, q, H.coff, g->Nc);
+  REAL **QC = jag_view(&H, qc, H.coff, g->Nc);
+  Corrector(QC, &H.grid, &H.phys, &H.prop, 0, 1, 0);
+  harness_free(&H);
+}

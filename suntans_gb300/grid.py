@@ -150,6 +150,30 @@ class HProblem:
 
 
 @dataclasses.dataclass
+class StepFields:
+    """Fields of the nonhydrostatic pressure step around CGSolveQ (Solve,
+    main/phys.c:1273-1287): ComputeQSource reads u*, w* and their previous
+    values, Corrector updates u, w and the pressure q with the correction qc."""
+    grid: SunGrid
+    u: np.ndarray         # ragged per edge (Nke levels): predicted horizontal velocity, corrected in place
+    utmp2: np.ndarray     # ragged per edge: the previous step's u (theta-method term)
+    w: np.ndarray         # ragged per cell with Nk+1 levels: predicted vertical velocity, corrected in place
+    wtmp2: np.ndarray     # ragged per cell with Nk+1 levels: the previous step's w
+    q: np.ndarray         # ragged per cell: total nonhydrostatic pressure, += qc
+    qc: np.ndarray        # ragged per cell: pressure correction (warm start in, solution out)
+    c: np.ndarray         # ragged per cell: CGSolveQ's preconditioner buffer (read at type-3 cells)
+    etop: np.ndarray      # [Ne] top wet level of each edge
+    edgep: np.ndarray     # computational edges
+    edgedist: np.ndarray  # [2]: edgep[edgedist[0]:edgedist[1]]
+
+    @property
+    def woff(self) -> np.ndarray:
+        o = np.zeros(self.grid.Nc + 1, dtype=np.int64)
+        np.cumsum(self.grid.Nk + 1, out=o[1:])
+        return o
+
+
+@dataclasses.dataclass
 class SolverProps:
     """The propT fields the two solves read (main/phys.h:183-203)."""
     qprecond: int = 1

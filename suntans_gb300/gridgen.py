@@ -382,3 +382,37 @@ def serving_pool(n=24, seed=5, nc_range=(1000, 200000), nkmax_range=(10, 60), rh
         gseed = int(rng.integers(1 << 30))
         params.append((nc, nkmax, gseed, [int(rng.integers(1 << 30)) for _ in range(rhs_per_grid)]))
     return _build_all(params, workers)
+
+
+def make_step_fields(g: SunGrid, seed=0, sigma_u=0.05, sigma_w=0.002, sigma_q=0.01) -> "StepFields":
+    """Seeded fields for the pressure step around CGSolveQ: u*, w* and their
+    previous values, the total pressure q, a zero correction qc.  Computational
+    edges are the interior edges (two cells); an edge's top wet level is the
+    deeper of its cells' tops."""
+    from .grid import StepFields
+    rng = np.random.default_rng(seed)
+    grad = g.grad.reshape(g.Ne, 2)
+    interior = (grad[:, 0] >= 0) & (grad[:, 1] >= 0)
+    ct = g.ctop
+    etop = np.where(interior, np.maximum(ct[np.maximum(grad[:, 0], 0)], ct[np.maximum(grad[:, 1], 0)]),
+                    ct[np.maximum(grad[:, 0], 0)])
+    etop = np.minimum(etop, np.maximum(g.Nke - 1, 0)).astype(np.int32)
+    ne3 = int(g.Nke.sum())
+    eoff = g.eoff
+    lev = np.arange(ne3) - np.repeat(eoff[:-1], g.Nke)
+    wet_e = lev >= np.repeat(etop, g.Nke)
+    u = np.where(wet_e, rng.normal(0.0, sigma_u, ne3), 0.0)
+    utmp2 = np.where(wet_e, rng.normal(0.0, sigma_u, ne3), 0.0)
+    nw = int((g.Nk + 1).sum())
+    woff = np.zeros(g.Nc + 1, dtype=np.int64)
+    np.cumsum(g.Nk + 1, out=woff[1:])
+    wlev = np.arange(nw) - np.repeat(woff[:-1], g.Nk + 1)
+    wet_w = wlev >= np.repeat(ct, g.Nk + 1)
+    w = np.where(wet_w, rng.normal(0.0, sigma_w, nw), 0.0)
+    wtmp2 = np.where(wet_w, rng.normal(0.0, sigma_w, nw), 0.0)
+    clev = np.arange(g.n3) - np.repeat(g.coff[:-1], g.Nk)
+    wet_c = clev >= np.repeat(ct, g.Nk)
+    q = np.where(wet_c, rng.normal(0.0, sigma_q, g.n3), 0.0)
+    edgep = np.nonzero(interior)[0].astype(np.int32)
+    return StepFields(grid=g, u=u, utmp2=utmp2, w=w, wtmp2=wtmp2, q=q, qc=np.zeros(g.n3), c=np.ones(g.n3),
+                      etop=etop, edgep=edgep, edgedist=np.array([0, edgep.size], dtype=np.int32))

@@ -27,5 +27,14 @@ def load(name):
     return g, qp, hp, props, d
 
 
+def step_fields(g, d):
+    """The step fields stored with a fixture (ComputeQSource / Corrector inputs)."""
+    import numpy as np
+    from suntans_gb300.grid import StepFields
+    g.normal, g.grad = d["normal"], d["grad"]
+    return StepFields(grid=g, u=d["u"], utmp2=d["utmp2"], w=d["w"], wtmp2=d["wtmp2"], q=d["qtot"],
+                      qc=np.zeros(g.n3), c=np.ones(g.n3), etop=d["etop"], edgep=d["edgep"], edgedist=d["edgedist"])
+
+
 def props_for(props, **kw):
     return SolverProps(**{**props, **kw})

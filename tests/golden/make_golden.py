@@ -11,7 +11,9 @@ read, and the reference's outputs for:
   CGSolveQ with qprecond 0, 1, 2 (solution q and the iteration count),
   CGSolve with hprecond 0, 1 (solution h and the iteration count),
   QCoefficients (qprecond 0 and 1), OperatorQ, OperatorQC, ConditionQ,
-  Preconditioner, HCoefficients and OperatorH on a seeded vector.
+  Preconditioner, HCoefficients and OperatorH on a seeded vector,
+  ComputeQSource on seeded velocity fields and Corrector with the qprecond-1
+  solution as the pressure correction (the steps around CGSolveQ).
 The inputs are stored (not regenerated) so that the check is bit-exact on any
 host: tests/test_oracle.py runs the C restatement (oracle/cg_oracle.c) on them
 and requires identical bits.
@@ -81,6 +83,13 @@ def main():
         hcoef, hfcoef = ref.hcoefficients(g, hp.D, SolverProps(**props))
         out.update(hcoef=hcoef, hfcoef=hfcoef)
         out["oph"] = ref.operator_h(g, hcoef, hfcoef, x[:g.Nc])
+        st = gg.make_step_fields(g, seed=34)
+        out.update(normal=g.normal, grad=g.grad, u=st.u, utmp2=st.utmp2, w=st.w, wtmp2=st.wtmp2, qtot=st.q,
+                   etop=st.etop, edgep=st.edgep, edgedist=st.edgedist)
+        qs_src, qs_D = ref.compute_qsource(st, SolverProps(**props))
+        out.update(qs_src=qs_src, qs_D=qs_D)
+        cu, cw, cq = ref.corrector(st, out["q_qp1"], qs_D, SolverProps(**props))
+        out.update(corr_u=cu, corr_w=cw, corr_q=cq)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
         print(f"{path}: Nc={g.Nc} n3={g.n3} iters q={[int(out[f'n_qp{k}']) for k in range(3)]} "

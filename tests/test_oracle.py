@@ -92,3 +92,25 @@ def test_port_matches_reference_library(port, gname):
         a, na = port.cgsolve(hp, h_props(hpc))
         b, nb = ref.cgsolve(hp, h_props(hpc))
         assert na == nb and np.array_equal(a, b)
+    st = gg.make_step_fields(g, seed=10)
+    pr = q_props(1)
+    sa, Da = port.compute_qsource(st, pr)
+    sb, Db = ref.compute_qsource(st, pr)
+    assert np.array_equal(sa, sb) and np.array_equal(Da, Db)
+    qc = port.cgsolveq(gg.QProblem(grid=g, D=Da, src=sa, q=st.qc, c=st.c), pr)[0]
+    for x, y in zip(port.corrector(st, qc, Da, pr), ref.corrector(st, qc, Da, pr)):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_port_step_functions_match_golden_bitwise(port, name):
+    """ComputeQSource and Corrector of the restatement reproduce the reference's bits."""
+    from tests._golden import step_fields
+    g, qp, hp, props, d = load(name)
+    st = step_fields(g, d)
+    src, D = port.compute_qsource(st, props_for(props))
+    assert np.array_equal(src, d["qs_src"]) and np.array_equal(D, d["qs_D"])
+    u, w, q = port.corrector(st, d["q_qp1"], d["qs_D"], props_for(props))
+    assert np.array_equal(u, d["corr_u"]) and np.array_equal(w, d["corr_w"]) and np.array_equal(q, d["corr_q"])
+    # the fixtures exercise both branches of the edge and column conditions
+    assert np.any(u != d["u"]) and np.any(w != d["w"]) and np.any(q != d["qtot"])
