@@ -116,6 +116,41 @@ int sgpu_cgsolveq(sgpu_context *ctx, const int *ctop, const double *const *dzz, 
 int sgpu_cgsolve(sgpu_context *ctx, const double *D, double *h, const double *htmp,
                  const sgpu_props *prop, sgpu_stats *stats);
 
+/* ---- the steps on either side of CGSolveQ in Solve (main/phys.c:1273-1287) ----
+ * Field layouts as the reference's jagged rows: u, utmp2 and dzf per edge
+ * (Nke[j] levels), w and wtmp2 per cell with Nk[i]+1 levels, q, qc, src, dzz
+ * per cell (Nk[i] levels). */
+
+/* The gridT fields these steps read beyond sgpu_grid_desc, uploaded once:
+ *   normal[Nc*maxfaces] gridT.normal (+1/-1), grad[2*Ne] gridT.grad (the two
+ *   cells of each edge, -1 = none), edgep[] / edgedist[2] gridT.edgep and
+ *   edgedist (computational edges edgep[edgedist[0]..edgedist[1])). */
+int sgpu_step_grid(sgpu_context *ctx, const int *normal, const int *grad, const int *edgep, const int *edgedist);
+
+/* ComputeQSource drop-in (main/phys.c:2345-2395): src = div(u*, w*)/dt on the
+ * wet levels of the computational cells, 0 on levels [ctop, Nk) elsewhere;
+ * D = df/dg.  theta, dt are propT.theta, propT.dt.  Same bits as the reference. */
+int sgpu_compute_qsource(sgpu_context *ctx, const int *ctop, const double *const *dzf, const double *const *u,
+                         const double *const *utmp2, const double *const *w, const double *const *wtmp2,
+                         double theta, double dt, double *const *src, double *D);
+
+/* Corrector drop-in (main/phys.c:2301-2333): u, w and q updated in place with
+ * the pressure correction qc (etop = gridT.etop, D from ComputeQSource).
+ * Same bits as the reference. */
+int sgpu_corrector(sgpu_context *ctx, const int *ctop, const int *etop, const double *const *dzz,
+                   const double *const *qc, const double *D, double dt, double *const *u, double *const *w,
+                   double *const *q);
+
+/* The three in one call (ComputeQSource -> CGSolveQ -> Corrector, as Solve
+ * runs them): the right-hand side and D are formed on the device and never
+ * leave it, the solution qc stays on the device for the correction.  qc is the
+ * warm start in and the solution out; u, w, q are updated in place; c as for
+ * sgpu_cgsolveq.  Returns the solve's status (stats as sgpu_cgsolveq). */
+int sgpu_pressure_step(sgpu_context *ctx, const int *ctop, const int *etop, const double *const *dzz,
+                       const double *const *dzf, const double *const *utmp2, const double *const *wtmp2,
+                       double *const *u, double *const *w, double *const *q, double *const *qc,
+                       const double *const *c, const sgpu_props *prop, sgpu_stats *stats);
+
 /* Staged forms of the same two solves, for callers that keep inputs resident:
  * upload (host -> HBM), solve (HBM only; repeatable on the same inputs), and
  * download (HBM -> host, computational cells / active levels only). */

@@ -26,6 +26,7 @@ EXPORTS = [
     "sgpu_h_upload", "sgpu_h_solve", "sgpu_h_download",
     "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream", "sgpu_phase_times",
     "sgpu_cgsolve_noalloc",
+    "sgpu_step_grid", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_pressure_step",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
     "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set", "sgpu_batch_set_tile_slots",
     "sgpu_batch_stream", "sgpu_batch_phase_times", "sgpu_batch_resubmit", "sgpu_batch_use_graph",
@@ -83,6 +84,12 @@ def load() -> C.CDLL:
     lib.sgpu_last_error.restype = C.c_char_p
     lib.sgpu_status_string.argtypes = [C.c_int]
     lib.sgpu_status_string.restype = C.c_char_p
+    lib.sgpu_step_grid.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
+    lib.sgpu_compute_qsource.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dpp, _dpp, _dpp, C.c_double, C.c_double,
+                                         _dpp, _dp]
+    lib.sgpu_corrector.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dp, C.c_double, _dpp, _dpp, _dpp]
+    lib.sgpu_pressure_step.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp,
+                                       C.POINTER(Props), C.POINTER(Stats)]
     lib.sgpu_cgsolveq.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dp, _dpp, _dpp, _dpp, C.POINTER(Props),
                                   C.POINTER(Stats)]
     lib.sgpu_cgsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, C.POINTER(Props), C.POINTER(Stats)]
@@ -251,6 +258,83 @@ class Context:
         ptr = jagged(q, self.coff)
         self._check(self.lib.sgpu_q_download(self.h, _vp(ptr)), "sgpu_q_download", allow=(OK,))
         return q
+
+    # ---- the steps around CGSolveQ ----
+    def step_grid(self, st):
+        """Uploads the extra gridT fields (normal, grad, computational edges) of step fields st."""
+        g = self.grid
+        self._step_keep = [np.ascontiguousarray(x, dtype=np.int32) for x in (g.normal, g.grad, st.edgep, st.edgedist)]
+        k = self._step_keep
+        self._check(self.lib.sgpu_step_grid(self.h, *[x.ctypes.data_as(_ip) for x in k]), "sgpu_step_grid",
+                    allow=(OK,))
+
+    def _step_ptrs(self, st):
+        g = self.grid
+        woff = st.woff
+        arrs = {n: np.ascontiguousarray(getattr(st, n), dtype=np.float64) for n in ("u", "utmp2", "w", "wtmp2")}
+        P = {"u": jagged(arrs["u"], self.eoff) if g.Ne else np.zeros(1, np.uint64),
+             "utmp2": jagged(arrs["utmp2"], self.eoff) if g.Ne else np.zeros(1, np.uint64),
+             "w": jagged(arrs["w"], woff), "wtmp2": jagged(arrs["wtmp2"], woff)}
+        return arrs, P
+
+    def compute_qsource(self, st, props: SolverProps):
+        """ComputeQSource on step fields st: returns (src, D)."""
+        g = self.grid
+        arrs, P = self._step_ptrs(st)
+        dzf = np.ascontiguousarray(g.dzf)
+        pdzf = jagged(dzf, self.eoff) if g.Ne else np.zeros(1, np.uint64)
+        src = np.zeros(g.n3)
+        psrc = jagged(src, self.coff)
+        D = np.zeros(max(g.Ne, 1))
+        ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        rc = self.lib.sgpu_compute_qsource(self.h, ctop.ctypes.data_as(_ip), _vp(pdzf), _vp(P["u"]), _vp(P["utmp2"]),
+                                           _vp(P["w"]), _vp(P["wtmp2"]), float(props.theta), float(props.dt),
+                                           _vp(psrc), D.ctypes.data_as(_dp))
+        self._check(rc, "sgpu_compute_qsource", allow=(OK,))
+        return src, D[:g.Ne]
+
+    def corrector(self, st, qc, D, props: SolverProps):
+        """Corrector with correction qc: returns updated copies (u, w, q) of st's."""
+        g = self.grid
+        u = np.array(st.u, dtype=np.float64, copy=True)
+        w = np.array(st.w, dtype=np.float64, copy=True)
+        q = np.array(st.q, dtype=np.float64, copy=True)
+        qc = np.ascontiguousarray(qc, dtype=np.float64)
+        dzz = np.ascontiguousarray(g.dzz)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        etop = np.ascontiguousarray(st.etop, dtype=np.int32)
+        pu = jagged(u, self.eoff) if g.Ne else np.zeros(1, np.uint64)
+        rc = self.lib.sgpu_corrector(self.h, ctop.ctypes.data_as(_ip), etop.ctypes.data_as(_ip),
+                                     _vp(jagged(dzz, self.coff)), _vp(jagged(qc, self.coff)), D.ctypes.data_as(_dp),
+                                     float(props.dt), _vp(pu), _vp(jagged(w, st.woff)), _vp(jagged(q, self.coff)))
+        self._check(rc, "sgpu_corrector", allow=(OK,))
+        return u, w, q
+
+    def pressure_step(self, st, props: SolverProps):
+        """ComputeQSource -> CGSolveQ -> Corrector in one call: returns (qc, u, w, q, Stats)."""
+        g = self.grid
+        u = np.array(st.u, dtype=np.float64, copy=True)
+        w = np.array(st.w, dtype=np.float64, copy=True)
+        q = np.array(st.q, dtype=np.float64, copy=True)
+        qc = np.array(st.qc, dtype=np.float64, copy=True)
+        ut2 = np.ascontiguousarray(st.utmp2, dtype=np.float64)
+        wt2 = np.ascontiguousarray(st.wtmp2, dtype=np.float64)
+        c = np.ascontiguousarray(st.c, dtype=np.float64)
+        dzz = np.ascontiguousarray(g.dzz)
+        dzf = np.ascontiguousarray(g.dzf)
+        ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        etop = np.ascontiguousarray(st.etop, dtype=np.int32)
+        E = (lambda a: jagged(a, self.eoff)) if g.Ne else (lambda a: np.zeros(1, np.uint64))
+        woff = st.woff
+        ptr = [jagged(dzz, self.coff), E(dzf), E(ut2), jagged(wt2, woff), E(u), jagged(w, woff),
+               jagged(q, self.coff), jagged(qc, self.coff), jagged(c, self.coff)]
+        pr = props_struct(props)
+        stt = Stats()
+        rc = self.lib.sgpu_pressure_step(self.h, ctop.ctypes.data_as(_ip), etop.ctypes.data_as(_ip),
+                                         *[_vp(x) for x in ptr], C.byref(pr), C.byref(stt))
+        self._check(rc, "sgpu_pressure_step")
+        return qc, u, w, q, stt
 
     # ---- free surface ----
     def cgsolve(self, prob, props: SolverProps):

@@ -20,6 +20,7 @@
 #include "../../include/suntans_gb300.h"
 #include "sgpu_common.cuh"
 #include "sgpu_q.h"
+#include "sgpu_step.h"
 
 using namespace sgpu;
 
@@ -38,7 +39,7 @@ struct sgpu_context {
 
   // host copies of the static grid
   int Nc = 0, Ne = 0, F = 0, Nkmax = 0, ncomp = 0, nbdy = 0;
-  std::vector<int> Nk, Nke, dev2cell, cell2dev, dcoff, eoff, tile_col, nbr, fedge, slotcol;
+  std::vector<int> Nk, Nke, nfaces, dev2cell, cell2dev, dcoff, eoff, tile_col, nbr, fedge, slotcol;
   long long n3 = 0, n3c = 0, ne3 = 0;
   int ntiles = 0;
 
@@ -56,6 +57,15 @@ struct sgpu_context {
          *d_tib = nullptr, *d_x = nullptr, *d_p = nullptr, *d_r = nullptr, *d_z = nullptr, *d_rt = nullptr;
   std::vector<int> h_ctop;  // last uploaded ctop (cell order), for the download scatter
   bool q_uploaded = false, q_solved = false;
+
+  // pressure-step buffers (ComputeQSource / Corrector)
+  bool step_grid = false, step_ready = false;
+  int ncedge = 0;
+  long long nw3 = 0;
+  std::vector<int> woff;
+  int *d_nfaces = nullptr, *d_normal = nullptr, *d_grad = nullptr, *d_cedge = nullptr, *d_woff = nullptr,
+      *d_etop = nullptr;
+  double *d_u = nullptr, *d_ut2 = nullptr, *d_w = nullptr, *d_wt2 = nullptr, *d_qtot = nullptr;
 
   // free-surface buffers
   bool h_ready = false;
@@ -208,6 +218,7 @@ static int build_layout(sgpu_context* ctx, const sgpu_grid_desc* g) {
   ctx->nbdy = cd[2] - cd[1];
   ctx->Nk.assign(g->Nk, g->Nk + Nc);
   ctx->Nke.assign(g->Nke, g->Nke + Ne);
+  ctx->nfaces.assign(g->nfaces, g->nfaces + Nc);
   for (int i = 0; i < Nc; ++i) {
     if (g->Nk[i] < 1 || g->Nk[i] > g->Nkmax) return fail(ctx, SGPU_BAD_GRID, "Nk[%d]=%d out of [1,Nkmax]", i, g->Nk[i]);
     if (g->nfaces[i] < 1 || g->nfaces[i] > mf)
@@ -684,6 +695,333 @@ int sgpu_cgsolve(sgpu_context* ctx, const double* D, double* h, const double* ht
   if (rc) return rc;
   if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return s_rc;
+}
+
+
+
+// ---------------------------------------------------------------------------
+// the steps around CGSolveQ: ComputeQSource, Corrector, and the fused step
+// ---------------------------------------------------------------------------
+static int alloc_step(sgpu_context* ctx) {
+  if (ctx->step_ready) return SGPU_OK;
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_u, ctx->ne3 + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_ut2, ctx->ne3 + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_w, (size_t)ctx->nw3 + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_wt2, (size_t)ctx->nw3 + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_qtot, ctx->n3 + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_etop, (size_t)ctx->Ne + 1))) return rc;
+  ctx->step_ready = true;
+  return SGPU_OK;
+}
+
+int sgpu_step_grid(sgpu_context* ctx, const int* normal, const int* grad, const int* edgep, const int* edgedist) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!normal || !grad || !edgedist || (!edgep && edgedist[1] > edgedist[0])) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  const int Nc = ctx->Nc, Ne = ctx->Ne, F = ctx->F, ncomp = ctx->ncomp;
+  if (edgedist[0] < 0 || edgedist[1] < edgedist[0]) return fail(ctx, SGPU_BAD_GRID, "edgedist out of order");
+  std::vector<int> nf(std::max(ncomp, 1)), nrm((size_t)std::max(ncomp, 1) * F, 0), gd(2 * (size_t)std::max(Ne, 1), -1),
+      ce;
+  for (int j = 0; j < ncomp; ++j) {
+    const int i = ctx->dev2cell[j];
+    nf[j] = ctx->nfaces[i];
+    for (int f = 0; f < nf[j]; ++f) {
+      const int v = normal[(size_t)i * F + f];
+      if (v != 1 && v != -1) return fail(ctx, SGPU_BAD_GRID, "normal[%d]=%d is not +1 or -1", i * F + f, v);
+      nrm[(size_t)j * F + f] = v;
+    }
+  }
+  for (int e = 0; e < Ne; ++e)
+    for (int s = 0; s < 2; ++s) {
+      const int c = grad[2 * e + s];
+      if (c < -1 || c >= Nc) return fail(ctx, SGPU_BAD_GRID, "grad[%d]=%d out of range", 2 * e + s, c);
+      gd[2 * (size_t)e + s] = c < 0 ? -1 : ctx->cell2dev[c];
+    }
+  for (int t = edgedist[0]; t < edgedist[1]; ++t) {
+    const int e = edgep[t];
+    if (e < 0 || e >= Ne) return fail(ctx, SGPU_BAD_GRID, "edgep[%d]=%d out of range", t, e);
+    if (gd[2 * (size_t)e] < 0 || gd[2 * (size_t)e + 1] < 0)
+      return fail(ctx, SGPU_BAD_GRID, "computational edge %d lacks a cell on one side", e);
+    ce.push_back(e);
+  }
+  ctx->woff.assign(Nc + 1, 0);
+  for (int j = 0; j < Nc; ++j) ctx->woff[j + 1] = ctx->woff[j] + ctx->Nk[ctx->dev2cell[j]] + 1;
+  ctx->nw3 = ctx->woff[Nc];
+  DeviceGuard dg(ctx->device);
+  int rc;
+  if (!ctx->step_grid) {
+    if ((rc = dalloc(ctx, &ctx->d_nfaces, nf.size()))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_normal, nrm.size()))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_grad, gd.size()))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_woff, ctx->woff.size()))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_cedge, (size_t)std::max(Ne, 1)))) return rc;
+  }
+  CK(cudaMemcpyAsync(ctx->d_nfaces, nf.data(), sizeof(int) * nf.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_normal, nrm.data(), sizeof(int) * nrm.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_grad, gd.data(), sizeof(int) * gd.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_woff, ctx->woff.data(), sizeof(int) * ctx->woff.size(), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  if (!ce.empty())
+    CK(cudaMemcpyAsync(ctx->d_cedge, ce.data(), sizeof(int) * ce.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->ncedge = (int)ce.size();
+  ctx->step_grid = true;
+  return SGPU_OK;
+}
+
+static StepArgs step_args(sgpu_context* ctx, double theta, double dt) {
+  StepArgs a{};
+  a.n3 = (int)ctx->n3;
+  a.n3c = (int)ctx->n3c;
+  a.ncomp = ctx->ncomp;
+  a.Ne = ctx->Ne;
+  a.F = ctx->F;
+  a.ncedge = ctx->ncedge;
+  a.thetafactor = (1 - theta) / theta;
+  a.dt = dt;
+  a.dcoff = ctx->d_dcoff;
+  a.woff = ctx->d_woff;
+  a.slotcol = ctx->d_slotcol;
+  a.nk = ctx->d_nk;
+  a.nfaces = ctx->d_nfaces;
+  a.fedge = ctx->d_fedge;
+  a.normal = ctx->d_normal;
+  a.nke = ctx->d_nke;
+  a.eoff = ctx->d_eoff;
+  a.grad = ctx->d_grad;
+  a.cedge = ctx->d_cedge;
+  a.Ac = ctx->d_Ac;
+  a.df = ctx->d_df;
+  a.dg = ctx->d_dg;
+  a.ctop = ctx->d_ctop;
+  a.etop = ctx->d_etop;
+  a.dzz = ctx->d_dzz;
+  a.dzf = ctx->d_dzf;
+  a.u = ctx->d_u;
+  a.utmp2 = ctx->d_ut2;
+  a.w = ctx->d_w;
+  a.wtmp2 = ctx->d_wt2;
+  a.src = ctx->d_srcin;
+  a.D = ctx->d_Dq;
+  a.u_out = ctx->d_u;
+  a.w_out = ctx->d_w;
+  a.q_out = ctx->d_qtot;
+  return a;
+}
+
+static void gather_edges(sgpu_context* ctx, const double* const* rows, double* dst) {
+  host_parallel(ctx->Ne, [&](long long b, long long e) {
+    for (long long k = b; k < e; ++k) std::memcpy(dst + ctx->eoff[k], rows[k], sizeof(double) * ctx->Nke[k]);
+  });
+}
+static void scatter_edges(sgpu_context* ctx, const double* src, double* const* rows) {
+  host_parallel(ctx->Ne, [&](long long b, long long e) {
+    for (long long k = b; k < e; ++k) std::memcpy(rows[k], src + ctx->eoff[k], sizeof(double) * ctx->Nke[k]);
+  });
+}
+static void gather_wrows(sgpu_context* ctx, const double* const* rows, double* dst) {
+  host_parallel(ctx->Nc, [&](long long b, long long e) {
+    for (long long j = b; j < e; ++j) {
+      const int i = ctx->dev2cell[j];
+      std::memcpy(dst + ctx->woff[j], rows[i], sizeof(double) * (ctx->Nk[i] + 1));
+    }
+  });
+}
+static void scatter_wrows(sgpu_context* ctx, const double* src, double* const* rows, int ncols) {
+  host_parallel(ncols, [&](long long b, long long e) {
+    for (long long j = b; j < e; ++j) {
+      const int i = ctx->dev2cell[j];
+      std::memcpy(rows[i], src + ctx->woff[j], sizeof(double) * (ctx->Nk[i] + 1));
+    }
+  });
+}
+// cell rows, levels [ctop, Nk) of the first ncols device columns
+static void scatter_cells_active(sgpu_context* ctx, const double* src, double* const* rows, const int* ctop,
+                                 int ncols) {
+  host_parallel(ncols, [&](long long b, long long e) {
+    for (long long j = b; j < e; ++j) {
+      const int i = ctx->dev2cell[j], k0 = ctop[i];
+      std::memcpy(rows[i] + k0, src + ctx->dcoff[j] + k0, sizeof(double) * (ctx->Nk[i] - k0));
+    }
+  });
+}
+
+static int check_ctop(sgpu_context* ctx, const int* ctop) {
+  for (int i = 0; i < ctx->Nc; ++i)
+    if (ctop[i] < 0 || ctop[i] >= ctx->Nk[i]) return fail(ctx, SGPU_BAD_ARG, "ctop[%d]=%d out of [0,Nk)", i, ctop[i]);
+  return SGPU_OK;
+}
+
+int sgpu_compute_qsource(sgpu_context* ctx, const int* ctop, const double* const* dzf, const double* const* u,
+                         const double* const* utmp2, const double* const* w, const double* const* wtmp2,
+                         double theta, double dt, double* const* src, double* D) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctop || !dzf || !u || !utmp2 || !w || !wtmp2 || !src || !D) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  if (!(theta != 0) || !(dt != 0)) return fail(ctx, SGPU_BAD_ARG, "theta and dt must be nonzero");
+  int rc;
+  if ((rc = check_ctop(ctx, ctop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx))) return rc;
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, n_ctop = (ctx->Nc + 1) / 2 + 1;
+  if ((rc = ensure_pinned(ctx, n_ctop + 3 * ne3 + 2 * nw3 + n3 + ctx->Ne + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  double* s_dzf = ctx->pin + n_ctop;
+  double* s_u = s_dzf + ne3;
+  double* s_ut2 = s_u + ne3;
+  double* s_w = s_ut2 + ne3;
+  double* s_wt2 = s_w + nw3;
+  for (int j = 0; j < ctx->Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  gather_edges(ctx, dzf, s_dzf);
+  gather_edges(ctx, u, s_u);
+  gather_edges(ctx, utmp2, s_ut2);
+  gather_wrows(ctx, w, s_w);
+  gather_wrows(ctx, wtmp2, s_wt2);
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_ut2, s_ut2, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_wt2, s_wt2, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
+  StepArgs a = step_args(ctx, theta, dt);
+  CK(launch_qsource(a, ctx->stream));
+  double* s_src = ctx->pin + n_ctop;  // staging reused after the uploads complete
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpyAsync(s_src, ctx->d_srcin, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(D, ctx->d_Dq, sizeof(double) * ctx->Ne, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  scatter_cells_active(ctx, s_src, src, ctop, ctx->Nc);  // every cell's levels [ctop, Nk), as the reference
+  ctx->q_uploaded = false;
+  return SGPU_OK;
+}
+
+int sgpu_corrector(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                   const double* const* qc, const double* D, double dt, double* const* u, double* const* w,
+                   double* const* q) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctop || !etop || !dzz || !qc || !D || !u || !w || !q) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  int rc;
+  if ((rc = check_ctop(ctx, ctop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx))) return rc;
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, n_ctop = (ctx->Nc + 1) / 2 + 1,
+               n_etop = (ctx->Ne + 1) / 2 + 1;
+  if ((rc = ensure_pinned(ctx, n_ctop + n_etop + 3 * n3 + ne3 + nw3 + ctx->Ne + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  int* s_etop = (int*)(ctx->pin + n_ctop);
+  double* s_dzz = ctx->pin + n_ctop + n_etop;
+  double* s_qc = s_dzz + n3;
+  double* s_q = s_qc + n3;
+  double* s_u = s_q + n3;
+  double* s_w = s_u + ne3;
+  double* s_D = s_w + nw3;
+  for (int j = 0; j < ctx->Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  for (int e = 0; e < ctx->Ne; ++e) s_etop[e] = etop[e];
+  gather_cells(ctx, dzz, s_dzz);
+  gather_cells(ctx, qc, s_qc);
+  gather_cells(ctx, (const double* const*)q, s_q);
+  gather_edges(ctx, (const double* const*)u, s_u);
+  gather_wrows(ctx, (const double* const*)w, s_w);
+  std::memcpy(s_D, D, sizeof(double) * ctx->Ne);
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * ctx->Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_qin, s_qc, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_qtot, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_Dq, s_D, sizeof(double) * ctx->Ne, cudaMemcpyHostToDevice, ctx->stream));
+  StepArgs a = step_args(ctx, 1.0, dt);
+  a.qc = ctx->d_qin;
+  CK(launch_corrector(a, ctx->stream));
+  CK(cudaMemcpyAsync(s_u, ctx->d_u, sizeof(double) * ne3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_w, ctx->d_w, sizeof(double) * nw3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_q, ctx->d_qtot, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  scatter_edges(ctx, s_u, u);
+  scatter_wrows(ctx, s_w, w, ctx->ncomp);
+  scatter_cells_active(ctx, s_q, q, ctop, ctx->ncomp);
+  ctx->q_uploaded = false;
+  return SGPU_OK;
+}
+
+int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                       const double* const* dzf, const double* const* utmp2, const double* const* wtmp2,
+                       double* const* u, double* const* w, double* const* q, double* const* qc,
+                       const double* const* c, const sgpu_props* prop, sgpu_stats* st) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctop || !etop || !dzz || !dzf || !utmp2 || !wtmp2 || !u || !w || !q || !qc || !prop)
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  if (!(prop->theta != 0) || !(prop->dt != 0)) return fail(ctx, SGPU_BAD_ARG, "theta and dt must be nonzero");
+  int rc;
+  if ((rc = check_ctop(ctx, ctop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx))) return rc;
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, n_ctop = (ctx->Nc + 1) / 2 + 1,
+               n_etop = (ctx->Ne + 1) / 2 + 1;
+  if ((rc = ensure_pinned(ctx, n_ctop + n_etop + 4 * n3 + 3 * ne3 + 2 * nw3 + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  int* s_etop = (int*)(ctx->pin + n_ctop);
+  double* s_dzz = ctx->pin + n_ctop + n_etop;
+  double* s_qc = s_dzz + n3;
+  double* s_q = s_qc + n3;
+  double* s_c = s_q + n3;
+  double* s_dzf = s_c + n3;
+  double* s_u = s_dzf + ne3;
+  double* s_ut2 = s_u + ne3;
+  double* s_w = s_ut2 + ne3;
+  double* s_wt2 = s_w + nw3;
+  for (int j = 0; j < ctx->Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  for (int e = 0; e < ctx->Ne; ++e) s_etop[e] = etop[e];
+  ctx->h_ctop.assign(ctop, ctop + ctx->Nc);
+  gather_cells(ctx, dzz, s_dzz);
+  gather_cells(ctx, (const double* const*)qc, s_qc);
+  gather_cells(ctx, (const double* const*)q, s_q);
+  if (c) gather_cells(ctx, c, s_c);
+  else std::fill(s_c, s_c + n3, 1.0);
+  gather_edges(ctx, dzf, s_dzf);
+  gather_edges(ctx, (const double* const*)u, s_u);
+  gather_edges(ctx, utmp2, s_ut2);
+  gather_wrows(ctx, (const double* const*)w, s_w);
+  gather_wrows(ctx, wtmp2, s_wt2);
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * ctx->Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_qin, s_qc, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_qtot, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_cin, s_c, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_ut2, s_ut2, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_wt2, s_wt2, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
+  // ComputeQSource straight into the solver's right-hand side and D
+  StepArgs a = step_args(ctx, prop->theta, prop->dt);
+  CK(launch_qsource(a, ctx->stream));
+  ctx->q_uploaded = true;
+  ctx->q_solved = false;
+  rc = sgpu_q_solve(ctx, prop, st);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER && rc != SGPU_BREAKDOWN) return rc;
+  // Corrector with the solution, still on the device
+  a.qc = ctx->d_x;
+  CK(launch_corrector(a, ctx->stream));
+  CK(cudaMemcpyAsync(s_qc, ctx->d_x, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_q, ctx->d_qtot, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_u, ctx->d_u, sizeof(double) * ne3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_w, ctx->d_w, sizeof(double) * nw3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  scatter_cells_active(ctx, s_qc, qc, ctop, ctx->ncomp);
+  scatter_cells_active(ctx, s_q, q, ctop, ctx->ncomp);
+  scatter_edges(ctx, s_u, u);
+  scatter_wrows(ctx, s_w, w, ctx->ncomp);
+  if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
 }
 
 }  // extern "C"
