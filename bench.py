@@ -20,6 +20,10 @@ Workloads (--workload):
         Gaussian bump 10-60 m, Nkmax in {10, 20, 40}) in one persistent launch
         under a CUDA graph, launch shape from the autotuner; against a loop of
         the plain FP64 solver over the same problems.
+  step  the nonhydrostatic pressure step of the default grid: ComputeQSource ->
+        CGSolveQ (FP64, qprecond 1) -> Corrector, fused on the device
+        (sgpu_pressure_step) against the same three drop-in calls made one by
+        one with their host round trips, and the oracle chain on one core.
   cfg5  serving: open-loop Poisson arrivals at 2000 requests/s drawn from a
         seeded pool of grids (Nc log-uniform in [1k, 200k], Nkmax uniform in
         [10, 60]), tolerance from {1e-8, 1e-10}, warm starts from the resident
@@ -85,7 +89,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "step"])
     ap.add_argument("--no-mixed", action="store_true", help="cfg2: skip the mixed_form measurement")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--cfg3-points", type=int, default=500_000, help="cfg3: random points (domain scaled to keep the density)")
@@ -643,16 +647,73 @@ def bench_cfg5(args):
     return line
 
 
+def bench_step(args):
+    """ComputeQSource -> CGSolveQ -> Corrector on the default grid, end to end."""
+    from suntans_gb300 import gridgen as gg
+    from suntans_gb300.capi import Context
+    from suntans_gb300.grid import QProblem
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    g, qp, hp, props, desc = make_workload(args)
+    st = gg.make_step_fields(g, seed=17)
+    ctx = Context(g, device=local)
+    ctx.step_grid(st)
+    for _ in range(args.warmup):
+        ctx.pressure_step(st, props)
+    sampler = ClockSampler(local)
+    sampler.start()
+    fused, iters = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        qc, u, w, q, s = ctx.pressure_step(st, props)
+        fused.append(time.perf_counter() - t0)
+        iters.append(s.niters)
+    sep = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        src, D = ctx.compute_qsource(st, props)
+        qc2, s2 = ctx.cgsolveq(QProblem(grid=g, D=D, src=src, q=st.qc, c=st.c), props)
+        ctx.corrector(st, qc2, D, props)
+        sep.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    ctx.close()
+    N = g.n_q()
+    t_f, t_s = float(np.median(fused)), float(np.median(sep))
+    it = int(np.median(iters))
+    n3, ne3, nw3 = g.n3, int(g.Nke.sum()), int((g.Nk + 1).sum())
+    line = {"metric": "Poisson CG unknown-iters/s of the pressure step (ComputeQSource+CGSolveQ+Corrector, "
+                      "1e-10 relative residual)",
+            "value": N * it / t_f, "unit": "unknown-iters/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_f * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid, velocities and pressure)",
+            "config": {**desc, "workload": desc["workload"] + "; pressure step", "iters_q": it},
+            "separate_calls_ms": t_s * 1e3, "fused_speedup_vs_separate": t_s / t_f,
+            "e2e": {"value": N * it / t_f, "unit": "unknown-iters/s",
+                    "h2d_bytes_per_step": 8 * (4 * n3 + 3 * ne3 + 2 * nw3) + 4 * (g.Nc + g.Ne),
+                    "d2h_bytes_per_step": 8 * (2 * n3 + ne3 + nw3)},
+            "gpu_launches": 4 * args.steps, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        from oracle.oracle import Oracle
+        o = Oracle("port")
+        t0 = time.perf_counter()
+        src, D = o.compute_qsource(st, props)
+        o.corrector(st, qp.q, D, props)
+        t_qc = time.perf_counter() - t0
+        cb = cpu_baseline(g, qp, None, props, args.cpu_seconds)
+        cb["sample"] += f"; ComputeQSource + Corrector on the full grid took {t_qc:.2f} s more per step"
+        line["cpu_baseline"] = cb
+    return line
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload in ("cfg3", "cfg4", "cfg5"):
+    elif args.workload in ("cfg3", "cfg4", "cfg5", "step"):
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         import __graft_entry__
         __graft_entry__.build()
-        fn = {"cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5}[args.workload]
+        fn = {"cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5, "step": bench_step}[args.workload]
         line = fn(args)
         if int(os.environ.get("RANK", "0")) == 0:
             print(json.dumps(line), flush=True)
