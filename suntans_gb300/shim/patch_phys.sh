@@ -1,12 +1,15 @@
 #!/bin/sh
 # Redirects the two elliptic solves of a SUNTANS main/phys.c to the GPU
-# adapter (sgpu_suntans.c).  Usage:  sh patch_phys.sh path/to/main/phys.c
+# adapter (sgpu_suntans.c).  Usage:  sh patch_phys.sh path/to/main/phys.c [step]
 # Edits in place and keeps phys.c.orig.  Exactly two call sites change:
 #   Solve       main/phys.c:1280  CGSolveQ(phys->qc,phys->stmp,phys->stmp3,...)
 #   UPredictor  main/phys.c:2989  CGSolve(grid,phys,prop,myproc,numprocs,comm)
+# With "step", the two steps around CGSolveQ in Solve move to the GPU too:
+#   main/phys.c:1274  ComputeQSource(phys->stmp,...)
+#   main/phys.c:1289  Corrector(phys->qc,...)
 set -e
 f="$1"
-[ -f "$f" ] || { echo "usage: $0 main/phys.c" >&2; exit 2; }
+[ -f "$f" ] || { echo "usage: $0 main/phys.c [step]" >&2; exit 2; }
 cp "$f" "$f.orig"
 sed -i \
   -e 's/^\([[:space:]]*\)CGSolveQ(phys->qc,phys->stmp,phys->stmp3,grid,phys,prop,myproc,numprocs,comm);/\1sgpu_CGSolveQ(phys->qc,phys->stmp,phys->stmp3,grid,phys,prop,myproc,numprocs,comm);/' \
@@ -16,6 +19,17 @@ sed -i \
 sed -i '0,/^#include "phys.h"/s//#include "phys.h"\
 void sgpu_CGSolveQ(REAL **q, REAL **src, REAL **c, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);\
 void sgpu_CGSolve(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);/' "$f"
+if [ "$2" = "step" ]; then
+  sed -i \
+    -e 's/^\([[:space:]]*\)ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);/\1sgpu_ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);/' \
+    -e 's/^\([[:space:]]*\)Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);/\1sgpu_Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);/' \
+    "$f"
+  sed -i '0,/^#include "phys.h"/s//#include "phys.h"\
+void sgpu_ComputeQSource(REAL **src, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs);\
+void sgpu_Corrector(REAL **qc, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);/' "$f"
+  m=$(grep -c 'sgpu_ComputeQSource\|sgpu_Corrector' "$f")
+  [ "$m" -ge 4 ] || { echo "patch_phys.sh: step call sites not found ($m)" >&2; mv "$f.orig" "$f"; exit 1; }
+fi
 n=$(grep -c 'sgpu_CGSolve' "$f")
 [ "$n" -ge 4 ] || { echo "patch_phys.sh: expected call sites not found ($n)" >&2; mv "$f.orig" "$f"; exit 1; }
 echo "patched $f ($n references)"

@@ -122,3 +122,39 @@ void sgpu_CGSolve(gridT *grid, physT *phys, propT *prop, int myproc, int numproc
              st.niters, res, prop->epsilon);
   }
 }
+
+/* The steps on either side of CGSolveQ in Solve (main/phys.c:1273-1287), with
+ * the reference's parameter lists: ComputeQSource (declared phys.c:53-54,
+ * defined 2345) and Corrector (declared phys.c:55-56, defined 2301).  The
+ * edge and normal fields they need beyond the solver's grid are uploaded once
+ * per grid.  Same bits as the reference. */
+static gridT *g_step_grid = NULL;
+
+static void sgpu_ensure_step(gridT *grid, int numprocs) {
+  int rc;
+  sgpu_ensure_context(grid, numprocs);
+  if (g_step_grid == grid) return;
+  rc = sgpu_step_grid(g_ctx, grid->normal, grid->grad, grid->edgep, grid->edgedist);
+  if (rc != SGPU_OK) sgpu_die("sgpu_step_grid", rc);
+  g_step_grid = grid;
+}
+
+void sgpu_ComputeQSource(REAL **src, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs) {
+  int rc;
+  (void)myproc;
+  sgpu_ensure_step(grid, numprocs);
+  rc = sgpu_compute_qsource(g_ctx, grid->ctop, (const double *const *)grid->dzf, (const double *const *)phys->u,
+                            (const double *const *)phys->utmp2, (const double *const *)phys->w,
+                            (const double *const *)phys->wtmp2, prop->theta, prop->dt, src, phys->D);
+  if (rc != SGPU_OK) sgpu_die("sgpu_compute_qsource", rc);
+}
+
+void sgpu_Corrector(REAL **qc, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm) {
+  int rc;
+  (void)myproc;
+  (void)comm;
+  sgpu_ensure_step(grid, numprocs);
+  rc = sgpu_corrector(g_ctx, grid->ctop, grid->etop, (const double *const *)grid->dzz, (const double *const *)qc,
+                      phys->D, prop->dt, phys->u, phys->w, phys->q);
+  if (rc != SGPU_OK) sgpu_die("sgpu_corrector", rc);
+}
