@@ -538,3 +538,117 @@ void sgo_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const 
   free(woff);
   layout_free(L);
 }
+
+/* ------------------------------------------------------------------------
+ * The vertical grid of the current step: UpdateDZ and SetFluxHeight.
+ * ------------------------------------------------------------------------ */
+#define SGO_DRYCELLHEIGHT 1e-10                       /* suntans.h:31 */
+static double sgo_max(double x1, double x2) { return x2 > x1 ? x2 : x1; }   /* util.c:212-217 */
+static double sgo_min(double x, double y) { return x < y ? x : y; }         /* util.c:242-246 */
+static double sgo_upwind(double u, double dz1, double dz2) {                 /* util.c:219-232 */
+  if (fabs(u) > 0) return u > 0 ? dz2 : dz1;
+  return sgo_max(dz1, dz2);
+}
+
+/* UpdateDZ, main/phys.c:816-941, option 0. */
+void sgo_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h, int linearFS,
+                   int *ctop, int *etop, double *dzz, int *ctopold, int *etopold, double *dzzold) {
+  layout_t Lv, *L = &Lv;
+  int i, j, k, flag, ne1, ne2;
+  double z;
+  if (linearFS) return;                                            /* 822-824 */
+  layout_make(g, L);
+  for (j = 0; j < g->Ne; j++) etopold[j] = etop[j];                /* 829-837 */
+  for (i = 0; i < g->Nc; i++) {
+    ctopold[i] = ctop[i];
+    for (k = 0; k < ctop[i]; k++) X3(dzzold, i, k) = 0;
+    for (k = ctop[i]; k < g->Nk[i]; k++) X3(dzzold, i, k) = X3(dzz, i, k);
+  }
+  for (i = 0; i < g->Nc; i++) {                                    /* 848-853 */
+    z = 0;
+    for (k = 0; k < g->Nk[i]; k++) z -= v->dz[k];
+    X3(dzz, i, g->Nk[i] - 1) = v->dz[g->Nk[i] - 1] + v->dv[i] + z;
+  }
+  if (g->Nkmax > 1) {                                              /* 857-886 */
+    for (i = 0; i < g->Nc; i++) {
+      z = 0;
+      flag = 0;
+      for (k = 0; k < g->Nk[i]; k++) {
+        z -= v->dz[k];
+        if (h[i] >= z) {
+          if (!flag) {
+            if (k == g->Nk[i] - 1) {
+              X3(dzz, i, k) = h[i] + v->dv[i];
+              ctop[i] = k;
+            } else if (h[i] == z) {
+              X3(dzz, i, k) = 0;
+              ctop[i] = k + 1;
+            } else {
+              X3(dzz, i, k) = h[i] - z;
+              ctop[i] = k;
+            }
+            flag = 1;
+          } else {
+            if (k == g->Nk[i] - 1)
+              X3(dzz, i, k) = v->dz[k] + v->dv[i] + z;
+            else if (z < -v->dv[i])
+              X3(dzz, i, k) = 0;
+            else
+              X3(dzz, i, k) = v->dz[k];
+          }
+        } else {
+          X3(dzz, i, k) = 0;
+        }
+      }
+    }
+  } else {
+    for (i = 0; i < g->Nc; i++) X3(dzz, i, 0) = v->dv[i] + h[i];  /* 887-889 */
+  }
+  for (j = 0; j < g->Ne; j++) {                                    /* 903-914 */
+    ne1 = x->grad[2 * j];
+    ne2 = x->grad[2 * j + 1];
+    if (ne1 == -1) etop[j] = ctop[ne2];
+    else if (ne2 == -1) etop[j] = ctop[ne1];
+    else if (ctop[ne1] < ctop[ne2]) etop[j] = ctop[ne1];
+    else etop[j] = ctop[ne2];
+  }
+  layout_free(L);
+}
+
+/* SetFluxHeight, main/phys.c:4338-4435. */
+void sgo_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
+                         const double *u, double *dzz, double *dzf) {
+  layout_t Lv, *L = &Lv;
+  int i, j, k, nc1, nc2;
+  long *foff;
+  layout_make(g, L);
+  foff = (long *)malloc(sizeof(long) * (g->Ne + 1));
+  foff[0] = 0;
+  for (j = 0; j < g->Ne; j++) foff[j + 1] = foff[j] + v->Nkc[j];
+  for (j = 0; j < g->Ne; j++)                                      /* 4380-4383 */
+    for (k = 0; k < v->Nkc[j]; k++) dzf[foff[j] + k] = 0;
+  if (v->smoothbot)                                                /* 4386-4392 */
+    for (i = 0; i < g->Nc; i++)
+      X3(dzz, i, g->Nk[i] - 1) = sgo_max(v->dzbot[i], v->smoothbot * v->dz[g->Nk[i] - 1]);
+  for (j = 0; j < g->Ne; j++) {                                    /* 4395-4426 */
+    nc1 = x->grad[2 * j];
+    nc2 = x->grad[2 * j + 1];
+    if (nc1 == -1) nc1 = nc2;
+    if (nc2 == -1) nc2 = nc1;
+    for (k = 0; k < x->etop[j]; k++) dzf[foff[j] + k] = 0;
+    for (k = x->etop[j]; k < g->Nke[j]; k++)
+      dzf[foff[j] + k] = sgo_upwind(u[L->eoff[j] + k], X3(dzz, nc1, k), X3(dzz, nc2, k));
+    k = g->Nke[j] - 1;
+    if (x->etop[j] == k)
+      dzf[foff[j] + k] = sgo_max(0, sgo_upwind(u[L->eoff[j] + k], h[nc1], h[nc2]) + sgo_min(v->dv[nc1], v->dv[nc2]));
+    else
+      dzf[foff[j] + k] = sgo_min(X3(dzz, nc1, k), X3(dzz, nc2, k));
+    for (k = x->etop[j]; k < g->Nke[j]; k++)
+      if (dzf[foff[j] + k] <= SGO_DRYCELLHEIGHT) dzf[foff[j] + k] = 0;
+  }
+  if (v->smoothbot)                                                /* 4430-4433 */
+    for (i = 0; i < g->Nc; i++)
+      X3(dzz, i, g->Nk[i] - 1) = sgo_max(X3(dzz, i, g->Nk[i] - 1), v->dzsmall * v->dz[g->Nk[i] - 1]);
+  free(foff);
+  layout_free(L);
+}

@@ -74,6 +74,17 @@ typedef struct sgo_ext {
   const int *etop;     /* [Ne] gridT.etop                                          */
 } sgo_ext;
 
+/* The vertical-grid fields of UpdateDZ (main/phys.c:816-941) and SetFluxHeight
+ * (main/phys.c:4338-4435). */
+typedef struct sgo_vgrid {
+  const double *dz;    /* [Nkmax] gridT.dz, layer thicknesses                    */
+  const double *dv;    /* [Nc] gridT.dv, depth                                   */
+  const double *dzbot; /* [Nc] gridT.dzbot (read when smoothbot != 0)            */
+  const int *Nkc;      /* [Ne] gridT.Nkc, levels stored per dzf row (>= Nke)      */
+  double smoothbot;    /* gridT.smoothbot                                          */
+  double dzsmall;      /* gridT.dzsmall                                            */
+} sgo_vgrid;
+
 /* Ragged layouts of the step fields: u, utmp2 per edge with Nke[j] levels (as
  * dzf); w, wtmp2 per cell with Nk[i]+1 levels (offsets the prefix sum of
  * Nk+1); src, q, qc per cell with Nk[i] levels (as dzz). */
@@ -100,6 +111,16 @@ void sgo_compute_qsource(const sgo_grid *g, const sgo_ext *x, const double *u, c
                          const double *w, const double *wtmp2, const sgo_prop *p, double *src, double *D);
 void sgo_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const double *D,
                    const sgo_prop *p, double *u, double *w, double *q);
+/* UpdateDZ with option 0 (the per-step call, main/phys.c:3024): ctop, etop and
+   dzz (rows of Nk) are updated in place from h; the old values go to ctopold,
+   etopold, dzzold.  g->ctop and g->dzz are not read. */
+void sgo_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h, int linearFS,
+                   int *ctop, int *etop, double *dzz, int *ctopold, int *etopold, double *dzzold);
+/* SetFluxHeight: dzf (rows of Nkc levels) from u, dzz, h; dzz's bottom level is
+   adjusted in place when smoothbot != 0.  x->etop and x->grad are read;
+   g->dzz and g->dzf are not. */
+void sgo_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
+                         const double *u, double *dzz, double *dzf);
 
 /* ---- the reference itself (ref_harness.c, oracle/_ref only) ---- */
 void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
@@ -122,6 +143,10 @@ void ref_compute_qsource(const sgo_grid *g, const sgo_ext *x, const double *u, c
                          const double *w, const double *wtmp2, const sgo_prop *p, double *src, double *D);
 void ref_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const double *D,
                    const sgo_prop *p, double *u, double *w, double *q);
+void ref_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h, int linearFS,
+                   int *ctop, int *etop, double *dzz, int *ctopold, int *etopold, double *dzzold);
+void ref_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
+                         const double *u, double *dzz, double *dzf);
 
 #ifdef __cplusplus
 }

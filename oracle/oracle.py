@@ -46,6 +46,11 @@ class SgoExt(C.Structure):
     _fields_ = [("normal", _ip), ("grad", _ip), ("edgep", _ip), ("edgedist", _ip), ("etop", _ip)]
 
 
+class SgoVgrid(C.Structure):
+    _fields_ = [("dz", _dp), ("dv", _dp), ("dzbot", _dp), ("Nkc", _ip), ("smoothbot", C.c_double),
+                ("dzsmall", C.c_double)]
+
+
 class SgoResult(C.Structure):
     _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double)]
 
@@ -221,6 +226,55 @@ class Oracle:
         self._fn("corrector")(C.byref(s), C.byref(x), _ptr(qc, _dp), _ptr(D, _dp), C.byref(pr), _ptr(u, _dp),
                               _ptr(w, _dp), _ptr(q, _dp))
         return u, w, q
+
+
+    # ---- the vertical grid of the step ----
+    @staticmethod
+    def _vgrid(vf):
+        g = vf.grid
+        keep = [np.ascontiguousarray(g.dz, dtype=np.float64), np.ascontiguousarray(g.dv, dtype=np.float64),
+                np.ascontiguousarray(vf.dzbot, dtype=np.float64), np.ascontiguousarray(vf.Nkc, dtype=np.int32)]
+        return SgoVgrid(_ptr(keep[0], _dp), _ptr(keep[1], _dp), _ptr(keep[2], _dp), _ptr(keep[3], _ip),
+                        vf.smoothbot, vf.dzsmall), keep
+
+    def _vext(self, vf, etop):
+        g = vf.grid
+        keep = [np.ascontiguousarray(g.normal, dtype=np.int32), np.ascontiguousarray(g.grad, dtype=np.int32),
+                np.zeros(1, np.int32), np.zeros(2, np.int32), etop]
+        return SgoExt(*[_ptr(x, _ip) for x in keep]), keep
+
+    def update_dz(self, vf, linearFS=0):
+        """UpdateDZ(option 0): returns (ctop, etop, dzz, ctopold, etopold, dzzold)."""
+        g = vf.grid
+        s, keep = self._grid(g)
+        v, keepv = self._vgrid(vf)
+        ctop = np.array(vf.ctop, dtype=np.int32, copy=True)
+        etop = np.array(vf.etop, dtype=np.int32, copy=True)
+        x, keepx = self._vext(vf, etop)
+        dzz = np.array(vf.dzz, dtype=np.float64, copy=True)
+        ctopold = np.full(g.Nc, -7, dtype=np.int32)
+        etopold = np.full(max(g.Ne, 1), -7, dtype=np.int32)
+        dzzold = np.full(g.n3, -7.0)
+        h = np.ascontiguousarray(vf.h, dtype=np.float64)
+        self._fn("update_dz")(C.byref(s), C.byref(x), C.byref(v), _ptr(h, _dp), C.c_int(linearFS),
+                              _ptr(ctop, _ip), _ptr(etop, _ip), _ptr(dzz, _dp), _ptr(ctopold, _ip),
+                              _ptr(etopold, _ip), _ptr(dzzold, _dp))
+        return ctop, etop[:g.Ne], dzz, ctopold, etopold[:g.Ne], dzzold
+
+    def set_flux_height(self, vf, dzz=None, etop=None):
+        """SetFluxHeight: returns (dzf rows of Nkc levels, dzz after the smoothbot adjustments)."""
+        g = vf.grid
+        s, keep = self._grid(g)
+        v, keepv = self._vgrid(vf)
+        et = np.array(vf.etop if etop is None else etop, dtype=np.int32, copy=True)
+        x, keepx = self._vext(vf, et)
+        dzz = np.array(vf.dzz if dzz is None else dzz, dtype=np.float64, copy=True)
+        dzf = np.full(int(np.sum(vf.Nkc)), -7.0)
+        h = np.ascontiguousarray(vf.h, dtype=np.float64)
+        u = np.ascontiguousarray(vf.u, dtype=np.float64)
+        self._fn("set_flux_height")(C.byref(s), C.byref(x), C.byref(v), _ptr(h, _dp), _ptr(u, _dp), _ptr(dzz, _dp),
+                                    _ptr(dzf, _dp))
+        return dzf, dzz
 
 
 def available(which: str) -> bool:

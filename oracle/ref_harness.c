@@ -309,3 +309,53 @@ void ref_corrector(const sgo_grid *g, const sgo_ext *x, const double *qc, const 
   Corrector(QC, &H.grid, &H.phys, &H.prop, 0, 1, 0);
   harness_free(&H);
 }
+
+static void harness_vgrid(harness_t *H, const sgo_vgrid *v) {
+  H->grid.dz = (REAL *)v->dz;
+  H->grid.dv = (REAL *)v->dv;
+  H->grid.dzbot = (REAL *)v->dzbot;
+  H->grid.Nkc = (int *)v->Nkc;
+  H->grid.smoothbot = v->smoothbot;
+  H->grid.dzsmall = v->dzsmall;
+}
+
+void ref_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h, int linearFS,
+                   int *ctop, int *etop, double *dzz, int *ctopold, int *etopold, double *dzzold) {
+  harness_t H;
+  sgo_prop pr;
+  memset(&pr, 0, sizeof(pr));
+  harness_init(&H, g, NULL, &pr);
+  harness_ext(&H, g, x);
+  harness_vgrid(&H, v);
+  H.grid.ctop = ctop;
+  H.grid.etop = etop;
+  H.grid.ctopold = ctopold;
+  H.grid.etopold = etopold;
+  H.grid.dzz = jag_view(&H, dzz, H.coff, g->Nc);
+  H.grid.dzzold = jag_view(&H, dzzold, H.coff, g->Nc);
+  H.phys.h = (REAL *)h;
+  H.prop.linearFS = linearFS;
+  UpdateDZ(&H.grid, &H.phys, &H.prop, 0);
+  harness_free(&H);
+}
+
+void ref_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
+                         const double *u, double *dzz, double *dzf) {
+  harness_t H;
+  long *foff;
+  int j;
+  sgo_prop pr;
+  memset(&pr, 0, sizeof(pr));
+  harness_init(&H, g, NULL, &pr);
+  harness_ext(&H, g, x);
+  harness_vgrid(&H, v);
+  foff = (long *)blk_new(&H, sizeof(long) * (g->Ne + 1));
+  foff[0] = 0;
+  for (j = 0; j < g->Ne; j++) foff[j + 1] = foff[j] + v->Nkc[j];
+  H.grid.dzz = jag_view(&H, dzz, H.coff, g->Nc);
+  H.grid.dzf = jag_view(&H, dzf, foff, g->Ne);
+  H.phys.h = (REAL *)h;
+  H.phys.u = jag_view(&H, u, H.eoff, g->Ne);
+  SetFluxHeight(&H.grid, &H.phys, &H.prop);
+  harness_free(&H);
+}

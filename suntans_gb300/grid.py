@@ -45,6 +45,8 @@ class SunGrid:
     grad: Optional[np.ndarray] = None     # [2*Ne] int32
     xv: Optional[np.ndarray] = None
     yv: Optional[np.ndarray] = None
+    dz: Optional[np.ndarray] = None       # [Nkmax] layer thicknesses (gridT.dz)
+    dv: Optional[np.ndarray] = None       # [Nc] depth (gridT.dv)
     name: str = "grid"
 
     def __post_init__(self):
@@ -170,6 +172,29 @@ class StepFields:
     def woff(self) -> np.ndarray:
         o = np.zeros(self.grid.Nc + 1, dtype=np.int64)
         np.cumsum(self.grid.Nk + 1, out=o[1:])
+        return o
+
+
+@dataclasses.dataclass
+class VGridFields:
+    """Inputs of UpdateDZ and SetFluxHeight beyond the grid: the free surface,
+    the edge velocity, the gridT vertical-grid settings and the per-step
+    ctop / etop / dzz they start from."""
+    grid: SunGrid
+    h: np.ndarray         # [Nc] free surface
+    u: np.ndarray         # ragged per edge (Nke levels)
+    dzbot: np.ndarray     # [Nc] gridT.dzbot
+    Nkc: np.ndarray       # [Ne] levels stored per dzf row
+    smoothbot: float
+    dzsmall: float
+    ctop: np.ndarray      # [Nc] current ctop
+    etop: np.ndarray      # [Ne] current etop
+    dzz: np.ndarray       # ragged per cell: current dzz
+
+    @property
+    def foff(self) -> np.ndarray:
+        o = np.zeros(self.grid.Ne + 1, dtype=np.int64)
+        np.cumsum(self.Nkc, out=o[1:])
         return o
 
 

@@ -214,7 +214,7 @@ def _assemble(points, cells, nfaces, maxfaces, depth_fn, Nkmax, rstretch, stairs
 
     g = SunGrid(Nc=Nc, Ne=Ne, maxfaces=maxfaces, Nkmax=Nkmax, nfaces=nfaces, neigh=neigh, face=face,
                 Nk=Nk, Nke=Nke, ctop=ctop, cellp=cellp, celldist=celldist, Ac=Ac, df=df, dg=dg,
-                dzz=dzz, dzf=dzf, normal=normal, grad=grad.ravel(), xv=xv, yv=yv, name=name)
+                dzz=dzz, dzf=dzf, normal=normal, grad=grad.ravel(), xv=xv, yv=yv, dz=dz, dv=depth, name=name)
     return g
 
 
@@ -416,3 +416,27 @@ def make_step_fields(g: SunGrid, seed=0, sigma_u=0.05, sigma_w=0.002, sigma_q=0.
     edgep = np.nonzero(interior)[0].astype(np.int32)
     return StepFields(grid=g, u=u, utmp2=utmp2, w=w, wtmp2=wtmp2, q=q, qc=np.zeros(g.n3), c=np.ones(g.n3),
                       etop=etop, edgep=edgep, edgedist=np.array([0, edgep.size], dtype=np.int32))
+
+
+def make_vgrid_fields(g: SunGrid, seed=0, sigma_h=None, smoothbot=0.0, dzsmall=0.1) -> "VGridFields":
+    """Seeded inputs of UpdateDZ / SetFluxHeight: a free surface that moves
+    some cells' top level (N(0, sigma_h), default half the top layer), an edge
+    velocity with exact zeros on some levels (UpWind's third branch), dzbot =
+    the bottom cells' thickness, Nkc = the deeper of an edge's two cells."""
+    from .grid import VGridFields
+    rng = np.random.default_rng(seed)
+    sig = 0.5 * float(g.dz[0]) if sigma_h is None else sigma_h
+    h = rng.normal(0.0, sig, g.Nc)
+    ne3 = int(g.Nke.sum())
+    u = rng.normal(0.0, 0.05, ne3)
+    u[rng.random(ne3) < 0.05] = 0.0
+    last = g.coff[1:] - 1
+    dzbot = g.dzz[last].copy()
+    grad = g.grad.reshape(g.Ne, 2)
+    c0, c1 = grad[:, 0], grad[:, 1]
+    nk0 = g.Nk[np.where(c0 >= 0, c0, c1)]
+    nk1 = g.Nk[np.where(c1 >= 0, c1, c0)]
+    Nkc = np.maximum(np.maximum(nk0, nk1), g.Nke).astype(np.int32)
+    st = make_step_fields(g, seed=seed + 1)
+    return VGridFields(grid=g, h=h, u=u, dzbot=dzbot, Nkc=Nkc, smoothbot=float(smoothbot), dzsmall=float(dzsmall),
+                       ctop=g.ctop.copy(), etop=st.etop.copy(), dzz=g.dzz.copy())

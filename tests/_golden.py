@@ -36,5 +36,13 @@ def step_fields(g, d):
                       qc=np.zeros(g.n3), c=np.ones(g.n3), etop=d["etop"], edgep=d["edgep"], edgedist=d["edgedist"])
 
 
+def vgrid_fields(g, d, smoothbot=0.0):
+    """The UpdateDZ / SetFluxHeight inputs stored with a fixture."""
+    from suntans_gb300.grid import VGridFields
+    g.dz, g.dv, g.grad, g.normal = d["vg_dz"], d["vg_dv"], d["grad"], d["normal"]
+    return VGridFields(grid=g, h=d["vg_h"], u=d["vg_u"], dzbot=d["vg_dzbot"], Nkc=d["vg_Nkc"], smoothbot=smoothbot,
+                       dzsmall=0.1, ctop=d["vg_ctop"], etop=d["vg_etop"], dzz=d["vg_dzz"])
+
+
 def props_for(props, **kw):
     return SolverProps(**{**props, **kw})

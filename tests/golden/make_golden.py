@@ -13,7 +13,9 @@ read, and the reference's outputs for:
   QCoefficients (qprecond 0 and 1), OperatorQ, OperatorQC, ConditionQ,
   Preconditioner, HCoefficients and OperatorH on a seeded vector,
   ComputeQSource on seeded velocity fields and Corrector with the qprecond-1
-  solution as the pressure correction (the steps around CGSolveQ).
+  solution as the pressure correction (the steps around CGSolveQ),
+  UpdateDZ (option 0) and SetFluxHeight (smoothbot 0 and 0.3) on a seeded
+  free surface and edge velocity.
 The inputs are stored (not regenerated) so that the check is bit-exact on any
 host: tests/test_oracle.py runs the C restatement (oracle/cg_oracle.c) on them
 and requires identical bits.
@@ -90,6 +92,18 @@ def main():
         out.update(qs_src=qs_src, qs_D=qs_D)
         cu, cw, cq = ref.corrector(st, out["q_qp1"], qs_D, SolverProps(**props))
         out.update(corr_u=cu, corr_w=cw, corr_q=cq)
+        vf = gg.make_vgrid_fields(g, seed=35)
+        out.update(vg_dz=g.dz, vg_dv=g.dv, vg_h=vf.h, vg_u=vf.u, vg_dzbot=vf.dzbot, vg_Nkc=vf.Nkc,
+                   vg_ctop=vf.ctop, vg_etop=vf.etop, vg_dzz=vf.dzz)
+        for k, val in zip(("udz_ctop", "udz_etop", "udz_dzz", "udz_ctopold", "udz_etopold", "udz_dzzold"),
+                          ref.update_dz(vf)):
+            out[k] = val
+        for sb in (0.0, 0.3):
+            vf.smoothbot = sb
+            dzf, dzz2 = ref.set_flux_height(vf)
+            tag = "sfh%d" % int(round(10 * sb))
+            out[tag + "_dzf"] = dzf
+            out[tag + "_dzz"] = dzz2
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
         print(f"{path}: Nc={g.Nc} n3={g.n3} iters q={[int(out[f'n_qp{k}']) for k in range(3)]} "

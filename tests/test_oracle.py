@@ -100,6 +100,12 @@ def test_port_matches_reference_library(port, gname):
     qc = port.cgsolveq(gg.QProblem(grid=g, D=Da, src=sa, q=st.qc, c=st.c), pr)[0]
     for x, y in zip(port.corrector(st, qc, Da, pr), ref.corrector(st, qc, Da, pr)):
         assert np.array_equal(x, y)
+    if g.dz is not None:
+        vf = gg.make_vgrid_fields(g, seed=11, smoothbot=0.2)
+        for x, y in zip(port.update_dz(vf), ref.update_dz(vf)):
+            assert np.array_equal(x, y)
+        for x, y in zip(port.set_flux_height(vf), ref.set_flux_height(vf)):
+            assert np.array_equal(x, y)
 
 
 @pytest.mark.parametrize("name", fixture_names())
@@ -114,3 +120,20 @@ def test_port_step_functions_match_golden_bitwise(port, name):
     assert np.array_equal(u, d["corr_u"]) and np.array_equal(w, d["corr_w"]) and np.array_equal(q, d["corr_q"])
     # the fixtures exercise both branches of the edge and column conditions
     assert np.any(u != d["u"]) and np.any(w != d["w"]) and np.any(q != d["qtot"])
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_port_vertical_grid_functions_match_golden_bitwise(port, name):
+    """UpdateDZ (option 0) and SetFluxHeight of the restatement reproduce the reference's bits."""
+    from tests._golden import vgrid_fields
+    g, qp, hp, props, d = load(name)
+    vf = vgrid_fields(g, d)
+    for k, val in zip(("udz_ctop", "udz_etop", "udz_dzz", "udz_ctopold", "udz_etopold", "udz_dzzold"),
+                      port.update_dz(vf)):
+        assert np.array_equal(val, d[k]), k
+    assert np.any(d["udz_ctop"] != d["vg_ctop"])  # the free surface moved some tops
+    for sb in (0.0, 0.3):
+        vf.smoothbot = sb
+        dzf, dzz = port.set_flux_height(vf)
+        tag = "sfh%d" % int(round(10 * sb))
+        assert np.array_equal(dzf, d[tag + "_dzf"]) and np.array_equal(dzz, d[tag + "_dzz"])
