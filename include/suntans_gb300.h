@@ -151,6 +151,30 @@ int sgpu_pressure_step(sgpu_context *ctx, const int *ctop, const int *etop, cons
                        double *const *u, double *const *w, double *const *q, double *const *qc,
                        const double *const *c, const sgpu_props *prop, sgpu_stats *stats);
 
+/* ---- the vertical grid of the step (it drives both solvers' coefficients) ---- */
+typedef struct sgpu_vgrid {
+  const double *dz;    /* [Nkmax] gridT.dz, layer thicknesses                        */
+  const double *dv;    /* [Nc] gridT.dv, depth                                       */
+  const double *dzbot; /* [Nc] gridT.dzbot (needed when smoothbot != 0)              */
+  const int *Nkc;      /* [Ne] gridT.Nkc, levels stored per dzf row (>= Nke)          */
+  double smoothbot;    /* gridT.smoothbot                                              */
+  double dzsmall;      /* gridT.dzsmall                                                */
+} sgpu_vgrid;
+
+/* UpdateDZ drop-in for the per-step call (option 0, main/phys.c:816-941, called
+ * at 3024): from the free surface h, dzz (rows of Nk), ctop and etop are updated
+ * in place and their previous values written to dzzold, ctopold, etopold.
+ * linearFS != 0 returns at once, as the reference.  Needs sgpu_step_grid (grad).
+ * Same bits as the reference. */
+int sgpu_update_dz(sgpu_context *ctx, const sgpu_vgrid *v, const double *h, int linearFS, int *ctop, int *etop,
+                   double *const *dzz, int *ctopold, int *etopold, double *const *dzzold);
+
+/* SetFluxHeight drop-in (main/phys.c:4338-4435): dzf (rows of Nkc levels) from
+ * u (rows of Nke), dzz and h; with smoothbot != 0 the bottom level of dzz is
+ * adjusted in place as in the reference.  Same bits as the reference. */
+int sgpu_set_flux_height(sgpu_context *ctx, const sgpu_vgrid *v, const int *etop, const double *h,
+                         const double *const *u, double *const *dzz, double *const *dzf);
+
 /* Staged forms of the same two solves, for callers that keep inputs resident:
  * upload (host -> HBM), solve (HBM only; repeatable on the same inputs), and
  * download (HBM -> host, computational cells / active levels only). */

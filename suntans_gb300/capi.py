@@ -27,6 +27,7 @@ EXPORTS = [
     "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream", "sgpu_phase_times",
     "sgpu_cgsolve_noalloc",
     "sgpu_step_grid", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_pressure_step",
+    "sgpu_update_dz", "sgpu_set_flux_height",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
     "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set", "sgpu_batch_set_tile_slots",
     "sgpu_batch_stream", "sgpu_batch_phase_times", "sgpu_batch_resubmit", "sgpu_batch_use_graph",
@@ -59,6 +60,11 @@ class NoallocGrid(C.Structure):
                 ("Ac", C.c_void_p), ("df", C.c_void_p), ("dg", C.c_void_p)]
 
 
+class VGrid(C.Structure):
+    _fields_ = [("dz", _dp), ("dv", _dp), ("dzbot", _dp), ("Nkc", _ip), ("smoothbot", C.c_double),
+                ("dzsmall", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [("status", C.c_int), ("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double),
                 ("ms_solve", C.c_double), ("ms_total", C.c_double), ("unknowns", C.c_longlong)]
@@ -85,6 +91,8 @@ def load() -> C.CDLL:
     lib.sgpu_status_string.argtypes = [C.c_int]
     lib.sgpu_status_string.restype = C.c_char_p
     lib.sgpu_step_grid.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
+    lib.sgpu_update_dz.argtypes = [C.c_void_p, C.POINTER(VGrid), _dp, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp]
+    lib.sgpu_set_flux_height.argtypes = [C.c_void_p, C.POINTER(VGrid), _ip, _dp, _dpp, _dpp, _dpp]
     lib.sgpu_compute_qsource.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dpp, _dpp, _dpp, C.c_double, C.c_double,
                                          _dpp, _dp]
     lib.sgpu_corrector.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dp, C.c_double, _dpp, _dpp, _dpp]
@@ -335,6 +343,47 @@ class Context:
                                          *[_vp(x) for x in ptr], C.byref(pr), C.byref(stt))
         self._check(rc, "sgpu_pressure_step")
         return qc, u, w, q, stt
+
+    # ---- the vertical grid of the step ----
+    def _vgrid(self, vf):
+        g = self.grid
+        keep = [np.ascontiguousarray(g.dz, dtype=np.float64), np.ascontiguousarray(g.dv, dtype=np.float64),
+                np.ascontiguousarray(vf.dzbot, dtype=np.float64), np.ascontiguousarray(vf.Nkc, dtype=np.int32)]
+        v = VGrid(keep[0].ctypes.data_as(_dp), keep[1].ctypes.data_as(_dp), keep[2].ctypes.data_as(_dp),
+                  keep[3].ctypes.data_as(_ip), float(vf.smoothbot), float(vf.dzsmall))
+        return v, keep
+
+    def update_dz(self, vf, linearFS=0):
+        """UpdateDZ (option 0): returns (ctop, etop, dzz, ctopold, etopold, dzzold)."""
+        g = self.grid
+        v, keep = self._vgrid(vf)
+        ctop = np.array(vf.ctop, dtype=np.int32, copy=True)
+        etop = np.array(vf.etop, dtype=np.int32, copy=True)
+        dzz = np.array(vf.dzz, dtype=np.float64, copy=True)
+        ctopold = np.full(g.Nc, -7, dtype=np.int32)
+        etopold = np.full(max(g.Ne, 1), -7, dtype=np.int32)
+        dzzold = np.full(g.n3, -7.0)
+        h = np.ascontiguousarray(vf.h, dtype=np.float64)
+        rc = self.lib.sgpu_update_dz(self.h, C.byref(v), h.ctypes.data_as(_dp), int(linearFS), ctop.ctypes.data_as(_ip),
+                                     etop.ctypes.data_as(_ip), _vp(jagged(dzz, self.coff)), ctopold.ctypes.data_as(_ip),
+                                     etopold.ctypes.data_as(_ip), _vp(jagged(dzzold, self.coff)))
+        self._check(rc, "sgpu_update_dz", allow=(OK,))
+        return ctop, etop[:g.Ne], dzz, ctopold, etopold[:g.Ne], dzzold
+
+    def set_flux_height(self, vf, dzz=None, etop=None):
+        """SetFluxHeight: returns (dzf rows of Nkc levels, dzz after the smoothbot adjustments)."""
+        g = self.grid
+        v, keep = self._vgrid(vf)
+        et = np.ascontiguousarray(vf.etop if etop is None else etop, dtype=np.int32)
+        dzz = np.array(vf.dzz if dzz is None else dzz, dtype=np.float64, copy=True)
+        dzf = np.full(int(np.sum(vf.Nkc)), -7.0)
+        h = np.ascontiguousarray(vf.h, dtype=np.float64)
+        uu = np.ascontiguousarray(vf.u, dtype=np.float64)
+        rc = self.lib.sgpu_set_flux_height(self.h, C.byref(v), et.ctypes.data_as(_ip), h.ctypes.data_as(_dp),
+                                           _vp(jagged(uu, self.eoff)), _vp(jagged(dzz, self.coff)),
+                                           _vp(jagged(dzf, vf.foff)))
+        self._check(rc, "sgpu_set_flux_height", allow=(OK,))
+        return dzf, dzz
 
     # ---- free surface ----
     def cgsolve(self, prob, props: SolverProps):

@@ -66,6 +66,10 @@ struct sgpu_context {
   int *d_nfaces = nullptr, *d_normal = nullptr, *d_grad = nullptr, *d_cedge = nullptr, *d_woff = nullptr,
       *d_etop = nullptr;
   double *d_u = nullptr, *d_ut2 = nullptr, *d_w = nullptr, *d_wt2 = nullptr, *d_qtot = nullptr;
+  // vertical-grid refresh buffers (UpdateDZ / SetFluxHeight)
+  bool vgrid_ready = false;
+  int *d_ctopold = nullptr, *d_etopold = nullptr;
+  double *d_dz = nullptr, *d_dv = nullptr, *d_dzbot = nullptr, *d_hv = nullptr, *d_dzzold = nullptr;
 
   // free-surface buffers
   bool h_ready = false;
@@ -1022,6 +1026,177 @@ int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, cons
   scatter_wrows(ctx, s_w, w, ctx->ncomp);
   if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return rc;
+}
+
+
+
+// ---------------------------------------------------------------------------
+// the vertical grid of the step: UpdateDZ (option 0) and SetFluxHeight
+// ---------------------------------------------------------------------------
+static int alloc_vgrid(sgpu_context* ctx) {
+  if (ctx->vgrid_ready) return SGPU_OK;
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_ctopold, ctx->Nc))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_etopold, (size_t)ctx->Ne + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_dz, (size_t)ctx->Nkmax + 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_dv, ctx->Nc))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_dzbot, ctx->Nc))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_hv, ctx->Nc))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_dzzold, ctx->n3 + 1))) return rc;
+  ctx->vgrid_ready = true;
+  return SGPU_OK;
+}
+
+static VGridArgs vgrid_args(sgpu_context* ctx, const sgpu_vgrid* v, int linearFS) {
+  VGridArgs a{};
+  a.Nc = ctx->Nc;
+  a.Ne = ctx->Ne;
+  a.Nkmax = ctx->Nkmax;
+  a.n3 = (int)ctx->n3;
+  a.linearFS = linearFS;
+  a.smoothbot = v->smoothbot;
+  a.dzsmall = v->dzsmall;
+  a.dcoff = ctx->d_dcoff;
+  a.nk = ctx->d_nk;
+  a.nke = ctx->d_nke;
+  a.eoff = ctx->d_eoff;
+  a.grad = ctx->d_grad;
+  a.dz = ctx->d_dz;
+  a.dv = ctx->d_dv;
+  a.dzbot = ctx->d_dzbot;
+  a.h = ctx->d_hv;
+  a.u = ctx->d_u;
+  a.ctop = ctx->d_ctop;
+  a.etop = ctx->d_etop;
+  a.ctopold = ctx->d_ctopold;
+  a.etopold = ctx->d_etopold;
+  a.dzz = ctx->d_dzz;
+  a.dzzold = ctx->d_dzzold;
+  a.dzf = ctx->d_dzf;
+  return a;
+}
+
+// the per-cell (device order) and per-level uploads shared by both calls
+static int upload_vgrid_common(sgpu_context* ctx, const sgpu_vgrid* v, const double* h, double* s_dv, double* s_dzbot,
+                               double* s_h) {
+  for (int j = 0; j < ctx->Nc; ++j) {
+    const int i = ctx->dev2cell[j];
+    s_dv[j] = v->dv[i];
+    s_dzbot[j] = v->dzbot ? v->dzbot[i] : 0.0;
+    s_h[j] = h[i];
+  }
+  CK(cudaMemcpyAsync(ctx->d_dz, v->dz, sizeof(double) * ctx->Nkmax, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dv, s_dv, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzbot, s_dzbot, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_hv, s_h, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  return SGPU_OK;
+}
+
+static void scatter_cells_all(sgpu_context* ctx, const double* src, double* const* rows) {
+  host_parallel(ctx->Nc, [&](long long b, long long e) {
+    for (long long j = b; j < e; ++j) {
+      const int i = ctx->dev2cell[j];
+      std::memcpy(rows[i], src + ctx->dcoff[j], sizeof(double) * ctx->Nk[i]);
+    }
+  });
+}
+
+int sgpu_update_dz(sgpu_context* ctx, const sgpu_vgrid* v, const double* h, int linearFS, int* ctop, int* etop,
+                   double* const* dzz, int* ctopold, int* etopold, double* const* dzzold) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!v || !v->dz || !v->dv || !h || !ctop || !etop || !dzz || !ctopold || !etopold || !dzzold)
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  if (linearFS) return SGPU_OK;  // UpdateDZ returns at once for a linearised free surface (822-824)
+  int rc;
+  if ((rc = check_ctop(ctx, ctop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx)) || (rc = alloc_vgrid(ctx))) return rc;
+  const size_t n3 = ctx->n3, Nc = ctx->Nc, Ne = ctx->Ne, ni = (Nc + Ne + 1) / 2 + 1;
+  if ((rc = ensure_pinned(ctx, 2 * ni + 2 * n3 + 3 * Nc + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  int* s_etop = s_ctop + Nc;
+  double* s_dzz = ctx->pin + ni;
+  double* s_old = s_dzz + n3;
+  double* s_dv = s_old + n3;
+  double* s_dzbot = s_dv + Nc;
+  double* s_h = s_dzbot + Nc;
+  for (size_t j = 0; j < Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  std::memcpy(s_etop, etop, sizeof(int) * Ne);
+  gather_cells(ctx, (const double* const*)dzz, s_dzz);
+  if ((rc = upload_vgrid_common(ctx, v, h, s_dv, s_dzbot, s_h))) return rc;
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  VGridArgs a = vgrid_args(ctx, v, linearFS);
+  CK(launch_update_dz(a, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* o_ctop = (int*)(ctx->pin);
+  int* o_etop = o_ctop + Nc;
+  CK(cudaMemcpyAsync(o_ctop, ctx->d_ctop, sizeof(int) * Nc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(o_etop, ctx->d_etop, sizeof(int) * Ne, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_dzz, ctx->d_dzz, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_old, ctx->d_dzzold, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<int> old_c(Nc), old_e(Ne + 1);
+  CK(cudaMemcpyAsync(old_c.data(), ctx->d_ctopold, sizeof(int) * Nc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(old_e.data(), ctx->d_etopold, sizeof(int) * Ne, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t j = 0; j < Nc; ++j) {
+    const int i = ctx->dev2cell[j];
+    ctop[i] = o_ctop[j];
+    ctopold[i] = old_c[j];
+  }
+  std::memcpy(etop, o_etop, sizeof(int) * Ne);
+  std::memcpy(etopold, old_e.data(), sizeof(int) * Ne);
+  scatter_cells_all(ctx, s_dzz, dzz);
+  scatter_cells_all(ctx, s_old, dzzold);
+  ctx->q_uploaded = false;
+  return SGPU_OK;
+}
+
+int sgpu_set_flux_height(sgpu_context* ctx, const sgpu_vgrid* v, const int* etop, const double* h,
+                         const double* const* u, double* const* dzz, double* const* dzf) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!v || !v->dz || !v->dv || !v->Nkc || !etop || !h || !u || !dzz || !dzf) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (v->smoothbot != 0 && !v->dzbot) return fail(ctx, SGPU_BAD_ARG, "dzbot is needed when smoothbot != 0");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  for (int e = 0; e < ctx->Ne; ++e)
+    if (v->Nkc[e] < ctx->Nke[e]) return fail(ctx, SGPU_BAD_ARG, "Nkc[%d]=%d below Nke", e, v->Nkc[e]);
+  int rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx)) || (rc = alloc_vgrid(ctx))) return rc;
+  const size_t n3 = ctx->n3, Nc = ctx->Nc, Ne = ctx->Ne, ne3 = ctx->ne3, ni = (Ne + 1) / 2 + 1;
+  if ((rc = ensure_pinned(ctx, ni + n3 + 2 * ne3 + 3 * Nc + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_etop = (int*)ctx->pin;
+  double* s_dzz = ctx->pin + ni;
+  double* s_u = s_dzz + n3;
+  double* s_dzf = s_u + ne3;
+  double* s_dv = s_dzf + ne3;
+  double* s_dzbot = s_dv + Nc;
+  double* s_h = s_dzbot + Nc;
+  std::memcpy(s_etop, etop, sizeof(int) * Ne);
+  gather_cells(ctx, (const double* const*)dzz, s_dzz);
+  gather_edges(ctx, u, s_u);
+  if ((rc = upload_vgrid_common(ctx, v, h, s_dv, s_dzbot, s_h))) return rc;
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
+  VGridArgs a = vgrid_args(ctx, v, 0);
+  CK(launch_set_flux_height(a, ctx->stream));
+  CK(cudaMemcpyAsync(s_dzf, ctx->d_dzf, sizeof(double) * ne3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_dzz, ctx->d_dzz, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  host_parallel(ctx->Ne, [&](long long b, long long e) {
+    for (long long k = b; k < e; ++k) {
+      std::memcpy(dzf[k], s_dzf + ctx->eoff[k], sizeof(double) * ctx->Nke[k]);
+      for (int l = ctx->Nke[k]; l < v->Nkc[k]; ++l) dzf[k][l] = 0;  // rows beyond Nke (4380-4383)
+    }
+  });
+  if (v->smoothbot != 0) scatter_cells_all(ctx, s_dzz, dzz);
+  ctx->q_uploaded = false;
+  return SGPU_OK;
 }
 
 }  // extern "C"

@@ -43,6 +43,32 @@ struct StepArgs {
   double* q_out;        // [n3]
 };
 
+// UpdateDZ (option 0) and SetFluxHeight: device order as above.
+struct VGridArgs {
+  int Nc, Ne, Nkmax, n3;
+  int linearFS;
+  double smoothbot, dzsmall;
+  const int* dcoff;     // [Nc+1]
+  const int* nk;        // [Nc]
+  const int* nke;       // [Ne]
+  const int* eoff;      // [Ne+1]
+  const int* grad;      // [2*Ne] device columns (-1 none)
+  const double* dz;     // [Nkmax]
+  const double* dv;     // [Nc]
+  const double* dzbot;  // [Nc]
+  const double* h;      // [Nc]
+  const double* u;      // [ne3]
+  int* ctop;            // [Nc] in/out
+  int* etop;            // [Ne] in/out
+  int* ctopold;         // [Nc] out
+  int* etopold;         // [Ne] out
+  double* dzz;          // [n3] in/out
+  double* dzzold;       // [n3] out
+  double* dzf;          // [ne3] out (Nke levels per edge)
+};
+
+cudaError_t launch_update_dz(const VGridArgs& a, cudaStream_t st);
+cudaError_t launch_set_flux_height(const VGridArgs& a, cudaStream_t st);
 cudaError_t launch_qsource(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_corrector(const StepArgs& a, cudaStream_t st);
 

@@ -18,7 +18,7 @@ from suntans_gb300 import gridgen as gg
 from suntans_gb300.capi import Context, OK
 from suntans_gb300.grid import QProblem
 from tests._cases import grid_cases, q_props
-from tests._golden import fixture_names, load, props_for, step_fields
+from tests._golden import fixture_names, load, props_for, step_fields, vgrid_fields
 
 pytestmark = pytest.mark.gpu
 
@@ -78,3 +78,37 @@ def test_pressure_step_matches_oracle_chain(gpu_lib, oracle, gname, qprecond):
     for a, b, a0 in ((u, u_ref, st.u), (w, w_ref, st.w), (q, q_ref, st.q)):
         scale = max(np.abs(b - a0).max(), 1e-300)
         assert np.abs(a - b).max() <= 1e-8 * scale
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_vertical_grid_functions_match_golden_bitwise(gpu_lib, name):
+    """UpdateDZ (option 0) and SetFluxHeight on the device: the reference's bits."""
+    g, qp, hp, props, d = load(name)
+    st = step_fields(g, d)
+    vf = vgrid_fields(g, d)
+    ctx = Context(g)
+    ctx.step_grid(st)
+    for k, val in zip(("udz_ctop", "udz_etop", "udz_dzz", "udz_ctopold", "udz_etopold", "udz_dzzold"),
+                      ctx.update_dz(vf)):
+        assert np.array_equal(val, d[k]), k
+    for sb in (0.0, 0.3):
+        vf.smoothbot = sb
+        dzf, dzz = ctx.set_flux_height(vf)
+        tag = "sfh%d" % int(round(10 * sb))
+        assert np.array_equal(dzf, d[tag + "_dzf"]) and np.array_equal(dzz, d[tag + "_dzz"])
+    ctx.close()
+
+
+@pytest.mark.parametrize("gname", [n for n, _ in grid_cases()])
+def test_vertical_grid_functions_match_oracle_bitwise(gpu_lib, oracle, gname):
+    g = dict(grid_cases())[gname]()
+    st = gg.make_step_fields(g, seed=45)
+    ctx = Context(g)
+    ctx.step_grid(st)
+    for sb in (0.0, 0.25):
+        vf = gg.make_vgrid_fields(g, seed=46, smoothbot=sb)
+        for a, b in zip(ctx.update_dz(vf), oracle.update_dz(vf)):
+            assert np.array_equal(a, b)
+        for a, b in zip(ctx.set_flux_height(vf), oracle.set_flux_height(vf)):
+            assert np.array_equal(a, b)
+    ctx.close()
