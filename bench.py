@@ -674,6 +674,14 @@ def bench_step(args):
         qc2, s2 = ctx.cgsolveq(QProblem(grid=g, D=D, src=src, q=st.qc, c=st.c), props)
         ctx.corrector(st, qc2, D, props)
         sep.append(time.perf_counter() - t0)
+    # the vertical-grid refresh of the step (UpdateDZ, SetFluxHeight) through the drop-in calls
+    vf = gg.make_vgrid_fields(g, seed=18)
+    vg = []
+    for _ in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        ctx.update_dz(vf)
+        ctx.set_flux_height(vf)
+        vg.append(time.perf_counter() - t0)
     clocks = sampler.stop()
     ctx.close()
     N = g.n_q()
@@ -687,6 +695,7 @@ def bench_step(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid, velocities and pressure)",
             "config": {**desc, "workload": desc["workload"] + "; pressure step", "iters_q": it},
             "separate_calls_ms": t_s * 1e3, "fused_speedup_vs_separate": t_s / t_f,
+            "vertical_grid_refresh_ms": float(np.median(vg)) * 1e3,
             "e2e": {"value": N * it / t_f, "unit": "unknown-iters/s",
                     "h2d_bytes_per_step": 8 * (4 * n3 + 3 * ne3 + 2 * nw3) + 4 * (g.Nc + g.Ne),
                     "d2h_bytes_per_step": 8 * (2 * n3 + ne3 + nw3)},
@@ -698,6 +707,10 @@ def bench_step(args):
         src, D = o.compute_qsource(st, props)
         o.corrector(st, qp.q, D, props)
         t_qc = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o.update_dz(vf)
+        o.set_flux_height(vf)
+        line["vertical_grid_refresh_cpu_ms"] = (time.perf_counter() - t0) * 1e3
         cb = cpu_baseline(g, qp, None, props, args.cpu_seconds)
         cb["sample"] += f"; ComputeQSource + Corrector on the full grid took {t_qc:.2f} s more per step"
         line["cpu_baseline"] = cb
