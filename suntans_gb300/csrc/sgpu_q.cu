@@ -504,6 +504,7 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
             s_tri.r[sl] = ru;
             s_tri.w[sl] = a.tw[u];
             s_tri.ib[sl] = a.tib[u];
+            s_tri.out[sl] = 0.0;  // dry levels (k < ctop) are not solved and stay 0
           }
           s_tri.cf[sl] = a.coef[u];
         }
