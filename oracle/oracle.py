@@ -277,5 +277,43 @@ class Oracle:
         return dzf, dzz
 
 
+    # ---- the reference's grid reader and field writers (ref library only) ----
+    def read_grid(self, datadir: str) -> dict:
+        """ReadGrid (main/gridio.c:54-187) on a folder holding suntans.dat and
+        the grid files; returns the gridT arrays by name."""
+        if self.which != "ref":
+            raise RuntimeError("read_grid needs the reference library")
+        sizes = np.zeros(6, dtype=np.int32)
+        self.lib.ref_read_grid(datadir.encode(), _ptr(sizes, _ip))
+        Nc, Ne, Np, mf, Nkmax, nneigh = (int(x) for x in sizes)
+        out = {"Nc": Nc, "Ne": Ne, "Np": Np, "maxfaces": mf, "Nkmax": Nkmax, "Nneighs": nneigh}
+        self.lib.ref_grid_ints.restype = C.c_long
+        self.lib.ref_grid_dbls.restype = C.c_long
+        cap = max(16, 8 * (Nc * mf + 2 * Ne + 8 * Np + Nkmax + 16))
+        for name in ("nfaces", "Nk", "mnptr", "cellp", "face", "neigh", "normal", "cells", "Nke", "Nkc",
+                     "mark", "edge_id", "eptr", "edgep", "grad", "gradf", "celldist", "edgedist",
+                     "localtoglobalpoints", "numppneighs", "numpeneighs", "numpcneighs", "Nkp", "edges",
+                     "ppneighs", "peneighs", "pcneighs"):
+            buf = np.zeros(cap, dtype=np.int32)
+            n = self.lib.ref_grid_ints(name.encode(), _ptr(buf, _ip))
+            out[name] = buf[:n].copy()
+        for name in ("xv", "yv", "Ac", "dv", "def", "df", "dg", "n1", "n2", "xe", "ye", "xp", "yp", "dz",
+                     "Actotal"):
+            buf = np.zeros(cap, dtype=np.float64)
+            n = self.lib.ref_grid_dbls(name.encode(), _ptr(buf, _dp))
+            out[name] = buf[:n].copy()
+        return out
+
+    def write_2d(self, path: str, x) -> None:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self.lib.ref_write_2d(path.encode(), C.c_int(x.size), _ptr(x, _dp))
+
+    def write_3d(self, path: str, Nk, Nkmax: int, flat, extra: int = 0) -> None:
+        Nk = np.ascontiguousarray(Nk, dtype=np.int32)
+        flat = np.ascontiguousarray(flat, dtype=np.float64)
+        self.lib.ref_write_3d(path.encode(), C.c_int(Nk.size), C.c_int(Nkmax), _ptr(Nk, _ip), _ptr(flat, _dp),
+                              C.c_int(extra))
+
+
 def available(which: str) -> bool:
     return os.path.exists(PORT_SO if which == "port" else REF_SO)

@@ -359,3 +359,121 @@ void ref_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v
   SetFluxHeight(&H.grid, &H.phys, &H.prop);
   harness_free(&H);
 }
+
+/* ---- formats: the reference's own run-time grid reader and field writers ----
+ * ref_read_grid points DATADIR / DATAFILE at a folder holding a suntans.dat and
+ * the grid files, and calls ReadGrid (main/gridio.c:54-187) for processor 0 of
+ * 1; ref_grid_ints / ref_grid_dbls copy one named array of that gridT out.
+ * Per-face arrays are copied whole (maxfaces per cell; slots past nfaces are
+ * whatever ReadGrid left there).  Jagged nodal lists are copied flat. */
+static gridT *g_rg;
+
+int ref_read_grid(const char *dir, int *sizes) {
+  snprintf(DATADIR, BUFFERLENGTH, "%s", dir);
+  snprintf(DATAFILE, BUFFERLENGTH, "%s/suntans.dat", dir);
+  VERBOSE = 0;
+  g_rg = NULL;
+  ReadGrid(&g_rg, 0, 1, 0);
+  sizes[0] = g_rg->Nc;
+  sizes[1] = g_rg->Ne;
+  sizes[2] = g_rg->Np;
+  sizes[3] = g_rg->maxfaces;
+  sizes[4] = g_rg->Nkmax;
+  sizes[5] = g_rg->Nneighs;
+  return 0;
+}
+
+static long rg_flat_int(int **rows, const int *count, int n, int *out) {
+  long p = 0;
+  int i, k;
+  for (i = 0; i < n; i++)
+    for (k = 0; k < count[i]; k++) out[p++] = rows[i][k];
+  return p;
+}
+
+long ref_grid_ints(const char *name, int *out) {
+  gridT *G = g_rg;
+  int n, Nc = G->Nc, Ne = G->Ne, Np = G->Np, mf = G->maxfaces;
+#define RG_COPY(field, count)                                  \
+  if (!strcmp(name, #field)) {                                 \
+    memcpy(out, G->field, sizeof(int) * (size_t)(count));      \
+    return (count);                                            \
+  }
+  RG_COPY(nfaces, Nc) RG_COPY(Nk, Nc) RG_COPY(mnptr, Nc) RG_COPY(cellp, Nc)
+  RG_COPY(face, Nc * mf) RG_COPY(neigh, Nc * mf) RG_COPY(normal, Nc * mf) RG_COPY(cells, Nc * mf)
+  RG_COPY(Nke, Ne) RG_COPY(Nkc, Ne) RG_COPY(mark, Ne) RG_COPY(edge_id, Ne) RG_COPY(eptr, Ne)
+  RG_COPY(edgep, Ne) RG_COPY(grad, 2 * Ne) RG_COPY(gradf, 2 * Ne)
+  RG_COPY(celldist, MAXBCTYPES - 1) RG_COPY(edgedist, MAXMARKS - 1)
+  RG_COPY(localtoglobalpoints, Np) RG_COPY(numppneighs, Np) RG_COPY(numpeneighs, Np)
+  RG_COPY(numpcneighs, Np) RG_COPY(Nkp, Np)
+#undef RG_COPY
+  if (!strcmp(name, "edges")) {
+    for (n = 0; n < Ne; n++) {
+      out[2 * n] = G->edges[NUMEDGECOLUMNS * n];
+      out[2 * n + 1] = G->edges[NUMEDGECOLUMNS * n + 1];
+    }
+    return 2 * Ne;
+  }
+  if (!strcmp(name, "ppneighs")) return rg_flat_int(G->ppneighs, G->numppneighs, Np, out);
+  if (!strcmp(name, "peneighs")) return rg_flat_int(G->peneighs, G->numpeneighs, Np, out);
+  if (!strcmp(name, "pcneighs")) return rg_flat_int(G->pcneighs, G->numpcneighs, Np, out);
+  return -1;
+}
+
+long ref_grid_dbls(const char *name, double *out) {
+  gridT *G = g_rg;
+  int i, k, Nc = G->Nc, Ne = G->Ne, Np = G->Np, mf = G->maxfaces;
+  long p = 0;
+#define RG_COPY(field, count)                                  \
+  if (!strcmp(name, #field)) {                                 \
+    memcpy(out, G->field, sizeof(double) * (size_t)(count));   \
+    return (count);                                            \
+  }
+  RG_COPY(xv, Nc) RG_COPY(yv, Nc) RG_COPY(Ac, Nc) RG_COPY(dv, Nc) RG_COPY(def, Nc * mf)
+  RG_COPY(df, Ne) RG_COPY(dg, Ne) RG_COPY(n1, Ne) RG_COPY(n2, Ne) RG_COPY(xe, Ne) RG_COPY(ye, Ne)
+  RG_COPY(xp, Np) RG_COPY(yp, Np) RG_COPY(dz, G->Nkmax)
+#undef RG_COPY
+  if (!strcmp(name, "Actotal")) {
+    for (i = 0; i < Np; i++)
+      for (k = 0; k < G->Nkp[i]; k++) out[p++] = G->Actotal[i][k];
+    return p;
+  }
+  return -1;
+}
+
+/* Write2DData / Write3DData (main/physio.c:29-105) without merging, on a gridT
+ * that holds only what they read (Nc, Nkmax, Nk).  Rows of the 3-D field hold
+ * Nk[i] + extra values laid end to end in flat. */
+int ref_write_2d(const char *path, int Nc, const double *x) {
+  gridT G;
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  memset(&G, 0, sizeof(G));
+  G.Nc = Nc;
+  Write2DData((REAL *)x, 0, f, "", &G, 1, 0, 0);
+  fclose(f);
+  return 0;
+}
+
+int ref_write_3d(const char *path, int Nc, int Nkmax, const int *Nk, const double *flat, int extra) {
+  gridT G;
+  long p = 0;
+  int i;
+  REAL **rows = (REAL **)malloc(sizeof(REAL *) * (Nc > 0 ? Nc : 1));
+  REAL *tmp = (REAL *)malloc(sizeof(REAL) * (Nc > 0 ? Nc : 1));
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  for (i = 0; i < Nc; i++) {
+    rows[i] = (REAL *)(flat + p);
+    p += Nk[i] + extra;
+  }
+  memset(&G, 0, sizeof(G));
+  G.Nc = Nc;
+  G.Nkmax = Nkmax;
+  G.Nk = (int *)Nk;
+  Write3DData(rows, tmp, 0, f, "", &G, 1, 0, 0);
+  fclose(f);
+  free(rows);
+  free(tmp);
+  return 0;
+}

@@ -47,6 +47,12 @@ class SunGrid:
     yv: Optional[np.ndarray] = None
     dz: Optional[np.ndarray] = None       # [Nkmax] layer thicknesses (gridT.dz)
     dv: Optional[np.ndarray] = None       # [Nc] depth (gridT.dv)
+    # plan-view geometry for the grid files (gridT.xp/yp/cells/edges/mark)
+    xp: Optional[np.ndarray] = None       # [Np] node coordinates
+    yp: Optional[np.ndarray] = None
+    cnodes: Optional[np.ndarray] = None   # [Nc*maxfaces] node ids of each cell, -1 pad
+    enodes: Optional[np.ndarray] = None   # [2*Ne] node ids of each edge
+    mark: Optional[np.ndarray] = None     # [Ne] 0 interior, 1 closed, 3 open (type-3) boundary
     name: str = "grid"
 
     def __post_init__(self):

@@ -207,6 +207,9 @@ def _assemble(points, cells, nfaces, maxfaces, depth_fn, Nkmax, rstretch, stairs
         xmin = points[:, 0].min()
         on_left = (np.abs(points[e0, 0] - xmin) < 1e-9) & (np.abs(points[e1, 0] - xmin) < 1e-9) & ~interior
         celltype[g0[on_left]] = 1
+    mark = np.where(interior, 0, 1).astype(I32)
+    if open_x0:
+        mark[on_left] = 3
     comp = np.nonzero(celltype == 0)[0]
     bdy = np.nonzero(celltype == 1)[0]
     cellp = np.concatenate([comp, bdy]).astype(I32)
@@ -214,7 +217,10 @@ def _assemble(points, cells, nfaces, maxfaces, depth_fn, Nkmax, rstretch, stairs
 
     g = SunGrid(Nc=Nc, Ne=Ne, maxfaces=maxfaces, Nkmax=Nkmax, nfaces=nfaces, neigh=neigh, face=face,
                 Nk=Nk, Nke=Nke, ctop=ctop, cellp=cellp, celldist=celldist, Ac=Ac, df=df, dg=dg,
-                dzz=dzz, dzf=dzf, normal=normal, grad=grad.ravel(), xv=xv, yv=yv, dz=dz, dv=depth, name=name)
+                dzz=dzz, dzf=dzf, normal=normal, grad=grad.ravel(), xv=xv, yv=yv, dz=dz, dv=depth,
+                xp=np.ascontiguousarray(points[:, 0], dtype=F64), yp=np.ascontiguousarray(points[:, 1], dtype=F64),
+                cnodes=np.where(np.arange(maxfaces)[None, :] < nfaces[:, None], cells, -1).astype(I32).ravel(),
+                enodes=enodes.astype(I32).ravel(), mark=mark, name=name)
     return g
 
 
