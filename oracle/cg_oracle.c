@@ -652,3 +652,350 @@ void sgo_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v
   free(foff);
   layout_free(L);
 }
+
+/* ------------------------------------------------------------------------
+ * UPredictor, main/phys.c:2579-3077.
+ * ------------------------------------------------------------------------ */
+#define UE(a, j, k) (a)[L->eoff[(j)] + (k)]
+
+/* The scratch columns of the vertical solve.  The reference keeps them in
+   physT (a, b, c, d, ap, am, bp, bm, each Nkmax+1 long) across edges; they are
+   kept across edges here too, starting from zero, because the single-layer
+   no-slip branch reads c[Nke] (2862-2871), which the edge itself never set. */
+typedef struct {
+  double *a, *b, *c, *d, *e1, *a0, *b0, *c0;
+} ucols_t;
+
+static void ucols_make(ucols_t *S, int n) {
+  S->a = (double *)calloc(n, sizeof(double));
+  S->b = (double *)calloc(n, sizeof(double));
+  S->c = (double *)calloc(n, sizeof(double));
+  S->d = (double *)calloc(n, sizeof(double));
+  S->e1 = (double *)calloc(n, sizeof(double));
+  S->a0 = (double *)calloc(n, sizeof(double));
+  S->b0 = (double *)calloc(n, sizeof(double));
+  S->c0 = (double *)calloc(n, sizeof(double));
+}
+static void ucols_free(ucols_t *S) {
+  free(S->a); free(S->b); free(S->c); free(S->d); free(S->e1); free(S->a0); free(S->b0); free(S->c0);
+}
+
+/* One computational edge of the vertical solve (2656-2945). */
+static void upred_edge(const sgo_grid *g, const layout_t *L, const sgo_ext *x, const sgo_upred *up,
+                       const sgo_prop *p, long *woff, ucols_t *S, int j, double *utmp, double *E, double *D) {
+  const double dt = p->dt, theta = 1, alpha = 1;   /* drag fully implicit (2637-2646) */
+  double *a = S->a, *b = S->b, *c = S->c, *d = S->d, *e1 = S->e1, *a0 = S->a0, *b0 = S->b0, *c0 = S->c0;
+  int nc1 = x->grad[2 * j], nc2 = x->grad[2 * j + 1], et = x->etop[j], nk = g->Nke[j], k, n0, n1;
+  const double *u = up->u;
+  if (nc1 == -1) nc1 = nc2;
+  if (nc2 == -1) nc2 = nc1;
+#define Z1(k) DZZ(nc1, k)
+#define Z2(k) DZZ(nc2, k)
+#define UU(k) UE(u, j, k)
+#define UT(k) UE(utmp, j, k)
+  UT(et) += 2.0 * dt * up->tau_T[j] / (Z1(et) + Z2(et));                                 /* 2662-2663 */
+  if (Z1(et) == 0 && Z2(et) == 0) return;                                                /* 2667 */
+  for (k = et; k < nk; k++) a[k] = b[k] = c[k] = d[k] = 0;
+  for (k = et + 1; k < nk; k++)                                                         /* 2679-2683 */
+    c[k] = 0.25 * (X3(up->nu_tv, nc1, k - 1) + X3(up->nu_tv, nc2, k - 1) + X3(up->nu_tv, nc1, k) +
+                   X3(up->nu_tv, nc2, k) +
+                   up->laxWendroff_Vertical * (X3(up->nu_lax, nc1, k - 1) + X3(up->nu_lax, nc2, k - 1) +
+                                               X3(up->nu_lax, nc1, k) + X3(up->nu_lax, nc2, k)));
+  for (k = et + 1; k < nk; k++)                                                         /* 2687-2690 */
+    a[k] = 2.0 * (up->nu + c[k]) / (0.25 * (Z1(k) + Z2(k)) * (Z1(k - 1) + Z2(k - 1) + Z1(k) + Z2(k)));
+  for (k = et; k < nk - 1; k++)                                                         /* 2692-2696 */
+    b[k] = 2.0 * (up->nu + c[k + 1]) / (0.25 * (Z1(k) + Z2(k)) * (Z1(k) + Z2(k) + Z1(k + 1) + Z2(k + 1)));
+  /* k is left at et when the column has one layer, as the reference's is */
+  if (up->nonlinear && up->thetaM >= 0 && nk - et > 1) {                                /* 2702-2723 */
+    int kk;
+    if (g->ctop[nc1] > g->ctop[nc2]) { n0 = nc2; n1 = nc1; } else { n0 = nc1; n1 = nc2; }
+    for (kk = 0; kk < g->ctop[n1]; kk++) d[kk] = 0;
+    for (kk = g->ctop[n1]; kk < nk; kk++) d[kk] = 0.5 * (up->w[woff[n0] + kk] + up->w[woff[n1] + kk]);
+    d[nk] = 0;
+    for (kk = et; kk < nk; kk++) {
+      a0[kk] = (alpha * 0.5 * (d[kk] - fabs(d[kk])) + 0.5 * (1 - alpha) * d[kk]) / (0.5 * (Z1(kk) + Z2(kk)));
+      b0[kk] = (alpha * 0.5 * (d[kk] + fabs(d[kk]) - d[kk + 1] + fabs(d[kk + 1])) +
+                0.5 * (1 - alpha) * (d[kk] - d[kk + 1])) / (0.5 * (Z1(kk) + Z2(kk)));
+      c0[kk] = -(alpha * 0.5 * (d[kk + 1] + fabs(d[kk + 1])) + 0.5 * (1 - alpha) * d[kk + 1]) /
+               (0.5 * (Z1(kk) + Z2(kk)));
+    }
+  }
+  if (nk - et > 1) {                                                                     /* 2726-2771 */
+    int kk;
+    for (kk = et + 1; kk < nk - 1; kk++)
+      UT(kk) += dt * (1 - theta) * (a[kk] * UU(kk - 1) - (a[kk] + b[kk]) * UU(kk) + b[kk] * UU(kk + 1));
+    if (up->CdT[j] == -1)
+      UT(et) += dt * (1 - theta) * (a[et] * -UU(et) - (a[et] + b[et]) * UU(et) + b[et] * UU(et + 1));
+    else
+      UT(et) += dt * (1 - theta) *
+                (-(b[et] + 2.0 * up->CdT[j] * fabs(UU(et)) / (Z1(et) + Z2(et))) * UU(et) + b[et] * UU(et + 1));
+    if (up->CdB[j] == -1)
+      UT(nk - 1) += dt * (1 - theta) *
+                    (a[nk - 1] * UU(nk - 2) - (a[nk - 1] + b[nk - 1]) * UU(nk - 1) + b[nk - 1] * -UU(nk - 1));
+    else
+      UT(nk - 1) += dt * (1 - theta) *
+                    (a[nk - 1] * UU(nk - 2) -
+                     (a[nk - 1] + 2.0 * up->CdB[j] * fabs(UU(nk - 1)) / (Z1(nk - 1) + Z2(nk - 1))) * UU(nk - 1));
+  } else {                                                                               /* 2772-2798 */
+    k = et;
+    if (up->CdB[j] == -1)
+      UT(et) -= 2.0 * dt * (1 - theta) *
+                (2.0 * (2.0 * (up->nu + c[k])) * UU(et) / ((Z1(et) + Z2(et)) * (Z1(et) + Z2(et))));
+    else
+      UT(et) -= 2.0 * dt * (1 - theta) * (up->CdB[j]) / (Z1(et) + Z2(et)) * fabs(UU(et)) * UU(et);
+    if (up->CdT[j] == -1)
+      UT(et) -= 2.0 * dt * (1 - theta) *
+                (2.0 * (2.0 * (up->nu + c[k])) * UU(et) / ((Z1(et) + Z2(et)) * (Z1(et) + Z2(et))));
+    else
+      UT(et) -= 2.0 * dt * (1 - theta) * (up->CdT[j]) / (Z1(et) + Z2(et)) * fabs(UU(et)) * UU(et);
+  }
+  if (up->nonlinear && up->thetaM >= 0 && nk - et > 1) {                                /* 2801-2813 */
+    int kk;
+    for (kk = et + 1; kk < nk - 1; kk++)
+      UT(kk) -= p->dt * (1 - up->thetaM) * (a0[kk] * UU(kk - 1) + b0[kk] * UU(kk) + c0[kk] * UU(kk + 1));
+    UT(et) -= p->dt * (1 - up->thetaM) * ((a0[et] + b0[et]) * UU(et) + c0[et] * UU(et + 1));
+    UT(nk - 1) -= p->dt * (1 - up->thetaM) * (a0[nk - 1] * UU(nk - 2) + (b0[nk - 1] + c0[nk - 1]) * UU(nk - 1));
+  }
+  for (k = et; k < nk; k++) {                                                           /* 2822-2825 */
+    e1[k] = 1.0;
+    d[k] = UT(k);
+  }
+  /* k == nk here, as in the reference */
+  if (nk - et > 1) {                                                                     /* 2827-2861 */
+    int kk;
+    c[et] = -theta * dt * b[et];
+    if (up->CdT[j] == -1)
+      b[et] = 1.0 + theta * dt * (a[et] + a[et + 1] + b[et]);
+    else
+      b[et] = 1.0 + theta * dt * (b[et] + 2.0 * up->CdT[j] * fabs(UU(et)) / (Z1(et) + Z2(et)));
+    a[et] = 0;
+    c[nk - 1] = 0;
+    if (up->CdB[j] == -1)
+      b[nk - 1] = 1.0 + theta * dt * (a[nk - 1] + b[nk - 1] + b[nk - 2]);
+    else
+      b[nk - 1] = 1.0 + theta * dt * (a[nk - 1] + 2.0 * up->CdB[j] * fabs(UU(nk - 1)) / (Z1(nk - 1) + Z2(nk - 1)));
+    a[nk - 1] = -theta * dt * a[nk - 1];
+    for (kk = et + 1; kk < nk - 1; kk++) {
+      c[kk] = -theta * dt * b[kk];
+      b[kk] = 1.0 + theta * dt * (a[kk] + b[kk]);
+      a[kk] = -theta * dt * a[kk];
+    }
+  } else {                                                                               /* 2862-2887 */
+    b[et] = 1.0;
+    if (up->CdB[j] == -1)
+      b[et] += 4.0 * theta * dt * 2.0 * (up->nu + c[k]) / ((Z1(et) + Z2(et)) * (Z1(et) + Z2(et)));
+    else
+      b[et] += 2.0 * theta * dt * fabs(UT(et)) / (Z1(et) + Z2(et)) * (up->CdB[j]);
+    if (up->CdT[j] == -1)
+      b[et] += 4.0 * theta * dt * 2.0 * (up->nu + c[k]) / ((Z1(et) + Z2(et)) * (Z1(et) + Z2(et)));
+    else
+      b[et] += 2.0 * theta * dt * fabs(UT(et)) / (Z1(et) + Z2(et)) * (up->CdT[j]);
+  }
+  if (up->nonlinear && up->thetaM >= 0 && nk - et > 1) {                                /* 2890-2904 */
+    int kk;
+    for (kk = et + 1; kk < nk - 1; kk++) {
+      a[kk] += p->dt * up->thetaM * a0[kk];
+      b[kk] += p->dt * up->thetaM * b0[kk];
+      c[kk] += p->dt * up->thetaM * c0[kk];
+    }
+    b[et] += p->dt * up->thetaM * (a0[et] + b0[et]);
+    c[et] += p->dt * up->thetaM * c0[et];
+    a[nk - 1] += p->dt * up->thetaM * a0[nk - 1];
+    b[nk - 1] += p->dt * up->thetaM * (b0[nk - 1] + c0[nk - 1]);
+  }
+  for (k = 0; k < nk; k++) {                                                             /* 2922-2926 */
+    a0[k] = a[k];
+    b0[k] = b[k];
+    c0[k] = c[k];
+  }
+  if (nk - et > 1) {                                                                     /* 2927-2935 */
+    trisolve(a + et, b + et, c + et, d + et, &UT(et), nk - et);
+    trisolve(a0 + et, b0 + et, c0 + et, e1 + et, &UE(E, j, et), nk - et);
+  } else {
+    UT(et) /= b[et];
+    UE(E, j, et) = 1.0 / b[et];
+  }
+  D[j] = 0;                                                                              /* 2941-2943 */
+  for (k = et; k < nk; k++) D[j] += UE(E, j, k) * DZF(j, k);
+#undef Z1
+#undef Z2
+#undef UU
+#undef UT
+}
+
+static long *woff_make(const sgo_grid *g) {
+  long *woff = (long *)malloc(sizeof(long) * (g->Nc + 1));
+  int i;
+  woff[0] = 0;
+  for (i = 0; i < g->Nc; i++) woff[i + 1] = woff[i] + g->Nk[i] + 1;
+  return woff;
+}
+
+static int upred_vertical_impl(const sgo_grid *g, const layout_t *L, const sgo_ext *x, const sgo_upred *up,
+                               const double *h, const sgo_prop *p, double *utmp, double *E, double *D) {
+  ucols_t S;
+  long *woff = woff_make(g);
+  int j, jptr, k, nnan = 0;
+  ucols_make(&S, g->Nkmax + 2);
+  for (j = 0; j < g->Ne; j++) D[j] = 0;                                                  /* 2602-2603 */
+  for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++) {                           /* 2626-2635 */
+    int nc1, nc2;
+    j = x->edgep[jptr];
+    nc1 = x->grad[2 * j];
+    nc2 = x->grad[2 * j + 1];
+    for (k = x->etop[j]; k < g->Nke[j]; k++)
+      UE(utmp, j, k) -= p->grav * (1 - p->theta) * p->dt * (h[nc1] - h[nc2]) / g->dg[j];
+  }
+  for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++)                            /* 2649-2945 */
+    upred_edge(g, L, x, up, p, woff, &S, x->edgep[jptr], utmp, E, D);
+  for (j = 0; j < g->Ne; j++)                                                            /* 2948-2954 */
+    for (k = x->etop[j]; k < g->Nke[j]; k++)
+      if (UE(utmp, j, k) != UE(utmp, j, k)) nnan++;
+  free(woff);
+  ucols_free(&S);
+  return nnan;
+}
+
+int sgo_upredictor_vertical(const sgo_grid *g, const sgo_ext *x, const sgo_upred *up, const double *h,
+                            const sgo_prop *p, double *utmp, double *E, double *D) {
+  layout_t Lv;
+  int n;
+  layout_make(g, &Lv);
+  n = upred_vertical_impl(g, &Lv, x, up, h, p, utmp, E, D);
+  layout_free(&Lv);
+  return n;
+}
+
+/* htmp = Ac h - dt sum_faces sum_k ((1-theta) u + theta utmp) df normal dzf (2964-2977) */
+static void upred_rhs_impl(const sgo_grid *g, const layout_t *L, const sgo_ext *x, const sgo_upred *up,
+                           const double *h, const sgo_prop *p, const double *utmp, double *htmp) {
+  int iptr, i, nf, ne, normal, k;
+  double sum;
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+    i = g->cellp[iptr];
+    sum = 0;
+    for (nf = 0; nf < g->nfaces[i]; nf++) {
+      ne = g->face[i * g->maxfaces + nf];
+      normal = x->normal[i * g->maxfaces + nf];
+      for (k = x->etop[ne]; k < g->Nke[ne]; k++)
+        sum += ((1 - p->theta) * UE(up->u, ne, k) + p->theta * UE(utmp, ne, k)) * g->df[ne] * normal * DZF(ne, k);
+    }
+    htmp[i] = g->Ac[i] * h[i] - p->dt * sum;
+  }
+}
+
+void sgo_upredictor_rhs(const sgo_grid *g, const sgo_ext *x, const sgo_upred *up, const double *h,
+                        const sgo_prop *p, const double *utmp, double *htmp) {
+  layout_t Lv;
+  layout_make(g, &Lv);
+  upred_rhs_impl(g, &Lv, x, up, h, p, utmp, htmp);
+  layout_free(&Lv);
+}
+
+/* The dry-cell clip (2993-3002) and u = U*** - g theta dt E dh/dg on the
+   computational edges (3006-3019). */
+static void upred_velocity_impl(const sgo_grid *g, const layout_t *L, const sgo_ext *x, const sgo_vgrid *v,
+                                const sgo_prop *p, const double *utmp, const double *E, double *h,
+                                unsigned char *active, double *u) {
+  int i, j, jptr, k, nc1, nc2;
+  for (i = 0; i < g->Nc; i++)
+    if (h[i] <= -v->dv[i] + SGO_DRYCELLHEIGHT) {
+      h[i] = -v->dv[i] + SGO_DRYCELLHEIGHT;
+      active[i] = 0;
+    } else {
+      active[i] = 1;
+    }
+  for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++) {
+    j = x->edgep[jptr];
+    nc1 = x->grad[2 * j];
+    nc2 = x->grad[2 * j + 1];
+    for (k = x->etop[j]; k < g->Nke[j]; k++)
+      UE(u, j, k) = UE(utmp, j, k) - p->grav * p->theta * p->dt * UE(E, j, k) * (h[nc1] - h[nc2]) / g->dg[j];
+    if (x->etop[j] == g->Nke[j] - 1 && DZZ(nc1, x->etop[j]) == 0 && DZZ(nc2, x->etop[j]) == 0)
+      UE(u, j, x->etop[j]) = 0;
+  }
+}
+
+void sgo_upredictor_velocity(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_prop *p,
+                             const double *utmp, const double *E, double *h, unsigned char *active, double *u) {
+  layout_t Lv;
+  layout_make(g, &Lv);
+  upred_velocity_impl(g, &Lv, x, v, p, utmp, E, h, active, u);
+  layout_free(&Lv);
+}
+
+/* u = utmp on type-2 edges (3046-3051); on each mark-3 face of a type-3 cell,
+   the flux that closes the cell's continuity at every level (3055-3076).  The
+   reference reads u[face][k] of the cell's other faces for k up to the
+   mark-3 edge's Nke; where another face has fewer levels that read is past
+   its row, and here it counts as 0. */
+static void upred_boundary_impl(const sgo_grid *g, const layout_t *L, const sgo_ext *x, const sgo_ubnd *b,
+                                const double *utmp, double *u) {
+  int j, jptr, k, iptr, i, nf, nf1, ne, f1;
+  double sum;
+  for (jptr = b->edgedist[2]; jptr < b->edgedist[3]; jptr++) {
+    j = b->edgep[jptr];
+    for (k = x->etop[j]; k < g->Nke[j]; k++) UE(u, j, k) = UE(utmp, j, k);
+  }
+  for (iptr = g->celldist[1]; iptr < g->celldist[2]; iptr++) {
+    i = g->cellp[iptr];
+    for (nf = 0; nf < g->nfaces[i]; nf++) {
+      ne = g->face[i * g->maxfaces + nf];
+      if (b->mark[ne] != 3) continue;
+      for (k = x->etop[ne]; k < g->Nke[ne]; k++) {
+        UE(u, ne, k) = 0;
+        sum = 0;
+        for (nf1 = 0; nf1 < g->nfaces[i]; nf1++) {
+          f1 = g->face[i * g->maxfaces + nf1];
+          if (k < g->Nke[f1]) sum += UE(u, f1, k) * g->df[f1] * x->normal[i * g->maxfaces + nf1];
+        }
+        UE(u, ne, k) = -sum / g->df[ne] / x->normal[i * g->maxfaces + nf];
+      }
+    }
+  }
+}
+
+void sgo_upredictor_boundary(const sgo_grid *g, const sgo_ext *x, const sgo_ubnd *b, const double *utmp,
+                             double *u) {
+  layout_t Lv;
+  layout_make(g, &Lv);
+  upred_boundary_impl(g, &Lv, x, b, utmp, u);
+  layout_free(&Lv);
+}
+
+int sgo_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_upred *up,
+                   const sgo_ubnd *b, const sgo_prop *p, double *u, double *h, double *utmp, double *E,
+                   double *D, int *ctop, int *etop, double *dzz, unsigned char *active, sgo_result *res) {
+  layout_t Lv, *L = &Lv;
+  sgo_grid G = *g;
+  sgo_ext X = *x;
+  int i, j, jptr, k, nnan;
+  int *ctopold = (int *)malloc(sizeof(int) * (g->Nc + 1));
+  int *etopold = (int *)malloc(sizeof(int) * (g->Ne + 1));
+  double *dzzold, *htmp = (double *)malloc(sizeof(double) * (g->Nc + 1));
+  layout_make(g, L);
+  dzzold = (double *)malloc(sizeof(double) * (L->n3 + 1));
+  G.ctop = ctop;
+  G.dzz = dzz;
+  X.etop = etop;
+  nnan = upred_vertical_impl(&G, L, &X, up, h, p, utmp, E, D);
+  /* BoundaryVelocities without NetCDF data (boundaries.c:179-270) */
+  for (i = g->celldist[1]; i < g->celldist[2]; i++) h[g->cellp[i]] = 0;
+  sgo_update_dz(&G, &X, v, h, 0, ctop, etop, dzz, ctopold, etopold, dzzold);
+  /* OpenBoundaryFluxes (boundaries.c:41-58) with zero boundary velocities */
+  for (jptr = b->edgedist[2]; jptr < b->edgedist[5]; jptr++) {
+    j = b->edgep[jptr];
+    for (k = etop[j]; k < g->Nke[j]; k++) UE(utmp, j, k) = 0.0 * b->n1[j] + 0.0 * b->n2[j];
+  }
+  upred_rhs_impl(&G, L, &X, up, h, p, utmp, htmp);
+  sgo_cgsolve(&G, D, h, htmp, p, res);
+  upred_velocity_impl(&G, L, &X, v, p, utmp, E, h, active, u);
+  sgo_update_dz(&G, &X, v, h, 0, ctop, etop, dzz, ctopold, etopold, dzzold);
+  upred_boundary_impl(&G, L, &X, b, utmp, u);
+  free(ctopold);
+  free(etopold);
+  free(dzzold);
+  free(htmp);
+  layout_free(L);
+  return nnan;
+}

@@ -89,6 +89,31 @@ typedef struct sgo_vgrid {
  * dzf); w, wtmp2 per cell with Nk[i]+1 levels (offsets the prefix sum of
  * Nk+1); src, q, qc per cell with Nk[i] levels (as dzz). */
 
+/* UPredictor (main/phys.c:2579-3077): the fields it reads beyond the grid. */
+typedef struct sgo_upred {
+  const double *u;      /* [ne3] u at step n, rows of Nke                        */
+  const double *w;      /* [nw3] w at step n, rows of Nk+1 (vertical advection)  */
+  const double *tau_T;  /* [Ne] surface stress                                    */
+  const double *CdT;    /* [Ne] top drag coefficient, -1 = no slip                */
+  const double *CdB;    /* [Ne] bottom drag coefficient, -1 = no slip             */
+  const double *nu_tv;  /* [n3] vertical eddy viscosity at cell centres           */
+  const double *nu_lax; /* [n3] Lax-Wendroff viscosity                            */
+  double nu;            /* propT.nu                                               */
+  double laxWendroff_Vertical;
+  double thetaM;        /* < 0: no implicit vertical momentum advection           */
+  int nonlinear;
+} sgo_upred;
+
+/* The open-boundary part of UpdateDZ's caller: all edges ordered by mark
+   (edgep, edgedist[6], main/grid.c:1666-1679), their marks and normals. */
+typedef struct sgo_ubnd {
+  const int *edgep;
+  const int *edgedist;  /* [6] */
+  const int *mark;      /* [Ne] */
+  const double *n1;     /* [Ne] */
+  const double *n2;     /* [Ne] */
+} sgo_ubnd;
+
 /* ---- the restatement (cg_oracle.c) ---- */
 void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
                   const sgo_prop *p, sgo_result *res);
@@ -122,6 +147,31 @@ void sgo_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
 void sgo_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
                          const double *u, double *dzz, double *dzf);
 
+/* UPredictor in pieces.  _vertical: U*** in utmp (in: the horizontal source),
+   E = A^{-1} 1 and D = dzf^T E on the computational edges (main/phys.c:2604-2945;
+   D is zeroed on every edge, E rows of skipped edges are left alone); returns
+   the number of NaN values in utmp (the reference stops on any, 2948-2954).
+   _rhs: the free-surface right-hand side htmp on computational cells
+   (2964-2977).  _velocity: the dry-cell clip of h and u on the computational
+   edges after the solve (2991-3019).  _boundary: u on type-2 edges and on the
+   mark-3 faces of type-3 cells (3046-3076). */
+int sgo_upredictor_vertical(const sgo_grid *g, const sgo_ext *x, const sgo_upred *up, const double *h,
+                            const sgo_prop *p, double *utmp, double *E, double *D);
+void sgo_upredictor_rhs(const sgo_grid *g, const sgo_ext *x, const sgo_upred *up, const double *h,
+                        const sgo_prop *p, const double *utmp, double *htmp);
+void sgo_upredictor_velocity(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_prop *p,
+                             const double *utmp, const double *E, double *h, unsigned char *active, double *u);
+void sgo_upredictor_boundary(const sgo_grid *g, const sgo_ext *x, const sgo_ubnd *b, const double *utmp,
+                             double *u);
+/* The whole of UPredictor with CGSolve (cgsolver 1), for a model without
+   NetCDF boundary data: BoundaryVelocities sets h = 0 at type-3 cells and
+   calls UpdateDZ, OpenBoundaryFluxes sets utmp = 0*n1 + 0*n2 on edges of marks
+   2-4.  ctop, etop, dzz (rows of Nk) are the state before the call and are
+   updated in place; u, h, utmp, E, D as above; res = CGSolve's. */
+int sgo_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_upred *up,
+                   const sgo_ubnd *b, const sgo_prop *p, double *u, double *h, double *utmp, double *E,
+                   double *D, int *ctop, int *etop, double *dzz, unsigned char *active, sgo_result *res);
+
 /* ---- the reference itself (ref_harness.c, oracle/_ref only) ---- */
 void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
                   const sgo_prop *p, sgo_result *res);
@@ -147,6 +197,10 @@ void ref_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
                    int *ctop, int *etop, double *dzz, int *ctopold, int *etopold, double *dzzold);
 void ref_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
                          const double *u, double *dzz, double *dzf);
+
+int ref_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_upred *up,
+                   const sgo_ubnd *b, const sgo_prop *p, double *u, double *h, double *utmp, double *E,
+                   double *D, int *ctop, int *etop, double *dzz, unsigned char *active, sgo_result *res);
 
 #ifdef __cplusplus
 }

@@ -51,6 +51,16 @@ class SgoVgrid(C.Structure):
                 ("dzsmall", C.c_double)]
 
 
+class SgoUpred(C.Structure):
+    _fields_ = [("u", _dp), ("w", _dp), ("tau_T", _dp), ("CdT", _dp), ("CdB", _dp), ("nu_tv", _dp),
+                ("nu_lax", _dp), ("nu", C.c_double), ("laxWendroff_Vertical", C.c_double),
+                ("thetaM", C.c_double), ("nonlinear", C.c_int)]
+
+
+class SgoUbnd(C.Structure):
+    _fields_ = [("edgep", _ip), ("edgedist", _ip), ("mark", _ip), ("n1", _dp), ("n2", _dp)]
+
+
 class SgoResult(C.Structure):
     _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double)]
 
@@ -276,6 +286,112 @@ class Oracle:
                                     _ptr(dzf, _dp))
         return dzf, dzz
 
+
+    # ---- UPredictor (main/phys.c:2579-3077) ----
+    @staticmethod
+    def _upred(uf):
+        keep = [np.ascontiguousarray(a, dtype=np.float64)
+                for a in (uf.u, uf.w, uf.tau_T, uf.CdT, uf.CdB, uf.nu_tv, uf.nu_lax)]
+        return SgoUpred(*[_ptr(a, _dp) for a in keep], uf.nu, uf.laxWendroff_Vertical, uf.thetaM,
+                        uf.nonlinear), keep
+
+    @staticmethod
+    def _ubnd(uf):
+        ki = [np.ascontiguousarray(a, dtype=np.int32) for a in (uf.bedgep, uf.bedgedist, uf.mark)]
+        kd = [np.ascontiguousarray(a, dtype=np.float64) for a in (uf.n1, uf.n2)]
+        return SgoUbnd(*[_ptr(a, _ip) for a in ki], *[_ptr(a, _dp) for a in kd]), ki + kd
+
+    @staticmethod
+    def _uext(uf, etop):
+        g = uf.grid
+        keep = [np.ascontiguousarray(a, dtype=np.int32) for a in (g.normal, g.grad, uf.edgep, uf.edgedist, etop)]
+        return SgoExt(*[_ptr(x, _ip) for x in keep]), keep
+
+    def upredictor_vertical(self, uf, props, grid=None, etop=None):
+        """U***, E, D on the computational edges; returns (utmp, E, D, NaN count)."""
+        g = uf.grid if grid is None else grid
+        s, keep = self._grid(g)
+        x, kx = self._uext(uf, uf.etop if etop is None else etop)
+        up, ku = self._upred(uf)
+        h = np.ascontiguousarray(uf.h, dtype=np.float64)
+        utmp = np.array(uf.utmp, dtype=np.float64, copy=True)
+        E = np.zeros(max(int(g.Nke.sum()), 1))
+        D = np.full(max(g.Ne, 1), -7.0)
+        pr = self._prop(props)
+        n = self._fn("upredictor_vertical")(C.byref(s), C.byref(x), C.byref(up), _ptr(h, _dp), C.byref(pr),
+                                            _ptr(utmp, _dp), _ptr(E, _dp), _ptr(D, _dp))
+        return utmp, E[:int(g.Nke.sum())], D[:g.Ne], int(n)
+
+    def upredictor_rhs(self, uf, props, utmp, h=None, grid=None, etop=None):
+        """The free-surface right-hand side on computational cells (others left 0)."""
+        g = uf.grid if grid is None else grid
+        s, keep = self._grid(g)
+        x, kx = self._uext(uf, uf.etop if etop is None else etop)
+        up, ku = self._upred(uf)
+        hh = np.ascontiguousarray(uf.h if h is None else h, dtype=np.float64)
+        ut = np.ascontiguousarray(utmp, dtype=np.float64)
+        htmp = np.zeros(g.Nc)
+        pr = self._prop(props)
+        self._fn("upredictor_rhs")(C.byref(s), C.byref(x), C.byref(up), _ptr(hh, _dp), C.byref(pr), _ptr(ut, _dp),
+                                   _ptr(htmp, _dp))
+        return htmp
+
+    def upredictor_velocity(self, uf, vf, props, utmp, E, h, u=None, grid=None, etop=None):
+        """Dry-cell clip and u on the computational edges; returns (h, active, u)."""
+        g = uf.grid if grid is None else grid
+        s, keep = self._grid(g)
+        x, kx = self._uext(uf, uf.etop if etop is None else etop)
+        v, kv = self._vgrid(vf)
+        ut = np.ascontiguousarray(utmp, dtype=np.float64)
+        EE = np.ascontiguousarray(E, dtype=np.float64)
+        hh = np.array(h, dtype=np.float64, copy=True)
+        active = np.full(g.Nc, 7, dtype=np.uint8)
+        uu = np.array(uf.u if u is None else u, dtype=np.float64, copy=True)
+        pr = self._prop(props)
+        self._fn("upredictor_velocity")(C.byref(s), C.byref(x), C.byref(v), C.byref(pr), _ptr(ut, _dp),
+                                        _ptr(EE, _dp), _ptr(hh, _dp),
+                                        active.ctypes.data_as(C.POINTER(C.c_ubyte)), _ptr(uu, _dp))
+        return hh, active, uu
+
+    def upredictor_boundary(self, uf, utmp, u, grid=None, etop=None):
+        """u on type-2 edges and on the mark-3 faces of type-3 cells."""
+        g = uf.grid if grid is None else grid
+        s, keep = self._grid(g)
+        x, kx = self._uext(uf, uf.etop if etop is None else etop)
+        b, kb = self._ubnd(uf)
+        ut = np.ascontiguousarray(utmp, dtype=np.float64)
+        uu = np.array(u, dtype=np.float64, copy=True)
+        self._fn("upredictor_boundary")(C.byref(s), C.byref(x), C.byref(b), _ptr(ut, _dp), _ptr(uu, _dp))
+        return uu
+
+    def upredictor(self, uf, vf, props):
+        """The whole UPredictor with CGSolve, from the grid's ctop / dzz and
+        uf.etop; returns a dict of u, h, utmp, E, D, ctop, etop, dzz, active,
+        niters and the NaN count."""
+        g = uf.grid
+        s, keep = self._grid(g)
+        ctop = np.array(g.ctop, dtype=np.int32, copy=True)
+        etop = np.array(uf.etop, dtype=np.int32, copy=True)
+        dzz = np.array(g.dzz, dtype=np.float64, copy=True)
+        x, kx = self._uext(uf, etop)
+        x.etop = _ptr(etop, _ip)
+        v, kv = self._vgrid(vf)
+        up, ku = self._upred(uf)
+        b, kb = self._ubnd(uf)
+        u = np.array(uf.u, dtype=np.float64, copy=True)
+        h = np.array(uf.h, dtype=np.float64, copy=True)
+        utmp = np.array(uf.utmp, dtype=np.float64, copy=True)
+        E = np.zeros(max(int(g.Nke.sum()), 1))
+        D = np.zeros(max(g.Ne, 1))
+        active = np.full(g.Nc, 7, dtype=np.uint8)
+        res = SgoResult()
+        pr = self._prop(props)
+        n = self._fn("upredictor")(C.byref(s), C.byref(x), C.byref(v), C.byref(up), C.byref(b), C.byref(pr),
+                                   _ptr(u, _dp), _ptr(h, _dp), _ptr(utmp, _dp), _ptr(E, _dp), _ptr(D, _dp),
+                                   _ptr(ctop, _ip), _ptr(etop, _ip), _ptr(dzz, _dp),
+                                   active.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(res))
+        return dict(u=u, h=h, utmp=utmp, E=E[:int(g.Nke.sum())], D=D[:g.Ne], ctop=ctop, etop=etop, dzz=dzz,
+                    active=active, niters=res.niters, nnan=int(n))
 
     # ---- the reference's grid reader and field writers (ref library only) ----
     def read_grid(self, datadir: str) -> dict:

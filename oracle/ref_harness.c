@@ -39,9 +39,9 @@ typedef struct {
   physT phys;
   propT prop;
   long *coff, *eoff;
-  REAL **rows_free[16];
+  REAL **rows_free[64];
   int nrows_free;
-  void *blk_free[32];
+  void *blk_free[96];
   int nblk_free;
 } harness_t;
 
@@ -475,5 +475,79 @@ int ref_write_3d(const char *path, int Nc, int Nkmax, const int *Nk, const doubl
   fclose(f);
   free(rows);
   free(tmp);
+  return 0;
+}
+
+/* The reference's UPredictor (main/phys.c:2579-3077) with cgsolver 1 and no
+ * NetCDF boundary data.  Its scratch columns and physT fields are zeroed
+ * allocations; boundary_u/v/w have one row of Nkmax per edge of marks 2-4. */
+int ref_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_upred *up,
+                   const sgo_ubnd *b, const sgo_prop *p, double *u, double *h, double *utmp, double *E,
+                   double *D, int *ctop, int *etop, double *dzz, unsigned char *active, sgo_result *res) {
+  harness_t H;
+  int nb = b->edgedist[5] - b->edgedist[2], i, *brow;
+  harness_init(&H, g, D, p);
+  harness_ext(&H, g, x);
+  harness_vgrid(&H, v);
+  H.grid.edgep = (int *)b->edgep;
+  H.grid.edgedist = (int *)b->edgedist;
+  H.grid.mark = (int *)b->mark;
+  H.grid.n1 = (REAL *)b->n1;
+  H.grid.n2 = (REAL *)b->n2;
+  H.grid.ctop = ctop;
+  H.grid.etop = etop;
+  H.grid.ctopold = (int *)blk_new(&H, sizeof(int) * g->Nc);
+  H.grid.etopold = (int *)blk_new(&H, sizeof(int) * g->Ne);
+  H.grid.dzz = jag_view(&H, dzz, H.coff, g->Nc);
+  H.grid.dzzold = jag_new(&H, g->Nc, g->Nk, 0);
+  H.phys.a = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.b = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.c = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.d = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.ap = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.am = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.bp = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.bm = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.u = jag_view(&H, u, H.eoff, g->Ne);
+  H.phys.utmp = jag_view(&H, utmp, H.eoff, g->Ne);
+  H.phys.ut = jag_view(&H, E, H.eoff, g->Ne);
+  H.phys.utmp2 = jag_new(&H, g->Ne, g->Nke, 0);
+  H.phys.w = wrow_view(&H, g, up->w);
+  H.phys.wtmp2 = jag_new(&H, g->Nc, g->Nk, 1);
+  H.phys.h = h;
+  H.phys.htmp = (REAL *)blk_new(&H, sizeof(REAL) * g->Nc);
+  H.phys.hcorr = (REAL *)blk_new(&H, sizeof(REAL) * g->Nc);
+  H.phys.active = active;
+  H.phys.s = jag_new(&H, g->Nc, g->Nk, 0);
+  H.phys.uc = jag_new(&H, g->Nc, g->Nk, 0);
+  H.phys.vc = jag_new(&H, g->Nc, g->Nk, 0);
+  H.phys.tau_T = (REAL *)up->tau_T;
+  H.phys.CdT = (REAL *)up->CdT;
+  H.phys.CdB = (REAL *)up->CdB;
+  H.phys.nu_tv = jag_view(&H, up->nu_tv, H.coff, g->Nc);
+  H.phys.nu_lax = jag_view(&H, up->nu_lax, H.coff, g->Nc);
+  brow = (int *)malloc(sizeof(int) * (nb > 0 ? nb : 1));
+  for (i = 0; i < nb; i++) brow[i] = g->Nkmax;
+  H.phys.boundary_u = jag_new(&H, nb, brow, 0);
+  H.phys.boundary_v = jag_new(&H, nb, brow, 0);
+  H.phys.boundary_w = jag_new(&H, nb, brow, 0);
+  free(brow);
+  H.prop.nu = up->nu;
+  H.prop.laxWendroff_Vertical = up->laxWendroff_Vertical;
+  H.prop.thetaM = up->thetaM;
+  H.prop.nonlinear = up->nonlinear;
+  H.prop.cgsolver = 1;
+  H.prop.netcdfBdy = 0;
+  H.prop.thetaramptime = 0;
+  H.prop.linearFS = 0;
+  g_calls2d = 0;
+  UPredictor(&H.grid, &H.phys, &H.prop, 0, 1, 0);
+  if (res) {
+    /* BoundaryVelocities exchanges h once, then as in ref_cgsolve */
+    res->niters = g_calls2d - 3;
+    res->eps = -1;
+    res->eps0 = -1;
+  }
+  harness_free(&H);
   return 0;
 }

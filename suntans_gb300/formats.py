@@ -231,16 +231,13 @@ class GridFiles:
         if g.xp is None or g.cnodes is None or g.enodes is None or g.mark is None:
             raise ValueError("grid has no plan-view geometry (xp, cnodes, enodes, mark)")
         Nc, Ne, mf = g.Nc, g.Ne, g.maxfaces
+        from .gridgen import edge_normals, edges_by_mark
         grad = g.grad.reshape(Ne, 2)
         en = g.enodes.reshape(Ne, 2)
         x0, y0 = g.xp[en[:, 0]], g.yp[en[:, 0]]
         x1, y1 = g.xp[en[:, 1]], g.yp[en[:, 1]]
-        tx, ty = x1 - x0, y1 - y0
-        L = np.hypot(tx, ty)
-        nx, ny = ty / L, -tx / L
         c0 = grad[:, 0]
-        flip = (g.xv[c0] - x0) * nx + (g.yv[c0] - y0) * ny > 0
-        nx, ny = np.where(flip, -nx, nx), np.where(flip, -ny, ny)
+        nx, ny = edge_normals(g)
         slot = np.arange(mf)[None, :] < g.nfaces[:, None]
         fe = np.where(slot, g.face.reshape(Nc, mf), 0)
         cellof = np.repeat(np.arange(Nc), mf).reshape(Nc, mf)
@@ -255,11 +252,7 @@ class GridFiles:
         interior = grad[:, 1] >= 0
         Nkc = np.where(interior, np.maximum(g.Nk[c0], g.Nk[np.maximum(grad[:, 1], 0)]), g.Nk[c0]).astype(I32)
         mark = g.mark.astype(I32)
-        comp = np.nonzero((mark == 0) | (mark == 5))[0]
-        parts = [comp] + [np.nonzero(mark == m)[0] for m in range(1, MAXMARKS - 2)]
-        edgep = np.concatenate(parts).astype(I32)
-        edgedist = np.zeros(MAXMARKS - 1, dtype=I32)
-        edgedist[1:] = np.cumsum([p.size for p in parts])
+        edgep, edgedist = edges_by_mark(mark)
         # nodal neighbours (points, edges, cells around each node)
         Np = g.xp.size
         pp_a = np.concatenate([en[:, 0], en[:, 1]])

@@ -205,6 +205,42 @@ class VGridFields:
 
 
 @dataclasses.dataclass
+class UPredFields:
+    """Inputs of UPredictor (main/phys.c:2579-3077) beyond the grid: the state
+    at step n, the explicit horizontal source, the drag and viscosity fields,
+    and the edge orderings (computational edges, and all edges by mark as
+    main/grid.c:1666-1679 orders them)."""
+    grid: SunGrid
+    u: np.ndarray         # ragged per edge (Nke levels): u at step n
+    w: np.ndarray         # ragged per cell (Nk+1 levels): w at step n
+    h: np.ndarray         # [Nc] free surface at step n
+    utmp: np.ndarray      # ragged per edge: explicit horizontal source in, U*** out
+    tau_T: np.ndarray     # [Ne] surface stress
+    CdT: np.ndarray       # [Ne] top drag coefficient (-1 = no slip)
+    CdB: np.ndarray       # [Ne] bottom drag coefficient (-1 = no slip)
+    nu_tv: np.ndarray     # ragged per cell: vertical eddy viscosity
+    nu_lax: np.ndarray    # ragged per cell: Lax-Wendroff viscosity
+    nu: float
+    laxWendroff_Vertical: float
+    thetaM: float         # < 0: no implicit vertical momentum advection
+    nonlinear: int
+    etop: np.ndarray      # [Ne] top wet level of each edge
+    edgep: np.ndarray     # computational edges
+    edgedist: np.ndarray  # [2]
+    bedgep: np.ndarray    # all edges ordered by mark
+    bedgedist: np.ndarray # [6]
+    mark: np.ndarray      # [Ne]
+    n1: np.ndarray        # [Ne] unit normal, grad[0] towards grad[1]
+    n2: np.ndarray
+
+    @property
+    def woff(self) -> np.ndarray:
+        o = np.zeros(self.grid.Nc + 1, dtype=np.int64)
+        np.cumsum(self.grid.Nk + 1, out=o[1:])
+        return o
+
+
+@dataclasses.dataclass
 class SolverProps:
     """The propT fields the two solves read (main/phys.h:183-203)."""
     qprecond: int = 1

@@ -446,3 +446,60 @@ def make_vgrid_fields(g: SunGrid, seed=0, sigma_h=None, smoothbot=0.0, dzsmall=0
     st = make_step_fields(g, seed=seed + 1)
     return VGridFields(grid=g, h=h, u=u, dzbot=dzbot, Nkc=Nkc, smoothbot=float(smoothbot), dzsmall=float(dzsmall),
                        ctop=g.ctop.copy(), etop=st.etop.copy(), dzz=g.dzz.copy())
+
+
+def edge_normals(g: SunGrid):
+    """Unit normal of each edge pointing from grad[0] towards grad[1] (outward
+    on boundary edges), from the plan-view geometry (gridT.n1, n2)."""
+    grad = g.grad.reshape(g.Ne, 2)
+    en = g.enodes.reshape(g.Ne, 2)
+    x0, y0 = g.xp[en[:, 0]], g.yp[en[:, 0]]
+    tx, ty = g.xp[en[:, 1]] - x0, g.yp[en[:, 1]] - y0
+    L = np.hypot(tx, ty)
+    nx, ny = ty / L, -tx / L
+    c0 = grad[:, 0]
+    flip = (g.xv[c0] - x0) * nx + (g.yv[c0] - y0) * ny > 0
+    return np.where(flip, -nx, nx), np.where(flip, -ny, ny)
+
+
+def edges_by_mark(mark: np.ndarray):
+    """edgep / edgedist[6]: edges of mark 0 or 5 first, then marks 1..4
+    (main/grid.c:1666-1679)."""
+    comp = np.nonzero((mark == 0) | (mark == 5))[0]
+    parts = [comp] + [np.nonzero(mark == m)[0] for m in range(1, 5)]
+    edgep = np.concatenate(parts).astype(np.int32)
+    edgedist = np.zeros(6, dtype=np.int32)
+    edgedist[1:] = np.cumsum([p.size for p in parts])
+    return edgep, edgedist
+
+
+def make_upred_fields(g: SunGrid, seed=0, sigma_u=0.05, noslip_frac=0.2, nonlinear=1, thetaM=0.5,
+                      laxWendroff_Vertical=1.0, nu=1e-6) -> "UPredFields":
+    """Seeded inputs of UPredictor: u, w at step n (as the pressure step's),
+    a free surface N(0, 0.3 dz[0]), an explicit horizontal source, surface
+    stress, drag coefficients with a fraction of no-slip (-1) tops and bottoms
+    on edges of two or more wet levels, and vertical viscosities."""
+    from .grid import UPredFields
+    rng = np.random.default_rng(seed)
+    st = make_step_fields(g, seed=seed + 7, sigma_u=sigma_u)
+    ne3 = int(g.Nke.sum())
+    lev = np.arange(ne3) - np.repeat(g.eoff[:-1], g.Nke)
+    wet = lev >= np.repeat(st.etop, g.Nke)
+    utmp = np.where(wet, st.u + rng.normal(0.0, 0.1 * sigma_u, ne3), 0.0)
+    h = rng.normal(0.0, 0.3 * float(g.dz[0]), g.Nc)
+    tau_T = rng.normal(0.0, 1e-4, g.Ne)
+    CdB = rng.uniform(1e-3, 5e-3, g.Ne)
+    CdT = rng.uniform(0.0, 2e-3, g.Ne)
+    multi = (g.Nke - st.etop) > 1
+    CdB[multi & (rng.random(g.Ne) < noslip_frac)] = -1.0
+    CdT[multi & (rng.random(g.Ne) < noslip_frac)] = -1.0
+    nu_tv = rng.uniform(0.0, 1e-3, g.n3)
+    nu_lax = rng.uniform(0.0, 1e-4, g.n3)
+    mark = g.mark if g.mark is not None else np.where(g.grad.reshape(-1, 2)[:, 1] >= 0, 0, 1).astype(I32)
+    bedgep, bedgedist = edges_by_mark(mark)
+    n1, n2 = edge_normals(g)
+    return UPredFields(grid=g, u=st.u, w=st.w, h=h, utmp=utmp, tau_T=tau_T, CdT=CdT, CdB=CdB, nu_tv=nu_tv,
+                       nu_lax=nu_lax, nu=float(nu), laxWendroff_Vertical=float(laxWendroff_Vertical),
+                       thetaM=float(thetaM), nonlinear=int(nonlinear), etop=st.etop, edgep=st.edgep,
+                       edgedist=st.edgedist, bedgep=bedgep, bedgedist=bedgedist, mark=mark.astype(I32),
+                       n1=n1, n2=n2)

@@ -44,5 +44,17 @@ def vgrid_fields(g, d, smoothbot=0.0):
                        dzsmall=0.1, ctop=d["vg_ctop"], etop=d["vg_etop"], dzz=d["vg_dzz"])
 
 
+def upred_fields(g, d, nl):
+    """The UPredictor inputs stored with a fixture (nl: implicit vertical advection)."""
+    from suntans_gb300.grid import UPredFields
+    g.dz, g.dv, g.grad, g.normal = d["vg_dz"], d["vg_dv"], d["grad"], d["normal"]
+    pre = f"up{nl}_"
+    par = d[pre + "par"]
+    kw = {k: d[pre + k] for k in ("u", "w", "h", "utmp", "tau_T", "CdT", "CdB", "nu_tv", "nu_lax", "etop", "edgep",
+                                  "edgedist", "bedgep", "bedgedist", "mark", "n1", "n2")}
+    return UPredFields(grid=g, nu=float(par[0]), laxWendroff_Vertical=float(par[1]), thetaM=float(par[2]),
+                       nonlinear=int(par[3]), **kw)
+
+
 def props_for(props, **kw):
     return SolverProps(**{**props, **kw})

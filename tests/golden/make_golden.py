@@ -15,7 +15,9 @@ read, and the reference's outputs for:
   ComputeQSource on seeded velocity fields and Corrector with the qprecond-1
   solution as the pressure correction (the steps around CGSolveQ),
   UpdateDZ (option 0) and SetFluxHeight (smoothbot 0 and 0.3) on a seeded
-  free surface and edge velocity.
+  free surface and edge velocity,
+  UPredictor with CGSolve (main/phys.c:2579-3077) on seeded drag, viscosity
+  and velocity fields, with and without implicit vertical advection.
 The inputs are stored (not regenerated) so that the check is bit-exact on any
 host: tests/test_oracle.py runs the C restatement (oracle/cg_oracle.c) on them
 and requires identical bits.
@@ -104,6 +106,17 @@ def main():
             tag = "sfh%d" % int(round(10 * sb))
             out[tag + "_dzf"] = dzf
             out[tag + "_dzz"] = dzz2
+        for nl in (0, 1):
+            uf = gg.make_upred_fields(g, seed=36 + nl, nonlinear=nl)
+            pre = f"up{nl}_"
+            for k in ("u", "w", "h", "utmp", "tau_T", "CdT", "CdB", "nu_tv", "nu_lax", "etop", "edgep", "edgedist",
+                      "bedgep", "bedgedist", "mark", "n1", "n2"):
+                out[pre + k] = getattr(uf, k)
+            out[pre + "par"] = np.array([uf.nu, uf.laxWendroff_Vertical, uf.thetaM, uf.nonlinear])
+            r = ref.upredictor(uf, vf, SolverProps(**props))
+            for k in ("u", "h", "utmp", "E", "D", "ctop", "etop", "dzz", "active"):
+                out[pre + "out_" + k] = r[k]
+            out[pre + "out_niters"] = np.array(r["niters"])
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
         print(f"{path}: Nc={g.Nc} n3={g.n3} iters q={[int(out[f'n_qp{k}']) for k in range(3)]} "

@@ -137,3 +137,51 @@ def test_port_vertical_grid_functions_match_golden_bitwise(port, name):
         dzf, dzz = port.set_flux_height(vf)
         tag = "sfh%d" % int(round(10 * sb))
         assert np.array_equal(dzf, d[tag + "_dzf"]) and np.array_equal(dzz, d[tag + "_dzz"])
+
+
+@pytest.mark.parametrize("name", fixture_names())
+@pytest.mark.parametrize("nl", [0, 1])
+def test_port_upredictor_matches_golden_bitwise(port, name, nl):
+    """The whole of UPredictor (vertical solve, free-surface right-hand side,
+    CGSolve, velocity update, UpdateDZ, boundary fluxes) reproduces the
+    reference's bits, and its pieces compose to it."""
+    from tests._golden import upred_fields, vgrid_fields
+    g, qp, hp, props, d = load(name)
+    vf = vgrid_fields(g, d)
+    uf = upred_fields(g, d, nl)
+    pr = props_for(props)
+    r = port.upredictor(uf, vf, pr)
+    pre = f"up{nl}_out_"
+    for k in ("u", "h", "utmp", "E", "D", "ctop", "etop", "dzz", "active"):
+        assert np.array_equal(r[k], d[pre + k]), k
+    assert r["niters"] == int(d[pre + "niters"]) and r["nnan"] == 0
+    ut, E, D, nnan = port.upredictor_vertical(uf, pr)
+    ce = uf.edgep
+    eo = g.eoff
+    rows = np.concatenate([np.arange(eo[j], eo[j + 1]) for j in ce])
+    assert np.array_equal(D, r["D"]) and np.array_equal(E[rows], r["E"][rows])
+    assert np.array_equal(ut[rows], r["utmp"][rows])
+    assert np.any(r["ctop"] != g.ctop) or np.any(r["etop"] != uf.etop)
+
+
+@pytest.mark.parametrize("case", ["drag", "noslip_all", "no_lax", "no_advection"])
+def test_port_upredictor_matches_reference_library(port, case):
+    if not om.available("ref"):
+        pytest.skip("reference library not built here")
+    ref = Oracle("ref")
+    g = gg.delaunay_seamount(400, 3000, 1500, Nkmax=10, sigma=400, ctop_frac=0.3, h_sigma=0.05, open_x0=True,
+                             seed=41)
+    kw = dict(nonlinear=1, thetaM=0.5, laxWendroff_Vertical=1.0, noslip_frac=0.2)
+    if case == "no_lax":
+        kw["laxWendroff_Vertical"] = 0.0
+    if case == "no_advection":
+        kw["thetaM"] = -1.0
+    uf = gg.make_upred_fields(g, seed=42, **kw)
+    if case == "noslip_all":      # includes single-layer edges (the stale scratch read of phys.c:2864)
+        uf.CdB[:] = -1.0
+        uf.CdT[:] = -1.0
+    vf = gg.make_vgrid_fields(g, seed=43)
+    pr = h_props(1, dt=10.0)
+    a, b = port.upredictor(uf, vf, pr), ref.upredictor(uf, vf, pr)
+    for k in a:
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
