@@ -175,6 +175,67 @@ int sgpu_update_dz(sgpu_context *ctx, const sgpu_vgrid *v, const double *h, int 
 int sgpu_set_flux_height(sgpu_context *ctx, const sgpu_vgrid *v, const int *etop, const double *h,
                          const double *const *u, double *const *dzz, double *const *dzf);
 
+/* ---- UPredictor (main/phys.c:2579-3077): the predictor around CGSolve ---- */
+
+/* The edge description UPredictor's boundary steps read, once per grid: every
+ * edge ordered by mark as gridT.edgep / edgedist[6] (main/grid.c:1666-1679),
+ * gridT.mark, the edge normals gridT.n1 / n2, and every cell's faces and
+ * their signs (gridT.face, normal).  Needs sgpu_step_grid. */
+int sgpu_upredictor_grid(sgpu_context *ctx, const int *edgep, const int *edgedist, const int *mark, const double *n1,
+                         const double *n2, const int *face, const int *normal);
+
+typedef struct sgpu_upred_fields {
+  const double *const *u;      /* [Ne] rows of Nke: u at step n (phys->u)                       */
+  const double *const *w;      /* [Nc] rows of Nk+1: w (read when nonlinear && thetaM >= 0)     */
+  const double *const *nu_tv;  /* [Nc] rows of Nk: vertical eddy viscosity                       */
+  const double *const *nu_lax; /* [Nc] rows of Nk: Lax-Wendroff viscosity                        */
+  const double *tau_T;         /* [Ne] surface stress                                             */
+  const double *CdT;           /* [Ne] top drag coefficient, -1 = no slip                         */
+  const double *CdB;           /* [Ne] bottom drag coefficient, -1 = no slip                      */
+  double nu;                   /* propT.nu                                                        */
+  double laxWendroff_Vertical; /* propT.laxWendroff_Vertical                                      */
+  double thetaM;               /* propT.thetaM (< 0: no implicit vertical advection)              */
+  int nonlinear;               /* propT.nonlinear                                                 */
+} sgpu_upred_fields;
+
+/* The vertically implicit predictor (2602-2945) on the computational edges:
+ * utmp (in: the explicit horizontal source phys->utmp) becomes U***, E
+ * (phys->ut) = A^{-1} [1..1] on their rows, and D = dzf^T E (0 on every other
+ * edge).  h is the free surface at step n; prop gives dt, theta, grav.  Same
+ * bits as the reference, except that a no-slip single-layer edge reads c = 0
+ * where the reference reads a scratch value an earlier edge left (2864-2871).
+ * A NaN in U*** returns SGPU_BREAKDOWN (the reference stops the run). */
+int sgpu_upredictor_vertical(sgpu_context *ctx, const int *ctop, const int *etop, const double *const *dzz,
+                             const double *const *dzf, const double *h, const sgpu_upred_fields *f,
+                             const sgpu_props *prop, double *const *utmp, double *const *E, double *D);
+
+/* The free-surface right-hand side CGSolve reads (2964-2977), on the
+ * computational cells: htmp = Ac h - dt sum_faces sum_k ((1-theta) u + theta
+ * utmp) df normal dzf.  Same bits as the reference. */
+int sgpu_upredictor_rhs(sgpu_context *ctx, const int *etop, const double *const *dzf, const double *const *u,
+                        const double *const *utmp, const double *h, const sgpu_props *prop, double *htmp);
+
+/* After CGSolve (2991-3076): the dry-cell clip of h (active[i] = 0 where it
+ * clips, 1 elsewhere; the caller zeroes phys->s at the bottom of those
+ * cells), u = U*** - g theta dt E (h1 - h2)/dg on the computational edges,
+ * UpdateDZ (ctop, etop, dzz in place), u = utmp on type-2 edges and the
+ * continuity flux on the mark-3 faces of type-3 cells.  Needs
+ * sgpu_upredictor_grid.  Same bits as the reference. */
+int sgpu_upredictor_finish(sgpu_context *ctx, const sgpu_vgrid *v, const sgpu_props *prop, int *ctop, int *etop,
+                           double *const *dzz, const double *const *utmp, const double *const *E, double *h,
+                           unsigned char *active, double *const *u);
+
+/* The whole UPredictor on the device, with CGSolve (cgsolver 1) in between,
+ * for a model without NetCDF boundary data: the boundary step sets h = 0 on
+ * type-3 cells, runs UpdateDZ and sets utmp = 0 n1 + 0 n2 on edges of marks
+ * 2-4 (BoundaryVelocities / OpenBoundaryFluxes, boundaries.c:41-58, 179-270).
+ * Between the upload of the step's fields and the download of u, h, utmp, E,
+ * D, ctop, etop, dzz and active everything stays in HBM.  Returns CGSolve's
+ * status. */
+int sgpu_upredictor(sgpu_context *ctx, const sgpu_vgrid *v, const sgpu_upred_fields *f, const sgpu_props *prop,
+                    int *ctop, int *etop, double *const *dzz, const double *const *dzf, double *const *u, double *h,
+                    double *const *utmp, double *const *E, double *D, unsigned char *active, sgpu_stats *stats);
+
 /* Staged forms of the same two solves, for callers that keep inputs resident:
  * upload (host -> HBM), solve (HBM only; repeatable on the same inputs), and
  * download (HBM -> host, computational cells / active levels only). */

@@ -28,6 +28,8 @@ EXPORTS = [
     "sgpu_cgsolve_noalloc",
     "sgpu_step_grid", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_pressure_step",
     "sgpu_update_dz", "sgpu_set_flux_height",
+    "sgpu_upredictor_grid", "sgpu_upredictor_vertical", "sgpu_upredictor_rhs", "sgpu_upredictor_finish",
+    "sgpu_upredictor",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
     "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set", "sgpu_batch_set_tile_slots",
     "sgpu_batch_stream", "sgpu_batch_phase_times", "sgpu_batch_resubmit", "sgpu_batch_use_graph",
@@ -65,6 +67,12 @@ class VGrid(C.Structure):
                 ("dzsmall", C.c_double)]
 
 
+class UPredFieldsC(C.Structure):
+    _fields_ = [("u", _dpp), ("w", _dpp), ("nu_tv", _dpp), ("nu_lax", _dpp), ("tau_T", _dp), ("CdT", _dp),
+                ("CdB", _dp), ("nu", C.c_double), ("laxWendroff_Vertical", C.c_double), ("thetaM", C.c_double),
+                ("nonlinear", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("status", C.c_int), ("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double),
                 ("ms_solve", C.c_double), ("ms_total", C.c_double), ("unknowns", C.c_longlong)]
@@ -93,6 +101,15 @@ def load() -> C.CDLL:
     lib.sgpu_step_grid.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
     lib.sgpu_update_dz.argtypes = [C.c_void_p, C.POINTER(VGrid), _dp, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp]
     lib.sgpu_set_flux_height.argtypes = [C.c_void_p, C.POINTER(VGrid), _ip, _dp, _dpp, _dpp, _dpp]
+    _ucp = C.POINTER(C.c_ubyte)
+    lib.sgpu_upredictor_grid.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, _dp, _ip, _ip]
+    lib.sgpu_upredictor_vertical.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dp, C.POINTER(UPredFieldsC),
+                                             C.POINTER(Props), _dpp, _dpp, _dp]
+    lib.sgpu_upredictor_rhs.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dpp, _dp, C.POINTER(Props), _dp]
+    lib.sgpu_upredictor_finish.argtypes = [C.c_void_p, C.POINTER(VGrid), C.POINTER(Props), _ip, _ip, _dpp, _dpp,
+                                           _dpp, _dp, _ucp, _dpp]
+    lib.sgpu_upredictor.argtypes = [C.c_void_p, C.POINTER(VGrid), C.POINTER(UPredFieldsC), C.POINTER(Props), _ip,
+                                    _ip, _dpp, _dpp, _dpp, _dp, _dpp, _dpp, _dp, _ucp, C.POINTER(Stats)]
     lib.sgpu_compute_qsource.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dpp, _dpp, _dpp, C.c_double, C.c_double,
                                          _dpp, _dp]
     lib.sgpu_corrector.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dp, C.c_double, _dpp, _dpp, _dpp]
@@ -384,6 +401,113 @@ class Context:
                                            _vp(jagged(dzf, vf.foff)))
         self._check(rc, "sgpu_set_flux_height", allow=(OK,))
         return dzf, dzz
+
+    # ---- UPredictor ----
+    def upredictor_grid(self, uf):
+        """Edge orderings, marks, normals and every cell's faces (once per grid)."""
+        g = self.grid
+        ki = [np.ascontiguousarray(a, dtype=np.int32) for a in (uf.bedgep, uf.bedgedist, uf.mark)]
+        kd = [np.ascontiguousarray(a, dtype=np.float64) for a in (uf.n1, uf.n2)]
+        kf = [np.ascontiguousarray(a, dtype=np.int32) for a in (g.face, g.normal)]
+        self._up_keep = ki + kd + kf
+        rc = self.lib.sgpu_upredictor_grid(self.h, *[a.ctypes.data_as(_ip) for a in ki],
+                                           *[a.ctypes.data_as(_dp) for a in kd], *[a.ctypes.data_as(_ip) for a in kf])
+        self._check(rc, "sgpu_upredictor_grid", allow=(OK,))
+
+    def _upred_fields(self, uf):
+        g = self.grid
+        woff = uf.woff
+        keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (uf.u, uf.w, uf.nu_tv, uf.nu_lax, uf.tau_T,
+                                                                      uf.CdT, uf.CdB)]
+        rows = [jagged(keep[0], self.eoff), jagged(keep[1], woff), jagged(keep[2], self.coff),
+                jagged(keep[3], self.coff)]
+        f = UPredFieldsC(*[_vp(r) for r in rows], *[a.ctypes.data_as(_dp) for a in keep[4:]], float(uf.nu),
+                         float(uf.laxWendroff_Vertical), float(uf.thetaM), int(uf.nonlinear))
+        return f, keep + rows
+
+    def upredictor_vertical(self, uf, props: SolverProps, ctop=None, etop=None, dzz=None, dzf=None):
+        """U***, E (computational rows; others 0) and D; returns (utmp, E, D)."""
+        g = self.grid
+        f, keep = self._upred_fields(uf)
+        ct = np.ascontiguousarray(g.ctop if ctop is None else ctop, dtype=np.int32)
+        et = np.ascontiguousarray(uf.etop if etop is None else etop, dtype=np.int32)
+        zz = np.ascontiguousarray(g.dzz if dzz is None else dzz, dtype=np.float64)
+        zf = np.ascontiguousarray(g.dzf if dzf is None else dzf, dtype=np.float64)
+        h = np.ascontiguousarray(uf.h, dtype=np.float64)
+        utmp = np.array(uf.utmp, dtype=np.float64, copy=True)
+        E = np.zeros(max(int(g.Nke.sum()), 1))
+        D = np.full(max(g.Ne, 1), -7.0)
+        pr = props_struct(props)
+        rc = self.lib.sgpu_upredictor_vertical(self.h, ct.ctypes.data_as(_ip), et.ctypes.data_as(_ip),
+                                               _vp(jagged(zz, self.coff)), _vp(jagged(zf, self.eoff)),
+                                               h.ctypes.data_as(_dp), C.byref(f), C.byref(pr),
+                                               _vp(jagged(utmp, self.eoff)), _vp(jagged(E, self.eoff)),
+                                               D.ctypes.data_as(_dp))
+        self._check(rc, "sgpu_upredictor_vertical", allow=(OK,))
+        return utmp, E[:int(g.Nke.sum())], D[:g.Ne]
+
+    def upredictor_rhs(self, uf, props: SolverProps, utmp, h=None, etop=None, dzf=None):
+        g = self.grid
+        et = np.ascontiguousarray(uf.etop if etop is None else etop, dtype=np.int32)
+        zf = np.ascontiguousarray(g.dzf if dzf is None else dzf, dtype=np.float64)
+        u = np.ascontiguousarray(uf.u, dtype=np.float64)
+        ut = np.ascontiguousarray(utmp, dtype=np.float64)
+        hh = np.ascontiguousarray(uf.h if h is None else h, dtype=np.float64)
+        htmp = np.zeros(g.Nc)
+        pr = props_struct(props)
+        rc = self.lib.sgpu_upredictor_rhs(self.h, et.ctypes.data_as(_ip), _vp(jagged(zf, self.eoff)),
+                                          _vp(jagged(u, self.eoff)), _vp(jagged(ut, self.eoff)),
+                                          hh.ctypes.data_as(_dp), C.byref(pr), htmp.ctypes.data_as(_dp))
+        self._check(rc, "sgpu_upredictor_rhs", allow=(OK,))
+        return htmp
+
+    def upredictor_finish(self, uf, vf, props: SolverProps, utmp, E, h, ctop, etop, dzz, u=None):
+        """Returns (h, active, u, ctop, etop, dzz) after the post-solve steps."""
+        g = self.grid
+        v, keepv = self._vgrid(vf)
+        ct = np.array(ctop, dtype=np.int32, copy=True)
+        et = np.array(etop, dtype=np.int32, copy=True)
+        zz = np.array(dzz, dtype=np.float64, copy=True)
+        ut = np.ascontiguousarray(utmp, dtype=np.float64)
+        EE = np.ascontiguousarray(E, dtype=np.float64)
+        hh = np.array(h, dtype=np.float64, copy=True)
+        active = np.full(g.Nc, 7, dtype=np.uint8)
+        uu = np.array(uf.u if u is None else u, dtype=np.float64, copy=True)
+        pr = props_struct(props)
+        rc = self.lib.sgpu_upredictor_finish(self.h, C.byref(v), C.byref(pr), ct.ctypes.data_as(_ip),
+                                             et.ctypes.data_as(_ip), _vp(jagged(zz, self.coff)),
+                                             _vp(jagged(ut, self.eoff)), _vp(jagged(EE, self.eoff)),
+                                             hh.ctypes.data_as(_dp), active.ctypes.data_as(C.POINTER(C.c_ubyte)),
+                                             _vp(jagged(uu, self.eoff)))
+        self._check(rc, "sgpu_upredictor_finish", allow=(OK,))
+        return hh, active, uu, ct, et, zz
+
+    def upredictor(self, uf, vf, props: SolverProps):
+        """The whole UPredictor with CGSolve on the device, from the grid's ctop /
+        dzz / dzf and uf.etop; returns a dict like the oracle's."""
+        g = self.grid
+        v, keepv = self._vgrid(vf)
+        f, keep = self._upred_fields(uf)
+        ct = np.array(g.ctop, dtype=np.int32, copy=True)
+        et = np.array(uf.etop, dtype=np.int32, copy=True)
+        zz = np.array(g.dzz, dtype=np.float64, copy=True)
+        zf = np.ascontiguousarray(g.dzf, dtype=np.float64)
+        u = np.array(uf.u, dtype=np.float64, copy=True)
+        h = np.array(uf.h, dtype=np.float64, copy=True)
+        utmp = np.array(uf.utmp, dtype=np.float64, copy=True)
+        E = np.zeros(max(int(g.Nke.sum()), 1))
+        D = np.zeros(max(g.Ne, 1))
+        active = np.full(g.Nc, 7, dtype=np.uint8)
+        st = Stats()
+        pr = props_struct(props)
+        rc = self.lib.sgpu_upredictor(self.h, C.byref(v), C.byref(f), C.byref(pr), ct.ctypes.data_as(_ip),
+                                      et.ctypes.data_as(_ip), _vp(jagged(zz, self.coff)), _vp(jagged(zf, self.eoff)),
+                                      _vp(jagged(u, self.eoff)), h.ctypes.data_as(_dp), _vp(jagged(utmp, self.eoff)),
+                                      _vp(jagged(E, self.eoff)), D.ctypes.data_as(_dp),
+                                      active.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(st))
+        self._check(rc, "sgpu_upredictor")
+        return dict(u=u, h=h, utmp=utmp, E=E[:int(g.Nke.sum())], D=D[:g.Ne], ctop=ct, etop=et, dzz=zz,
+                    active=active, niters=st.niters, stats=st)
 
     # ---- free surface ----
     def cgsolve(self, prob, props: SolverProps):

@@ -71,6 +71,16 @@ struct sgpu_context {
   int *d_ctopold = nullptr, *d_etopold = nullptr;
   double *d_dz = nullptr, *d_dv = nullptr, *d_dzbot = nullptr, *d_hv = nullptr, *d_dzzold = nullptr;
 
+  // UPredictor buffers
+  std::vector<int> cedge_h;  // computational edges (host copy)
+  bool up_grid = false, up_ready = false;
+  int nb2 = 0, nbnd = 0;
+  int *d_b2edge = nullptr, *d_bedge = nullptr, *d_bnfaces = nullptr, *d_bfedge = nullptr, *d_bnormal = nullptr,
+      *d_mark = nullptr, *d_nnan = nullptr;
+  double *d_n1 = nullptr, *d_n2 = nullptr, *d_utmp = nullptr, *d_E = nullptr, *d_tauT = nullptr, *d_CdT = nullptr,
+         *d_CdB = nullptr, *d_nutv = nullptr, *d_nulax = nullptr;
+  unsigned char* d_active = nullptr;
+
   // free-surface buffers
   bool h_ready = false;
   double *d_Dh = nullptr, *d_hin = nullptr, *d_bin = nullptr, *d_hcoef = nullptr, *d_hf = nullptr,
@@ -769,6 +779,7 @@ int sgpu_step_grid(sgpu_context* ctx, const int* normal, const int* grad, const 
     CK(cudaMemcpyAsync(ctx->d_cedge, ce.data(), sizeof(int) * ce.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->ncedge = (int)ce.size();
+  ctx->cedge_h = ce;
   ctx->step_grid = true;
   return SGPU_OK;
 }
@@ -1197,6 +1208,448 @@ int sgpu_set_flux_height(sgpu_context* ctx, const sgpu_vgrid* v, const int* etop
   if (v->smoothbot != 0) scatter_cells_all(ctx, s_dzz, dzz);
   ctx->q_uploaded = false;
   return SGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// UPredictor: the predictor around CGSolve
+// ---------------------------------------------------------------------------
+static int alloc_upred(sgpu_context* ctx) {
+  if (ctx->up_ready) return SGPU_OK;
+  int rc;
+  const size_t ne3 = ctx->ne3 + 1, n3 = ctx->n3 + 1, Ne = ctx->Ne + 1;
+  if ((rc = dalloc(ctx, &ctx->d_utmp, ne3)) || (rc = dalloc(ctx, &ctx->d_E, ne3))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_tauT, Ne)) || (rc = dalloc(ctx, &ctx->d_CdT, Ne)) || (rc = dalloc(ctx, &ctx->d_CdB, Ne)))
+    return rc;
+  if ((rc = dalloc(ctx, &ctx->d_nutv, n3)) || (rc = dalloc(ctx, &ctx->d_nulax, n3))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_active, (size_t)ctx->Nc + 1)) || (rc = dalloc(ctx, &ctx->d_nnan, 1))) return rc;
+  ctx->up_ready = true;
+  return SGPU_OK;
+}
+
+int sgpu_upredictor_grid(sgpu_context* ctx, const int* edgep, const int* edgedist, const int* mark, const double* n1,
+                         const double* n2, const int* face, const int* normal) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!edgedist || !mark || !n1 || !n2 || !face || !normal) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  const int Ne = ctx->Ne, F = ctx->F, nb3 = ctx->nbdy;
+  for (int m = 0; m < 5; ++m)
+    if (edgedist[m] < 0 || edgedist[m + 1] < edgedist[m] || edgedist[m + 1] > Ne)
+      return fail(ctx, SGPU_BAD_GRID, "edgedist out of order");
+  if (!edgep && edgedist[5] > 0) return fail(ctx, SGPU_BAD_ARG, "null edgep");
+  std::vector<int> b2, bn, bnf(std::max(nb3, 1)), bfe((size_t)std::max(nb3, 1) * F, 0), bnr((size_t)std::max(nb3, 1) * F, 0);
+  for (int t = edgedist[2]; t < edgedist[5]; ++t) {
+    const int e = edgep[t];
+    if (e < 0 || e >= Ne) return fail(ctx, SGPU_BAD_GRID, "edgep[%d]=%d out of range", t, e);
+    bn.push_back(e);
+    if (t < edgedist[3]) b2.push_back(e);
+  }
+  for (int e = 0; e < Ne; ++e)
+    if (mark[e] < 0 || mark[e] > 6) return fail(ctx, SGPU_BAD_GRID, "mark[%d]=%d out of range", e, mark[e]);
+  for (int b = 0; b < nb3; ++b) {
+    const int i = ctx->dev2cell[ctx->ncomp + b];
+    bnf[b] = ctx->nfaces[i];
+    for (int f = 0; f < bnf[b]; ++f) {
+      const int e = face[(size_t)i * F + f], v = normal[(size_t)i * F + f];
+      if (e < 0 || e >= Ne) return fail(ctx, SGPU_BAD_GRID, "face[%d]=%d out of range", i * F + f, e);
+      if (v != 1 && v != -1) return fail(ctx, SGPU_BAD_GRID, "normal[%d]=%d is not +1 or -1", i * F + f, v);
+      bfe[(size_t)b * F + f] = e;
+      bnr[(size_t)b * F + f] = v;
+    }
+  }
+  DeviceGuard dg(ctx->device);
+  int rc;
+  if (!ctx->up_grid) {
+    if ((rc = dalloc(ctx, &ctx->d_b2edge, (size_t)Ne + 1)) || (rc = dalloc(ctx, &ctx->d_bedge, (size_t)Ne + 1)) ||
+        (rc = dalloc(ctx, &ctx->d_bnfaces, bnf.size())) || (rc = dalloc(ctx, &ctx->d_bfedge, bfe.size())) ||
+        (rc = dalloc(ctx, &ctx->d_bnormal, bnr.size())) || (rc = dalloc(ctx, &ctx->d_mark, (size_t)Ne + 1)) ||
+        (rc = dalloc(ctx, &ctx->d_n1, (size_t)Ne + 1)) || (rc = dalloc(ctx, &ctx->d_n2, (size_t)Ne + 1)))
+      return rc;
+  }
+  if (!b2.empty()) CK(cudaMemcpyAsync(ctx->d_b2edge, b2.data(), sizeof(int) * b2.size(), cudaMemcpyHostToDevice, ctx->stream));
+  if (!bn.empty()) CK(cudaMemcpyAsync(ctx->d_bedge, bn.data(), sizeof(int) * bn.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_bnfaces, bnf.data(), sizeof(int) * bnf.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_bfedge, bfe.data(), sizeof(int) * bfe.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_bnormal, bnr.data(), sizeof(int) * bnr.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_mark, mark, sizeof(int) * Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_n1, n1, sizeof(double) * Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_n2, n2, sizeof(double) * Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->nb2 = (int)b2.size();
+  ctx->nbnd = (int)bn.size();
+  ctx->up_grid = true;
+  return SGPU_OK;
+}
+
+static int kmax_for(int Nkmax) {
+  const int need = Nkmax + 1;
+  return need <= 16 ? 16 : need <= 32 ? 32 : need <= 64 ? 64 : 128;
+}
+
+static UPredArgs upred_args(sgpu_context* ctx, const sgpu_props* p, const sgpu_upred_fields* f) {
+  UPredArgs a{};
+  a.Nc = ctx->Nc;
+  a.Ne = ctx->Ne;
+  a.ncomp = ctx->ncomp;
+  a.ncell3 = ctx->nbdy;
+  a.F = ctx->F;
+  a.ncedge = ctx->ncedge;
+  a.nb2 = ctx->nb2;
+  a.nbnd = ctx->nbnd;
+  a.kmax = kmax_for(ctx->Nkmax);
+  a.dt = p->dt;
+  a.theta = p->theta;
+  a.grav = p->grav;
+  if (f) {
+    a.nu = f->nu;
+    a.lax = f->laxWendroff_Vertical;
+    a.thetaM = f->thetaM;
+    a.nonlinear = f->nonlinear;
+  }
+  a.cedge = ctx->d_cedge;
+  a.b2edge = ctx->d_b2edge;
+  a.bedge = ctx->d_bedge;
+  a.grad = ctx->d_grad;
+  a.nke = ctx->d_nke;
+  a.eoff = ctx->d_eoff;
+  a.dcoff = ctx->d_dcoff;
+  a.woff = ctx->d_woff;
+  a.ctop = ctx->d_ctop;
+  a.etop = ctx->d_etop;
+  a.nfaces = ctx->d_nfaces;
+  a.fedge = ctx->d_fedge;
+  a.normal = ctx->d_normal;
+  a.bnfaces = ctx->d_bnfaces;
+  a.bfedge = ctx->d_bfedge;
+  a.bnormal = ctx->d_bnormal;
+  a.mark = ctx->d_mark;
+  a.n1 = ctx->d_n1;
+  a.n2 = ctx->d_n2;
+  a.dzz = ctx->d_dzz;
+  a.dzf = ctx->d_dzf;
+  a.dg = ctx->d_dg;
+  a.df = ctx->d_df;
+  a.Ac = ctx->d_Ac;
+  a.dv = ctx->d_dv;
+  a.tau_T = ctx->d_tauT;
+  a.CdT = ctx->d_CdT;
+  a.CdB = ctx->d_CdB;
+  a.nu_tv = ctx->d_nutv;
+  a.nu_lax = ctx->d_nulax;
+  a.w = ctx->d_w;
+  a.u = ctx->d_u;
+  a.h = ctx->d_hv;
+  a.utmp = ctx->d_utmp;
+  a.E = ctx->d_E;
+  a.D = ctx->d_Dh;
+  a.htmp = ctx->d_bin;
+  a.u_out = ctx->d_u;
+  a.active = ctx->d_active;
+  a.nnan = ctx->d_nnan;
+  return a;
+}
+
+static int upred_common_checks(sgpu_context* ctx) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  if (ctx->Nkmax + 1 > 128) return fail(ctx, SGPU_BAD_GRID, "UPredictor on the device needs Nkmax <= 127");
+  DeviceGuard dg(ctx->device);
+  int rc;
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx)) || (rc = alloc_vgrid(ctx)) || (rc = alloc_h(ctx)) ||
+      (rc = alloc_upred(ctx)))
+    return rc;
+  return SGPU_OK;
+}
+
+static int check_etop(sgpu_context* ctx, const int* etop) {
+  for (int e = 0; e < ctx->Ne; ++e)
+    if (etop[e] < 0 || (ctx->Nke[e] > 0 && etop[e] >= ctx->Nke[e]) || (ctx->Nke[e] == 0 && etop[e] != 0))
+      return fail(ctx, SGPU_BAD_ARG, "etop[%d]=%d out of [0,Nke)", e, etop[e]);
+  return SGPU_OK;
+}
+
+// the inputs of the vertical predictor, staged and uploaded (ctop, etop, dzz,
+// dzf, u, w, h, utmp and the drag / viscosity fields)
+static int upload_upred_inputs(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                               const double* const* dzf, const double* h, const sgpu_upred_fields* f,
+                               const double* const* utmp) {
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, Nc = ctx->Nc, Ne = ctx->Ne, ni = (Nc + Ne + 1) / 2 + 1;
+  int rc;
+  if ((rc = ensure_pinned(ctx, ni + 3 * n3 + 3 * ne3 + nw3 + Nc + 3 * Ne + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  int* s_etop = s_ctop + Nc;
+  double* s_dzz = ctx->pin + ni;
+  double* s_nut = s_dzz + n3;
+  double* s_nul = s_nut + n3;
+  double* s_dzf = s_nul + n3;
+  double* s_u = s_dzf + ne3;
+  double* s_ut = s_u + ne3;
+  double* s_w = s_ut + ne3;
+  double* s_h = s_w + nw3;
+  double* s_tc = s_h + Nc;
+  for (size_t j = 0; j < Nc; ++j) {
+    s_ctop[j] = ctop[ctx->dev2cell[j]];
+    s_h[j] = h[ctx->dev2cell[j]];
+  }
+  std::memcpy(s_etop, etop, sizeof(int) * Ne);
+  gather_cells(ctx, dzz, s_dzz);
+  gather_cells(ctx, f->nu_tv, s_nut);
+  gather_cells(ctx, f->nu_lax, s_nul);
+  gather_edges(ctx, dzf, s_dzf);
+  gather_edges(ctx, f->u, s_u);
+  gather_edges(ctx, utmp, s_ut);
+  const bool adv = f->nonlinear && f->thetaM >= 0;
+  if (adv) gather_wrows(ctx, f->w, s_w);
+  std::memcpy(s_tc, f->tau_T, sizeof(double) * Ne);
+  std::memcpy(s_tc + Ne, f->CdT, sizeof(double) * Ne);
+  std::memcpy(s_tc + 2 * Ne, f->CdB, sizeof(double) * Ne);
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * Nc, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * Ne, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_nutv, s_nut, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_nulax, s_nul, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_utmp, s_ut, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  if (adv) CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_hv, s_h, sizeof(double) * Nc, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_tauT, s_tc, sizeof(double) * Ne, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_CdT, s_tc + Ne, sizeof(double) * Ne, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_CdB, s_tc + 2 * Ne, sizeof(double) * Ne, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(ctx->d_nnan, 0, sizeof(int), st));
+  return SGPU_OK;
+}
+
+static bool upred_fields_ok(const sgpu_upred_fields* f) {
+  return f && f->u && f->nu_tv && f->nu_lax && f->tau_T && f->CdT && f->CdB &&
+         (f->w || !(f->nonlinear && f->thetaM >= 0));
+}
+
+// E rows of the computational edges, from device staging to the caller's rows
+static void scatter_cedge_rows(sgpu_context* ctx, const double* src, double* const* rows) {
+  host_parallel((long long)ctx->cedge_h.size(), [&](long long b, long long e) {
+    for (long long t = b; t < e; ++t) {
+      const int k = ctx->cedge_h[t];
+      std::memcpy(rows[k], src + ctx->eoff[k], sizeof(double) * ctx->Nke[k]);
+    }
+  });
+}
+
+int sgpu_upredictor_vertical(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                             const double* const* dzf, const double* h, const sgpu_upred_fields* f,
+                             const sgpu_props* prop, double* const* utmp, double* const* E, double* D) {
+  int rc;
+  if ((rc = upred_common_checks(ctx))) return rc;
+  if (!ctop || !etop || !dzz || !dzf || !h || !upred_fields_ok(f) || !prop || !utmp || !E || !D)
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if ((rc = check_ctop(ctx, ctop)) || (rc = check_etop(ctx, etop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = upload_upred_inputs(ctx, ctop, etop, dzz, dzf, h, f, (const double* const*)utmp))) return rc;
+  UPredArgs a = upred_args(ctx, prop, f);
+  CK(launch_upred_vertical(a, ctx->stream));
+  const size_t ne3 = ctx->ne3;
+  double* s_ut = ctx->pin;
+  double* s_E = s_ut + ne3;
+  int nnan = 0;
+  CK(cudaMemcpyAsync(s_ut, ctx->d_utmp, sizeof(double) * ne3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(s_E, ctx->d_E, sizeof(double) * ne3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(D, ctx->d_Dh, sizeof(double) * ctx->Ne, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&nnan, ctx->d_nnan, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  scatter_edges(ctx, s_ut, utmp);
+  scatter_cedge_rows(ctx, s_E, E);
+  ctx->q_uploaded = false;
+  ctx->h_uploaded = false;
+  if (nnan) return fail(ctx, SGPU_BREAKDOWN, "U*** has %d NaN values (the reference stops here)", nnan);
+  return SGPU_OK;
+}
+
+int sgpu_upredictor_rhs(sgpu_context* ctx, const int* etop, const double* const* dzf, const double* const* u,
+                        const double* const* utmp, const double* h, const sgpu_props* prop, double* htmp) {
+  int rc;
+  if ((rc = upred_common_checks(ctx))) return rc;
+  if (!etop || !dzf || !u || !utmp || !h || !prop || !htmp) return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if ((rc = check_etop(ctx, etop))) return rc;
+  DeviceGuard dg(ctx->device);
+  const size_t ne3 = ctx->ne3, Nc = ctx->Nc, Ne = ctx->Ne, ni = Ne / 2 + 1;
+  if ((rc = ensure_pinned(ctx, ni + 3 * ne3 + 2 * Nc + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_etop = (int*)ctx->pin;
+  double* s_dzf = ctx->pin + ni;
+  double* s_u = s_dzf + ne3;
+  double* s_ut = s_u + ne3;
+  double* s_h = s_ut + ne3;
+  std::memcpy(s_etop, etop, sizeof(int) * Ne);
+  gather_edges(ctx, dzf, s_dzf);
+  gather_edges(ctx, u, s_u);
+  gather_edges(ctx, utmp, s_ut);
+  for (size_t j = 0; j < Nc; ++j) s_h[j] = h[ctx->dev2cell[j]];
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * Ne, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_utmp, s_ut, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_hv, s_h, sizeof(double) * Nc, cudaMemcpyHostToDevice, st));
+  UPredArgs a = upred_args(ctx, prop, nullptr);
+  CK(launch_upred_rhs(a, st));
+  double* s_b = s_h + Nc;
+  CK(cudaMemcpyAsync(s_b, ctx->d_bin, sizeof(double) * ctx->ncomp, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int j = 0; j < ctx->ncomp; ++j) htmp[ctx->dev2cell[j]] = s_b[j];
+  ctx->h_uploaded = false;
+  return SGPU_OK;
+}
+
+// download of the state the finish step and the whole predictor leave
+static int download_upred_state(sgpu_context* ctx, int* ctop, int* etop, double* const* dzz, double* h,
+                                unsigned char* active, double* const* u) {
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, Nc = ctx->Nc, Ne = ctx->Ne, ni = (Nc + Ne + 1) / 2 + 1;
+  int rc;
+  if ((rc = ensure_pinned(ctx, ni + n3 + ne3 + 2 * Nc + 8))) return rc;
+  int* o_ctop = (int*)ctx->pin;
+  int* o_etop = o_ctop + Nc;
+  double* s_dzz = ctx->pin + ni;
+  double* s_u = s_dzz + n3;
+  double* s_h = s_u + ne3;
+  unsigned char* s_act = (unsigned char*)(s_h + Nc);
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(o_ctop, ctx->d_ctop, sizeof(int) * Nc, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(o_etop, ctx->d_etop, sizeof(int) * Ne, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_dzz, ctx->d_dzz, sizeof(double) * n3, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_u, ctx->d_u, sizeof(double) * ne3, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_h, ctx->d_hv, sizeof(double) * Nc, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_act, ctx->d_active, Nc, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (size_t j = 0; j < Nc; ++j) {
+    const int i = ctx->dev2cell[j];
+    ctop[i] = o_ctop[j];
+    h[i] = s_h[j];
+    active[i] = s_act[j];
+  }
+  std::memcpy(etop, o_etop, sizeof(int) * Ne);
+  scatter_cells_all(ctx, s_dzz, dzz);
+  scatter_edges(ctx, s_u, u);
+  return SGPU_OK;
+}
+
+// dry-cell clip, u on computational edges, UpdateDZ, type-2 / type-3 boundaries
+static cudaError_t launch_upred_finish(sgpu_context* ctx, const sgpu_vgrid* v, const UPredArgs& a) {
+  cudaError_t e;
+  if ((e = launch_upred_velocity(a, ctx->stream))) return e;
+  VGridArgs va = vgrid_args(ctx, v, 0);
+  if ((e = launch_update_dz(va, ctx->stream))) return e;
+  return launch_upred_boundary(a, ctx->stream);
+}
+
+int sgpu_upredictor_finish(sgpu_context* ctx, const sgpu_vgrid* v, const sgpu_props* prop, int* ctop, int* etop,
+                           double* const* dzz, const double* const* utmp, const double* const* E, double* h,
+                           unsigned char* active, double* const* u) {
+  int rc;
+  if ((rc = upred_common_checks(ctx))) return rc;
+  if (!v || !v->dz || !v->dv || !prop || !ctop || !etop || !dzz || !utmp || !E || !h || !active || !u)
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->up_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_upredictor_grid has not been called");
+  if ((rc = check_ctop(ctx, ctop)) || (rc = check_etop(ctx, etop))) return rc;
+  DeviceGuard dg(ctx->device);
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, Nc = ctx->Nc, Ne = ctx->Ne, ni = (Nc + Ne + 1) / 2 + 1;
+  if ((rc = ensure_pinned(ctx, ni + n3 + 3 * ne3 + 3 * Nc + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  int* s_etop = s_ctop + Nc;
+  double* s_dzz = ctx->pin + ni;
+  double* s_ut = s_dzz + n3;
+  double* s_E = s_ut + ne3;
+  double* s_u = s_E + ne3;
+  double* s_dv = s_u + ne3;
+  double* s_dzbot = s_dv + Nc;
+  double* s_h = s_dzbot + Nc;
+  for (size_t j = 0; j < Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  std::memcpy(s_etop, etop, sizeof(int) * Ne);
+  gather_cells(ctx, (const double* const*)dzz, s_dzz);
+  gather_edges(ctx, utmp, s_ut);
+  gather_edges(ctx, E, s_E);
+  gather_edges(ctx, (const double* const*)u, s_u);
+  if ((rc = upload_vgrid_common(ctx, v, h, s_dv, s_dzbot, s_h))) return rc;
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * Nc, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_etop, s_etop, sizeof(int) * Ne, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_utmp, s_ut, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_E, s_E, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  UPredArgs a = upred_args(ctx, prop, nullptr);
+  CK(launch_upred_finish(ctx, v, a));
+  CK(cudaStreamSynchronize(st));
+  if ((rc = download_upred_state(ctx, ctop, etop, dzz, h, active, u))) return rc;
+  ctx->q_uploaded = false;
+  return SGPU_OK;
+}
+
+int sgpu_upredictor(sgpu_context* ctx, const sgpu_vgrid* v, const sgpu_upred_fields* f, const sgpu_props* prop,
+                    int* ctop, int* etop, double* const* dzz, const double* const* dzf, double* const* u, double* h,
+                    double* const* utmp, double* const* E, double* D, unsigned char* active, sgpu_stats* stats) {
+  auto t0 = std::chrono::steady_clock::now();
+  int rc;
+  if ((rc = upred_common_checks(ctx))) return rc;
+  if (!v || !v->dz || !v->dv || !upred_fields_ok(f) || !prop || !ctop || !etop || !dzz || !dzf || !u || !h ||
+      !utmp || !E || !D || !active)
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->up_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_upredictor_grid has not been called");
+  if ((rc = check_ctop(ctx, ctop)) || (rc = check_etop(ctx, etop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = upload_upred_inputs(ctx, ctop, etop, (const double* const*)dzz, dzf, h, f, (const double* const*)utmp)))
+    return rc;
+  {
+    double* s_dv = ctx->pin + ((ctx->Nc + ctx->Ne + 1) / 2 + 1) + 3 * ctx->n3;  // staging behind the dzz block
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int j = 0; j < ctx->Nc; ++j) {
+      const int i = ctx->dev2cell[j];
+      s_dv[j] = v->dv[i];
+      s_dv[ctx->Nc + j] = v->dzbot ? v->dzbot[i] : 0.0;
+    }
+    CK(cudaMemcpyAsync(ctx->d_dz, v->dz, sizeof(double) * ctx->Nkmax, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_dv, s_dv, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_dzbot, s_dv + ctx->Nc, sizeof(double) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  cudaStream_t st = ctx->stream;
+  UPredArgs a = upred_args(ctx, prop, f);
+  // U***, E, D
+  CK(launch_upred_vertical(a, st));
+  int nnan = 0;
+  CK(cudaMemcpyAsync(&nnan, ctx->d_nnan, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (nnan) return fail(ctx, SGPU_BREAKDOWN, "U*** has %d NaN values (the reference stops here)", nnan);
+  // BoundaryVelocities / OpenBoundaryFluxes without boundary data
+  if (ctx->nbdy > 0) CK(cudaMemsetAsync(ctx->d_hv + ctx->ncomp, 0, sizeof(double) * ctx->nbdy, st));
+  VGridArgs va = vgrid_args(ctx, v, 0);
+  CK(launch_update_dz(va, st));
+  CK(launch_upred_open_fluxes(a, st));
+  // the free-surface right-hand side and CGSolve, all in HBM
+  CK(launch_upred_rhs(a, st));
+  CK(cudaMemcpyAsync(ctx->d_hin, ctx->d_hv, sizeof(double) * ctx->Nc, cudaMemcpyDeviceToDevice, st));
+  ctx->h_uploaded = true;
+  ctx->h_solved = false;
+  int s_rc = sgpu_h_solve(ctx, prop, stats);
+  if (s_rc != SGPU_OK && s_rc != SGPU_MAXITER && s_rc != SGPU_BREAKDOWN) return s_rc;
+  if (ctx->ncomp > 0)
+    CK(cudaMemcpyAsync(ctx->d_hv, ctx->d_hx, sizeof(double) * ctx->ncomp, cudaMemcpyDeviceToDevice, st));
+  CK(launch_upred_finish(ctx, v, a));
+  // results
+  const size_t ne3 = ctx->ne3;
+  if ((rc = download_upred_state(ctx, ctop, etop, dzz, h, active, u))) return rc;
+  double* s_ut = ctx->pin;
+  double* s_E = s_ut + ne3;
+  CK(cudaMemcpyAsync(s_ut, ctx->d_utmp, sizeof(double) * ne3, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_E, ctx->d_E, sizeof(double) * ne3, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(D, ctx->d_Dh, sizeof(double) * ctx->Ne, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  scatter_edges(ctx, s_ut, utmp);
+  scatter_cedge_rows(ctx, s_E, E);
+  ctx->q_uploaded = false;
+  ctx->h_uploaded = false;
+  if (stats) stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return s_rc;
 }
 
 }  // extern "C"

@@ -67,6 +67,61 @@ struct VGridArgs {
   double* dzf;          // [ne3] out (Nke levels per edge)
 };
 
+// UPredictor (main/phys.c:2579-3077): device order as above; edge rows of
+// u, utmp, E, dzf in edge order.
+struct UPredArgs {
+  int Nc, Ne, ncomp, ncell3, F, ncedge, nb2, nbnd;
+  int kmax;             // the local columns hold kmax levels (>= Nkmax + 1)
+  double dt, theta, grav, nu, lax, thetaM;
+  int nonlinear;
+  const int* cedge;     // [ncedge] computational edges
+  const int* b2edge;    // [nb2] type-2 edges (mark 2)
+  const int* bedge;     // [nbnd] edges of marks 2-4
+  const int* grad;      // [2*Ne] device columns
+  const int* nke;
+  const int* eoff;
+  const int* dcoff;
+  const int* woff;
+  const int* ctop;      // [Nc] device order
+  const int* etop;      // [Ne]
+  const int* nfaces;    // [ncomp] computational columns
+  const int* fedge;     // [ncomp*F]
+  const int* normal;    // [ncomp*F]
+  const int* bnfaces;   // [ncell3] type-3 columns (device columns ncomp..)
+  const int* bfedge;    // [ncell3*F]
+  const int* bnormal;   // [ncell3*F]
+  const int* mark;      // [Ne]
+  const double* n1;     // [Ne]
+  const double* n2;
+  const double* dzz;    // [n3]
+  const double* dzf;    // [ne3]
+  const double* dg;
+  const double* df;
+  const double* Ac;     // [Nc] device order
+  const double* dv;     // [Nc] device order
+  const double* tau_T;  // [Ne]
+  const double* CdT;
+  const double* CdB;
+  const double* nu_tv;  // [n3]
+  const double* nu_lax; // [n3]
+  const double* w;      // [nw3]
+  const double* u;      // [ne3] u at step n (read)
+  double* h;            // [Nc] device order
+  double* utmp;         // [ne3]
+  double* E;            // [ne3]
+  double* D;            // [Ne]
+  double* htmp;         // [Nc] device order (computational columns written)
+  double* u_out;        // [ne3]
+  unsigned char* active;  // [Nc] device order
+  int* nnan;            // [1] NaN count of utmp
+};
+
+cudaError_t launch_upred_vertical(const UPredArgs& a, cudaStream_t st);
+cudaError_t launch_upred_rhs(const UPredArgs& a, cudaStream_t st);
+cudaError_t launch_upred_open_fluxes(const UPredArgs& a, cudaStream_t st);
+cudaError_t launch_upred_velocity(const UPredArgs& a, cudaStream_t st);
+cudaError_t launch_upred_boundary(const UPredArgs& a, cudaStream_t st);
+
 cudaError_t launch_update_dz(const VGridArgs& a, cudaStream_t st);
 cudaError_t launch_set_flux_height(const VGridArgs& a, cudaStream_t st);
 cudaError_t launch_qsource(const StepArgs& a, cudaStream_t st);
