@@ -89,7 +89,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "step"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "step", "upred"])
     ap.add_argument("--no-mixed", action="store_true", help="cfg2: skip the mixed_form measurement")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--cfg3-points", type=int, default=500_000, help="cfg3: random points (domain scaled to keep the density)")
@@ -717,16 +717,86 @@ def bench_step(args):
     return line
 
 
+def bench_upred(args):
+    """UPredictor (main/phys.c:2579-3077) on the default grid: the vertical
+    predictor of every computational edge, the free-surface right-hand side,
+    CGSolve and the velocity update, end to end through the C ABI."""
+    from suntans_gb300 import gridgen as gg
+    from suntans_gb300.capi import Context
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    g, qp, hp, props, desc = make_workload(args)
+    uf = gg.make_upred_fields(g, seed=19)
+    vf = gg.make_vgrid_fields(g, seed=20)
+    ctx = Context(g, device=local)
+    ctx.step_grid(uf)
+    ctx.upredictor_grid(uf)
+    for _ in range(args.warmup):
+        ctx.upredictor(uf, vf, props)
+    sampler = ClockSampler(local)
+    sampler.start()
+    whole, iters, vert, rhs = [], [], [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = ctx.upredictor(uf, vf, props)
+        whole.append(time.perf_counter() - t0)
+        iters.append(r["niters"])
+    for _ in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        ut, E, D = ctx.upredictor_vertical(uf, props)
+        vert.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        ctx.upredictor_rhs(uf, props, ut)
+        rhs.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    ctx.close()
+    levels = int(sum(int(g.Nke[j] - uf.etop[j]) for j in uf.edgep))
+    # kernels per whole-predictor call: zero D, predictor, NaN count; UpdateDZ (2) twice; open-boundary fluxes,
+    # right-hand side, CGSolve (one persistent launch); dry clip, edge velocity; type-2 and type-3 boundaries
+    nbnd = int(uf.bedgedist[5] - uf.bedgedist[2])
+    nb2 = int(uf.bedgedist[3] - uf.bedgedist[2])
+    per_call = int(3 + 2 + (nbnd > 0) + 1 + 1 + 2 + 2 + (nb2 > 0) + int(g.celldist[2] > g.celldist[1]))
+    N = g.n_h()
+    t_w = float(np.median(whole))
+    it = int(np.median(iters))
+    n3, ne3, nw3 = g.n3, int(g.Nke.sum()), int((g.Nk + 1).sum())
+    line = {"metric": "UPredictor end to end (vertical predictor + free-surface rhs + CGSolve + velocity update), "
+                      "unknown-iters/s of its CGSolve at 1e-10",
+            "value": N * it / t_w, "unit": "unknown-iters/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_w * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid, velocities, drag, viscosity)",
+            "config": {**desc, "workload": desc["workload"] + "; UPredictor", "iters_h": it,
+                       "predictor_edge_levels": levels},
+            "vertical_predictor_call_ms": float(np.median(vert)) * 1e3,
+            "rhs_call_ms": float(np.median(rhs)) * 1e3,
+            "e2e": {"value": N * it / t_w, "unit": "unknown-iters/s",
+                    "h2d_bytes_per_step": 8 * (3 * n3 + 3 * ne3 + nw3 + 2 * g.Nc + 3 * g.Ne) + 4 * (g.Nc + g.Ne),
+                    "d2h_bytes_per_step": 8 * (n3 + 3 * ne3 + g.Nc + g.Ne) + 4 * (g.Nc + g.Ne) + g.Nc},
+            "gpu_launches": per_call * args.steps, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        from oracle.oracle import Oracle
+        o = Oracle("port")
+        t0 = time.perf_counter()
+        o.upredictor_vertical(uf, props)
+        t_v = time.perf_counter() - t0
+        line["vertical_predictor_cpu_ms"] = t_v * 1e3
+        line["cpu_baseline"] = {"value": levels / t_v, "unit": "predictor edge-levels/s", "cores": 1, "kind": "port",
+                                "sample": "the oracle's vertical predictor (bit-identical to the reference) on every "
+                                          "computational edge of the full grid, one core"}
+        line["vertical_predictor_edge_levels_per_s"] = levels / (float(np.median(vert)))
+    return line
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload in ("cfg3", "cfg4", "cfg5", "step"):
+    elif args.workload in ("cfg3", "cfg4", "cfg5", "step", "upred"):
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         import __graft_entry__
         __graft_entry__.build()
-        fn = {"cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5, "step": bench_step}[args.workload]
+        fn = {"cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5, "step": bench_step,
+              "upred": bench_upred}[args.workload]
         line = fn(args)
         if int(os.environ.get("RANK", "0")) == 0:
             print(json.dumps(line), flush=True)

@@ -758,6 +758,9 @@ int sgpu_step_grid(sgpu_context* ctx, const int* normal, const int* grad, const 
       return fail(ctx, SGPU_BAD_GRID, "computational edge %d lacks a cell on one side", e);
     ce.push_back(e);
   }
+  // deepest edges first: the per-edge kernels (UPredictor's vertical solve, Corrector) stride over this list,
+  // so each thread gets a like share of levels and the lanes of a warp have like column lengths
+  std::stable_sort(ce.begin(), ce.end(), [&](int x, int y) { return ctx->Nke[x] > ctx->Nke[y]; });
   ctx->woff.assign(Nc + 1, 0);
   for (int j = 0; j < Nc; ++j) ctx->woff[j + 1] = ctx->woff[j] + ctx->Nk[ctx->dev2cell[j]] + 1;
   ctx->nw3 = ctx->woff[Nc];

@@ -328,14 +328,32 @@ static int blocks_for(long long n, int bs) {
   return (int)std::max(1LL, std::min(b, 152LL * 16));
 }
 
+// one wave: every SM holds as many CTAs as fit, and the threads stride over
+// the computational edges (sorted deepest first), so no partial second wave
+// leaves SMs idle at the end
+template <int KMAX>
+static void vertical_launch(const UPredArgs& a, cudaStream_t st) {
+  static int per_sm = -1, nsm = 0;
+  if (per_sm < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, upred_vertical_kernel<KMAX>, 128, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+  }
+  const long long need = (a.ncedge + 127) / 128;
+  const int nb = (int)std::max(1LL, std::min(need, (long long)per_sm * std::max(nsm, 1)));
+  upred_vertical_kernel<KMAX><<<nb, 128, 0, st>>>(a);
+}
+
 cudaError_t launch_upred_vertical(const UPredArgs& a, cudaStream_t st) {
   upred_zero_d_kernel<<<blocks_for(a.Ne, 256), 256, 0, st>>>(a);
   if (a.ncedge > 0) {
-    const int nb = blocks_for(a.ncedge, 128);
-    if (a.kmax <= 16) upred_vertical_kernel<16><<<nb, 128, 0, st>>>(a);
-    else if (a.kmax <= 32) upred_vertical_kernel<32><<<nb, 128, 0, st>>>(a);
-    else if (a.kmax <= 64) upred_vertical_kernel<64><<<nb, 128, 0, st>>>(a);
-    else upred_vertical_kernel<128><<<nb, 128, 0, st>>>(a);
+    if (a.kmax <= 16) vertical_launch<16>(a, st);
+    else if (a.kmax <= 32) vertical_launch<32>(a, st);
+    else if (a.kmax <= 64) vertical_launch<64>(a, st);
+    else vertical_launch<128>(a, st);
   }
   upred_nan_kernel<<<blocks_for(a.Ne, 256), 256, 0, st>>>(a);
   return cudaGetLastError();

@@ -1,15 +1,21 @@
 #!/bin/sh
 # Redirects the two elliptic solves of a SUNTANS main/phys.c to the GPU
-# adapter (sgpu_suntans.c).  Usage:  sh patch_phys.sh path/to/main/phys.c [step]
+# adapter (sgpu_suntans.c).  Usage:  sh patch_phys.sh path/to/main/phys.c [step] [upred]
 # Edits in place and keeps phys.c.orig.  Exactly two call sites change:
 #   Solve       main/phys.c:1280  CGSolveQ(phys->qc,phys->stmp,phys->stmp3,...)
 #   UPredictor  main/phys.c:2989  CGSolve(grid,phys,prop,myproc,numprocs,comm)
 # With "step", the two steps around CGSolveQ in Solve move to the GPU too:
 #   main/phys.c:1274  ComputeQSource(phys->stmp,...)
 #   main/phys.c:1289  Corrector(phys->qc,...)
+# With "upred", the whole predictor does (its call in Solve):
+#   main/phys.c:1170  UPredictor(grid,phys,prop,myproc,numprocs,comm)
 set -e
 f="$1"
-[ -f "$f" ] || { echo "usage: $0 main/phys.c [step]" >&2; exit 2; }
+[ -f "$f" ] || { echo "usage: $0 main/phys.c [step] [upred]" >&2; exit 2; }
+step=0; upred=0
+for a in "$2" "$3"; do
+  case "$a" in step) step=1 ;; upred) upred=1 ;; "") ;; *) echo "unknown mode $a" >&2; exit 2 ;; esac
+done
 cp "$f" "$f.orig"
 sed -i \
   -e 's/^\([[:space:]]*\)CGSolveQ(phys->qc,phys->stmp,phys->stmp3,grid,phys,prop,myproc,numprocs,comm);/\1sgpu_CGSolveQ(phys->qc,phys->stmp,phys->stmp3,grid,phys,prop,myproc,numprocs,comm);/' \
@@ -19,7 +25,14 @@ sed -i \
 sed -i '0,/^#include "phys.h"/s//#include "phys.h"\
 void sgpu_CGSolveQ(REAL **q, REAL **src, REAL **c, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);\
 void sgpu_CGSolve(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);/' "$f"
-if [ "$2" = "step" ]; then
+if [ "$upred" = 1 ]; then
+  sed -i -e 's/^\([[:space:]]*\)UPredictor(grid,phys,prop,myproc,numprocs,comm);/\1sgpu_UPredictor(grid,phys,prop,myproc,numprocs,comm);/' "$f"
+  sed -i '0,/^#include "phys.h"/s//#include "phys.h"\
+void sgpu_UPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);/' "$f"
+  m=$(grep -c 'sgpu_UPredictor' "$f")
+  [ "$m" -ge 2 ] || { echo "patch_phys.sh: UPredictor call site not found ($m)" >&2; mv "$f.orig" "$f"; exit 1; }
+fi
+if [ "$step" = 1 ]; then
   sed -i \
     -e 's/^\([[:space:]]*\)ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);/\1sgpu_ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);/' \
     -e 's/^\([[:space:]]*\)Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);/\1sgpu_Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);/' \

@@ -23,6 +23,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 
+#include "boundaries.h"
 #include "grid.h"
 #include "phys.h"
 #include "suntans_gb300.h"
@@ -157,4 +158,86 @@ void sgpu_Corrector(REAL **qc, gridT *grid, physT *phys, propT *prop, int myproc
   rc = sgpu_corrector(g_ctx, grid->ctop, grid->etop, (const double *const *)grid->dzz, (const double *const *)qc,
                       phys->D, prop->dt, phys->u, phys->w, phys->q);
   if (rc != SGPU_OK) sgpu_die("sgpu_corrector", rc);
+}
+
+/* UPredictor (declared static at main/phys.c:39-40, defined 2579, called from
+ * Solve at 1170) with the reference's parameter list.  The vertical predictor
+ * (U***, E, D), the free-surface right-hand side, CGSolve and the steps after
+ * it run on the device; the model's own BoundaryVelocities and
+ * OpenBoundaryFluxes run on the host between them, where the reference calls
+ * them, because they read the case's boundary data.  Needs cgsolver 1 and a
+ * nonlinear free surface (linearFS 0).  Same bits as the reference apart from
+ * CGSolve's parity bound. */
+static gridT *g_up_grid = NULL;
+
+void sgpu_UPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm) {
+  sgpu_upred_fields f;
+  sgpu_props p;
+  sgpu_vgrid v;
+  int rc, i, j, jptr, k;
+  sgpu_ensure_step(grid, numprocs);
+  if (prop->cgsolver != 1 || prop->linearFS) {
+    fprintf(stderr, "sgpu: UPredictor on the GPU needs cgsolver 1 and linearFS 0\n");
+    exit(EXIT_FAILURE);
+  }
+  if (g_up_grid != grid) {
+    rc = sgpu_upredictor_grid(g_ctx, grid->edgep, grid->edgedist, grid->mark, grid->n1, grid->n2, grid->face,
+                              grid->normal);
+    if (rc != SGPU_OK) sgpu_die("sgpu_upredictor_grid", rc);
+    g_up_grid = grid;
+  }
+  for (i = 0; i < grid->Nc; i++) /* 2595-2598 */
+    for (k = 0; k < grid->Nk[i] + 1; k++) phys->wtmp2[i][k] = phys->w[i][k];
+  for (j = 0; j < grid->Ne; j++) /* 2600-2604 */
+    for (k = 0; k < grid->Nke[j]; k++) phys->utmp2[j][k] = phys->u[j][k];
+  for (jptr = grid->edgedist[2]; jptr < grid->edgedist[3]; jptr++) { /* 2611-2618 */
+    j = grid->edgep[jptr];
+    for (k = grid->etop[j]; k < grid->Nke[j]; k++) phys->utmp[j][k] = phys->u[j][k];
+  }
+  f.u = (const double *const *)phys->u;
+  f.w = (const double *const *)phys->w;
+  f.nu_tv = (const double *const *)phys->nu_tv;
+  f.nu_lax = (const double *const *)phys->nu_lax;
+  f.tau_T = phys->tau_T;
+  f.CdT = phys->CdT;
+  f.CdB = phys->CdB;
+  f.nu = prop->nu;
+  f.laxWendroff_Vertical = prop->laxWendroff_Vertical;
+  f.thetaM = prop->thetaM;
+  f.nonlinear = prop->nonlinear;
+  sgpu_props_from(prop, &p);
+  rc = sgpu_upredictor_vertical(g_ctx, grid->ctop, grid->etop, (const double *const *)grid->dzz,
+                                (const double *const *)grid->dzf, phys->h, &f, &p, phys->utmp, phys->ut, phys->D);
+  if (rc == SGPU_BREAKDOWN) {
+    printf("Error in function Predictor (U***=nan): %s\n", sgpu_last_error(g_ctx));
+    exit(EXIT_FAILURE);
+  }
+  if (rc != SGPU_OK) sgpu_die("sgpu_upredictor_vertical", rc);
+  BoundaryVelocities(grid, phys, prop, myproc, comm); /* 2961-2962 */
+  OpenBoundaryFluxes(NULL, phys->utmp, NULL, grid, phys, prop);
+  rc = sgpu_upredictor_rhs(g_ctx, grid->etop, (const double *const *)grid->dzf, (const double *const *)phys->u,
+                           (const double *const *)phys->utmp, phys->h, &p, phys->htmp);
+  if (rc != SGPU_OK) sgpu_die("sgpu_upredictor_rhs", rc);
+  sgpu_CGSolve(grid, phys, prop, myproc, numprocs, comm);
+  /* UpdateDZ's first block (option 0, 826-839): the old vertical grid */
+  for (j = 0; j < grid->Ne; j++) grid->etopold[j] = grid->etop[j];
+  for (i = 0; i < grid->Nc; i++) {
+    grid->ctopold[i] = grid->ctop[i];
+    for (k = 0; k < grid->ctop[i]; k++) grid->dzzold[i][k] = 0;
+    for (k = grid->ctop[i]; k < grid->Nk[i]; k++) grid->dzzold[i][k] = grid->dzz[i][k];
+  }
+  v.dz = grid->dz;
+  v.dv = grid->dv;
+  v.dzbot = grid->dzbot;
+  v.Nkc = grid->Nkc;
+  v.smoothbot = grid->smoothbot;
+  v.dzsmall = grid->dzsmall;
+  rc = sgpu_upredictor_finish(g_ctx, &v, &p, grid->ctop, grid->etop, grid->dzz, (const double *const *)phys->utmp,
+                              (const double *const *)phys->ut, phys->h, phys->active, phys->u);
+  if (rc != SGPU_OK) sgpu_die("sgpu_upredictor_finish", rc);
+  for (i = 0; i < grid->Nc; i++) /* 2993-3002 */
+    if (!phys->active[i])
+      phys->s[i][grid->Nk[i] - 1] = 0;
+    else
+      phys->hcorr[i] = 0;
 }

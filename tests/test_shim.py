@@ -62,3 +62,30 @@ def test_patch_step_mode_and_compile(tmp_path):
     syms = subprocess.run(["nm", str(tmp_path / "shim.o")], capture_output=True, text=True).stdout
     for s_ in ("sgpu_ComputeQSource", "sgpu_Corrector", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_step_grid"):
         assert s_ in syms
+
+
+def test_patch_upred_mode_and_compile(tmp_path):
+    """With "upred", the predictor's call in Solve moves to the adapter; the
+    model's boundary functions stay where the reference calls them."""
+    phys = tmp_path / "phys.c"
+    shutil.copy(os.path.join(REF, "phys.c"), phys)
+    r = subprocess.run(["sh", os.path.join(SHIM, "patch_phys.sh"), str(phys), "step", "upred"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    new = phys.read_text()
+    assert new.count("sgpu_UPredictor(grid,phys,prop,myproc,numprocs,comm);") == 1
+    old = open(os.path.join(REF, "phys.c")).read()
+    diff = [a for a in new.splitlines() if "sgpu_" not in a]
+    assert diff == [a for a in old.splitlines()
+                    if not a.strip().startswith(("CGSolveQ(phys->qc", "CGSolve(grid", "ComputeQSource(phys->stmp",
+                                                 "Corrector(phys->qc", "UPredictor(grid,phys"))]
+    cc = ["gcc", "-fcommon", "-DNOMPI", "-DNONETCDF", "-w", f"-I{REF}", f"-I{ROOT}/include", "-c"]
+    r = subprocess.run(cc + [str(phys), "-o", str(tmp_path / "phys.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(cc + [os.path.join(SHIM, "sgpu_suntans.c"), "-o", str(tmp_path / "shim.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    syms = subprocess.run(["nm", str(tmp_path / "shim.o")], capture_output=True, text=True).stdout
+    for s in ("sgpu_UPredictor", "sgpu_upredictor_vertical", "sgpu_upredictor_rhs", "sgpu_upredictor_finish",
+              "BoundaryVelocities", "OpenBoundaryFluxes"):
+        assert s in syms
