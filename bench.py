@@ -566,6 +566,10 @@ def bench_cfg4(args):
             "plain_fp64_loop_device_ms": dev_ms, "plain_fp64_loop_wall_ms": loop_s * 1e3,
             "speedup_vs_plain_fp64_loop": equiv / plain_rate,
             "iters_inner_over_fp64": float(itm.sum() / it64.sum()),
+            "launch_ms_per_step": [float(v) for v in per],
+            "iters_inner_quantiles": [int(v) for v in np.quantile(itm, [0, 0.25, 0.5, 0.75, 1.0])],
+            "unknowns_quantiles": [int(v) for v in np.quantile(Ns, [0, 0.25, 0.5, 0.75, 1.0])],
+            "work_weighted_mean_iters": float((Ns * itm).sum() / Ns.sum()),
             "errors": {"max_rel_l2": max(e["rel_l2"] for e in errs),
                        "max_abs_rel": max(e["max_abs_rel"] for e in errs),
                        "status_ok": int(sum(st.status == 0 for _, st in res))},

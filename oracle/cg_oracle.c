@@ -999,3 +999,150 @@ int sgo_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
   layout_free(L);
   return nnan;
 }
+
+/* ------------------------------------------------------------------------
+ * WPredictor, main/phys.c:2025-2287, for grids without type-2 / type-4 edges
+ * and nonlinear 0 or 1.  The reference keeps its scratch column a (phys->a)
+ * across cells; with conserveMomentum it reads a[k] for levels above the
+ * cell's top (2137-2138), so the column is kept across cells here too.
+ * Where a cell is deeper than a face's edge the reference reads phys->ut and
+ * utmp2 past the edge's Nke levels (2131-2133), memory nothing in the step
+ * writes (zero at allocation); those terms are 0 here.
+ * ------------------------------------------------------------------------ */
+int sgo_wpredictor(const sgo_grid *g, const sgo_ext *x, const sgo_wpred *wp, const sgo_prop *p, double *w,
+                   double *Cn_W, double *Cn_W2) {
+  layout_t Lv, *L = &Lv;
+  long *woff;
+  int i, iptr, j, jptr, k, nf, ne, nc1, nc2, kmin;
+  double fab1, fab2, fab3, *a, *b, *c, *wtmp, *stmp, *wc, *ut;
+  const double dt = p->dt;
+  if (wp->nonlinear != 0 && wp->nonlinear != 1) return -1;
+  layout_make(g, L);
+  woff = woff_make(g);
+#define W(i, k) w[woff[(i)] + (k)]
+  a = (double *)calloc(g->Nkmax + 2, sizeof(double));
+  b = (double *)calloc(g->Nkmax + 2, sizeof(double));
+  c = (double *)calloc(g->Nkmax + 2, sizeof(double));
+  wtmp = (double *)calloc(L->n3 + 1, sizeof(double));
+  stmp = (double *)calloc(L->n3 + 1, sizeof(double));
+  wc = (double *)calloc(L->n3 + 1, sizeof(double));
+  ut = (double *)calloc(L->eoff[g->Ne] + 1, sizeof(double));
+  if (wp->n == 1) {                                                                /* 2044-2067 */
+    fab1 = 1;
+    fab2 = fab3 = 0;
+    for (i = 0; i < g->Nc; i++)
+      for (k = 0; k < g->Nk[i]; k++) X3(Cn_W, i, k) = X3(Cn_W2, i, k) = 0;
+  } else if (wp->n == 2 || wp->AB == 2) {
+    fab1 = 3.0 / 2.0;
+    fab2 = -1.0 / 2.0;
+    fab3 = 0;
+  } else {
+    fab1 = 23.0 / 12.0;
+    fab2 = -4.0 / 3.0;
+    fab3 = 5.0 / 12.0;
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {                     /* 2071-2089 */
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) {
+      X3(wtmp, i, k) = W(i, k) + fab2 * X3(Cn_W, i, k) + fab3 * X3(Cn_W2, i, k);
+      X3(Cn_W2, i, k) = X3(Cn_W, i, k);
+      X3(Cn_W, i, k) = 0;
+    }
+    for (k = g->ctop[i] + 1; k < g->Nk[i]; k++)
+      X3(wtmp, i, k) -= 2.0 * dt / (DZZ(i, k - 1) + DZZ(i, k)) * (X3(wp->q, i, k - 1) - X3(wp->q, i, k));
+    X3(wtmp, i, g->ctop[i]) += 2.0 * dt / DZZ(i, g->ctop[i]) * X3(wp->q, i, g->ctop[i]);
+  }
+  if (wp->nonlinear) {                                                             /* 2095-2146 */
+    for (i = 0; i < g->Nc; i++)
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(wc, i, k) = 0.5 * (W(i, k) + W(i, k + 1));
+    /* GetMomentumFaceValues, first-order upwind (4879-4968) */
+    for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++) {
+      j = x->edgep[jptr];
+      nc1 = x->grad[2 * j];
+      nc2 = x->grad[2 * j + 1];
+      kmin = g->ctop[nc1] > g->ctop[nc2] ? g->ctop[nc1] : g->ctop[nc2];
+      for (k = 0; k < kmin && k < g->Nke[j]; k++) UE(ut, j, k) = 0;
+      for (k = kmin; k < g->Nke[j]; k++) UE(ut, j, k) = UE(wp->utmp2, j, k) > 0 ? X3(wc, nc2, k) : X3(wc, nc1, k);
+    }
+    /* faces of type-3 cells: the same first-order upwind values */
+    if (wp->conserveMomentum)
+      for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++) {
+        j = x->edgep[jptr];
+        for (k = x->etop[j]; k < g->Nke[j]; k++) UE(ut, j, k) *= DZF(j, k);
+      }
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) a[k] = wp->conserveMomentum ? DZZ(i, k) : 1.0;
+      for (nf = 0; nf < g->nfaces[i]; nf++) {
+        const double nrm = x->normal[i * g->maxfaces + nf];
+        ne = g->face[i * g->maxfaces + nf];
+        for (k = g->ctop[i]; k < g->Nk[i] && k < g->Nke[ne]; k++)
+          X3(stmp, i, k) += UE(ut, ne, k) * UE(wp->utmp2, ne, k) * g->df[ne] * nrm / (a[k] * g->Ac[i]);
+        if (wp->conserveMomentum)
+          for (k = x->etop[ne]; k < g->ctop[i]; k++)
+            X3(stmp, i, g->ctop[i]) += UE(ut, ne, k) * UE(wp->utmp2, ne, k) * g->df[ne] * nrm / (a[k] * g->Ac[i]);
+      }
+      for (k = g->ctop[i]; k < g->Nk[i]; k++)    /* pow(w,2) is w*w */
+        X3(stmp, i, k) += (W(i, k) * W(i, k) - W(i, k + 1) * W(i, k + 1)) / DZZ(i, k);
+    }
+  }
+  for (jptr = x->edgedist[0]; jptr < x->edgedist[1]; jptr++) {                     /* 2159-2185 */
+    j = x->edgep[jptr];
+    nc1 = x->grad[2 * j];
+    nc2 = x->grad[2 * j + 1];
+    kmin = g->ctop[nc1] > g->ctop[nc2] ? g->ctop[nc1] : g->ctop[nc2];
+    for (k = kmin; k < g->Nke[j]; k++) {
+      a[k] = .5 * (wp->nu_H + 0.5 * (X3(wp->nu_lax, nc1, k) + X3(wp->nu_lax, nc2, k))) *
+             (W(nc2, k) - W(nc1, k) + W(nc2, k + 1) - W(nc1, k + 1)) * g->df[j] / g->dg[j];
+      X3(stmp, nc1, k) -= a[k] / g->Ac[nc1];
+      X3(stmp, nc2, k) += a[k] / g->Ac[nc2];
+    }
+    for (k = g->Nke[j]; k < g->Nk[nc1]; k++)
+      X3(stmp, nc1, k) += 0.25 * wp->CdW * fabs(W(nc1, k) + W(nc1, k + 1)) * (W(nc1, k) + W(nc1, k + 1)) * g->df[j] /
+                          g->Ac[nc1];
+    for (k = g->Nke[j]; k < g->Nk[nc2]; k++)
+      X3(stmp, nc2, k) += 0.25 * wp->CdW * fabs(W(nc2, k) + W(nc2, k + 1)) * (W(nc2, k) + W(nc2, k + 1)) * g->df[j] /
+                          g->Ac[nc2];
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {                     /* 2210-2220 */
+    i = g->cellp[iptr];
+    for (k = g->ctop[i] + 1; k < g->Nk[i]; k++)
+      X3(Cn_W, i, k) -= dt * (DZZ(i, k - 1) * X3(stmp, i, k - 1) + DZZ(i, k) * X3(stmp, i, k)) /
+                        (DZZ(i, k - 1) + DZZ(i, k));
+    k = g->ctop[i];
+    X3(Cn_W, i, k) -= dt * X3(stmp, i, k);
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {                     /* 2236-2241 */
+    i = g->cellp[iptr];
+    for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(wtmp, i, k) += fab1 * X3(Cn_W, i, k);
+  }
+  for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {                     /* 2246-2284 */
+    const int ct = g->ctop[i = g->cellp[iptr]], nk = g->Nk[i];
+    const double lv = wp->laxWendroff_Vertical;
+    if (nk - ct > 1) {
+      for (k = ct + 1; k < nk; k++) {
+        a[k] = 2 * (wp->nu + lv * X3(wp->nu_lax, i, k - 1) + X3(wp->nu_tv, i, k - 1)) / DZZ(i, k - 1) /
+               (DZZ(i, k) + DZZ(i, k - 1));
+        b[k] = 2 * (wp->nu + lv * X3(wp->nu_lax, i, k) + X3(wp->nu_tv, i, k)) / DZZ(i, k) / (DZZ(i, k) + DZZ(i, k - 1));
+      }
+      b[ct] = (wp->nu + lv * X3(wp->nu_lax, i, ct) + X3(wp->nu_tv, i, ct)) / (DZZ(i, ct) * DZZ(i, ct));
+      a[ct] = b[ct];
+      for (k = ct + 1; k < nk; k++)
+        X3(wtmp, i, k) += dt * (1 - p->theta) * (a[k] * W(i, k - 1) - (a[k] + b[k]) * W(i, k) + b[k] * W(i, k + 1));
+      X3(wtmp, i, ct) += dt * (1 - p->theta) * (-(a[ct] + b[ct]) * W(i, ct) + (a[ct] + b[ct]) * W(i, ct + 1));
+      for (k = ct; k < nk; k++) {
+        c[k] = 1 + dt * p->theta * (a[k] + b[k]);
+        a[k] *= (-dt * p->theta);
+        b[k] *= (-dt * p->theta);
+      }
+      b[ct] += a[ct];
+      trisolve(a + ct, c + ct, b + ct, &X3(wtmp, i, ct), &W(i, ct), nk - ct);
+    } else {
+      for (k = ct; k < nk; k++) W(i, k) = X3(wtmp, i, k);
+    }
+  }
+#undef W
+  free(a); free(b); free(c); free(wtmp); free(stmp); free(wc); free(ut); free(woff);
+  layout_free(L);
+  return 0;
+}

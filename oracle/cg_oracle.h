@@ -114,6 +114,18 @@ typedef struct sgo_ubnd {
   const double *n2;     /* [Ne] */
 } sgo_ubnd;
 
+/* WPredictor (main/phys.c:2025-2287): the fields it reads beyond the grid. */
+typedef struct sgo_wpred {
+  const double *q;      /* [n3] nonhydrostatic pressure                           */
+  const double *nu_tv;  /* [n3]                                                    */
+  const double *nu_lax; /* [n3]                                                    */
+  const double *utmp2;  /* [ne3] rows of Nke: the advecting face velocity          */
+  double nu, nu_H, CdW, laxWendroff_Vertical;
+  int nonlinear;        /* 0 or 1 (first-order upwind face values)                */
+  int conserveMomentum;
+  int n, AB;            /* propT.n (time step) and propT.AB (2 or 3)               */
+} sgo_wpred;
+
 /* ---- the restatement (cg_oracle.c) ---- */
 void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
                   const sgo_prop *p, sgo_result *res);
@@ -172,6 +184,14 @@ int sgo_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
                    const sgo_ubnd *b, const sgo_prop *p, double *u, double *h, double *utmp, double *E,
                    double *D, int *ctop, int *etop, double *dzz, unsigned char *active, sgo_result *res);
 
+/* WPredictor for a grid without type-2 or type-4 edges: w (rows of Nk+1) is
+   advanced on the computational cells; Cn_W and Cn_W2 (rows of Nk) are the
+   Adams-Bashforth histories, updated in place.  x->edgep / edgedist are the
+   computational edges, x->etop is read with conserveMomentum.  Returns 0, or
+   -1 for a nonlinear scheme other than 0 and 1. */
+int sgo_wpredictor(const sgo_grid *g, const sgo_ext *x, const sgo_wpred *wp, const sgo_prop *p, double *w,
+                   double *Cn_W, double *Cn_W2);
+
 /* ---- the reference itself (ref_harness.c, oracle/_ref only) ---- */
 void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, double *c,
                   const sgo_prop *p, sgo_result *res);
@@ -198,6 +218,8 @@ void ref_update_dz(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
 void ref_set_flux_height(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const double *h,
                          const double *u, double *dzz, double *dzf);
 
+int ref_wpredictor(const sgo_grid *g, const sgo_ext *x, const sgo_wpred *wp, const sgo_prop *p, double *w,
+                   double *Cn_W, double *Cn_W2);
 int ref_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, const sgo_upred *up,
                    const sgo_ubnd *b, const sgo_prop *p, double *u, double *h, double *utmp, double *E,
                    double *D, int *ctop, int *etop, double *dzz, unsigned char *active, sgo_result *res);

@@ -61,6 +61,12 @@ class SgoUbnd(C.Structure):
     _fields_ = [("edgep", _ip), ("edgedist", _ip), ("mark", _ip), ("n1", _dp), ("n2", _dp)]
 
 
+class SgoWpred(C.Structure):
+    _fields_ = [("q", _dp), ("nu_tv", _dp), ("nu_lax", _dp), ("utmp2", _dp), ("nu", C.c_double),
+                ("nu_H", C.c_double), ("CdW", C.c_double), ("laxWendroff_Vertical", C.c_double),
+                ("nonlinear", C.c_int), ("conserveMomentum", C.c_int), ("n", C.c_int), ("AB", C.c_int)]
+
+
 class SgoResult(C.Structure):
     _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double)]
 
@@ -392,6 +398,25 @@ class Oracle:
                                    active.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(res))
         return dict(u=u, h=h, utmp=utmp, E=E[:int(g.Nke.sum())], D=D[:g.Ne], ctop=ctop, etop=etop, dzz=dzz,
                     active=active, niters=res.niters, nnan=int(n))
+
+    # ---- WPredictor (main/phys.c:2025-2287) ----
+    def wpredictor(self, wf, props):
+        """Returns (w, Cn_W, Cn_W2) after one WPredictor."""
+        g = wf.grid
+        s, keep = self._grid(g)
+        x, kx = self._uext(wf, wf.etop)
+        kd = [np.ascontiguousarray(a, dtype=np.float64) for a in (wf.q, wf.nu_tv, wf.nu_lax, wf.utmp2)]
+        wp = SgoWpred(*[_ptr(a, _dp) for a in kd], wf.nu, wf.nu_H, wf.CdW, wf.laxWendroff_Vertical, wf.nonlinear,
+                      wf.conserveMomentum, wf.n, wf.AB)
+        w = np.array(wf.w, dtype=np.float64, copy=True)
+        cw = np.array(wf.Cn_W, dtype=np.float64, copy=True)
+        cw2 = np.array(wf.Cn_W2, dtype=np.float64, copy=True)
+        pr = self._prop(props)
+        rc = self._fn("wpredictor")(C.byref(s), C.byref(x), C.byref(wp), C.byref(pr), _ptr(w, _dp), _ptr(cw, _dp),
+                                    _ptr(cw2, _dp))
+        if rc != 0:
+            raise ValueError("wpredictor: unsupported settings")
+        return w, cw, cw2
 
     # ---- the reference's grid reader and field writers (ref library only) ----
     def read_grid(self, datadir: str) -> dict:

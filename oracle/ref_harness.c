@@ -551,3 +551,68 @@ int ref_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
   harness_free(&H);
   return 0;
 }
+
+/* The reference's WPredictor (main/phys.c:2025-2287).  Its edge loops read
+ * edgedist[0..5]; the harness passes the computational edges with empty
+ * ranges for marks 1-4.  phys->ut and utmp2 get rows of max(Nk) of the
+ * edge's cells (the model's Nkc), zero past Nke, as the model allocates them;
+ * Cn_W / Cn_W2 rows of Nk+1 are copied in and out of the caller's rows of Nk. */
+int ref_wpredictor(const sgo_grid *g, const sgo_ext *x, const sgo_wpred *wp, const sgo_prop *p, double *w,
+                   double *Cn_W, double *Cn_W2) {
+  harness_t H;
+  int i, j, k, ed[6], *nkc;
+  REAL **cw, **cw2, **ut2;
+  harness_init(&H, g, NULL, p);
+  harness_ext(&H, g, x);
+  ed[0] = x->edgedist[0];
+  ed[1] = ed[2] = ed[3] = ed[4] = ed[5] = x->edgedist[1];
+  H.grid.edgedist = ed;
+  nkc = (int *)blk_new(&H, sizeof(int) * (g->Ne + 1));
+  for (j = 0; j < g->Ne; j++) {
+    int c0 = x->grad[2 * j], c1 = x->grad[2 * j + 1], m = 0;
+    if (c0 >= 0 && g->Nk[c0] > m) m = g->Nk[c0];
+    if (c1 >= 0 && g->Nk[c1] > m) m = g->Nk[c1];
+    nkc[j] = m > g->Nke[j] ? m : g->Nke[j];
+  }
+  H.phys.a = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.b = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.c = (REAL *)blk_new(&H, sizeof(REAL) * (g->Nkmax + 2));
+  H.phys.w = wrow_view(&H, g, w);
+  H.phys.wtmp = jag_new(&H, g->Nc, g->Nk, 1);
+  H.phys.stmp = jag_new(&H, g->Nc, g->Nk, 0);
+  H.phys.wc = jag_new(&H, g->Nc, g->Nk, 0);
+  H.phys.ut = jag_new(&H, g->Ne, nkc, 0);
+  ut2 = jag_new(&H, g->Ne, nkc, 0);
+  for (j = 0; j < g->Ne; j++)
+    for (k = 0; k < g->Nke[j]; k++) ut2[j][k] = wp->utmp2[H.eoff[j] + k];
+  H.phys.utmp2 = ut2;
+  cw = jag_new(&H, g->Nc, g->Nk, 1);
+  cw2 = jag_new(&H, g->Nc, g->Nk, 1);
+  for (i = 0; i < g->Nc; i++)
+    for (k = 0; k < g->Nk[i]; k++) {
+      cw[i][k] = Cn_W[H.coff[i] + k];
+      cw2[i][k] = Cn_W2[H.coff[i] + k];
+    }
+  H.phys.Cn_W = cw;
+  H.phys.Cn_W2 = cw2;
+  H.phys.q = jag_view(&H, wp->q, H.coff, g->Nc);
+  H.phys.nu_tv = jag_view(&H, wp->nu_tv, H.coff, g->Nc);
+  H.phys.nu_lax = jag_view(&H, wp->nu_lax, H.coff, g->Nc);
+  H.phys.boundary_w = jag_new(&H, 1, g->Nk, 0);
+  H.prop.n = wp->n;
+  H.prop.AB = wp->AB;
+  H.prop.nonlinear = wp->nonlinear;
+  H.prop.conserveMomentum = wp->conserveMomentum;
+  H.prop.nu = wp->nu;
+  H.prop.nu_H = wp->nu_H;
+  H.prop.CdW = wp->CdW;
+  H.prop.laxWendroff_Vertical = wp->laxWendroff_Vertical;
+  WPredictor(&H.grid, &H.phys, &H.prop, 0, 1, 0);
+  for (i = 0; i < g->Nc; i++)
+    for (k = 0; k < g->Nk[i]; k++) {
+      Cn_W[H.coff[i] + k] = cw[i][k];
+      Cn_W2[H.coff[i] + k] = cw2[i][k];
+    }
+  harness_free(&H);
+  return 0;
+}

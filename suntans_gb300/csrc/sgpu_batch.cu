@@ -1421,6 +1421,7 @@ struct HostInst {
   std::vector<int> dev2cell, Nk, ctop, coff;  // device column -> cell; per cell Nk/ctop; device column -> relative slot
   std::vector<HostTile> tiles;
   long long unk = 0;                          // pressure unknowns: sum of Nk - ctop over computational cells
+  int last_iters = 0;                         // iterations of its last finished solve (0 = none yet)
 };
 
 }  // namespace sgpu
@@ -1908,6 +1909,15 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
   int ntiles = 0;
   int ninst = 0;
   bool tiles_changed = false;
+  // Tile t runs on CTA t mod G, so the tiles of the problems still iterating
+  // stay evenly spread over the CTAs as long as they are a prefix of the tile
+  // list: problems are laid out longest expected remaining solve first (their
+  // last solve's iteration count less the iterations done; problems never
+  // solved before count as longest, larger first).  A problem's reductions
+  // group its tiles by their index within the problem modulo G, so the order
+  // does not change any result.
+  std::vector<int> order;
+  std::vector<long long> key(b->max_inst, 0);
   for (int i = 0; i < b->max_inst; ++i) {
     HostInst& H = b->inst[i];
     BInst& I = b->h_inst[i];
@@ -1918,6 +1928,16 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
       I.t0 = I.t1 = 0;
       continue;
     }
+    key[i] = H.last_iters > 0 ? std::max(1, H.last_iters - (I.state == INST_RUN ? I.n : 0)) : (1LL << 40);
+    order.push_back(i);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    if (key[x] != key[y]) return key[x] > key[y];
+    return b->inst[x].unk > b->inst[y].unk;
+  });
+  for (int i : order) {
+    HostInst& H = b->inst[i];
+    BInst& I = b->h_inst[i];
     if (I.t0 != ntiles) tiles_changed = true;
     I.t0 = ntiles;
     for (const HostTile& T : H.tiles) {
@@ -2046,6 +2066,7 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     const BInst& I = b->h_inst[i];
     run += I.state == INST_RUN || I.state == INST_SETUP;
     work += b->inst[i].unk * (long long)(I.n - b->n_before[i]);
+    if (I.state == INST_DONE && I.n > 0) b->inst[i].last_iters = I.n;
   }
   b->last_work = work;
   if (running) *running = run;

@@ -241,6 +241,38 @@ class UPredFields:
 
 
 @dataclasses.dataclass
+class WPredFields:
+    """Inputs of WPredictor (main/phys.c:2025-2287) beyond the grid: w and its
+    Adams-Bashforth histories, the pressure, the viscosities, the advecting face
+    velocity and the propT settings it reads."""
+    grid: SunGrid
+    w: np.ndarray         # ragged per cell (Nk+1 levels)
+    Cn_W: np.ndarray      # ragged per cell (Nk levels)
+    Cn_W2: np.ndarray     # ragged per cell (Nk levels)
+    q: np.ndarray         # ragged per cell: nonhydrostatic pressure
+    nu_tv: np.ndarray
+    nu_lax: np.ndarray
+    utmp2: np.ndarray     # ragged per edge (Nke levels): advecting velocity
+    nu: float
+    nu_H: float
+    CdW: float
+    laxWendroff_Vertical: float
+    nonlinear: int        # 0 or 1
+    conserveMomentum: int
+    n: int                # time step index (1: first step)
+    AB: int               # 2 or 3
+    etop: np.ndarray      # [Ne]
+    edgep: np.ndarray     # computational edges
+    edgedist: np.ndarray  # [2]
+
+    @property
+    def woff(self) -> np.ndarray:
+        o = np.zeros(self.grid.Nc + 1, dtype=np.int64)
+        np.cumsum(self.grid.Nk + 1, out=o[1:])
+        return o
+
+
+@dataclasses.dataclass
 class SolverProps:
     """The propT fields the two solves read (main/phys.h:183-203)."""
     qprecond: int = 1

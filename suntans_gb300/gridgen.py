@@ -503,3 +503,19 @@ def make_upred_fields(g: SunGrid, seed=0, sigma_u=0.05, noslip_frac=0.2, nonline
                        thetaM=float(thetaM), nonlinear=int(nonlinear), etop=st.etop, edgep=st.edgep,
                        edgedist=st.edgedist, bedgep=bedgep, bedgedist=bedgedist, mark=mark.astype(I32),
                        n1=n1, n2=n2)
+
+
+def make_wpred_fields(g: SunGrid, seed=0, nonlinear=1, conserveMomentum=0, n=5, AB=3, nu=1e-6, nu_H=0.1,
+                      CdW=0.002, laxWendroff_Vertical=1.0) -> "WPredFields":
+    """Seeded inputs of WPredictor: w and u as the pressure step's, Adams-Bashforth
+    histories, a pressure field, vertical viscosities."""
+    from .grid import WPredFields
+    rng = np.random.default_rng(seed)
+    st = make_step_fields(g, seed=seed + 3)
+    Cn_W = rng.normal(0.0, 1e-4, g.n3)
+    Cn_W2 = rng.normal(0.0, 1e-4, g.n3)
+    return WPredFields(grid=g, w=st.w, Cn_W=Cn_W, Cn_W2=Cn_W2, q=st.q, nu_tv=rng.uniform(0.0, 1e-3, g.n3),
+                       nu_lax=rng.uniform(0.0, 1e-4, g.n3), utmp2=st.u, nu=float(nu), nu_H=float(nu_H),
+                       CdW=float(CdW), laxWendroff_Vertical=float(laxWendroff_Vertical), nonlinear=int(nonlinear),
+                       conserveMomentum=int(conserveMomentum), n=int(n), AB=int(AB), etop=st.etop, edgep=st.edgep,
+                       edgedist=st.edgedist)

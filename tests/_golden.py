@@ -56,5 +56,17 @@ def upred_fields(g, d, nl):
                        nonlinear=int(par[3]), **kw)
 
 
+def wpred_fields(g, d, tag):
+    """The WPredictor inputs stored with a fixture (tag "wp1_" or "wp0_")."""
+    from suntans_gb300.grid import WPredFields
+    g.grad, g.normal = d["grad"], d["normal"]
+    par = d[tag + "par"]
+    kw = {k: d[tag + k] for k in ("w", "Cn_W", "Cn_W2", "q", "nu_tv", "nu_lax", "utmp2")}
+    return WPredFields(grid=g, nu=float(par[0]), nu_H=float(par[1]), CdW=float(par[2]),
+                       laxWendroff_Vertical=float(par[3]), nonlinear=int(par[4]), conserveMomentum=int(par[5]),
+                       n=int(par[6]), AB=int(par[7]), etop=d["etop"], edgep=d["edgep"], edgedist=d["edgedist"],
+                       **kw)
+
+
 def props_for(props, **kw):
     return SolverProps(**{**props, **kw})

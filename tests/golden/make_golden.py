@@ -17,7 +17,9 @@ read, and the reference's outputs for:
   UpdateDZ (option 0) and SetFluxHeight (smoothbot 0 and 0.3) on a seeded
   free surface and edge velocity,
   UPredictor with CGSolve (main/phys.c:2579-3077) on seeded drag, viscosity
-  and velocity fields, with and without implicit vertical advection.
+  and velocity fields, with and without implicit vertical advection,
+  WPredictor (main/phys.c:2025-2287) with first-order upwind advection (AB3)
+  and without advection on the first step.
 The inputs are stored (not regenerated) so that the check is bit-exact on any
 host: tests/test_oracle.py runs the C restatement (oracle/cg_oracle.c) on them
 and requires identical bits.
@@ -117,6 +119,14 @@ def main():
             for k in ("u", "h", "utmp", "E", "D", "ctop", "etop", "dzz", "active"):
                 out[pre + "out_" + k] = r[k]
             out[pre + "out_niters"] = np.array(r["niters"])
+        for tag, kw in (("wp1_", dict(nonlinear=1, n=5, AB=3)), ("wp0_", dict(nonlinear=0, n=1, AB=3))):
+            wf = gg.make_wpred_fields(g, seed=38, **kw)
+            for k in ("w", "Cn_W", "Cn_W2", "q", "nu_tv", "nu_lax", "utmp2"):
+                out[tag + k] = getattr(wf, k)
+            out[tag + "par"] = np.array([wf.nu, wf.nu_H, wf.CdW, wf.laxWendroff_Vertical, wf.nonlinear,
+                                         wf.conserveMomentum, wf.n, wf.AB])
+            w, cw, cw2 = ref.wpredictor(wf, SolverProps(**props))
+            out.update({tag + "out_w": w, tag + "out_Cn_W": cw, tag + "out_Cn_W2": cw2})
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
         print(f"{path}: Nc={g.Nc} n3={g.n3} iters q={[int(out[f'n_qp{k}']) for k in range(3)]} "

@@ -185,3 +185,32 @@ def test_port_upredictor_matches_reference_library(port, case):
     a, b = port.upredictor(uf, vf, pr), ref.upredictor(uf, vf, pr)
     for k in a:
         assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+
+
+@pytest.mark.parametrize("name", fixture_names())
+@pytest.mark.parametrize("tag", ["wp1_", "wp0_"])
+def test_port_wpredictor_matches_golden_bitwise(port, name, tag):
+    """WPredictor (Adams-Bashforth, pressure gradient, upwind advection,
+    horizontal diffusion and wall drag, the vertical diffusion solve)
+    reproduces the reference's bits."""
+    from tests._golden import wpred_fields
+    g, qp, hp, props, d = load(name)
+    wf = wpred_fields(g, d, tag)
+    w, cw, cw2 = port.wpredictor(wf, props_for(props))
+    assert np.array_equal(w, d[tag + "out_w"]) and np.array_equal(cw, d[tag + "out_Cn_W"])
+    assert np.array_equal(cw2, d[tag + "out_Cn_W2"])
+    assert np.any(w != wf.w)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(nonlinear=0), dict(n=1), dict(n=2), dict(AB=2),
+                                dict(conserveMomentum=1), dict(CdW=0.0, nu_H=0.0)])
+def test_port_wpredictor_matches_reference_library(port, kw):
+    if not om.available("ref"):
+        pytest.skip("reference library not built here")
+    ref = Oracle("ref")
+    g = gg.delaunay_seamount(400, 3000, 1500, Nkmax=10, sigma=400, ctop_frac=0.3, h_sigma=0.05, open_x0=True,
+                             seed=44)
+    wf = gg.make_wpred_fields(g, seed=45, **kw)
+    pr = h_props(1, dt=10.0)
+    for a, b in zip(port.wpredictor(wf, pr), ref.wpredictor(wf, pr)):
+        assert np.array_equal(a, b)
