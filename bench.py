@@ -686,6 +686,13 @@ def bench_step(args):
         ctx.update_dz(vf)
         ctx.set_flux_height(vf)
         vg.append(time.perf_counter() - t0)
+    # WPredictor, the step before ComputeQSource, through its drop-in call
+    wf = gg.make_wpred_fields(g, seed=19)
+    wpt = []
+    for _ in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        ctx.wpredictor(wf, props)
+        wpt.append(time.perf_counter() - t0)
     clocks = sampler.stop()
     ctx.close()
     N = g.n_q()
@@ -700,6 +707,7 @@ def bench_step(args):
             "config": {**desc, "workload": desc["workload"] + "; pressure step", "iters_q": it},
             "separate_calls_ms": t_s * 1e3, "fused_speedup_vs_separate": t_s / t_f,
             "vertical_grid_refresh_ms": float(np.median(vg)) * 1e3,
+            "wpredictor_ms": float(np.median(wpt)) * 1e3,
             "e2e": {"value": N * it / t_f, "unit": "unknown-iters/s",
                     "h2d_bytes_per_step": 8 * (4 * n3 + 3 * ne3 + 2 * nw3) + 4 * (g.Nc + g.Ne),
                     "d2h_bytes_per_step": 8 * (2 * n3 + ne3 + nw3)},
@@ -715,6 +723,9 @@ def bench_step(args):
         o.update_dz(vf)
         o.set_flux_height(vf)
         line["vertical_grid_refresh_cpu_ms"] = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        o.wpredictor(wf, props)
+        line["wpredictor_cpu_ms"] = (time.perf_counter() - t0) * 1e3
         cb = cpu_baseline(g, qp, None, props, args.cpu_seconds)
         cb["sample"] += f"; ComputeQSource + Corrector on the full grid took {t_qc:.2f} s more per step"
         line["cpu_baseline"] = cb

@@ -175,6 +175,27 @@ int sgpu_update_dz(sgpu_context *ctx, const sgpu_vgrid *v, const double *h, int 
 int sgpu_set_flux_height(sgpu_context *ctx, const sgpu_vgrid *v, const int *etop, const double *h,
                          const double *const *u, double *const *dzz, double *const *dzf);
 
+/* ---- WPredictor (main/phys.c:2025-2287): the vertical-velocity predictor ---- */
+
+typedef struct sgpu_wpred_fields {
+  const double *const *q;      /* [Nc] rows of Nk: nonhydrostatic pressure phys->q           */
+  const double *const *nu_tv;  /* [Nc] rows of Nk                                              */
+  const double *const *nu_lax; /* [Nc] rows of Nk                                              */
+  const double *const *utmp2;  /* [Ne] rows of Nke: advecting velocity (read when nonlinear)   */
+  double nu, nu_H, CdW, laxWendroff_Vertical; /* propT                                        */
+  int nonlinear;               /* 0 or 1 on the device                                         */
+  int conserveMomentum;        /* 0 on the device                                              */
+  int n, AB;                   /* propT.n (1 = first step) and propT.AB                        */
+} sgpu_wpred_fields;
+
+/* WPredictor drop-in for grids without type-2 or type-4 edges: w (rows of
+ * Nk+1) advances on the computational cells and the Adams-Bashforth histories
+ * Cn_W, Cn_W2 (rows of at least Nk) are updated in place; prop gives dt and
+ * theta.  Needs sgpu_step_grid, whose edge list sets the order of the
+ * horizontal-diffusion sums.  Same bits as the reference. */
+int sgpu_wpredictor(sgpu_context *ctx, const int *ctop, const double *const *dzz, const sgpu_wpred_fields *f,
+                    const sgpu_props *prop, double *const *w, double *const *Cn_W, double *const *Cn_W2);
+
 /* ---- UPredictor (main/phys.c:2579-3077): the predictor around CGSolve ---- */
 
 /* The edge description UPredictor's boundary steps read, once per grid: every

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libsuntans_gb300.so")
-SOURCES = ["sgpu_api.cu", "sgpu_q.cu", "sgpu_h.cu", "sgpu_batch.cu", "sgpu_noalloc.cu", "sgpu_step.cu", "sgpu_upred.cu"]
+SOURCES = ["sgpu_api.cu", "sgpu_q.cu", "sgpu_h.cu", "sgpu_batch.cu", "sgpu_noalloc.cu", "sgpu_step.cu", "sgpu_upred.cu", "sgpu_wpred.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-Xptxas", "-warn-spills"]
 

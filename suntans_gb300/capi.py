@@ -28,6 +28,7 @@ EXPORTS = [
     "sgpu_cgsolve_noalloc",
     "sgpu_step_grid", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_pressure_step",
     "sgpu_update_dz", "sgpu_set_flux_height",
+    "sgpu_wpredictor",
     "sgpu_upredictor_grid", "sgpu_upredictor_vertical", "sgpu_upredictor_rhs", "sgpu_upredictor_finish",
     "sgpu_upredictor",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
@@ -73,6 +74,12 @@ class UPredFieldsC(C.Structure):
                 ("nonlinear", C.c_int)]
 
 
+class WPredFieldsC(C.Structure):
+    _fields_ = [("q", _dpp), ("nu_tv", _dpp), ("nu_lax", _dpp), ("utmp2", _dpp), ("nu", C.c_double),
+                ("nu_H", C.c_double), ("CdW", C.c_double), ("laxWendroff_Vertical", C.c_double),
+                ("nonlinear", C.c_int), ("conserveMomentum", C.c_int), ("n", C.c_int), ("AB", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("status", C.c_int), ("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double),
                 ("ms_solve", C.c_double), ("ms_total", C.c_double), ("unknowns", C.c_longlong)]
@@ -102,6 +109,8 @@ def load() -> C.CDLL:
     lib.sgpu_update_dz.argtypes = [C.c_void_p, C.POINTER(VGrid), _dp, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp]
     lib.sgpu_set_flux_height.argtypes = [C.c_void_p, C.POINTER(VGrid), _ip, _dp, _dpp, _dpp, _dpp]
     _ucp = C.POINTER(C.c_ubyte)
+    lib.sgpu_wpredictor.argtypes = [C.c_void_p, _ip, _dpp, C.POINTER(WPredFieldsC), C.POINTER(Props), _dpp, _dpp,
+                                    _dpp]
     lib.sgpu_upredictor_grid.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, _dp, _ip, _ip]
     lib.sgpu_upredictor_vertical.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dp, C.POINTER(UPredFieldsC),
                                              C.POINTER(Props), _dpp, _dpp, _dp]
@@ -401,6 +410,28 @@ class Context:
                                            _vp(jagged(dzf, vf.foff)))
         self._check(rc, "sgpu_set_flux_height", allow=(OK,))
         return dzf, dzz
+
+    # ---- WPredictor ----
+    def wpredictor(self, wf, props: SolverProps, ctop=None, dzz=None):
+        """Returns (w, Cn_W, Cn_W2) after one WPredictor on the device."""
+        g = self.grid
+        keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (wf.q, wf.nu_tv, wf.nu_lax, wf.utmp2)]
+        rows = [jagged(keep[0], self.coff), jagged(keep[1], self.coff), jagged(keep[2], self.coff),
+                jagged(keep[3], self.eoff)]
+        f = WPredFieldsC(*[_vp(r) for r in rows], float(wf.nu), float(wf.nu_H), float(wf.CdW),
+                         float(wf.laxWendroff_Vertical), int(wf.nonlinear), int(wf.conserveMomentum), int(wf.n),
+                         int(wf.AB))
+        ct = np.ascontiguousarray(g.ctop if ctop is None else ctop, dtype=np.int32)
+        zz = np.ascontiguousarray(g.dzz if dzz is None else dzz, dtype=np.float64)
+        w = np.array(wf.w, dtype=np.float64, copy=True)
+        cw = np.array(wf.Cn_W, dtype=np.float64, copy=True)
+        cw2 = np.array(wf.Cn_W2, dtype=np.float64, copy=True)
+        pr = props_struct(props)
+        rc = self.lib.sgpu_wpredictor(self.h, ct.ctypes.data_as(_ip), _vp(jagged(zz, self.coff)), C.byref(f),
+                                      C.byref(pr), _vp(jagged(w, wf.woff)), _vp(jagged(cw, self.coff)),
+                                      _vp(jagged(cw2, self.coff)))
+        self._check(rc, "sgpu_wpredictor", allow=(OK,))
+        return w, cw, cw2
 
     # ---- UPredictor ----
     def upredictor_grid(self, uf):

@@ -71,6 +71,11 @@ struct sgpu_context {
   int *d_ctopold = nullptr, *d_etopold = nullptr;
   double *d_dz = nullptr, *d_dv = nullptr, *d_dzbot = nullptr, *d_hv = nullptr, *d_dzzold = nullptr;
 
+  // WPredictor buffers
+  bool wp_ready = false;
+  int *d_ecsr = nullptr, *d_eside = nullptr;
+  double *d_cnw = nullptr, *d_cnw2 = nullptr, *d_wt = nullptr, *d_wcc = nullptr, *d_wface = nullptr;
+
   // UPredictor buffers
   std::vector<int> cedge_h;  // computational edges (host copy)
   bool up_grid = false, up_ready = false;
@@ -758,6 +763,21 @@ int sgpu_step_grid(sgpu_context* ctx, const int* normal, const int* grad, const 
       return fail(ctx, SGPU_BAD_GRID, "computational edge %d lacks a cell on one side", e);
     ce.push_back(e);
   }
+  // each computational column's computational edges, in the caller's edge order (WPredictor adds their
+  // horizontal-diffusion terms in that order): 2*edge + side, side 0 where the column is grad[0]
+  std::vector<int> ecsr(std::max(ncomp, 0) + 1, 0), eside;
+  {
+    std::vector<std::vector<int>> per(std::max(ncomp, 0));
+    for (int e : ce)
+      for (int sd = 0; sd < 2; ++sd) {
+        const int c = gd[2 * (size_t)e + sd];
+        if (c >= 0 && c < ncomp) per[c].push_back(2 * e + sd);
+      }
+    for (int j = 0; j < ncomp; ++j) {
+      ecsr[j + 1] = ecsr[j] + (int)per[j].size();
+      eside.insert(eside.end(), per[j].begin(), per[j].end());
+    }
+  }
   // deepest edges first: the per-edge kernels (UPredictor's vertical solve, Corrector) stride over this list,
   // so each thread gets a like share of levels and the lanes of a warp have like column lengths
   std::stable_sort(ce.begin(), ce.end(), [&](int x, int y) { return ctx->Nke[x] > ctx->Nke[y]; });
@@ -780,6 +800,11 @@ int sgpu_step_grid(sgpu_context* ctx, const int* normal, const int* grad, const 
                      ctx->stream));
   if (!ce.empty())
     CK(cudaMemcpyAsync(ctx->d_cedge, ce.data(), sizeof(int) * ce.size(), cudaMemcpyHostToDevice, ctx->stream));
+  if (!ctx->d_ecsr && (rc = dalloc(ctx, &ctx->d_ecsr, (size_t)std::max(ncomp, 0) + 1))) return rc;
+  if (!ctx->d_eside && (rc = dalloc(ctx, &ctx->d_eside, 2 * (size_t)std::max(Ne, 1)))) return rc;
+  CK(cudaMemcpyAsync(ctx->d_ecsr, ecsr.data(), sizeof(int) * ecsr.size(), cudaMemcpyHostToDevice, ctx->stream));
+  if (!eside.empty())
+    CK(cudaMemcpyAsync(ctx->d_eside, eside.data(), sizeof(int) * eside.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->ncedge = (int)ce.size();
   ctx->cedge_h = ce;
@@ -1653,6 +1678,133 @@ int sgpu_upredictor(sgpu_context* ctx, const sgpu_vgrid* v, const sgpu_upred_fie
   ctx->h_uploaded = false;
   if (stats) stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return s_rc;
+}
+
+// ---------------------------------------------------------------------------
+// WPredictor
+// ---------------------------------------------------------------------------
+static int alloc_wpred(sgpu_context* ctx) {
+  if (ctx->wp_ready) return SGPU_OK;
+  int rc;
+  const size_t n3 = ctx->n3 + 1, ne3 = ctx->ne3 + 1;
+  if ((rc = dalloc(ctx, &ctx->d_cnw, n3)) || (rc = dalloc(ctx, &ctx->d_cnw2, n3)) || (rc = dalloc(ctx, &ctx->d_wt, n3)) ||
+      (rc = dalloc(ctx, &ctx->d_wcc, n3)) || (rc = dalloc(ctx, &ctx->d_wface, ne3)))
+    return rc;
+  ctx->wp_ready = true;
+  return SGPU_OK;
+}
+
+int sgpu_wpredictor(sgpu_context* ctx, const int* ctop, const double* const* dzz, const sgpu_wpred_fields* f,
+                    const sgpu_props* prop, double* const* w, double* const* Cn_W, double* const* Cn_W2) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctop || !dzz || !f || !f->q || !f->nu_tv || !f->nu_lax || !prop || !w || !Cn_W || !Cn_W2 ||
+      (f->nonlinear && !f->utmp2))
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  if (f->nonlinear != 0 && f->nonlinear != 1)
+    return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device supports nonlinear 0 and 1, not %d", f->nonlinear);
+  if (f->conserveMomentum) return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device needs conserveMomentum 0");
+  if (ctx->Nkmax + 1 > 128) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs Nkmax <= 127");
+  int rc;
+  if ((rc = check_ctop(ctx, ctop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx)) || (rc = alloc_upred(ctx)) || (rc = alloc_wpred(ctx))) return rc;
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, Nc = ctx->Nc, ni = Nc / 2 + 1;
+  if ((rc = ensure_pinned(ctx, ni + 6 * n3 + ne3 + nw3 + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  double* s_dzz = ctx->pin + ni;
+  double* s_q = s_dzz + n3;
+  double* s_nt = s_q + n3;
+  double* s_nl = s_nt + n3;
+  double* s_c1 = s_nl + n3;
+  double* s_c2 = s_c1 + n3;
+  double* s_u2 = s_c2 + n3;
+  double* s_w = s_u2 + ne3;
+  for (size_t j = 0; j < Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  gather_cells(ctx, dzz, s_dzz);
+  gather_cells(ctx, f->q, s_q);
+  gather_cells(ctx, f->nu_tv, s_nt);
+  gather_cells(ctx, f->nu_lax, s_nl);
+  gather_cells(ctx, (const double* const*)Cn_W, s_c1);
+  gather_cells(ctx, (const double* const*)Cn_W2, s_c2);
+  if (f->nonlinear) gather_edges(ctx, f->utmp2, s_u2);
+  gather_wrows(ctx, (const double* const*)w, s_w);
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * Nc, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_qtot, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_nutv, s_nt, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_nulax, s_nl, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_cnw, s_c1, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_cnw2, s_c2, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  if (f->nonlinear) CK(cudaMemcpyAsync(ctx->d_ut2, s_u2, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, st));
+  WPredArgs a{};
+  a.Nc = ctx->Nc;
+  a.ncomp = ctx->ncomp;
+  a.F = ctx->F;
+  a.ncedge = ctx->ncedge;
+  a.kmax = kmax_for(ctx->Nkmax);
+  a.n3 = (int)ctx->n3;
+  a.nonlinear = f->nonlinear;
+  a.first = f->n == 1;
+  if (f->n == 1) {  // main/phys.c:2044-2064
+    a.fab1 = 1;
+    a.fab2 = a.fab3 = 0;
+  } else if (f->n == 2 || f->AB == 2) {
+    a.fab1 = 3.0 / 2.0;
+    a.fab2 = -1.0 / 2.0;
+    a.fab3 = 0;
+  } else {
+    a.fab1 = 23.0 / 12.0;
+    a.fab2 = -4.0 / 3.0;
+    a.fab3 = 5.0 / 12.0;
+  }
+  a.dt = prop->dt;
+  a.theta = prop->theta;
+  a.nu = f->nu;
+  a.nu_H = f->nu_H;
+  a.CdW = f->CdW;
+  a.lax = f->laxWendroff_Vertical;
+  a.cedge = ctx->d_cedge;
+  a.grad = ctx->d_grad;
+  a.nke = ctx->d_nke;
+  a.eoff = ctx->d_eoff;
+  a.dcoff = ctx->d_dcoff;
+  a.woff = ctx->d_woff;
+  a.nk = ctx->d_nk;
+  a.ctop = ctx->d_ctop;
+  a.nfaces = ctx->d_nfaces;
+  a.fedge = ctx->d_fedge;
+  a.normal = ctx->d_normal;
+  a.ecsr = ctx->d_ecsr;
+  a.eside = ctx->d_eside;
+  a.dzz = ctx->d_dzz;
+  a.df = ctx->d_df;
+  a.dg = ctx->d_dg;
+  a.Ac = ctx->d_Ac;
+  a.q = ctx->d_qtot;
+  a.nu_tv = ctx->d_nutv;
+  a.nu_lax = ctx->d_nulax;
+  a.utmp2 = ctx->d_ut2;
+  a.w = ctx->d_w;
+  a.Cn_W = ctx->d_cnw;
+  a.Cn_W2 = ctx->d_cnw2;
+  a.wtmp = ctx->d_wt;
+  a.wc = ctx->d_wcc;
+  a.ut = ctx->d_wface;
+  if (f->nonlinear) CK(cudaMemsetAsync(ctx->d_wface, 0, sizeof(double) * ne3, st));
+  CK(launch_wpredictor(a, st));
+  CK(cudaMemcpyAsync(s_w, ctx->d_w, sizeof(double) * nw3, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_c1, ctx->d_cnw, sizeof(double) * n3, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s_c2, ctx->d_cnw2, sizeof(double) * n3, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  scatter_wrows(ctx, s_w, w, ctx->ncomp);
+  scatter_cells_all(ctx, s_c1, Cn_W);
+  scatter_cells_all(ctx, s_c2, Cn_W2);
+  ctx->q_uploaded = false;
+  return SGPU_OK;
 }
 
 }  // extern "C"

@@ -122,6 +122,42 @@ cudaError_t launch_upred_open_fluxes(const UPredArgs& a, cudaStream_t st);
 cudaError_t launch_upred_velocity(const UPredArgs& a, cudaStream_t st);
 cudaError_t launch_upred_boundary(const UPredArgs& a, cudaStream_t st);
 
+// WPredictor (main/phys.c:2025-2287): device order as above.
+struct WPredArgs {
+  int Nc, ncomp, F, ncedge, kmax, n3;
+  int nonlinear, first;  // first: the reference's time step 1 (histories start from 0)
+  double fab1, fab2, fab3, dt, theta, nu, nu_H, CdW, lax;
+  const int* cedge;      // [ncedge] computational edges
+  const int* grad;       // [2*Ne] device columns
+  const int* nke;
+  const int* eoff;
+  const int* dcoff;
+  const int* woff;
+  const int* nk;         // [Nc] device order
+  const int* ctop;       // [Nc] device order
+  const int* nfaces;     // [ncomp]
+  const int* fedge;      // [ncomp*F]
+  const int* normal;     // [ncomp*F]
+  const int* ecsr;       // [ncomp+1] offsets into eside
+  const int* eside;      // 2*edge + side (0: the column is grad[0]) in the computational edges' order
+  const double* dzz;
+  const double* df;
+  const double* dg;
+  const double* Ac;      // device order
+  const double* q;       // [n3]
+  const double* nu_tv;   // [n3]
+  const double* nu_lax;  // [n3]
+  const double* utmp2;   // [ne3]
+  double* w;             // [nw3] in/out
+  double* Cn_W;          // [n3]
+  double* Cn_W2;         // [n3]
+  double* wtmp;          // [n3] scratch
+  double* wc;            // [n3] scratch
+  double* ut;            // [ne3] scratch
+};
+
+cudaError_t launch_wpredictor(const WPredArgs& a, cudaStream_t st);
+
 cudaError_t launch_update_dz(const VGridArgs& a, cudaStream_t st);
 cudaError_t launch_set_flux_height(const VGridArgs& a, cudaStream_t st);
 cudaError_t launch_qsource(const StepArgs& a, cudaStream_t st);

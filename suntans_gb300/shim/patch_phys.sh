@@ -4,7 +4,8 @@
 # Edits in place and keeps phys.c.orig.  Exactly two call sites change:
 #   Solve       main/phys.c:1280  CGSolveQ(phys->qc,phys->stmp,phys->stmp3,...)
 #   UPredictor  main/phys.c:2989  CGSolve(grid,phys,prop,myproc,numprocs,comm)
-# With "step", the two steps around CGSolveQ in Solve move to the GPU too:
+# With "step", the nonhydrostatic steps around CGSolveQ in Solve move to the GPU too:
+#   main/phys.c:1271  WPredictor(grid,phys,prop,myproc,numprocs,comm)
 #   main/phys.c:1274  ComputeQSource(phys->stmp,...)
 #   main/phys.c:1289  Corrector(phys->qc,...)
 # With "upred", the whole predictor does (its call in Solve):
@@ -36,12 +37,14 @@ if [ "$step" = 1 ]; then
   sed -i \
     -e 's/^\([[:space:]]*\)ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);/\1sgpu_ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);/' \
     -e 's/^\([[:space:]]*\)Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);/\1sgpu_Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);/' \
+    -e 's/^\([[:space:]]*\)WPredictor(grid,phys,prop,myproc,numprocs,comm);/\1sgpu_WPredictor(grid,phys,prop,myproc,numprocs,comm);/' \
     "$f"
   sed -i '0,/^#include "phys.h"/s//#include "phys.h"\
 void sgpu_ComputeQSource(REAL **src, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs);\
-void sgpu_Corrector(REAL **qc, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);/' "$f"
-  m=$(grep -c 'sgpu_ComputeQSource\|sgpu_Corrector' "$f")
-  [ "$m" -ge 4 ] || { echo "patch_phys.sh: step call sites not found ($m)" >&2; mv "$f.orig" "$f"; exit 1; }
+void sgpu_Corrector(REAL **qc, gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);\
+void sgpu_WPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm);/' "$f"
+  m=$(grep -c 'sgpu_ComputeQSource\|sgpu_Corrector\|sgpu_WPredictor' "$f")
+  [ "$m" -ge 6 ] || { echo "patch_phys.sh: step call sites not found ($m)" >&2; mv "$f.orig" "$f"; exit 1; }
 fi
 n=$(grep -c 'sgpu_CGSolve' "$f")
 [ "$n" -ge 4 ] || { echo "patch_phys.sh: expected call sites not found ($n)" >&2; mv "$f.orig" "$f"; exit 1; }

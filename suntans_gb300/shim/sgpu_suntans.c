@@ -241,3 +241,38 @@ void sgpu_UPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int nump
     else
       phys->hcorr[i] = 0;
 }
+
+/* WPredictor (declared static at main/phys.c:81-82, defined 2025, called from
+ * Solve at 1271) with the reference's parameter list, for nonlinear 0 or 1,
+ * conserveMomentum 0 and grids without type-2 or type-4 edges.  Its scratch
+ * fields (phys->wtmp, stmp, wc, ut) are left untouched; nothing reads them
+ * after it.  Same bits as the reference. */
+void sgpu_WPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm) {
+  sgpu_wpred_fields f;
+  sgpu_props p;
+  int rc;
+  (void)myproc;
+  (void)comm;
+  sgpu_ensure_step(grid, numprocs);
+  if ((prop->nonlinear != 0 && prop->nonlinear != 1) || prop->conserveMomentum ||
+      grid->edgedist[3] > grid->edgedist[2] || grid->edgedist[5] > grid->edgedist[4]) {
+    fprintf(stderr, "sgpu: WPredictor on the GPU needs nonlinear 0 or 1, conserveMomentum 0 and no type-2/4 edges\n");
+    exit(EXIT_FAILURE);
+  }
+  f.q = (const double *const *)phys->q;
+  f.nu_tv = (const double *const *)phys->nu_tv;
+  f.nu_lax = (const double *const *)phys->nu_lax;
+  f.utmp2 = (const double *const *)phys->utmp2;
+  f.nu = prop->nu;
+  f.nu_H = prop->nu_H;
+  f.CdW = prop->CdW;
+  f.laxWendroff_Vertical = prop->laxWendroff_Vertical;
+  f.nonlinear = prop->nonlinear;
+  f.conserveMomentum = prop->conserveMomentum;
+  f.n = prop->n;
+  f.AB = prop->AB;
+  sgpu_props_from(prop, &p);
+  rc = sgpu_wpredictor(g_ctx, grid->ctop, (const double *const *)grid->dzz, &f, &p, phys->w, phys->Cn_W,
+                       phys->Cn_W2);
+  if (rc != SGPU_OK) sgpu_die("sgpu_wpredictor", rc);
+}

@@ -48,11 +48,12 @@ def test_patch_step_mode_and_compile(tmp_path):
     new = phys.read_text()
     assert new.count("sgpu_ComputeQSource(phys->stmp,grid,phys,prop,myproc,numprocs);") == 1
     assert new.count("sgpu_Corrector(phys->qc,grid,phys,prop,myproc,numprocs,comm);") == 1
+    assert new.count("sgpu_WPredictor(grid,phys,prop,myproc,numprocs,comm);") == 1
     old = open(os.path.join(REF, "phys.c")).read()
     diff = [a for a in new.splitlines() if "sgpu_" not in a]
     assert diff == [a for a in old.splitlines()
                     if not a.strip().startswith(("CGSolveQ(phys->qc", "CGSolve(grid", "ComputeQSource(phys->stmp",
-                                                 "Corrector(phys->qc"))]
+                                                 "Corrector(phys->qc", "WPredictor(grid,phys"))]
     cc = ["gcc", "-fcommon", "-DNOMPI", "-DNONETCDF", "-w", f"-I{REF}", f"-I{ROOT}/include", "-c"]
     r = subprocess.run(cc + [str(phys), "-o", str(tmp_path / "phys.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -78,7 +79,7 @@ def test_patch_upred_mode_and_compile(tmp_path):
     diff = [a for a in new.splitlines() if "sgpu_" not in a]
     assert diff == [a for a in old.splitlines()
                     if not a.strip().startswith(("CGSolveQ(phys->qc", "CGSolve(grid", "ComputeQSource(phys->stmp",
-                                                 "Corrector(phys->qc", "UPredictor(grid,phys"))]
+                                                 "Corrector(phys->qc", "UPredictor(grid,phys", "WPredictor(grid,phys"))]
     cc = ["gcc", "-fcommon", "-DNOMPI", "-DNONETCDF", "-w", f"-I{REF}", f"-I{ROOT}/include", "-c"]
     r = subprocess.run(cc + [str(phys), "-o", str(tmp_path / "phys.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
