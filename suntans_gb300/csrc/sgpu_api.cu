@@ -1705,6 +1705,7 @@ int sgpu_wpredictor(sgpu_context* ctx, const int* ctop, const double* const* dzz
     return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device supports nonlinear 0 and 1, not %d", f->nonlinear);
   if (f->conserveMomentum) return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device needs conserveMomentum 0");
   if (ctx->Nkmax + 1 > 128) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs Nkmax <= 127");
+  if (ctx->F > 8) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs maxfaces <= 8");
   int rc;
   if ((rc = check_ctop(ctx, ctop))) return rc;
   DeviceGuard dg(ctx->device);

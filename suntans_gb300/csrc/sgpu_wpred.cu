@@ -71,7 +71,12 @@ __global__ void wp_face_kernel(WPredArgs A) {
   }
 }
 
-template <int KMAX>
+// One pass down the column: every level's terms are summed in the
+// reference's order (faces, the vertical term, then the edges in edge
+// order), and the history at k needs only the sums at k-1 and k, so nothing
+// is kept per level but two sums; each face's and each edge's data sit in
+// registers (at most kMaxF of each).
+constexpr int kMaxF = 8;
 __global__ void __launch_bounds__(128) wp_column_kernel(WPredArgs A) {
   const int T = gridDim.x * blockDim.x;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.ncomp; j += T) {
@@ -79,57 +84,84 @@ __global__ void __launch_bounds__(128) wp_column_kernel(WPredArgs A) {
     const double* w = A.w + A.woff[j];
     const double* z = A.dzz + co;
     const double* q = A.q + co;
-    double wt[KMAX], st[KMAX], cn[KMAX];
-    for (int k = ct; k < nk; ++k) {  // 2071-2079
-      wt[k] = ADD(ADD(w[k], MUL(A.fab2, A.Cn_W[co + k])), MUL(A.fab3, A.Cn_W2[co + k]));
-      A.Cn_W2[co + k] = A.Cn_W[co + k];
-      cn[k] = 0;
-      st[k] = 0;
-    }
-    const double tdt = MUL(2.0, A.dt);
-    for (int k = ct + 1; k < nk; ++k) wt[k] = SUB(wt[k], MUL(DIV(tdt, ADD(z[k - 1], z[k])), SUB(q[k - 1], q[k])));
-    wt[ct] = ADD(wt[ct], MUL(DIV(tdt, z[ct]), q[ct]));
     const double Ac = A.Ac[j];
-    if (A.nonlinear) {  // 2118-2146 (conserveMomentum 0: a[k] = 1)
-      const double aAc = MUL(1.0, Ac);
-      for (int f = 0; f < A.nfaces[j]; ++f) {
+    const double tdt = MUL(2.0, A.dt);
+    // faces (advection)
+    int f_eo[kMaxF], f_top[kMaxF];
+    double f_c[kMaxF];
+    const int nf = A.nonlinear ? A.nfaces[j] : 0;
+#pragma unroll
+    for (int f = 0; f < kMaxF; ++f)
+      if (f < nf) {
         const int ne = A.fedge[j * A.F + f];
-        const double nrm = (double)A.normal[j * A.F + f];
-        const int eo = A.eoff[ne], top = min(nk, A.nke[ne]);
-        const double dfe = A.df[ne];
-        for (int k = ct; k < top; ++k)
-          st[k] = ADD(st[k], DIV(MUL(MUL(MUL(A.ut[eo + k], A.utmp2[eo + k]), dfe), nrm), aAc));
+        f_eo[f] = A.eoff[ne];
+        f_top[f] = A.nke[ne];
+        f_c[f] = A.df[ne];  // times the normal below, in the reference's order
       }
-      for (int k = ct; k < nk; ++k) st[k] = ADD(st[k], DIV(SUB(MUL(w[k], w[k]), MUL(w[k + 1], w[k + 1])), z[k]));
-    }
-    // horizontal diffusion and wall drag, edge by edge in the reference's order (2159-2185)
-    for (int p = A.ecsr[j]; p < A.ecsr[j + 1]; ++p) {
-      const int e = A.eside[p] >> 1, side = A.eside[p] & 1;
-      const int c1 = A.grad[2 * e], c2 = A.grad[2 * e + 1];
-      const int kmin = max(A.ctop[c1], A.ctop[c2]), ne = A.nke[e];
-      const double* w1 = A.w + A.woff[c1];
-      const double* w2 = A.w + A.woff[c2];
-      const double* l1 = A.nu_lax + A.dcoff[c1];
-      const double* l2 = A.nu_lax + A.dcoff[c2];
-      const double dfe = A.df[e], dge = A.dg[e];
-      for (int k = max(kmin, ct); k < ne; ++k) {
-        const double ak = DIV(MUL(MUL(MUL(0.5, ADD(A.nu_H, MUL(0.5, ADD(l1[k], l2[k])))),
-                                      SUB(ADD(SUB(w2[k], w1[k]), w2[k + 1]), w1[k + 1])),
-                                  dfe),
-                              dge);
-        st[k] = side == 0 ? SUB(st[k], DIV(ak, Ac)) : ADD(st[k], DIV(ak, Ac));
+    // computational edges of the column, in the reference's edge order
+    const int p0 = A.ecsr[j], ned = min(A.ecsr[j + 1] - p0, kMaxF);
+    int e_kmin[kMaxF], e_ne[kMaxF], e_side[kMaxF], e_w1[kMaxF], e_w2[kMaxF], e_l1[kMaxF], e_l2[kMaxF];
+    double e_df[kMaxF], e_dg[kMaxF];
+#pragma unroll
+    for (int p = 0; p < kMaxF; ++p)
+      if (p < ned) {
+        const int e = A.eside[p0 + p] >> 1;
+        const int c1 = A.grad[2 * e], c2 = A.grad[2 * e + 1];
+        e_side[p] = A.eside[p0 + p] & 1;
+        e_kmin[p] = max(A.ctop[c1], A.ctop[c2]);
+        e_ne[p] = A.nke[e];
+        e_w1[p] = A.woff[c1];
+        e_w2[p] = A.woff[c2];
+        e_l1[p] = A.dcoff[c1];
+        e_l2[p] = A.dcoff[c2];
+        e_df[p] = A.df[e];
+        e_dg[p] = A.dg[e];
       }
-      for (int k = max(ne, ct); k < nk; ++k) {
-        const double sw = ADD(w[k], w[k + 1]);
-        st[k] = ADD(st[k], DIV(MUL(MUL(MUL(MUL(0.25, A.CdW), fabs(sw)), sw), dfe), Ac));
+    const double aAc = MUL(1.0, Ac);
+    double st_prev = 0;
+    for (int k = ct; k < nk; ++k) {
+      // Adams-Bashforth start and the pressure gradient (2071-2089)
+      const double c1v = A.Cn_W[co + k];
+      double wt = ADD(ADD(w[k], MUL(A.fab2, c1v)), MUL(A.fab3, A.Cn_W2[co + k]));
+      A.Cn_W2[co + k] = c1v;
+      if (k > ct)
+        wt = SUB(wt, MUL(DIV(tdt, ADD(z[k - 1], z[k])), SUB(q[k - 1], q[k])));
+      else
+        wt = ADD(wt, MUL(DIV(tdt, z[ct]), q[ct]));
+      // the level's source: advection (2118-2146), diffusion and wall drag (2159-2185)
+      double st = 0;
+      if (A.nonlinear) {
+#pragma unroll
+        for (int f = 0; f < kMaxF; ++f)
+          if (f < nf && k < f_top[f]) {
+            const double nrm = (double)A.normal[j * A.F + f];
+            st = ADD(st, DIV(MUL(MUL(MUL(A.ut[f_eo[f] + k], A.utmp2[f_eo[f] + k]), f_c[f]), nrm), aAc));
+          }
+        st = ADD(st, DIV(SUB(MUL(w[k], w[k]), MUL(w[k + 1], w[k + 1])), z[k]));
       }
-    }
-    for (int k = ct + 1; k < nk; ++k)  // 2210-2220
-      cn[k] = SUB(cn[k], DIV(MUL(A.dt, ADD(MUL(z[k - 1], st[k - 1]), MUL(z[k], st[k]))), ADD(z[k - 1], z[k])));
-    cn[ct] = SUB(cn[ct], MUL(A.dt, st[ct]));
-    for (int k = ct; k < nk; ++k) {  // 2236-2241
-      A.Cn_W[co + k] = cn[k];
-      A.wtmp[co + k] = ADD(wt[k], MUL(A.fab1, cn[k]));
+#pragma unroll
+      for (int p = 0; p < kMaxF; ++p)
+        if (p < ned) {
+          if (k >= e_kmin[p] && k < e_ne[p]) {
+            const double* w1 = A.w + e_w1[p];
+            const double* w2 = A.w + e_w2[p];
+            const double ak =
+                DIV(MUL(MUL(MUL(0.5, ADD(A.nu_H, MUL(0.5, ADD(A.nu_lax[e_l1[p] + k], A.nu_lax[e_l2[p] + k])))),
+                            SUB(ADD(SUB(w2[k], w1[k]), w2[k + 1]), w1[k + 1])),
+                        e_df[p]),
+                    e_dg[p]);
+            st = e_side[p] == 0 ? SUB(st, DIV(ak, Ac)) : ADD(st, DIV(ak, Ac));
+          } else if (k >= e_ne[p]) {
+            const double sw = ADD(w[k], w[k + 1]);
+            st = ADD(st, DIV(MUL(MUL(MUL(MUL(0.25, A.CdW), fabs(sw)), sw), e_df[p]), Ac));
+          }
+        }
+      // the new history (2210-2220) and the right-hand side (2236-2241)
+      const double cn = k > ct ? SUB(0.0, DIV(MUL(A.dt, ADD(MUL(z[k - 1], st_prev), MUL(z[k], st))), ADD(z[k - 1], z[k])))
+                               : SUB(0.0, MUL(A.dt, st));
+      st_prev = st;
+      A.Cn_W[co + k] = cn;
+      A.wtmp[co + k] = ADD(wt, MUL(A.fab1, cn));
     }
   }
 }
@@ -174,7 +206,7 @@ __global__ void __launch_bounds__(128) wp_solve_kernel(WPredArgs A) {
 template <int KMAX>
 static void wp_columns(const WPredArgs& a, cudaStream_t st) {
   const int nb = blocks(a.ncomp, 128);
-  wp_column_kernel<KMAX><<<nb, 128, 0, st>>>(a);
+  wp_column_kernel<<<nb, 128, 0, st>>>(a);
   wp_solve_kernel<KMAX><<<nb, 128, 0, st>>>(a);
 }
 
