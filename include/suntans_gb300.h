@@ -327,6 +327,16 @@ int sgpu_batch_add(sgpu_batch *b, const sgpu_grid_desc *grid, const int *ctop, c
  * iterations done in this launch. */
 int sgpu_batch_run(sgpu_batch *b, int max_iters, int *running, double *ms, long long *unknown_iters);
 
+/* sgpu_batch_run in two halves, for a host loop that works while the device
+ * runs: sgpu_batch_launch enqueues the launch and returns at once; until
+ * sgpu_batch_wait, problems may be added and finished problems re-submitted,
+ * read back or released (uploads and downloads go on a second stream and touch
+ * only problems outside the launch); they join the next launch.
+ * sgpu_batch_wait blocks until the launch is done and reports as
+ * sgpu_batch_run. */
+int sgpu_batch_launch(sgpu_batch *b, int max_iters);
+int sgpu_batch_wait(sgpu_batch *b, int *running, double *ms, long long *unknown_iters);
+
 /* State of problem `id` (1 set-up pending, 2 running, 3 done; -1 unknown id). */
 int sgpu_batch_state(const sgpu_batch *b, int id);
 

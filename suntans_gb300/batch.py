@@ -106,6 +106,22 @@ class Batch:
             raise SolverError(rc, f"sgpu_batch_run: {self.error()}")
         return running.value, ms.value, work.value
 
+    def launch(self, max_iters=0):
+        """Enqueues one launch and returns at once (see `wait`)."""
+        rc = self.lib.sgpu_batch_launch(self.h, int(max_iters))
+        if rc != OK:
+            raise SolverError(rc, f"sgpu_batch_launch: {self.error()}")
+
+    def wait(self):
+        """Waits for the launch in flight; returns (running, ms, unknown_iterations)."""
+        running = C.c_int(0)
+        ms = C.c_double(0)
+        work = C.c_longlong(0)
+        rc = self.lib.sgpu_batch_wait(self.h, C.byref(running), C.byref(ms), C.byref(work))
+        if rc != OK:
+            raise SolverError(rc, f"sgpu_batch_wait: {self.error()}")
+        return running.value, ms.value, work.value
+
     def state(self, i) -> int:
         return self.lib.sgpu_batch_state(self.h, int(i))
 

@@ -1432,7 +1432,9 @@ struct sgpu_batch {
   int device = 0;
   int qprecond = 1;
   int F = 3;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;   // launches
+  cudaStream_t ustream = nullptr;  // uploads of added / re-submitted problems and result downloads, which touch
+                                   // only problems outside the launch in flight
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   long long timeout_ns = 2000000000LL;
@@ -1443,7 +1445,12 @@ struct sgpu_batch {
   int max_inst = 0, max_tiles = 0;
   Arena slots, cols, eslots, hdrs;
   std::vector<HostInst> inst;
-  BInst* h_inst = nullptr;         // pinned, max_inst entries
+  BInst* h_inst = nullptr;         // pinned, max_inst entries: the host's view
+  BInst* h_inst_up = nullptr;      // pinned: the table a launch uploads (a copy taken when it is enqueued)
+  BInst* h_inst_dev = nullptr;     // pinned: the table a launch writes back
+  bool inflight = false;           // a launch is enqueued and not yet waited for
+  std::vector<int> launched;       // problems that launch runs (their rows of h_inst_dev are taken after it)
+  int launched_ninst = 0;
   TileDesc* h_tiles = nullptr;     // pinned, max_tiles entries
   int* h_tinst = nullptr;          // pinned
   int* h_gflags = nullptr;         // pinned [4]
@@ -1573,12 +1580,15 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   b->n_before.assign(max_instances, 0);
   Guard g(device);
   BCK(cudaMallocHost((void**)&b->h_inst, sizeof(BInst) * max_instances));
+  BCK(cudaMallocHost((void**)&b->h_inst_up, sizeof(BInst) * max_instances));
+  BCK(cudaMallocHost((void**)&b->h_inst_dev, sizeof(BInst) * max_instances));
   std::memset(b->h_inst, 0, sizeof(BInst) * max_instances);
   BCK(cudaMallocHost((void**)&b->h_tiles, sizeof(TileDesc) * ((size_t)b->max_tiles + 1)));
   std::memset(b->h_tiles, 0xff, sizeof(TileDesc) * ((size_t)b->max_tiles + 1));
   BCK(cudaMallocHost((void**)&b->h_tinst, sizeof(int) * ((size_t)b->max_tiles + 1)));
   BCK(cudaMallocHost((void**)&b->h_gflags, 4 * sizeof(int)));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BCK(cudaStreamCreateWithFlags(&b->ustream, cudaStreamNonBlocking));
   BCK(cudaEventCreate(&b->ev0));
   BCK(cudaEventCreate(&b->ev1));
   BCK(cudaMallocHost((void**)&b->h_ctl, sizeof(SolveCtl)));
@@ -1659,10 +1669,13 @@ int sgpu_batch_destroy(sgpu_batch* b) {
   {
     Guard g(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->ustream) cudaStreamSynchronize(b->ustream);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     for (void* p : b->allocs) cudaFree(p);
     if (b->h_ctl) cudaFreeHost(b->h_ctl);
     if (b->h_inst) cudaFreeHost(b->h_inst);
+    if (b->h_inst_up) cudaFreeHost(b->h_inst_up);
+    if (b->h_inst_dev) cudaFreeHost(b->h_inst_dev);
     if (b->h_tiles) cudaFreeHost(b->h_tiles);
     if (b->h_tinst) cudaFreeHost(b->h_tinst);
     if (b->h_gflags) cudaFreeHost(b->h_gflags);
@@ -1670,6 +1683,7 @@ int sgpu_batch_destroy(sgpu_batch* b) {
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->ustream) cudaStreamDestroy(b->ustream);
   }
   delete b;
   return SGPU_OK;
@@ -1864,7 +1878,7 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
   }
   std::vector<float> v_dzfD32(v_dzfD.size());
   for (size_t k = 0; k < v_dzfD.size(); ++k) v_dzfD32[k] = (float)v_dzfD[k];
-  cudaStream_t s = b->stream;
+  cudaStream_t s = b->ustream;
   BCK(cudaMemcpyAsync(b->d_dzz64 + H.s_off, v_dzz.data(), 8 * H.n3, cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->d_src64 + H.s_off, v_src.data(), 8 * H.n3, cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->d_q64 + H.s_off, v_q.data(), 8 * H.n3, cudaMemcpyHostToDevice, s));
@@ -1904,7 +1918,18 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
 // Runs up to max_iters global iterations (<= 0: until every instance is done).
 // Returns the number of instances still running in *running.
 int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long long* unknown_iters) {
+  int rc = sgpu_batch_launch(b, max_iters);
+  if (rc != SGPU_OK) return rc;
+  return sgpu_batch_wait(b, running, ms, unknown_iters);
+}
+
+// Enqueues one launch over every problem in set-up or running state and
+// returns at once.  Until sgpu_batch_wait, problems may be added, finished
+// problems re-submitted or read back (those touch only problems the launch
+// does not run); they join the next launch.
+int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
   if (!b) return SGPU_BAD_ARG;
+  if (b->inflight) return bfail(b, SGPU_BAD_ARG, "a launch is already in flight");
   Guard gd(b->device);
   int ntiles = 0;
   int ninst = 0;
@@ -1959,10 +1984,12 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     I.t1 = ntiles;
     I.cnt = 0;
   }
+  b->launched = order;
+  b->launched_ninst = ninst;
   if (ntiles == 0) {
-    if (running) *running = 0;
-    if (ms) *ms = 0;
-    if (unknown_iters) *unknown_iters = 0;
+    b->launched.clear();
+    b->last_ms = 0;
+    b->last_work = 0;
     return SGPU_OK;
   }
   int maxg = batch_max_grid(b);
@@ -1991,7 +2018,7 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     cudaError_t e;
     if ((e = cudaMemcpyAsync(b->d_tiles, b->h_tiles, sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice, st))) return e;
     if ((e = cudaMemcpyAsync(b->d_tile_inst, b->h_tinst, sizeof(int) * ntiles, cudaMemcpyHostToDevice, st))) return e;
-    if ((e = cudaMemcpyAsync(b->d_inst, b->h_inst, sizeof(BInst) * ninst, cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(b->d_inst, b->h_inst_up, sizeof(BInst) * ninst, cudaMemcpyHostToDevice, st))) return e;
     if ((e = cudaMemcpyAsync(b->d_ctl, b->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, st))) return e;
     if ((e = cudaMemcpyAsync(b->d_gflags, b->h_gflags, 4 * sizeof(int), cudaMemcpyHostToDevice, st))) return e;
     BatchArgs a = b->a;
@@ -2012,10 +2039,12 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     void* args[] = {(void*)&a};
-    if ((e = cudaLaunchKernelExC(&cfg, kernel_of(b->qprecond), args))) return e;
-    if ((e = cudaMemcpyAsync(b->h_inst, b->d_inst, sizeof(BInst) * ninst, cudaMemcpyDeviceToHost, st))) return e;
-    return cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, st);
+    // the instance table and status come back in sgpu_batch_wait, after the
+    // stream has drained: a device-to-host copy queued behind the kernel here
+    // would hold up the read-backs of finished problems on the other stream
+    return cudaLaunchKernelExC(&cfg, kernel_of(b->qprecond), args);
   };
+  std::memcpy(b->h_inst_up, b->h_inst, sizeof(BInst) * ninst);
   BCK(cudaEventRecord(b->ev0, st));
   bool launched = false;
   if (b->use_graph) {
@@ -2053,20 +2082,42 @@ int sgpu_batch_run(sgpu_batch* b, int max_iters, int* running, double* ms, long 
   }
   if (!launched) BCK(enqueue());
   BCK(cudaEventRecord(b->ev1, st));
-  BCK(cudaStreamSynchronize(st));
-  float fms = 0.f;
-  cudaEventElapsedTime(&fms, b->ev0, b->ev1);
-  b->last_ms = fms;
-  if (b->h_ctl->status == SGPU_TIMEOUT)
-    return bfail(b, SGPU_TIMEOUT, "device wait timed out (phase %d)", b->h_ctl->phase_err);
-  int run = 0;
+  b->inflight = true;
+  return SGPU_OK;
+}
+
+// Waits for the launch in flight (none: returns the current counts) and takes
+// the state of the problems it ran.  *running counts problems in set-up or
+// running state afterwards.
+int sgpu_batch_wait(sgpu_batch* b, int* running, double* ms, long long* unknown_iters) {
+  if (!b) return SGPU_BAD_ARG;
+  Guard gd(b->device);
   long long work = 0;
-  for (int i = 0; i < ninst; ++i) {
+  float fms = 0.f;
+  if (b->inflight) {
+    b->inflight = false;
+    BCK(cudaStreamSynchronize(b->stream));
+    cudaEventElapsedTime(&fms, b->ev0, b->ev1);
+    BCK(cudaMemcpyAsync(b->h_inst_dev, b->d_inst, sizeof(BInst) * b->launched_ninst, cudaMemcpyDeviceToHost,
+                        b->stream));
+    BCK(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    b->last_ms = fms;
+    for (int i : b->launched) {
+      b->h_inst[i] = b->h_inst_dev[i];
+      const BInst& I = b->h_inst[i];
+      work += b->inst[i].unk * (long long)(I.n - b->n_before[i]);
+      if (I.state == INST_DONE && I.n > 0) b->inst[i].last_iters = I.n;
+    }
+    b->launched.clear();
+    if (b->h_ctl->status == SGPU_TIMEOUT)
+      return bfail(b, SGPU_TIMEOUT, "device wait timed out (phase %d)", b->h_ctl->phase_err);
+  }
+  int run = 0;
+  for (int i = 0; i < b->max_inst; ++i) {
     if (!b->inst[i].live) continue;
     const BInst& I = b->h_inst[i];
     run += I.state == INST_RUN || I.state == INST_SETUP;
-    work += b->inst[i].unk * (long long)(I.n - b->n_before[i]);
-    if (I.state == INST_DONE && I.n > 0) b->inst[i].last_iters = I.n;
   }
   b->last_work = work;
   if (running) *running = run;
@@ -2104,9 +2155,9 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
     }
     double* x = b->h_stage;
     double* c = b->h_stage + n;
-    BCK(cudaMemcpyAsync(x, b->a.x64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->stream));
-    if (b->qprecond == 1) BCK(cudaMemcpyAsync(c, b->a.c64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->stream));
-    BCK(cudaStreamSynchronize(b->stream));
+    BCK(cudaMemcpyAsync(x, b->a.x64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->ustream));
+    if (b->qprecond == 1) BCK(cudaMemcpyAsync(c, b->a.c64 + H.s_off, 8 * n, cudaMemcpyDeviceToHost, b->ustream));
+    BCK(cudaStreamSynchronize(b->ustream));
     const bool scaled = b->qprecond == 1;
     host_split(H.ncomp, 8192, [&](long long jb, long long je) {
       for (long long j = jb; j < je; ++j) {
@@ -2143,7 +2194,7 @@ int sgpu_batch_resubmit(sgpu_batch* b, int id, const double* const* src, double 
   Guard gd(b->device);
   const int n = (int)H.n3c;
   if (warm) {
-    finalize_q_kernel<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, b->stream>>>(
+    finalize_q_kernel<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, b->ustream>>>(
         b->a.x64, b->a.c64, b->d_q64, (int)H.s_off, n, b->qprecond == 1);
     BCK(cudaGetLastError());
   }
@@ -2164,9 +2215,9 @@ int sgpu_batch_resubmit(sgpu_batch* b, int id, const double* const* src, double 
         std::fill(stg + o + H.Nk[i], stg + end, 0.0);
       }
     });
-    BCK(cudaMemcpyAsync(b->d_src64 + H.s_off, b->h_stage, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->d_src64 + H.s_off, b->h_stage, sizeof(double) * n, cudaMemcpyHostToDevice, b->ustream));
   }
-  if (warm || src) BCK(cudaStreamSynchronize(b->stream));
+  if (warm || src) BCK(cudaStreamSynchronize(b->ustream));
   I.tol2 = qepsilon * qepsilon;
   I.maxiters = qmaxiters;
   I.state = INST_SETUP;

@@ -183,8 +183,10 @@ class Server:
         r.t_admit = self.clock() - self.t0
         return True
 
-    def _harvest(self):
+    def _harvest(self, only=None):
         for g, r in list(self.busy.items()):
+            if only is not None and g not in only:
+                continue
             iid = self.resident[g]
             if self.engine.state(iid) == 3:  # INST_DONE
                 if self.keep_q:
@@ -204,7 +206,15 @@ class Server:
     def run(self, requests, realtime=True, drain_limit=None):
         """Serves `requests` (sorted by t_arrival).  realtime=False admits every
         request at once (arrival times ignored).  drain_limit (s) stops the loop
-        with requests unfinished.  Returns the requests."""
+        with requests unfinished.  Returns the requests.
+
+        With an engine that can launch and wait separately, the host reads back
+        the problems the previous launch finished while the next launch runs,
+        except those whose grid has a request waiting: those are read back and
+        the waiting request admitted before the launch, so that a grid's
+        requests follow one another launch by launch as in the serial loop."""
+        if hasattr(self.engine, "launch") and hasattr(self.engine, "wait"):
+            return self._run_overlapped(requests, realtime, drain_limit)
         reqs = sorted(requests, key=lambda r: r.t_arrival)
         queues = collections.OrderedDict()  # grid -> deque of waiting requests, in arrival order
         npending = 0
@@ -247,6 +257,74 @@ class Server:
                 break
             if drain_limit is not None and self.clock() - self.t0 > drain_limit:
                 break
+        self.t_end = self.clock() - self.t0
+        return reqs
+
+
+    def _admit_waiting(self, queues):
+        """Admits the oldest waiting request of every idle grid, oldest first
+        (a grid's later requests wait for its earlier ones); returns how many."""
+        n = 0
+        heads = sorted((q[0].t_arrival, g) for g, q in queues.items() if q and g not in self.busy)
+        for _, g in heads:
+            if self._admit(queues[g][0]):
+                queues[g].popleft()
+                n += 1
+                if not queues[g]:
+                    del queues[g]
+        return n
+
+    def _run_overlapped(self, requests, realtime, drain_limit):
+        reqs = sorted(requests, key=lambda r: r.t_arrival)
+        queues = collections.OrderedDict()
+        npending = 0
+        self.t0 = self.clock()
+        i = 0
+        inflight = False
+        while True:
+            now = self.clock() - self.t0
+            while i < len(reqs) and (not realtime or reqs[i].t_arrival <= now):
+                queues.setdefault(reqs[i].grid, collections.deque()).append(reqs[i])
+                npending += 1
+                i += 1
+            t1 = self.clock()
+            if inflight:
+                _, ms, work = self.engine.wait()
+                inflight = False
+                if ms > 0 or work > 0:
+                    self.launches += 1
+                self.work += work
+                self.device_ms += ms
+            t2 = self.clock()
+            self.host_s["launch"] += t2 - t1
+            # grids with a request waiting: read back now, so that request joins the next launch
+            self._harvest(only={g for g, q in queues.items() if q})
+            t3 = self.clock()
+            self.host_s["harvest"] += t3 - t2
+            npending -= self._admit_waiting(queues)
+            t4 = self.clock()
+            self.host_s["admit"] += t4 - t3
+            if self.busy:
+                self.engine.launch(max_iters=self.chunk)
+                inflight = True
+                # the other finished problems are read back while this launch runs
+                self._harvest()
+                self.host_s["harvest"] += self.clock() - t4
+            elif npending:
+                raise RuntimeError("requests pending with nothing running: budget too small")
+            elif i < len(reqs):
+                wait = reqs[i].t_arrival - (self.clock() - self.t0)
+                if wait > 0:
+                    time.sleep(min(wait, 0.001))
+            else:
+                break
+            if drain_limit is not None and self.clock() - self.t0 > drain_limit:
+                break
+        if inflight:
+            _, ms, work = self.engine.wait()
+            self.work += work
+            self.device_ms += ms
+            self._harvest()
         self.t_end = self.clock() - self.t0
         return reqs
 

@@ -207,3 +207,57 @@ def test_graph_replay_equals_direct(gpu_lib):
     for ra, rb in zip(res_direct, res_graph):
         for a, c in zip(ra, rb):
             assert np.array_equal(a, c)
+
+
+def test_overlapped_launch_wait_equals_solo(gpu_lib):
+    """sgpu_batch_launch / sgpu_batch_wait: while a launch runs, finished
+    problems are read back, new problems added and a finished problem
+    re-submitted (a warm start on a new right-hand side); every result equals
+    the same sequence run launch by launch, bit for bit."""
+    grids = tri_grids()
+    probs = [gg.make_q_problem(g, seed=60 + k) for k, g in enumerate(grids)]
+    p_re = gg.make_q_problem(grids[2], seed=70)
+
+    def solo(k, resubmit=None):
+        b = Batch(qprecond=1, maxfaces=3, **capacity_for([grids[k]]))
+        i = b.add(probs[k])
+        b.run()
+        out = b.result(i, probs[k].q, release=False)
+        if resubmit is not None:
+            b.resubmit(i, resubmit.src)
+            b.run()
+            out = b.result(i, probs[k].q, release=False)
+        b.close()
+        return out
+
+    ref = [solo(k) for k in range(4)]
+    ref_re = solo(2, p_re)
+    b = Batch(qprecond=1, maxfaces=3, **capacity_for(grids))
+    live = {b.add(probs[2]): 2, b.add(probs[0]): 0}
+    pending = [1, 3]
+    results, resubmitted = {}, False
+    b.launch(max_iters=5)
+    for step in range(10000):
+        # work while the launch runs
+        done = [(i, k) for i, k in live.items() if b.state(i) == 3]
+        for i, k in done:
+            if k == 2 and not resubmitted:
+                results["first2"] = b.result(i, probs[2].q, release=False)
+                b.resubmit(i, p_re.src)
+                resubmitted = True
+                continue
+            results[k] = b.result(i, probs[k].q, release=False)
+            del live[i]
+        if pending and step >= 1:
+            k = pending.pop(0)
+            live[b.add(probs[k])] = k
+        running, ms, work = b.wait()
+        if not live and not pending:
+            break
+        b.launch(max_iters=5)
+    assert sorted(k for k in results if k != "first2") == [0, 1, 2, 3]
+    for k in (0, 1, 3):
+        assert results[k][1].niters == ref[k][1].niters and np.array_equal(results[k][0], ref[k][0])
+    assert np.array_equal(results["first2"][0], ref[2][0])
+    assert results[2][1].niters == ref_re[1].niters and np.array_equal(results[2][0], ref_re[0])
+    b.close()

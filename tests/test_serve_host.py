@@ -66,6 +66,51 @@ class FakeEngine:
         self.used -= self.inst.pop(i)["n"]
 
 
+class FakeAsyncEngine(FakeEngine):
+    """FakeEngine with the batched engine's launch / wait split: a launch runs
+    the problems active when it is enqueued; their state changes only at wait,
+    and adds, re-submissions and read-backs meanwhile touch other problems."""
+
+    def __init__(self, cap):
+        super().__init__(cap)
+        self.pending = None
+
+    def launch(self, max_iters=0):
+        assert self.pending is None, "one launch in flight at a time"
+        self.pending = ([i for i, I in self.inst.items() if I["state"] in (1, 2)], max_iters)
+
+    def wait(self):
+        if self.pending is None:
+            return 0, 0.0, 0
+        ids, max_iters = self.pending
+        self.pending = None
+        work, running = 0, 0
+        for i in ids:
+            I = self.inst[i]
+            k = I["left"] if max_iters <= 0 else min(I["left"], max_iters)
+            I["left"] -= k
+            I["it"] += k
+            work += k * I["n"]
+            I["state"] = 3 if I["left"] == 0 else 2
+            running += I["state"] != 3
+        return running, (0.1 if ids else 0.0), work
+
+    def resubmit(self, i, src, tol, maxiters, warm):
+        assert self.pending is None or i not in self.pending[0]
+        super().resubmit(i, src, tol, maxiters, warm)
+
+    def result(self, i, q0, release=False, out=None):
+        assert self.pending is None or i not in self.pending[0]
+        return super().result(i, q0, release, out)
+
+    def release(self, i):
+        assert self.pending is None or i not in self.pending[0]
+        super().release(i)
+
+
+ENGINES = [FakeEngine, FakeAsyncEngine]
+
+
 def fake_pool(sizes, rhs=2):
     pool = []
     for gid, n in enumerate(sizes):
@@ -82,9 +127,10 @@ def requests(seq, tols=(1e-8, 1e-10)):
     return [Request(k, gid, k % 2, tols[k % 2], 0.0001 * k) for k, gid in enumerate(seq)]
 
 
-def test_every_request_served_and_grid_order_kept():
+@pytest.mark.parametrize("Eng", ENGINES)
+def test_every_request_served_and_grid_order_kept(Eng):
     pool = fake_pool([100, 200, 300, 400, 500])
-    eng = FakeEngine(10_000)
+    eng = Eng(10_000)
     srv = Server(pool, eng, 1e12, rbytes, chunk=8, keep_q=False)
     rng = np.random.default_rng(0)
     reqs = requests(rng.integers(0, 5, 60))
@@ -101,10 +147,11 @@ def test_every_request_served_and_grid_order_kept():
     assert srv.work == sum(r.iters * r.unknowns for r in reqs)
 
 
-def test_requests_join_running_launches():
+@pytest.mark.parametrize("Eng", ENGINES)
+def test_requests_join_running_launches(Eng):
     """Continuous batching: requests admitted together share their launches."""
     pool = fake_pool([100, 100, 100])
-    srv = Server(pool, FakeEngine(10_000), 1e12, rbytes, chunk=4, keep_q=False)
+    srv = Server(pool, Eng(10_000), 1e12, rbytes, chunk=4, keep_q=False)
     reqs = requests([0, 1, 2])
     srv.run(reqs, realtime=False)
     # 40 iterations at 1e-8 (requests 0, 2) and 80 at 1e-10 (request 1) in chunks of 4
@@ -112,9 +159,10 @@ def test_requests_join_running_launches():
     assert srv.launches == 20
 
 
-def test_budget_admission_and_lru_eviction():
+@pytest.mark.parametrize("Eng", ENGINES)
+def test_budget_admission_and_lru_eviction(Eng):
     pool = fake_pool([1000, 1000, 1000, 1000])
-    eng = FakeEngine(10_000)
+    eng = Eng(10_000)
     budget = 2.5 * 100 * 1000  # room for two grids
     srv = Server(pool, eng, budget, rbytes, chunk=8, keep_q=False)
     reqs = requests([0, 1, 2, 3, 0, 1, 2, 3, 0])
@@ -126,9 +174,10 @@ def test_budget_admission_and_lru_eviction():
     assert not any(r.warm for r in reqs[4:8])  # each revisit found its grid evicted
 
 
-def test_engine_capacity_triggers_eviction():
+@pytest.mark.parametrize("Eng", ENGINES)
+def test_engine_capacity_triggers_eviction(Eng):
     pool = fake_pool([600, 600, 600])
-    eng = FakeEngine(1300)  # the arena holds two grids although the budget holds all
+    eng = Eng(1300)  # the arena holds two grids although the budget holds all
     srv = Server(pool, eng, 1e12, rbytes, chunk=8, keep_q=False)
     reqs = requests([0, 1, 2, 0])
     srv.run(reqs, realtime=False)
@@ -149,7 +198,8 @@ def test_request_right_hand_side_mix():
     assert request_src(pool, Request(1, 0, 0, 1e-8, 0.0)) is pool[0][0].src
 
 
-def test_poisson_stream_and_realtime_loop():
+@pytest.mark.parametrize("Eng", ENGINES)
+def test_poisson_stream_and_realtime_loop(Eng):
     reqs = poisson_stream(3, 2, rate=2000.0, seconds=0.05, seed=3)
     n = len(reqs)
     assert abs(n - 100) < 5 * np.sqrt(100)
@@ -157,7 +207,7 @@ def test_poisson_stream_and_realtime_loop():
     assert t == sorted(t) and t[-1] < 0.05
     assert {r.tol for r in reqs} <= {1e-8, 1e-10}
     assert all(0.0 <= r.mix < 1.0 for r in reqs)
-    srv = Server(fake_pool([100, 100, 100]), FakeEngine(10_000), 1e12, rbytes, chunk=16, keep_q=False)
+    srv = Server(fake_pool([100, 100, 100]), Eng(10_000), 1e12, rbytes, chunk=16, keep_q=False)
     srv.run(reqs, realtime=True)
     assert all(r.t_done >= r.t_arrival and r.t_admit >= r.t_arrival for r in reqs)
     rep = latency_report(reqs, srv.t_end)
@@ -178,3 +228,24 @@ def test_prefetched_sources_equal_direct():
                  sources=PrefetchedSources(pool, reqs).get)
     srv.run(reqs, realtime=False)
     assert all(r.t_done >= 0 for r in reqs)
+
+
+def test_overlapped_loop_admits_during_launches():
+    """With launch / wait, a request arriving while a launch runs is admitted
+    before that launch is waited for and joins the next one."""
+    pool = fake_pool([100, 100])
+    eng = FakeAsyncEngine(10_000)
+    srv = Server(pool, eng, 1e12, rbytes, chunk=4, keep_q=False)
+    reqs = requests([0, 1])
+    seen = []
+    orig_wait = eng.wait
+
+    def wait():
+        seen.append(sorted(eng.inst))  # problems resident when the launch in flight is waited for
+        return orig_wait()
+
+    eng.wait = wait
+    srv.run(reqs, realtime=False)
+    assert all(r.t_done >= 0 for r in reqs)
+    assert srv.launches == 20 and srv.work == sum(r.iters * r.unknowns for r in reqs)
+    assert seen[0] == [0, 1]
