@@ -438,24 +438,34 @@ int sgpu_q_upload(sgpu_context* ctx, const int* ctop, const double* const* dzz, 
   double* s_c = s_src + n3;
   double* s_dzf = s_c + n3;
   double* s_D = s_dzf + ne3;
+  // each array goes up as soon as it is gathered, so its copy overlaps the next gather
+  cudaStream_t st = ctx->stream;
   for (int j = 0; j < ctx->Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
   ctx->h_ctop.assign(ctop, ctop + ctx->Nc);
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * ctx->Nc, cudaMemcpyHostToDevice, st));
   gather_cells(ctx, dzz, s_dzz);
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
   gather_cells(ctx, q, s_q);
+  CK(cudaMemcpyAsync(ctx->d_qin, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
   gather_cells(ctx, src, s_src);
-  if (c) gather_cells(ctx, c, s_c);
-  else std::fill(s_c, s_c + n3, 1.0);
+  CK(cudaMemcpyAsync(ctx->d_srcin, s_src, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  // c is read only at the type-3 boundary columns (the solver conditions the
+  // computational ones itself), so only their slots go up
+  const size_t n3c = ctx->n3c;
+  if (n3 > n3c) {
+    for (int j = ctx->ncomp; j < ctx->Nc; ++j) {
+      const int i = ctx->dev2cell[j];
+      if (c) std::memcpy(s_c + ctx->dcoff[j], c[i], sizeof(double) * ctx->Nk[i]);
+      else std::fill(s_c + ctx->dcoff[j], s_c + ctx->dcoff[j] + ctx->Nk[i], 1.0);
+    }
+    CK(cudaMemcpyAsync(ctx->d_cin + n3c, s_c + n3c, sizeof(double) * (n3 - n3c), cudaMemcpyHostToDevice, st));
+  }
   host_parallel(ctx->Ne, [&](long long b, long long e) {
     for (long long k = b; k < e; ++k) std::memcpy(s_dzf + ctx->eoff[k], dzf[k], sizeof(double) * ctx->Nke[k]);
   });
+  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
   std::memcpy(s_D, D, sizeof(double) * ctx->Ne);
-  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * ctx->Nc, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_qin, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_srcin, s_src, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_cin, s_c, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_Dq, s_D, sizeof(double) * ctx->Ne, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_Dq, s_D, sizeof(double) * ctx->Ne, cudaMemcpyHostToDevice, st));
   ctx->q_uploaded = true;
   ctx->q_solved = false;
   return SGPU_OK;
@@ -1026,8 +1036,11 @@ int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, cons
   gather_cells(ctx, dzz, s_dzz);
   gather_cells(ctx, (const double* const*)qc, s_qc);
   gather_cells(ctx, (const double* const*)q, s_q);
-  if (c) gather_cells(ctx, c, s_c);
-  else std::fill(s_c, s_c + n3, 1.0);
+  for (int j = ctx->ncomp; j < ctx->Nc; ++j) {  // c is read only at the type-3 boundary columns
+    const int i = ctx->dev2cell[j];
+    if (c) std::memcpy(s_c + ctx->dcoff[j], c[i], sizeof(double) * ctx->Nk[i]);
+    else std::fill(s_c + ctx->dcoff[j], s_c + ctx->dcoff[j] + ctx->Nk[i], 1.0);
+  }
   gather_edges(ctx, dzf, s_dzf);
   gather_edges(ctx, (const double* const*)u, s_u);
   gather_edges(ctx, utmp2, s_ut2);
@@ -1038,7 +1051,9 @@ int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, cons
   CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_qin, s_qc, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_qtot, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_cin, s_c, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  if (n3 > (size_t)ctx->n3c)
+    CK(cudaMemcpyAsync(ctx->d_cin + ctx->n3c, s_c + ctx->n3c, sizeof(double) * (n3 - ctx->n3c), cudaMemcpyHostToDevice,
+                       ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_dzf, s_dzf, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_u, s_u, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_ut2, s_ut2, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
