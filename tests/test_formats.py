@@ -233,3 +233,38 @@ def test_store_round_trip_and_layout(tmp_path, turbmodel):
     assert np.array_equal(np.frombuffer(raw[off:off + 8 * ne3].tobytes(), dtype=np.float64), fields["u"])
     with pytest.raises(ValueError):
         fm.read_store(p, g.Nk, g.Nke, 1 - turbmodel)
+
+
+def _hybrid_grid():
+    """A quad channel with every third quad split into two triangles (maxfaces 4, mixed nfaces)."""
+    nx, ny, dx = 9, 4, 10.0
+    X, Y = np.meshgrid(np.arange(nx + 1) * dx, np.arange(ny + 1) * dx, indexing="xy")
+    pts = np.stack([X.ravel(), Y.ravel()], 1)
+    pid = lambda ix, iy: iy * (nx + 1) + ix
+    cells, nf = [], []
+    for iy in range(ny):
+        for ix in range(nx):
+            a, b, c, d = pid(ix, iy), pid(ix + 1, iy), pid(ix + 1, iy + 1), pid(ix, iy + 1)
+            if (ix + iy) % 3 == 0:
+                cells += [[a, b, c, -1], [a, c, d, -1]]
+                nf += [3, 3]
+            else:
+                cells.append([a, b, c, d])
+                nf.append(4)
+    cells = np.array(cells)
+    cells = np.where(cells < 0, cells[:, :1], cells)  # padding slots are ignored past nfaces
+    return gg._assemble(pts, cells, np.array(nf, dtype=np.int32), 4, lambda x, y: 6.0 + 0.1 * x, 5, 1.0, False,
+                        np.random.default_rng(1), "hybrid")
+
+
+def test_hybrid_grid_round_trip_and_reference(tmp_path):
+    g = _hybrid_grid()
+    g.validate()
+    assert set(np.unique(g.nfaces)) == {3, 4}
+    gf, d = _write(tmp_path, g)
+    rd = fm.read_grid(d, maxfaces=4)
+    assert np.array_equal(rd.nfaces, g.nfaces) and np.array_equal(rd.face, gf.face)
+    assert np.array_equal(rd.neigh, gf.neigh) and np.array_equal(rd.cells, gf.cells)
+    assert np.array_equal(rd.def_, _round(gf.def_))
+    if om.available("ref"):
+        _compare_ref(om.Oracle("ref").read_grid(d), rd)
