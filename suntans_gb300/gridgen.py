@@ -241,6 +241,29 @@ def quad_channel(nx=64, ny=16, dx=10.0, dy=10.0, depth=20.0, Nkmax=32, rstretch=
                      open_x0=open_x0, maxdepth=None if depth_fn is None else None)
 
 
+def hybrid_channel(nx=12, ny=6, dx=10.0, Nkmax=8, split_every=3, seed=0, h_sigma=0.0, ctop_frac=0.0,
+                   depth_fn=None, open_x0=False):
+    """A quad channel with every `split_every`-th quad (in a diagonal pattern)
+    split into two triangles: maxfaces 4 with cells of 3 and 4 faces."""
+    rng = np.random.default_rng(seed)
+    X, Y = np.meshgrid(np.arange(nx + 1) * dx, np.arange(ny + 1) * dx, indexing="xy")
+    pts = np.stack([X.ravel(), Y.ravel()], 1)
+    cells, nf = [], []
+    for iy in range(ny):
+        for ix in range(nx):
+            a, b = iy * (nx + 1) + ix, iy * (nx + 1) + ix + 1
+            c, d = (iy + 1) * (nx + 1) + ix + 1, (iy + 1) * (nx + 1) + ix
+            if (ix + iy) % split_every == 0:
+                cells += [[a, b, c, a], [a, c, d, a]]
+                nf += [3, 3]
+            else:
+                cells.append([a, b, c, d])
+                nf.append(4)
+    dfn = depth_fn if depth_fn is not None else (lambda x, y: 6.0 + 0.1 * x)
+    return _assemble(pts, np.array(cells), np.array(nf, dtype=I32), 4, dfn, Nkmax, 1.0, False, rng,
+                     name=f"hybrid{nx}x{ny}x{Nkmax}", h_sigma=h_sigma, ctop_frac=ctop_frac, open_x0=open_x0)
+
+
 def seamount_depth(Lx, Ly, H0=50.0, amp=30.0, sigma=2000.0):
     def f(x, y):
         r2 = (x - 0.5 * Lx) ** 2 + (y - 0.5 * Ly) ** 2

@@ -18,6 +18,8 @@ def grid_cases():
                                                         rstretch=1.05, ctop_frac=0.05, h_sigma=0.02, seed=7)),
         ("tri400_shallow", lambda: gg.delaunay_seamount(400, 1000, 500, Nkmax=6, H0=6.0, amp=5.5, sigma=150,
                                                        ctop_frac=0.5, h_sigma=0.05, seed=11)),
+        ("hybrid30x12", lambda: gg.hybrid_channel(30, 12, Nkmax=10, h_sigma=0.05, ctop_frac=0.2, seed=13,
+                                                  open_x0=True)),
     ]
 
 
