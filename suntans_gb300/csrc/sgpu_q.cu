@@ -425,6 +425,11 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
   }
 
   // ---- the CG loop (2478-2525) ----
+  // x += nu p (2506-2507) is carried out in C, where p is read anyway, before
+  // p changes: the same operation on the same operands, one read and one
+  // write of p fewer per iteration.  When the loop ends after B, the last one
+  // is still pending and is done at the end.
+  bool x_pending = false;
   for (;;) {
     if (ld_volatile_int(&ctl->done)) break;
     // A: z = A p, p.z -- flat over the computational storage: slot u of
@@ -483,7 +488,6 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
         const int T = G * kBlock;
 #pragma unroll 4
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
-          a.x[u] += nu * a.p[u];
           const double ru = a.r[u] - nu * a.z[u];
           a.r[u] = ru;
           part[0] += ru * ru;
@@ -498,7 +502,6 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
         for (int sl = tid; sl <= len; sl += kBlock) {
           const int u = base + sl;
           if (sl < len) {
-            a.x[u] += nu * a.p[u];
             const double ru = a.r[u] - nu * a.z[u];
             a.r[u] = ru;
             s_tri.r[sl] = ru;
@@ -556,25 +559,38 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
             }
           }))
         return;
+      x_pending = true;
       if (ld_volatile_int(&ctl->done)) break;
     }
-    // C: p = r + mu p  (or rt + mu p)
+    // C: x += nu p; p = r + mu p  (or rt + mu p)
     {
       const double mu = *(volatile double*)&ctl->mu;
+      const double nu = *(volatile double*)&ctl->nu;
       const double* src = (QP == 2) ? a.rt : a.r;
       const int T = G * kBlock;
 #pragma unroll 4
-      for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) a.p[u] = src[u] + mu * a.p[u];
+      for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
+        const double pu = a.p[u];
+        a.x[u] += nu * pu;
+        a.p[u] = src[u] + mu * pu;
+      }
+      x_pending = false;
       if (!grid_sync(ctl, 6, [] {})) return;
     }
   }
+  const double nu_last = *(volatile double*)&ctl->nu;
 
-  // ---- rescale (2539-2546) ----
+  // ---- the pending x update, and the rescale (2539-2546), each slot by one thread ----
   if (QP == 1) {
     for (int t = blockIdx.x; t < a.ntiles; t += G) {
       const int base = a.dcoff[a.tile_col[t]], end = a.dcoff[a.tile_col[t + 1]];
-      for (int u = base + tid; u < end; u += kBlock) a.x[u] /= a.c[u];
+      for (int u = base + tid; u < end; u += kBlock) {
+        if (x_pending) a.x[u] += nu_last * a.p[u];
+        a.x[u] /= a.c[u];
+      }
     }
+  } else if (x_pending) {
+    for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += G * kBlock) a.x[u] += nu_last * a.p[u];
   }
 }
 
