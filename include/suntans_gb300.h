@@ -196,6 +196,18 @@ typedef struct sgpu_wpred_fields {
 int sgpu_wpredictor(sgpu_context *ctx, const int *ctop, const double *const *dzz, const sgpu_wpred_fields *f,
                     const sgpu_props *prop, double *const *w, double *const *Cn_W, double *const *Cn_W2);
 
+/* The nonhydrostatic part of Solve in one call (main/phys.c:1271-1289):
+ * WPredictor -> ComputeQSource -> CGSolveQ -> Corrector, with w, q, the
+ * right-hand side, D and the correction kept in HBM between the steps.  wf
+ * supplies WPredictor's viscosities and settings (its q and utmp2 are the q
+ * and utmp2 given here); Cn_W / Cn_W2 are its histories, updated in place.
+ * Every step but the solve has the reference's bits. */
+int sgpu_nonhydrostatic_step(sgpu_context *ctx, const int *ctop, const int *etop, const double *const *dzz,
+                             const double *const *dzf, const double *const *utmp2, const double *const *wtmp2,
+                             const sgpu_wpred_fields *wf, double *const *u, double *const *w, double *const *q,
+                             double *const *qc, const double *const *c, double *const *Cn_W, double *const *Cn_W2,
+                             const sgpu_props *prop, sgpu_stats *stats);
+
 /* ---- UPredictor (main/phys.c:2579-3077): the predictor around CGSolve ---- */
 
 /* The edge description UPredictor's boundary steps read, once per grid: every

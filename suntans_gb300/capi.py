@@ -26,7 +26,7 @@ EXPORTS = [
     "sgpu_h_upload", "sgpu_h_solve", "sgpu_h_download",
     "sgpu_set_timeout_ns", "sgpu_set_grid", "sgpu_stream", "sgpu_phase_times",
     "sgpu_cgsolve_noalloc",
-    "sgpu_step_grid", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_pressure_step",
+    "sgpu_step_grid", "sgpu_compute_qsource", "sgpu_corrector", "sgpu_pressure_step", "sgpu_nonhydrostatic_step",
     "sgpu_update_dz", "sgpu_set_flux_height",
     "sgpu_wpredictor",
     "sgpu_upredictor_grid", "sgpu_upredictor_vertical", "sgpu_upredictor_rhs", "sgpu_upredictor_finish",
@@ -124,6 +124,9 @@ def load() -> C.CDLL:
     lib.sgpu_corrector.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dp, C.c_double, _dpp, _dpp, _dpp]
     lib.sgpu_pressure_step.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp,
                                        C.POINTER(Props), C.POINTER(Stats)]
+    lib.sgpu_nonhydrostatic_step.argtypes = [C.c_void_p, _ip, _ip, _dpp, _dpp, _dpp, _dpp, C.POINTER(WPredFieldsC),
+                                             _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, _dpp, C.POINTER(Props),
+                                             C.POINTER(Stats)]
     lib.sgpu_cgsolveq.argtypes = [C.c_void_p, _ip, _dpp, _dpp, _dp, _dpp, _dpp, _dpp, C.POINTER(Props),
                                   C.POINTER(Stats)]
     lib.sgpu_cgsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, C.POINTER(Props), C.POINTER(Stats)]
@@ -371,6 +374,43 @@ class Context:
                                          *[_vp(x) for x in ptr], C.byref(pr), C.byref(stt))
         self._check(rc, "sgpu_pressure_step")
         return qc, u, w, q, stt
+
+    def nonhydrostatic_step(self, st, wf, props: SolverProps):
+        """WPredictor -> ComputeQSource -> CGSolveQ -> Corrector in one call, on
+        the step's w, q and utmp2 (wf gives the viscosities, histories and
+        settings): returns (qc, u, w, q, Cn_W, Cn_W2, Stats)."""
+        g = self.grid
+        u = np.array(st.u, dtype=np.float64, copy=True)
+        w = np.array(st.w, dtype=np.float64, copy=True)
+        q = np.array(st.q, dtype=np.float64, copy=True)
+        qc = np.array(st.qc, dtype=np.float64, copy=True)
+        cw = np.array(wf.Cn_W, dtype=np.float64, copy=True)
+        cw2 = np.array(wf.Cn_W2, dtype=np.float64, copy=True)
+        ut2 = np.ascontiguousarray(st.utmp2, dtype=np.float64)
+        wt2 = np.ascontiguousarray(st.wtmp2, dtype=np.float64)
+        c = np.ascontiguousarray(st.c, dtype=np.float64)
+        dzz = np.ascontiguousarray(g.dzz)
+        dzf = np.ascontiguousarray(g.dzf)
+        nt = np.ascontiguousarray(wf.nu_tv, dtype=np.float64)
+        nl = np.ascontiguousarray(wf.nu_lax, dtype=np.float64)
+        ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        etop = np.ascontiguousarray(st.etop, dtype=np.int32)
+        E = (lambda a: jagged(a, self.eoff)) if g.Ne else (lambda a: np.zeros(1, np.uint64))
+        woff = st.woff
+        f_rows = [jagged(q, self.coff), jagged(nt, self.coff), jagged(nl, self.coff), E(ut2)]
+        f = WPredFieldsC(*[_vp(r) for r in f_rows], float(wf.nu), float(wf.nu_H), float(wf.CdW),
+                         float(wf.laxWendroff_Vertical), int(wf.nonlinear), int(wf.conserveMomentum), int(wf.n),
+                         int(wf.AB))
+        ptr = [jagged(dzz, self.coff), E(dzf), E(ut2), jagged(wt2, woff)]
+        out = [E(u), jagged(w, woff), jagged(q, self.coff), jagged(qc, self.coff), jagged(c, self.coff),
+               jagged(cw, self.coff), jagged(cw2, self.coff)]
+        pr = props_struct(props)
+        stt = Stats()
+        rc = self.lib.sgpu_nonhydrostatic_step(self.h, ctop.ctypes.data_as(_ip), etop.ctypes.data_as(_ip),
+                                               *[_vp(x) for x in ptr], C.byref(f), *[_vp(x) for x in out],
+                                               C.byref(pr), C.byref(stt))
+        self._check(rc, "sgpu_nonhydrostatic_step")
+        return qc, u, w, q, cw, cw2, stt
 
     # ---- the vertical grid of the step ----
     def _vgrid(self, vf):

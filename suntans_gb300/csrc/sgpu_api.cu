@@ -1001,23 +1001,42 @@ int sgpu_corrector(sgpu_context* ctx, const int* ctop, const int* etop, const do
   return SGPU_OK;
 }
 
-int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
-                       const double* const* dzf, const double* const* utmp2, const double* const* wtmp2,
-                       double* const* u, double* const* w, double* const* q, double* const* qc,
-                       const double* const* c, const sgpu_props* prop, sgpu_stats* st) {
+static int alloc_upred(sgpu_context* ctx);
+static int alloc_wpred(sgpu_context* ctx);
+static int kmax_for(int Nkmax);
+static WPredArgs wpred_args(sgpu_context* ctx, const sgpu_wpred_fields* f, const sgpu_props* prop);
+static void scatter_cells_all(sgpu_context* ctx, const double* src, double* const* rows);
+
+// ComputeQSource -> CGSolveQ -> Corrector with the right-hand side and the
+// correction in HBM; with wf, WPredictor first (its w, the pressure q and the
+// histories stay in HBM into ComputeQSource and Corrector).
+static int pressure_step_impl(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                              const double* const* dzf, const double* const* utmp2, const double* const* wtmp2,
+                              double* const* u, double* const* w, double* const* q, double* const* qc,
+                              const double* const* c, const sgpu_wpred_fields* wf, double* const* Cn_W,
+                              double* const* Cn_W2, const sgpu_props* prop, sgpu_stats* st) {
   auto t0 = std::chrono::steady_clock::now();
   if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
   if (!ctop || !etop || !dzz || !dzf || !utmp2 || !wtmp2 || !u || !w || !q || !qc || !prop)
     return fail(ctx, SGPU_BAD_ARG, "null argument");
   if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
   if (!(prop->theta != 0) || !(prop->dt != 0)) return fail(ctx, SGPU_BAD_ARG, "theta and dt must be nonzero");
+  if (wf) {
+    if (!wf->nu_tv || !wf->nu_lax || !Cn_W || !Cn_W2) return fail(ctx, SGPU_BAD_ARG, "null argument");
+    if (wf->nonlinear != 0 && wf->nonlinear != 1)
+      return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device supports nonlinear 0 and 1, not %d", wf->nonlinear);
+    if (wf->conserveMomentum) return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device needs conserveMomentum 0");
+    if (ctx->Nkmax + 1 > 128) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs Nkmax <= 127");
+    if (ctx->F > 8) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs maxfaces <= 8");
+  }
   int rc;
   if ((rc = check_ctop(ctx, ctop))) return rc;
   DeviceGuard dg(ctx->device);
   if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx))) return rc;
+  if (wf && ((rc = alloc_upred(ctx)) || (rc = alloc_wpred(ctx)))) return rc;
   const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, n_ctop = (ctx->Nc + 1) / 2 + 1,
                n_etop = (ctx->Ne + 1) / 2 + 1;
-  if ((rc = ensure_pinned(ctx, n_ctop + n_etop + 4 * n3 + 3 * ne3 + 2 * nw3 + 8))) return rc;
+  if ((rc = ensure_pinned(ctx, n_ctop + n_etop + (wf ? 8 : 4) * n3 + 3 * ne3 + 2 * nw3 + 8))) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   int* s_ctop = (int*)ctx->pin;
   int* s_etop = (int*)(ctx->pin + n_ctop);
@@ -1030,6 +1049,10 @@ int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, cons
   double* s_ut2 = s_u + ne3;
   double* s_w = s_ut2 + ne3;
   double* s_wt2 = s_w + nw3;
+  double* s_nt = s_wt2 + nw3;  // WPredictor only: nu_tv, nu_lax, Cn_W, Cn_W2
+  double* s_nl = s_nt + n3;
+  double* s_c1 = s_nl + n3;
+  double* s_c2 = s_c1 + n3;
   for (int j = 0; j < ctx->Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
   for (int e = 0; e < ctx->Ne; ++e) s_etop[e] = etop[e];
   ctx->h_ctop.assign(ctop, ctop + ctx->Nc);
@@ -1059,6 +1082,20 @@ int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, cons
   CK(cudaMemcpyAsync(ctx->d_ut2, s_ut2, sizeof(double) * ne3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_wt2, s_wt2, sizeof(double) * nw3, cudaMemcpyHostToDevice, ctx->stream));
+  if (wf) {
+    gather_cells(ctx, wf->nu_tv, s_nt);
+    gather_cells(ctx, wf->nu_lax, s_nl);
+    gather_cells(ctx, (const double* const*)Cn_W, s_c1);
+    gather_cells(ctx, (const double* const*)Cn_W2, s_c2);
+    CK(cudaMemcpyAsync(ctx->d_nutv, s_nt, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_nulax, s_nl, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_cnw, s_c1, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_cnw2, s_c2, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+    // WPredictor on the uploaded w, u (advecting velocity utmp2) and q
+    WPredArgs wa = wpred_args(ctx, wf, prop);
+    if (wf->nonlinear) CK(cudaMemsetAsync(ctx->d_wface, 0, sizeof(double) * ne3, ctx->stream));
+    CK(launch_wpredictor(wa, ctx->stream));
+  }
   // ComputeQSource straight into the solver's right-hand side and D
   StepArgs a = step_args(ctx, prop->theta, prop->dt);
   CK(launch_qsource(a, ctx->stream));
@@ -1073,13 +1110,38 @@ int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, cons
   CK(cudaMemcpyAsync(s_q, ctx->d_qtot, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(s_u, ctx->d_u, sizeof(double) * ne3, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(s_w, ctx->d_w, sizeof(double) * nw3, cudaMemcpyDeviceToHost, ctx->stream));
+  if (wf) {
+    CK(cudaMemcpyAsync(s_c1, ctx->d_cnw, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(s_c2, ctx->d_cnw2, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   scatter_cells_active(ctx, s_qc, qc, ctop, ctx->ncomp);
   scatter_cells_active(ctx, s_q, q, ctop, ctx->ncomp);
   scatter_edges(ctx, s_u, u);
   scatter_wrows(ctx, s_w, w, ctx->ncomp);
+  if (wf) {
+    scatter_cells_all(ctx, s_c1, Cn_W);
+    scatter_cells_all(ctx, s_c2, Cn_W2);
+  }
   if (st) st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return rc;
+}
+
+int sgpu_pressure_step(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                       const double* const* dzf, const double* const* utmp2, const double* const* wtmp2,
+                       double* const* u, double* const* w, double* const* q, double* const* qc,
+                       const double* const* c, const sgpu_props* prop, sgpu_stats* st) {
+  return pressure_step_impl(ctx, ctop, etop, dzz, dzf, utmp2, wtmp2, u, w, q, qc, c, nullptr, nullptr, nullptr, prop,
+                            st);
+}
+
+int sgpu_nonhydrostatic_step(sgpu_context* ctx, const int* ctop, const int* etop, const double* const* dzz,
+                             const double* const* dzf, const double* const* utmp2, const double* const* wtmp2,
+                             const sgpu_wpred_fields* wf, double* const* u, double* const* w, double* const* q,
+                             double* const* qc, const double* const* c, double* const* Cn_W, double* const* Cn_W2,
+                             const sgpu_props* prop, sgpu_stats* st) {
+  if (!wf) return ctx ? fail(ctx, SGPU_BAD_ARG, "null argument") : SGPU_BAD_ARG;
+  return pressure_step_impl(ctx, ctop, etop, dzz, dzf, utmp2, wtmp2, u, w, q, qc, c, wf, Cn_W, Cn_W2, prop, st);
 }
 
 
@@ -1709,53 +1771,7 @@ static int alloc_wpred(sgpu_context* ctx) {
   return SGPU_OK;
 }
 
-int sgpu_wpredictor(sgpu_context* ctx, const int* ctop, const double* const* dzz, const sgpu_wpred_fields* f,
-                    const sgpu_props* prop, double* const* w, double* const* Cn_W, double* const* Cn_W2) {
-  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
-  if (!ctop || !dzz || !f || !f->q || !f->nu_tv || !f->nu_lax || !prop || !w || !Cn_W || !Cn_W2 ||
-      (f->nonlinear && !f->utmp2))
-    return fail(ctx, SGPU_BAD_ARG, "null argument");
-  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
-  if (f->nonlinear != 0 && f->nonlinear != 1)
-    return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device supports nonlinear 0 and 1, not %d", f->nonlinear);
-  if (f->conserveMomentum) return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device needs conserveMomentum 0");
-  if (ctx->Nkmax + 1 > 128) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs Nkmax <= 127");
-  if (ctx->F > 8) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs maxfaces <= 8");
-  int rc;
-  if ((rc = check_ctop(ctx, ctop))) return rc;
-  DeviceGuard dg(ctx->device);
-  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx)) || (rc = alloc_upred(ctx)) || (rc = alloc_wpred(ctx))) return rc;
-  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, Nc = ctx->Nc, ni = Nc / 2 + 1;
-  if ((rc = ensure_pinned(ctx, ni + 6 * n3 + ne3 + nw3 + 8))) return rc;
-  CK(cudaStreamSynchronize(ctx->stream));
-  int* s_ctop = (int*)ctx->pin;
-  double* s_dzz = ctx->pin + ni;
-  double* s_q = s_dzz + n3;
-  double* s_nt = s_q + n3;
-  double* s_nl = s_nt + n3;
-  double* s_c1 = s_nl + n3;
-  double* s_c2 = s_c1 + n3;
-  double* s_u2 = s_c2 + n3;
-  double* s_w = s_u2 + ne3;
-  for (size_t j = 0; j < Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
-  gather_cells(ctx, dzz, s_dzz);
-  gather_cells(ctx, f->q, s_q);
-  gather_cells(ctx, f->nu_tv, s_nt);
-  gather_cells(ctx, f->nu_lax, s_nl);
-  gather_cells(ctx, (const double* const*)Cn_W, s_c1);
-  gather_cells(ctx, (const double* const*)Cn_W2, s_c2);
-  if (f->nonlinear) gather_edges(ctx, f->utmp2, s_u2);
-  gather_wrows(ctx, (const double* const*)w, s_w);
-  cudaStream_t st = ctx->stream;
-  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * Nc, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_qtot, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_nutv, s_nt, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_nulax, s_nl, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_cnw, s_c1, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_cnw2, s_c2, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-  if (f->nonlinear) CK(cudaMemcpyAsync(ctx->d_ut2, s_u2, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, st));
+static WPredArgs wpred_args(sgpu_context* ctx, const sgpu_wpred_fields* f, const sgpu_props* prop) {
   WPredArgs a{};
   a.Nc = ctx->Nc;
   a.ncomp = ctx->ncomp;
@@ -1810,6 +1826,57 @@ int sgpu_wpredictor(sgpu_context* ctx, const int* ctop, const double* const* dzz
   a.wtmp = ctx->d_wt;
   a.wc = ctx->d_wcc;
   a.ut = ctx->d_wface;
+  return a;
+}
+
+int sgpu_wpredictor(sgpu_context* ctx, const int* ctop, const double* const* dzz, const sgpu_wpred_fields* f,
+                    const sgpu_props* prop, double* const* w, double* const* Cn_W, double* const* Cn_W2) {
+  if (!ctx || !ctx->stream) return ctx ? fail(ctx, SGPU_NO_DEVICE, "context has no device state") : SGPU_BAD_ARG;
+  if (!ctop || !dzz || !f || !f->q || !f->nu_tv || !f->nu_lax || !prop || !w || !Cn_W || !Cn_W2 ||
+      (f->nonlinear && !f->utmp2))
+    return fail(ctx, SGPU_BAD_ARG, "null argument");
+  if (!ctx->step_grid) return fail(ctx, SGPU_BAD_ARG, "sgpu_step_grid has not been called");
+  if (f->nonlinear != 0 && f->nonlinear != 1)
+    return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device supports nonlinear 0 and 1, not %d", f->nonlinear);
+  if (f->conserveMomentum) return fail(ctx, SGPU_BAD_ARG, "WPredictor on the device needs conserveMomentum 0");
+  if (ctx->Nkmax + 1 > 128) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs Nkmax <= 127");
+  if (ctx->F > 8) return fail(ctx, SGPU_BAD_GRID, "WPredictor on the device needs maxfaces <= 8");
+  int rc;
+  if ((rc = check_ctop(ctx, ctop))) return rc;
+  DeviceGuard dg(ctx->device);
+  if ((rc = alloc_q(ctx)) || (rc = alloc_step(ctx)) || (rc = alloc_upred(ctx)) || (rc = alloc_wpred(ctx))) return rc;
+  const size_t n3 = ctx->n3, ne3 = ctx->ne3, nw3 = ctx->nw3, Nc = ctx->Nc, ni = Nc / 2 + 1;
+  if ((rc = ensure_pinned(ctx, ni + 6 * n3 + ne3 + nw3 + 8))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int* s_ctop = (int*)ctx->pin;
+  double* s_dzz = ctx->pin + ni;
+  double* s_q = s_dzz + n3;
+  double* s_nt = s_q + n3;
+  double* s_nl = s_nt + n3;
+  double* s_c1 = s_nl + n3;
+  double* s_c2 = s_c1 + n3;
+  double* s_u2 = s_c2 + n3;
+  double* s_w = s_u2 + ne3;
+  for (size_t j = 0; j < Nc; ++j) s_ctop[j] = ctop[ctx->dev2cell[j]];
+  gather_cells(ctx, dzz, s_dzz);
+  gather_cells(ctx, f->q, s_q);
+  gather_cells(ctx, f->nu_tv, s_nt);
+  gather_cells(ctx, f->nu_lax, s_nl);
+  gather_cells(ctx, (const double* const*)Cn_W, s_c1);
+  gather_cells(ctx, (const double* const*)Cn_W2, s_c2);
+  if (f->nonlinear) gather_edges(ctx, f->utmp2, s_u2);
+  gather_wrows(ctx, (const double* const*)w, s_w);
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->d_ctop, s_ctop, sizeof(int) * Nc, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_dzz, s_dzz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_qtot, s_q, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_nutv, s_nt, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_nulax, s_nl, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_cnw, s_c1, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_cnw2, s_c2, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+  if (f->nonlinear) CK(cudaMemcpyAsync(ctx->d_ut2, s_u2, sizeof(double) * ne3, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->d_w, s_w, sizeof(double) * nw3, cudaMemcpyHostToDevice, st));
+  WPredArgs a = wpred_args(ctx, f, prop);
   if (f->nonlinear) CK(cudaMemsetAsync(ctx->d_wface, 0, sizeof(double) * ne3, st));
   CK(launch_wpredictor(a, st));
   CK(cudaMemcpyAsync(s_w, ctx->d_w, sizeof(double) * nw3, cudaMemcpyDeviceToHost, st));

@@ -247,6 +247,26 @@ void sgpu_UPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int nump
  * conserveMomentum 0 and grids without type-2 or type-4 edges.  Its scratch
  * fields (phys->wtmp, stmp, wc, ut) are left untouched; nothing reads them
  * after it.  Same bits as the reference. */
+static void sgpu_wpred_from(gridT *grid, physT *phys, propT *prop, sgpu_wpred_fields *f) {
+  if ((prop->nonlinear != 0 && prop->nonlinear != 1) || prop->conserveMomentum ||
+      grid->edgedist[3] > grid->edgedist[2] || grid->edgedist[5] > grid->edgedist[4]) {
+    fprintf(stderr, "sgpu: WPredictor on the GPU needs nonlinear 0 or 1, conserveMomentum 0 and no type-2/4 edges\n");
+    exit(EXIT_FAILURE);
+  }
+  f->q = (const double *const *)phys->q;
+  f->nu_tv = (const double *const *)phys->nu_tv;
+  f->nu_lax = (const double *const *)phys->nu_lax;
+  f->utmp2 = (const double *const *)phys->utmp2;
+  f->nu = prop->nu;
+  f->nu_H = prop->nu_H;
+  f->CdW = prop->CdW;
+  f->laxWendroff_Vertical = prop->laxWendroff_Vertical;
+  f->nonlinear = prop->nonlinear;
+  f->conserveMomentum = prop->conserveMomentum;
+  f->n = prop->n;
+  f->AB = prop->AB;
+}
+
 void sgpu_WPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm) {
   sgpu_wpred_fields f;
   sgpu_props p;
@@ -254,25 +274,42 @@ void sgpu_WPredictor(gridT *grid, physT *phys, propT *prop, int myproc, int nump
   (void)myproc;
   (void)comm;
   sgpu_ensure_step(grid, numprocs);
-  if ((prop->nonlinear != 0 && prop->nonlinear != 1) || prop->conserveMomentum ||
-      grid->edgedist[3] > grid->edgedist[2] || grid->edgedist[5] > grid->edgedist[4]) {
-    fprintf(stderr, "sgpu: WPredictor on the GPU needs nonlinear 0 or 1, conserveMomentum 0 and no type-2/4 edges\n");
-    exit(EXIT_FAILURE);
-  }
-  f.q = (const double *const *)phys->q;
-  f.nu_tv = (const double *const *)phys->nu_tv;
-  f.nu_lax = (const double *const *)phys->nu_lax;
-  f.utmp2 = (const double *const *)phys->utmp2;
-  f.nu = prop->nu;
-  f.nu_H = prop->nu_H;
-  f.CdW = prop->CdW;
-  f.laxWendroff_Vertical = prop->laxWendroff_Vertical;
-  f.nonlinear = prop->nonlinear;
-  f.conserveMomentum = prop->conserveMomentum;
-  f.n = prop->n;
-  f.AB = prop->AB;
+  sgpu_wpred_from(grid, phys, prop, &f);
   sgpu_props_from(prop, &p);
   rc = sgpu_wpredictor(g_ctx, grid->ctop, (const double *const *)grid->dzz, &f, &p, phys->w, phys->Cn_W,
                        phys->Cn_W2);
   if (rc != SGPU_OK) sgpu_die("sgpu_wpredictor", rc);
+}
+
+/* The nonhydrostatic block of Solve (main/phys.c:1271-1289) in one call:
+ * WPredictor -> ComputeQSource -> CGSolveQ -> Corrector with w, q, the
+ * right-hand side, D and the correction kept on the device between them.
+ * Same settings as sgpu_WPredictor; phys->stmp (the right-hand side) and
+ * phys->D are not written back, because nothing in Solve reads them before
+ * UPredictor forms them again. */
+void sgpu_NonhydrostaticStep(gridT *grid, physT *phys, propT *prop, int myproc, int numprocs, MPI_Comm comm) {
+  sgpu_wpred_fields f;
+  sgpu_props p;
+  sgpu_stats st;
+  int rc;
+  (void)comm;
+  sgpu_ensure_step(grid, numprocs);
+  sgpu_wpred_from(grid, phys, prop, &f);
+  sgpu_props_from(prop, &p);
+  rc = sgpu_nonhydrostatic_step(g_ctx, grid->ctop, grid->etop, (const double *const *)grid->dzz,
+                                (const double *const *)grid->dzf, (const double *const *)phys->utmp2,
+                                (const double *const *)phys->wtmp2, &f, phys->u, phys->w, phys->q, phys->qc,
+                                (const double *const *)phys->stmp3, phys->Cn_W, phys->Cn_W2, &p, &st);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER) sgpu_die("sgpu_nonhydrostatic_step", rc);
+  if (myproc == 0 && VERBOSE > 2) {
+    double res = st.eps0 != 0 ? sqrt(st.eps / st.eps0) : 0;
+    if (st.eps == 0)
+      printf("Warning...Time step %d, norm of pressure source is 0.\n", prop->n);
+    else if (rc == SGPU_MAXITER)
+      printf("Warning... Time step %d, Pressure iteration not converging after %d steps! RES=%e > %.2e\n",
+             prop->n, st.niters, res, prop->qepsilon);
+    else
+      printf("Time step %d, CGSolve pressure converged after %d iterations, res=%e < %.2e\n", prop->n,
+             st.niters, res, prop->qepsilon);
+  }
 }

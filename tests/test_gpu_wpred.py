@@ -3,14 +3,25 @@ Adams-Bashforth start, the pressure gradient, first-order upwind advection,
 horizontal diffusion and wall drag gathered per column in the reference's edge
 order, and the vertical diffusion solve give the reference's bits (the oracle
 is pinned bit for bit against the reference's WPredictor and its golden
-vectors)."""
+vectors).
+
+The nonhydrostatic step (WPredictor -> ComputeQSource -> CGSolveQ ->
+Corrector in one call, main/phys.c:1271-1289) matches the oracle's chain of
+the four functions: w and the histories after WPredictor bit for bit (they
+leave the device only at the end), the correction within relative L2 1e-9
+(the solve's parity bound), u, w, q within 1e-8 of the size of the
+correction they received."""
+import dataclasses
+
 import numpy as np
 import pytest
 
 from oracle.oracle import Oracle
 from suntans_gb300 import gridgen as gg
 from suntans_gb300.capi import Context, SolverError
-from tests._cases import h_props
+from suntans_gb300.capi import OK
+from suntans_gb300.grid import QProblem
+from tests._cases import h_props, q_props
 from tests._golden import fixture_names, load, props_for, wpred_fields
 
 pytestmark = pytest.mark.gpu
@@ -69,4 +80,41 @@ def test_unsupported_settings_are_refused(gpu_lib):
         ctx.step_grid(wf)
         with pytest.raises(SolverError):
             ctx.wpredictor(wf, h_props(1))
+    ctx.close()
+
+
+@pytest.mark.parametrize("qprecond", [0, 1])
+@pytest.mark.parametrize("gname,kw", [("tri_open", dict()), ("quad", dict(nonlinear=0, n=1))])
+def test_nonhydrostatic_step_matches_oracle_chain(gpu_lib, oracle, gname, kw, qprecond):
+    g = _grids()[gname]()
+    st = gg.make_step_fields(g, seed=79)
+    wf = dataclasses.replace(gg.make_wpred_fields(g, seed=76, **kw), w=st.w, q=st.q, utmp2=st.utmp2)
+    pr = q_props(qprecond)
+    w_o, cw_o, cw2_o = oracle.wpredictor(wf, pr)
+    st_o = dataclasses.replace(st, w=w_o)
+    src, D = oracle.compute_qsource(st_o, pr)
+    qc_ref, _ = oracle.cgsolveq(QProblem(grid=g, D=D, src=src, q=st.qc, c=st.c), pr)
+    u_ref, w_ref, q_ref = oracle.corrector(st_o, qc_ref, D, pr)
+    ctx = Context(g)
+    ctx.step_grid(st)
+    qc, u, w, q, cw, cw2, stats = ctx.nonhydrostatic_step(st, wf, pr)
+    ctx.close()
+    assert stats.status == OK
+    assert np.array_equal(cw, cw_o) and np.array_equal(cw2, cw2_o)
+    m = g.active_mask()
+    assert np.linalg.norm(qc[m] - qc_ref[m]) <= 1e-9 * np.linalg.norm(qc_ref[m])
+    for a, b, a0 in ((u, u_ref, st.u), (w, w_ref, w_o), (q, q_ref, st.q)):
+        scale = max(np.abs(b - a0).max(), 1e-300)
+        assert np.abs(a - b).max() <= 1e-8 * scale
+
+
+def test_nonhydrostatic_step_refuses_unsupported_settings(gpu_lib):
+    g = _grids()["quad"]()
+    st = gg.make_step_fields(g, seed=80)
+    ctx = Context(g)
+    ctx.step_grid(st)
+    for kw in (dict(nonlinear=2), dict(conserveMomentum=1)):
+        wf = gg.make_wpred_fields(g, seed=81, **kw)
+        with pytest.raises(SolverError):
+            ctx.nonhydrostatic_step(st, wf, q_props(1))
     ctx.close()

@@ -90,3 +90,36 @@ def test_patch_upred_mode_and_compile(tmp_path):
     for s in ("sgpu_UPredictor", "sgpu_upredictor_vertical", "sgpu_upredictor_rhs", "sgpu_upredictor_finish",
               "BoundaryVelocities", "OpenBoundaryFluxes"):
         assert s in syms
+
+
+def test_patch_fused_mode_and_compile(tmp_path):
+    """With "fused", WPredictor's call becomes the one-call nonhydrostatic step
+    and the three calls after it are commented out; nothing else changes."""
+    phys = tmp_path / "phys.c"
+    shutil.copy(os.path.join(REF, "phys.c"), phys)
+    r = subprocess.run(["sh", os.path.join(SHIM, "patch_phys.sh"), str(phys), "fused", "upred"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    new = phys.read_text()
+    assert new.count("sgpu_NonhydrostaticStep(grid,phys,prop,myproc,numprocs,comm);") == 1
+    assert new.count("in sgpu_NonhydrostaticStep */") == 3
+    lines = new.splitlines()
+    i = next(n for n, a in enumerate(lines) if "sgpu_NonhydrostaticStep(grid,phys" in a)
+    assert "ComputeQSource: in" in "\n".join(lines[i:i + 6])
+    old = open(os.path.join(REF, "phys.c")).read()
+    diff = [a for a in new.splitlines() if "sgpu_" not in a]
+    assert diff == [a for a in old.splitlines()
+                    if not a.strip().startswith(("CGSolveQ(phys->qc", "CGSolve(grid", "ComputeQSource(phys->stmp",
+                                                 "Corrector(phys->qc", "UPredictor(grid,phys", "WPredictor(grid,phys"))]
+    cc = ["gcc", "-fcommon", "-DNOMPI", "-DNONETCDF", "-w", f"-I{REF}", f"-I{ROOT}/include", "-c"]
+    r = subprocess.run(cc + [str(phys), "-o", str(tmp_path / "phys.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(cc + [os.path.join(SHIM, "sgpu_suntans.c"), "-o", str(tmp_path / "shim.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    syms = subprocess.run(["nm", str(tmp_path / "shim.o")], capture_output=True, text=True).stdout
+    for s in ("sgpu_NonhydrostaticStep", "sgpu_nonhydrostatic_step", "sgpu_WPredictor"):
+        assert s in syms
+    bad = subprocess.run(["sh", os.path.join(SHIM, "patch_phys.sh"), str(phys) + ".orig", "step", "fused"],
+                         capture_output=True, text=True)
+    assert bad.returncode == 2
