@@ -106,6 +106,10 @@ def parse():
     ap.add_argument("--points", type=int, default=200_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=None,
+                    help="--impl reference: seconds of CPU work per step (default: about a minute in all)")
+    ap.add_argument("--ref-threads", type=int, default=None,
+                    help="--impl reference: concurrent replicas (default: every host core, memory permitting)")
     return ap.parse_args()
 
 
@@ -199,17 +203,28 @@ def peaks():
 
 
 # ---------------------------------------------------------------------------
+def _oracle_iteration_cost(o, qp, props):
+    """(set-up seconds, seconds per iteration) of the oracle's CGSolveQ on this
+    problem, from two short capped runs (2 and 6 iterations)."""
+    from suntans_gb300.grid import SolverProps
+    ts, ns = [], []
+    for cap in (2, 6):
+        t = time.perf_counter()
+        _, n = o.cgsolveq(qp, SolverProps(**{**props.__dict__, "qmaxiters": cap}))
+        ts.append(time.perf_counter() - t)
+        ns.append(max(n, 1))
+    per_iter = (ts[1] - ts[0]) / (ns[1] - ns[0]) if ns[1] > ns[0] else ts[1] / ns[1]
+    per_iter = max(per_iter, ts[1] / ns[1] * 0.05, 1e-7)
+    return max(ts[1] - ns[1] * per_iter, 0.0), per_iter
+
+
 def cpu_baseline(g, qp, hp, props, seconds: float):
-    """The oracle port on a bounded sample: CGSolveQ capped at M iterations (plus a full CGSolve)."""
+    """The oracle port on a bounded sample: CGSolveQ capped at M iterations, one thread."""
     from oracle.oracle import Oracle
     from suntans_gb300.grid import SolverProps
     o = Oracle("port")
-    probe = SolverProps(**{**props.__dict__, "qmaxiters": 2})
-    t = time.perf_counter()
-    _, n = o.cgsolveq(qp, probe)
-    t_probe = time.perf_counter() - t
-    per_iter = max(t_probe / max(n, 1), 1e-6)
-    m = int(max(2, min(props.qmaxiters, seconds * 0.8 / per_iter)))
+    setup, per_iter = _oracle_iteration_cost(o, qp, props)
+    m = int(max(2, min(props.qmaxiters, (seconds * 0.8 - setup) / per_iter)))
     capped = SolverProps(**{**props.__dict__, "qmaxiters": m})
     t = time.perf_counter()
     _, nq = o.cgsolveq(qp, capped)
@@ -218,6 +233,65 @@ def cpu_baseline(g, qp, hp, props, seconds: float):
     return {"value": work / tq, "unit": "unknown-iters/s", "cores": 1, "kind": "port",
             "sample": f"oracle CGSolveQ (qprecond {props.qprecond}) capped at {nq} iterations on the full "
                       f"N_q={g.n_q()} grid, {tq:.1f} s, 1 thread"}
+
+
+def host_threads(bytes_per_thread: float) -> int:
+    """Host threads for the CPU baseline: every core this process may run on,
+    capped so that the replicas' working sets stay within half of the host's
+    available memory."""
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except AttributeError:
+        cores = os.cpu_count() or 1
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    if avail is not None:
+        cores = min(cores, max(1, int(0.5 * avail // max(bytes_per_thread, 1.0))))
+    return max(1, cores)
+
+
+def cpu_baseline_parallel(g, qp, props, seconds: float, threads: int, cost=None):
+    """The oracle port on every host thread: `threads` independent replicas of
+    the bounded CGSolveQ sample run at once (the reference solver is serial; a
+    host runs one replica per core), unknown-iterations of all replicas ÷ the
+    wall time of the slowest."""
+    import threading
+    from oracle.oracle import Oracle
+    from suntans_gb300.grid import SolverProps
+    o = Oracle("port")
+    setup, per_iter = cost or _oracle_iteration_cost(o, qp, props)
+    # replicas share the memory bandwidth: budget for a 2x slowdown per replica
+    m = int(max(2, min(props.qmaxiters, (seconds * 0.5 - setup) / per_iter)))
+    capped = SolverProps(**{**props.__dict__, "qmaxiters": m})
+    iters = [0] * threads
+    errors = []
+
+    def one(k):
+        try:
+            iters[k] = o.cgsolveq(qp, capped)[1]
+        except Exception as e:  # reported after the join
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
+    t = time.perf_counter()
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    wall = time.perf_counter() - t
+    if errors:
+        raise RuntimeError("CPU baseline replica failed: " + errors[0])
+    work = g.n_q() * sum(iters)
+    return {"value": work / wall, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} concurrent replicas of the oracle CGSolveQ (qprecond {props.qprecond}) capped at "
+                      f"{iters[0]} iterations on the full N_q={g.n_q()} grid, {wall:.1f} s wall; the reference "
+                      f"solver is serial (-DNOMPI), so the host's cores run one replica each"}
 
 
 def run_reference(args):
@@ -229,10 +303,13 @@ def run_reference(args):
         om.build_port()
     g, qp, hp, props, desc = make_workload(args)
     per_step = []
-    total_work = 0
-    seconds = max(5.0, 60.0 / max(args.steps + args.warmup, 1))
+    seconds = args.ref_seconds or max(5.0, 60.0 / max(args.steps + args.warmup, 1))
+    # per replica: the solver's scratch (z, r, rtmp, coef, F face coefficients) and its copies of q, src, c
+    threads = args.ref_threads or host_threads(8.0 * g.n_q() * (7 + g.maxfaces) + 64e6)
+    from oracle.oracle import Oracle
+    cost = _oracle_iteration_cost(Oracle("port"), qp, props)
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(g, qp, hp, props, seconds)
+        r = cpu_baseline_parallel(g, qp, props, seconds, threads, cost)
         if i >= args.warmup:
             per_step.append(r)
     vals = [r["value"] for r in per_step]
@@ -241,8 +318,8 @@ def run_reference(args):
             "unit": "unknown-iters/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": desc, "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": "unknown-iters/s", "cores": 1, "kind": "port",
-                             "sample": per_step[0]["sample"] + "; reference built serial -DNOMPI uses one core"},
+            "cpu_baseline": {"value": v, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
+                             "sample": per_step[0]["sample"]},
             "e2e": {"value": v, "unit": "unknown-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
