@@ -445,6 +445,30 @@ class Oracle:
             out[name] = buf[:n].copy()
         return out
 
+    def read_main_grid(self, datadir: str) -> dict:
+        """ReadMainGrid (main/gridio.c:256-266) after InitMainGrid, on a folder
+        holding suntans.dat and the points / edges / cells files; returns the
+        gridT arrays it fills by name (cells and neigh whole: maxfaces per
+        cell, slots past nfaces as the reference left them)."""
+        if self.which != "ref":
+            raise RuntimeError("read_main_grid needs the reference library")
+        sizes = np.zeros(6, dtype=np.int32)
+        self.lib.ref_read_main_grid(datadir.encode(), _ptr(sizes, _ip))
+        Nc, Ne, Np, mf = (int(x) for x in sizes[:4])
+        out = {"Nc": Nc, "Ne": Ne, "Np": Np, "maxfaces": mf}
+        self.lib.ref_grid_ints.restype = C.c_long
+        self.lib.ref_grid_dbls.restype = C.c_long
+        cap = max(16, Nc * mf + 2 * Ne + Np + 16)
+        for name in ("nfaces", "cells", "neigh", "mark", "edge_id", "grad", "edges"):
+            buf = np.zeros(cap, dtype=np.int32)
+            n = self.lib.ref_grid_ints(name.encode(), _ptr(buf, _ip))
+            out[name] = buf[:n].copy()
+        for name in ("xv", "yv", "xp", "yp"):
+            buf = np.zeros(cap, dtype=np.float64)
+            n = self.lib.ref_grid_dbls(name.encode(), _ptr(buf, _dp))
+            out[name] = buf[:n].copy()
+        return out
+
     def write_2d(self, path: str, x) -> None:
         x = np.ascontiguousarray(x, dtype=np.float64)
         self.lib.ref_write_2d(path.encode(), C.c_int(x.size), _ptr(x, _dp))

@@ -20,6 +20,7 @@
  * exchange is a no-op (main/sendrecv.c:134-217 with Nneighs=0).
  */
 #include "phys.c"
+#include "gridio.h"
 #include "cg_oracle.h"
 
 static int g_calls3d, g_calls2d;
@@ -380,6 +381,32 @@ int ref_read_grid(const char *dir, int *sizes) {
   sizes[3] = g_rg->maxfaces;
   sizes[4] = g_rg->Nkmax;
   sizes[5] = g_rg->Nneighs;
+  return 0;
+}
+
+/* ref_read_main_grid: the grid step's own input reader on a folder holding a
+ * suntans.dat (maxFaces and the points / edges / cells names) and the three
+ * files: sizes from getsize, InitMainGrid (main/grid.c:337), ReadMainGrid
+ * (main/gridio.c:256-266), as GetGrid (grid.c:110-135) runs them.  The arrays
+ * are then read with ref_grid_ints / ref_grid_dbls. */
+int ref_read_main_grid(const char *dir, int *sizes) {
+  int Np, Ne, Nc;
+  snprintf(DATADIR, BUFFERLENGTH, "%s", dir);
+  snprintf(DATAFILE, BUFFERLENGTH, "%s/suntans.dat", dir);
+  VERBOSE = 0;
+  ReadGridFileNames(0);
+  Np = MPI_GetSize(POINTSFILE, "ref_read_main_grid", 0);
+  Ne = MPI_GetSize(EDGEFILE, "ref_read_main_grid", 0);
+  Nc = MPI_GetSize(CELLSFILE, "ref_read_main_grid", 0);
+  g_rg = NULL;
+  InitMainGrid(&g_rg, Np, Ne, Nc, 0);
+  ReadMainGrid(g_rg, 0);
+  sizes[0] = g_rg->Nc;
+  sizes[1] = g_rg->Ne;
+  sizes[2] = g_rg->Np;
+  sizes[3] = g_rg->maxfaces;
+  sizes[4] = 0;
+  sizes[5] = 0;
   return 0;
 }
 

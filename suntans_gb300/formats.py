@@ -15,6 +15,22 @@ leaves for each processor P (ReadGrid, main/gridio.c:54-187):
 ``cells.dat.P``, ``edges.dat.P``  the plan-view triangulation (WriteCellsData /
                     WriteEdgesData gridio.c:558-629, with nfaces and edge_id).
 
+The grid step itself starts from the input triangulation (ReadMainGrid,
+gridio.c:256-266), read by `read_main_grid`:
+
+``points.dat``      ``x y mark`` per node (ReadPointsData gridio.c:515-525)
+``edges.dat``       ``n1 n2 mark grad0 grad1 [edge_id]`` per edge (ReadEdgesData
+                    gridio.c:535-556; edge_id only when the first line has more
+                    than 5 columns)
+``cells.dat``       ``[nfaces] xv yv node[nfaces] neigh[nfaces]`` per cell
+                    (ReadCellsData gridio.c:574-611; nfaces only when the first
+                    line has more than 8 columns, else every cell has 3 faces)
+
+Columns are counted on the first line as getNumColumns does
+(fileio.c:205-228): a blank or tab after a character that is not a blank, a
+tab or the start of the file starts a column, and a blank right before the
+first newline takes one back.
+
 Every reader follows the reference's tokenizer (getfield, main/fileio.c:137-174):
 fields are separated by blanks, tabs, newlines or carriage returns; a field with
 a character other than ``0-9 . + - e`` is skipped; the value is the longest
@@ -51,7 +67,7 @@ EMPTY = 999999.0      # main/suntans.h:28, written below a column's bottom
 DEFAULT_NAMES = {     # the keys of suntans.dat (examples/*/rundata/suntans.dat)
     "celldata": "celldata.dat", "edgedata": "edgedata.dat", "nodes": "nodes.dat",
     "topology": "topology.dat", "vertspace": "vertspace.dat", "cells": "cells.dat",
-    "edges": "edges.dat",
+    "edges": "edges.dat", "points": "points.dat",
 }
 
 _SEP = re.compile(rb"[ \t\n\r]+")
@@ -494,6 +510,149 @@ def write_grid(gf: GridFiles, datadir: str, proc: int = 0, names: Optional[Dict[
 
     with open(os.path.join(datadir, nm["vertspace"]), "w") as f:   # WriteVertSpaceData gridio.c:506-512
         f.write("".join("%e\n" % v for v in gf.dz))
+
+
+# ----------------------------------------------------------------------------
+# the input triangulation (points, edges, cells)
+# ----------------------------------------------------------------------------
+COLUMNS_IN_TRIANGLE_CELLS_FILE = 8   # cells.dat columns without nfaces (gridio.c:16)
+COLUMNS_IN_TRIANGLE_EDGES_FILE = 5   # edges.dat columns without edge_id (gridio.c:17)
+DEFAULT_NFACES = 3                   # main/suntans.h:33
+
+
+def get_num_columns(path: str) -> int:
+    """Columns of a file's first line, counted as getNumColumns counts them
+    (main/fileio.c:205-228)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    n, old = 1, 0
+    for ch in data:
+        if ch in (0x20, 0x09) and old not in (0x20, 0x09, 0):
+            n += 1
+        if ch == 0x0A:
+            if old == 0x20:
+                n -= 1
+            break
+        old = ch
+    return n
+
+
+@dataclasses.dataclass
+class MainGrid:
+    """The input triangulation that ReadMainGrid fills (gridT.xp, yp, edges,
+    mark, grad, edge_id, nfaces, xv, yv, cells, neigh).  cells and neigh are
+    [Nc, maxfaces] with -1 past a cell's nfaces."""
+    maxfaces: int
+    xp: np.ndarray
+    yp: np.ndarray
+    edges: np.ndarray      # [Ne, 2] node indices
+    mark: np.ndarray
+    grad: np.ndarray       # [Ne, 2] cell indices (-1 outside)
+    edge_id: np.ndarray
+    nfaces: np.ndarray
+    xv: np.ndarray
+    yv: np.ndarray
+    cells: np.ndarray      # [Nc, maxfaces] node indices
+    neigh: np.ndarray      # [Nc, maxfaces] neighbour cells (-1: none)
+
+    @property
+    def Np(self) -> int:
+        return int(self.xp.size)
+
+    @property
+    def Ne(self) -> int:
+        return int(self.mark.size)
+
+    @property
+    def Nc(self) -> int:
+        return int(self.nfaces.size)
+
+
+def read_points(path: str):
+    """(xp, yp) of every node line (ReadPointsData, gridio.c:515-525: the third
+    field, the node's marker, is read and dropped)."""
+    Np = count_lines(path)
+    v = _Fields(read_fields(path), path).take(3 * Np).reshape(Np, 3)
+    return v[:, 0].copy(), v[:, 1].copy()
+
+
+def read_edges(path: str):
+    """(edges [Ne, 2], mark, grad [Ne, 2], edge_id) as ReadEdgesData reads
+    them (gridio.c:535-556); edge_id is 0 where the file has no such column."""
+    Ne = count_lines(path)
+    ncol = 6 if get_num_columns(path) > COLUMNS_IN_TRIANGLE_EDGES_FILE else 5
+    v = _trunc(_Fields(read_fields(path), path).take(ncol * Ne)).reshape(Ne, ncol)
+    edge_id = v[:, 5].copy() if ncol == 6 else np.zeros(Ne, dtype=I32)
+    return v[:, 0:2].copy(), v[:, 2].copy(), v[:, 3:5].copy(), edge_id
+
+
+def read_cells(path: str, maxfaces: int):
+    """(nfaces, xv, yv, cells [Nc, maxfaces], neigh [Nc, maxfaces]) as
+    ReadCellsData reads them (gridio.c:574-611).  A cell with more faces than
+    maxfaces raises, where the reference stops with an error."""
+    Nc = count_lines(path)
+    with_nf = get_num_columns(path) > COLUMNS_IN_TRIANGLE_CELLS_FILE
+    fl = _Fields(read_fields(path), path)
+    nfaces = np.full(Nc, DEFAULT_NFACES, dtype=I32)
+    xv = np.zeros(Nc, dtype=F64)
+    yv = np.zeros(Nc, dtype=F64)
+    cells = -np.ones((Nc, maxfaces), dtype=I32)
+    neigh = -np.ones((Nc, maxfaces), dtype=I32)
+    for n in range(Nc):
+        if with_nf:
+            nf = int(np.trunc(fl.one()))
+            if nf > maxfaces:
+                raise ValueError(f"{path}: cell {n} has {nf} faces, more than maxFaces {maxfaces}")
+            nfaces[n] = nf
+        nf = int(nfaces[n])
+        xv[n] = fl.one()
+        yv[n] = fl.one()
+        if nf > 0:
+            cells[n, :nf] = _trunc(fl.take(nf))
+            neigh[n, :nf] = _trunc(fl.take(nf))
+    return nfaces, xv, yv, cells, neigh
+
+
+def read_main_grid(datadir: str, maxfaces: int = DEFAULT_NFACES,
+                   names: Optional[Dict[str, str]] = None) -> MainGrid:
+    """Read the input triangulation the way ReadMainGrid does (gridio.c:256-266):
+    points, edges and cells files of ``datadir`` (names as in suntans.dat)."""
+    nm = _names(names)
+    xp, yp = read_points(os.path.join(datadir, nm["points"]))
+    edges, mark, grad, edge_id = read_edges(os.path.join(datadir, nm["edges"]))
+    nfaces, xv, yv, cells, neigh = read_cells(os.path.join(datadir, nm["cells"]), maxfaces)
+    return MainGrid(maxfaces=maxfaces, xp=xp, yp=yp, edges=edges, mark=mark, grad=grad, edge_id=edge_id,
+                    nfaces=nfaces, xv=xv, yv=yv, cells=cells, neigh=neigh)
+
+
+def write_main_grid(mg: MainGrid, datadir: str, names: Optional[Dict[str, str]] = None, with_nfaces: bool = True,
+                    with_edge_id: bool = True) -> None:
+    """Write the input triangulation in the reference's formats:
+    WritePointsData (gridio.c:527-533, marker written as 0), WriteEdgesData
+    (558-572) and WriteCellsData (613-629), with or without the nfaces and
+    edge_id columns."""
+    nm = _names(names)
+    os.makedirs(datadir, exist_ok=True)
+    with open(os.path.join(datadir, nm["points"]), "w") as f:
+        f.write("".join("%e %e 0\n" % (x, y) for x, y in zip(mg.xp, mg.yp)))
+    with open(os.path.join(datadir, nm["edges"]), "w") as f:
+        rows = []
+        for j in range(mg.Ne):
+            r = "%d %d %d %d %d " % (mg.edges[j, 0], mg.edges[j, 1], mg.mark[j], mg.grad[j, 0], mg.grad[j, 1])
+            if with_edge_id:
+                r += "%d " % mg.edge_id[j]
+            rows.append(r + "\n")
+        f.write("".join(rows))
+    with open(os.path.join(datadir, nm["cells"]), "w") as f:
+        rows = []
+        for j in range(mg.Nc):
+            nf = int(mg.nfaces[j])
+            r = ("%d " % nf) if with_nfaces else ""
+            r += "%e %e " % (mg.xv[j], mg.yv[j])
+            r += "".join("%d " % c for c in mg.cells[j, :nf])
+            r += "".join("%d " % c for c in mg.neigh[j, :nf])
+            rows.append(r + "\n")
+        f.write("".join(rows))
 
 
 # ----------------------------------------------------------------------------

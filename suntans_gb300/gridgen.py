@@ -224,6 +224,35 @@ def _assemble(points, cells, nfaces, maxfaces, depth_fn, Nkmax, rstretch, stairs
     return g
 
 
+def from_main_grid(mg, Nkmax=10, depth_fn=None, rstretch=1.0, stairstep=False, seed=0, name="main", h_sigma=0.0,
+                   ctop_frac=0.0):
+    """A solver grid on an input triangulation read from the model's files
+    (`formats.read_main_grid`): its nodes and each cell's node list, with the
+    geometry (areas, centroid Voronoi points, edge lengths and distances,
+    normals) and the z-level columns built as for the synthetic grids.  Cells
+    listed clockwise are reversed; the files' own edge list is not needed.
+    depth_fn(x, y) defaults to a Gaussian bump over the domain (10-60 m)."""
+    points = np.stack([np.asarray(mg.xp, dtype=F64), np.asarray(mg.yp, dtype=F64)], axis=1)
+    nfaces = np.asarray(mg.nfaces, dtype=I32)
+    cells = np.array(mg.cells, dtype=np.int64, copy=True)
+    mf = int(mg.maxfaces)
+    fidx = np.arange(mf)[None, :]
+    m = fidx < nfaces[:, None]
+    c0 = np.where(m, cells, 0)
+    nxt = np.take_along_axis(c0, (fidx + 1) % nfaces[:, None], axis=1)
+    cross = np.where(m, points[c0, 0] * points[nxt, 1] - points[nxt, 0] * points[c0, 1], 0.0).sum(1)
+    for j in np.nonzero(cross < 0)[0]:
+        cells[j, :nfaces[j]] = cells[j, :nfaces[j]][::-1]
+    if depth_fn is None:
+        x0, x1, y0, y1 = points[:, 0].min(), points[:, 0].max(), points[:, 1].min(), points[:, 1].max()
+        sig = 0.25 * max(x1 - x0, y1 - y0)
+        xc, yc = 0.5 * (x0 + x1), 0.5 * (y0 + y1)
+        depth_fn = lambda x, y: 60.0 - 50.0 * np.exp(-((x - xc) ** 2 + (y - yc) ** 2) / (2 * sig * sig))
+    rng = np.random.default_rng(seed)
+    return _assemble(points, cells, nfaces, mf, depth_fn, Nkmax, rstretch, stairstep, rng, name, h_sigma=h_sigma,
+                     ctop_frac=ctop_frac)
+
+
 def quad_channel(nx=64, ny=16, dx=10.0, dy=10.0, depth=20.0, Nkmax=32, rstretch=1.0, seed=0,
                  h_sigma=0.0, ctop_frac=0.0, open_x0=False, depth_fn=None, stairstep=True):
     """Structured quad channel (maxfaces 4), cells (ix, iy) counter-clockwise."""

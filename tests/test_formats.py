@@ -268,3 +268,108 @@ def test_hybrid_grid_round_trip_and_reference(tmp_path):
     assert np.array_equal(rd.def_, _round(gf.def_))
     if om.available("ref"):
         _compare_ref(om.Oracle("ref").read_grid(d), rd)
+
+
+# ---------------------------------------------------------------------------
+# the input triangulation (points / edges / cells) of the reference's examples
+# ---------------------------------------------------------------------------
+REF_EXAMPLES = os.path.join(os.path.dirname(os.environ.get("SUNTANS_REFDIR", "/root/reference/main")), "examples")
+# (folder, points, edges, cells, maxFaces): the grids the reference ships with its examples
+MAIN_GRIDS = [
+    ("riverplume/grids/tri", "points.dat", "edges.dat", "cells.dat", 3),
+    ("riverplume/grids/quad", "points.dat", "edges.dat", "cells.dat", 4),
+    ("riverplume/grids/hex", "points.dat", "edges.dat", "cells.dat", 7),
+    ("riverplume/grids/hybrid", "points.dat", "edges.dat", "cells.dat", 7),
+    ("riverplume/grids/gmsh", "points.dat", "edges.dat", "cells.dat", 4),
+    ("boundaries/data-files", "points-quad.dat", "edges-quad.dat", "cells-quad.dat", 4),
+    ("cylinder/data-files", "points-tri.dat", "edges-tri.dat", "cells-tri.dat", 3),
+    ("cylinder/data-files", "points-quad.dat", "edges-quad.dat", "cells-quad.dat", 4),
+    ("cavity/data-files", "pointsXZ.dat", "edgesXZ.dat", "cellsXZ.dat", 3),
+    ("cavity/data-files", "pointsXZ-quad.dat", "edgesXZ-quad.dat", "cellsXZ-quad.dat", 4),
+    ("EstuaryNetcdf/grid", "points.dat", "edges.dat", "cells.dat", 3),
+    ("heatflux/rundata", "points.dat", "edges.dat", "cells.dat", 4),
+]
+MAIN_IDS = [f"{d}:{c}" for d, _, _, c, _ in MAIN_GRIDS]
+MAIN_DAT = "maxFaces {mf}\t# faces per cell\npoints {p}\t# input\nedges {e}\t# input\ncells {c}\t# input\n" \
+           "depth depth.dat\t# input\nnodes nodes.dat\t# output\ncelldata celldata.dat\t# output\n" \
+           "edgedata edgedata.dat\t# output\nvertspace vertspace.dat\t# output\ntopology topology.dat\t# output\n"
+
+
+def _main_case(tmp_path, case):
+    d, p, e, c, mf = case
+    src = os.path.join(REF_EXAMPLES, d)
+    if not os.path.isfile(os.path.join(src, c)):
+        pytest.skip("the reference's example grids are not present on this host")
+    tmp_path.mkdir(parents=True, exist_ok=True)
+    (tmp_path / "suntans.dat").write_text(MAIN_DAT.format(mf=mf, p=os.path.join(src, p), e=os.path.join(src, e),
+                                                          c=os.path.join(src, c)))
+    names = {"points": os.path.join(src, p), "edges": os.path.join(src, e), "cells": os.path.join(src, c)}
+    return fm.read_main_grid(str(tmp_path), maxfaces=mf, names=names), str(tmp_path)
+
+
+def _compare_main(r, mg):
+    assert (r["Nc"], r["Ne"], r["Np"], r["maxfaces"]) == (mg.Nc, mg.Ne, mg.Np, mg.maxfaces)
+    slot = (np.arange(mg.maxfaces)[None, :] < mg.nfaces[:, None]).ravel()
+    assert np.array_equal(r["nfaces"], mg.nfaces)
+    assert np.array_equal(r["cells"][slot], mg.cells.ravel()[slot])
+    assert np.array_equal(r["neigh"][slot], mg.neigh.ravel()[slot])
+    assert np.array_equal(r["edges"], mg.edges.ravel()) and np.array_equal(r["grad"], mg.grad.ravel())
+    assert np.array_equal(r["mark"], mg.mark) and np.array_equal(r["edge_id"], mg.edge_id)
+    for f in ("xv", "yv", "xp", "yp"):
+        assert np.array_equal(r[f], getattr(mg, f)), f
+
+
+@pytest.mark.parametrize("case", MAIN_GRIDS, ids=MAIN_IDS)
+def test_example_grids_read_like_the_reference(tmp_path, case):
+    """The grids shipped with the reference's examples (triangles, quads,
+    hexagons, mixed cells up to 7 faces, with and without the nfaces and
+    edge_id columns) read into the arrays the reference's ReadMainGrid fills."""
+    ref = _ref()
+    mg, d = _main_case(tmp_path, case)
+    _compare_main(ref.read_main_grid(d), mg)
+
+
+@pytest.mark.parametrize("case", [MAIN_GRIDS[0], MAIN_GRIDS[3], MAIN_GRIDS[11]], ids=[MAIN_IDS[0], MAIN_IDS[3],
+                                                                                     MAIN_IDS[11]])
+def test_main_grid_writers_round_trip(tmp_path, case):
+    """write_main_grid's files (with and, for triangles, without the optional
+    columns) are read back alike here and by the reference."""
+    ref = _ref()
+    mg, _ = _main_case(tmp_path / "src", case)
+    variants = [(True, True), (True, False)]
+    if np.all(mg.nfaces == 3):
+        variants.append((False, True))
+    for k, (wnf, wid) in enumerate(variants):
+        d = tmp_path / f"w{k}"
+        fm.write_main_grid(mg, str(d), with_nfaces=wnf, with_edge_id=wid)
+        (d / "suntans.dat").write_text(MAIN_DAT.format(mf=mg.maxfaces, p="points.dat", e="edges.dat", c="cells.dat"))
+        back = fm.read_main_grid(str(d), maxfaces=mg.maxfaces)
+        assert np.array_equal(back.nfaces, mg.nfaces) and np.array_equal(back.cells, mg.cells)
+        assert np.array_equal(back.neigh, mg.neigh) and np.array_equal(back.grad, mg.grad)
+        assert np.array_equal(back.edge_id, mg.edge_id if wid else np.zeros_like(mg.edge_id))
+        assert np.array_equal(back.xv, _round(mg.xv)) and np.array_equal(back.xp, _round(mg.xp))
+        _compare_main(ref.read_main_grid(str(d)), back)
+
+
+def test_column_count_rules(tmp_path):
+    """get_num_columns counts as the reference's getNumColumns: leading blanks,
+    runs of blanks, a trailing blank (taken back) and a trailing tab (not)."""
+    ref = _ref()
+    cases = [b"  1 2 3\n", b"1 2 3 \n", b"1\t2\t\n", b"1  2   3    4\n5 6\n", b"1 2 3 \r\n", b"7", b"\n1 2\n",
+             b"\t\t1 \t2\n"]
+    ref.lib.getNumColumns.restype = __import__("ctypes").c_int
+    for k, data in enumerate(cases):
+        f = tmp_path / f"c{k}.dat"
+        f.write_bytes(data)
+        assert fm.get_num_columns(str(f)) == ref.lib.getNumColumns(str(f).encode()), data
+
+
+def test_main_grid_too_many_faces_raises(tmp_path):
+    mg = fm.MainGrid(maxfaces=4, xp=np.zeros(4), yp=np.zeros(4), edges=np.zeros((0, 2), dtype=np.int32),
+                     mark=np.zeros(0, dtype=np.int32), grad=np.zeros((0, 2), dtype=np.int32),
+                     edge_id=np.zeros(0, dtype=np.int32), nfaces=np.array([4], dtype=np.int32), xv=np.zeros(1),
+                     yv=np.zeros(1), cells=np.array([[0, 1, 2, 3]], dtype=np.int32),
+                     neigh=-np.ones((1, 4), dtype=np.int32))
+    fm.write_main_grid(mg, str(tmp_path))
+    with pytest.raises(ValueError):
+        fm.read_main_grid(str(tmp_path), maxfaces=3)

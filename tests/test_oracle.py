@@ -214,3 +214,37 @@ def test_port_wpredictor_matches_reference_library(port, kw):
     pr = h_props(1, dt=10.0)
     for a, b in zip(port.wpredictor(wf, pr), ref.wpredictor(wf, pr)):
         assert np.array_equal(a, b)
+
+
+# the reference's own example triangulations (main/gridio.c input files), as solver grids
+_EXAMPLES = __import__("os").path.join(
+    __import__("os").path.dirname(__import__("os").environ.get("SUNTANS_REFDIR", "/root/reference/main")), "examples")
+_EXAMPLE_GRIDS = [("riverplume/grids/hex", 7), ("riverplume/grids/hybrid", 7), ("riverplume/grids/quad", 4),
+                  ("riverplume/grids/tri", 3), ("heatflux/rundata", 4)]
+
+
+@pytest.mark.skipif(not ref_present, reason="reference sources not present on this host")
+@pytest.mark.parametrize("folder,mf", _EXAMPLE_GRIDS, ids=[f for f, _ in _EXAMPLE_GRIDS])
+def test_port_matches_reference_library_on_example_grids(port, folder, mf):
+    """CGSolveQ (qprecond 0, 1, 2) and CGSolve (hprecond 0, 1) bit for bit on
+    the reference's example grids: hexagons and mixed cells up to 7 faces,
+    quads, triangles; partial top cells and a perturbed free surface."""
+    import os
+    from suntans_gb300 import formats as fm
+    d = os.path.join(_EXAMPLES, folder)
+    if not os.path.isfile(os.path.join(d, "cells.dat")):
+        pytest.skip("the reference's example grids are not present on this host")
+    mg = fm.read_main_grid(d, maxfaces=mf)
+    g = gg.from_main_grid(mg, Nkmax=8, ctop_frac=0.2, h_sigma=0.1, seed=12, name=folder)
+    assert g.Ne == mg.Ne  # the edges rebuilt from the cells are the file's edges
+    ref = Oracle("ref")
+    qp = gg.make_q_problem(g, seed=13, q0_sigma=0.02)
+    for qpc in (0, 1, 2):
+        a, na = port.cgsolveq(qp, q_props(qpc))
+        b, nb = ref.cgsolveq(qp, q_props(qpc))
+        assert na == nb and na > 2 and np.array_equal(a, b)
+    hp = gg.make_h_problem(g, seed=14)
+    for hpc in (0, 1):
+        a, na = port.cgsolve(hp, h_props(hpc))
+        b, nb = ref.cgsolve(hp, h_props(hpc))
+        assert na == nb and na > 2 and np.array_equal(a, b)
