@@ -225,14 +225,16 @@ def _assemble(points, cells, nfaces, maxfaces, depth_fn, Nkmax, rstretch, stairs
 
 
 def from_main_grid(mg, Nkmax=10, depth_fn=None, rstretch=1.0, stairstep=False, seed=0, name="main", h_sigma=0.0,
-                   ctop_frac=0.0):
+                   ctop_frac=0.0, scale=1.0):
     """A solver grid on an input triangulation read from the model's files
     (`formats.read_main_grid`): its nodes and each cell's node list, with the
     geometry (areas, centroid Voronoi points, edge lengths and distances,
     normals) and the z-level columns built as for the synthetic grids.  Cells
     listed clockwise are reversed; the files' own edge list is not needed.
-    depth_fn(x, y) defaults to a Gaussian bump over the domain (10-60 m)."""
-    points = np.stack([np.asarray(mg.xp, dtype=F64), np.asarray(mg.yp, dtype=F64)], axis=1)
+    depth_fn(x, y) defaults to a Gaussian bump over the domain (10-60 m);
+    `scale` multiplies the node coordinates (cell size against depth sets how
+    strongly the columns couple)."""
+    points = float(scale) * np.stack([np.asarray(mg.xp, dtype=F64), np.asarray(mg.yp, dtype=F64)], axis=1)
     nfaces = np.asarray(mg.nfaces, dtype=I32)
     cells = np.array(mg.cells, dtype=np.int64, copy=True)
     mf = int(mg.maxfaces)

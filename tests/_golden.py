@@ -1,4 +1,5 @@
-"""Loads the golden fixtures (tests/golden/*.npz) written by make_golden.py."""
+"""Loads the golden fixtures (tests/golden/*.npz) written by make_golden.py, and the
+solver cases on the reference's example grids (tests/golden/examples/*.npz)."""
 import glob
 import os
 
@@ -13,8 +14,22 @@ def fixture_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz")))
 
 
+def example_names():
+    """Solver cases on the reference's example grids (tests/golden/examples/,
+    written by make_example_golden.py)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "examples", "*.npz")))
+
+
+def load_example(name):
+    return _load(os.path.join(HERE, "examples", name + ".npz"), name)
+
+
 def load(name):
-    d = dict(np.load(os.path.join(HERE, name + ".npz")))
+    return _load(os.path.join(HERE, name + ".npz"), name)
+
+
+def _load(path, name):
+    d = dict(np.load(path))
     Nc, Ne, mf, Nkmax = (int(v) for v in d["sizes"])
     g = SunGrid(Nc=Nc, Ne=Ne, maxfaces=mf, Nkmax=Nkmax,
                 **{k: d[k] for k in ("nfaces", "neigh", "face", "Nk", "Nke", "ctop", "cellp", "celldist",

@@ -10,7 +10,7 @@ from oracle import oracle as om
 from oracle.oracle import Oracle
 from suntans_gb300 import gridgen as gg
 from tests._cases import grid_cases, h_props, q_props
-from tests._golden import fixture_names, load, props_for
+from tests._golden import example_names, fixture_names, load, load_example, props_for
 
 
 @pytest.fixture(scope="module")
@@ -248,3 +248,17 @@ def test_port_matches_reference_library_on_example_grids(port, folder, mf):
         a, na = port.cgsolve(hp, h_props(hpc))
         b, nb = ref.cgsolve(hp, h_props(hpc))
         assert na == nb and na > 2 and np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", example_names())
+def test_port_matches_example_golden_bitwise(port, name):
+    """The oracle's solvers on the stored example-grid cases: the reference's
+    solutions and iteration counts, bit for bit."""
+    g, qp, hp, props, d = load_example(name)
+    assert int(g.nfaces.max()) >= 4
+    for qpc in (0, 1, 2):
+        q, n = port.cgsolveq(qp, props_for(props, qprecond=qpc))
+        assert n == int(d[f"n_qp{qpc}"]) and np.array_equal(q, d[f"q_qp{qpc}"])
+    for hpc in (0, 1):
+        h, n = port.cgsolve(hp, props_for(props, hprecond=hpc))
+        assert n == int(d[f"n_hp{hpc}"]) and np.array_equal(h, d[f"h_hp{hpc}"])
