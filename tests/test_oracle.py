@@ -3,6 +3,8 @@ bit-for-bit against the reference's own outputs: the golden vectors made by
 tests/golden/make_golden.py from the reference's compiled main/phys.c, and --
 where the reference tree is present -- the reference library itself on larger
 seeded grids."""
+import os
+
 import numpy as np
 import pytest
 
@@ -217,10 +219,20 @@ def test_port_wpredictor_matches_reference_library(port, kw):
 
 
 # the reference's own example triangulations (main/gridio.c input files), as solver grids
-_EXAMPLES = __import__("os").path.join(
-    __import__("os").path.dirname(__import__("os").environ.get("SUNTANS_REFDIR", "/root/reference/main")), "examples")
+_EXAMPLES = os.path.join(os.path.dirname(os.environ.get("SUNTANS_REFDIR", "/root/reference/main")), "examples")
 _EXAMPLE_GRIDS = [("riverplume/grids/hex", 7), ("riverplume/grids/hybrid", 7), ("riverplume/grids/quad", 4),
                   ("riverplume/grids/tri", 3), ("heatflux/rundata", 4)]
+
+
+def _example_grid(folder, mf, seed, **kw):
+    from suntans_gb300 import formats as fm
+    d = os.path.join(_EXAMPLES, folder)
+    if not os.path.isfile(os.path.join(d, "cells.dat")):
+        pytest.skip("the reference's example grids are not present on this host")
+    mg = fm.read_main_grid(d, maxfaces=mf)
+    g = gg.from_main_grid(mg, Nkmax=8, ctop_frac=0.2, h_sigma=0.1, seed=seed, name=folder, **kw)
+    assert g.Ne == mg.Ne  # the edges rebuilt from the cells are the file's edges
+    return g
 
 
 @pytest.mark.skipif(not ref_present, reason="reference sources not present on this host")
@@ -229,14 +241,7 @@ def test_port_matches_reference_library_on_example_grids(port, folder, mf):
     """CGSolveQ (qprecond 0, 1, 2) and CGSolve (hprecond 0, 1) bit for bit on
     the reference's example grids: hexagons and mixed cells up to 7 faces,
     quads, triangles; partial top cells and a perturbed free surface."""
-    import os
-    from suntans_gb300 import formats as fm
-    d = os.path.join(_EXAMPLES, folder)
-    if not os.path.isfile(os.path.join(d, "cells.dat")):
-        pytest.skip("the reference's example grids are not present on this host")
-    mg = fm.read_main_grid(d, maxfaces=mf)
-    g = gg.from_main_grid(mg, Nkmax=8, ctop_frac=0.2, h_sigma=0.1, seed=12, name=folder)
-    assert g.Ne == mg.Ne  # the edges rebuilt from the cells are the file's edges
+    g = _example_grid(folder, mf, seed=12)
     ref = Oracle("ref")
     qp = gg.make_q_problem(g, seed=13, q0_sigma=0.02)
     for qpc in (0, 1, 2):
@@ -262,3 +267,37 @@ def test_port_matches_example_golden_bitwise(port, name):
     for hpc in (0, 1):
         h, n = port.cgsolve(hp, props_for(props, hprecond=hpc))
         assert n == int(d[f"n_hp{hpc}"]) and np.array_equal(h, d[f"h_hp{hpc}"])
+
+
+@pytest.mark.skipif(not ref_present, reason="reference sources not present on this host")
+@pytest.mark.parametrize("folder,mf", _EXAMPLE_GRIDS[:2], ids=[f for f, _ in _EXAMPLE_GRIDS[:2]])
+def test_port_steps_match_reference_library_on_example_grids(port, folder, mf):
+    """The steps around the solves on hexagon / maxFaces-7 grids, bit for bit:
+    ComputeQSource, Corrector, UpdateDZ, SetFluxHeight, WPredictor (with and
+    without advection) and the whole UPredictor (cells of up to 7 faces in
+    the edge loops, the per-cell face sums and the free-surface solve)."""
+    g = _example_grid(folder, mf, seed=15, scale=0.02)
+    ref = Oracle("ref")
+    st = gg.make_step_fields(g, seed=16)
+    pr = q_props(1)
+    sa, Da = port.compute_qsource(st, pr)
+    sb, Db = ref.compute_qsource(st, pr)
+    assert np.array_equal(sa, sb) and np.array_equal(Da, Db)
+    qc = port.cgsolveq(gg.QProblem(grid=g, D=Da, src=sa, q=st.qc, c=st.c), pr)[0]
+    for x, y in zip(port.corrector(st, qc, Da, pr), ref.corrector(st, qc, Da, pr)):
+        assert np.array_equal(x, y)
+    vf = gg.make_vgrid_fields(g, seed=17, smoothbot=0.2)
+    for x, y in zip(port.update_dz(vf), ref.update_dz(vf)):
+        assert np.array_equal(x, y)
+    for x, y in zip(port.set_flux_height(vf), ref.set_flux_height(vf)):
+        assert np.array_equal(x, y)
+    hp = h_props(1, dt=10.0)
+    for kw in (dict(), dict(nonlinear=0, n=1)):
+        wf = gg.make_wpred_fields(g, seed=18, **kw)
+        for x, y in zip(port.wpredictor(wf, hp), ref.wpredictor(wf, hp)):
+            assert np.array_equal(x, y)
+    uf = gg.make_upred_fields(g, seed=19)
+    vf = gg.make_vgrid_fields(g, seed=20)
+    a, b = port.upredictor(uf, vf, hp), ref.upredictor(uf, vf, hp)
+    for k in a:
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
