@@ -88,10 +88,13 @@ void sgpu_CGSolveQ(REAL **q, REAL **src, REAL **c, gridT *grid, physT *phys, pro
   sgpu_props_from(prop, &p);
   rc = sgpu_cgsolveq(g_ctx, grid->ctop, (const double *const *)grid->dzz, (const double *const *)grid->dzf,
                      phys->D, q, (const double *const *)src, (const double *const *)c, &p, &st);
-  if (rc != SGPU_OK && rc != SGPU_MAXITER) sgpu_die("sgpu_cgsolveq", rc);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER && rc != SGPU_BREAKDOWN) sgpu_die("sgpu_cgsolveq", rc);
   if (myproc == 0 && VERBOSE > 2) {
     double res = st.eps0 != 0 ? sqrt(st.eps / st.eps0) : 0;
-    if (st.eps == 0)
+    if (rc == SGPU_BREAKDOWN)
+      printf("Warning... Time step %d, Pressure iteration broke down after %d steps (non-finite step)\n", prop->n,
+             st.niters);
+    else if (st.eps == 0)
       printf("Warning...Time step %d, norm of pressure source is 0.\n", prop->n);
     else if (rc == SGPU_MAXITER)
       printf("Warning... Time step %d, Pressure iteration not converging after %d steps! RES=%e > %.2e\n",
@@ -110,10 +113,13 @@ void sgpu_CGSolve(gridT *grid, physT *phys, propT *prop, int myproc, int numproc
   sgpu_ensure_context(grid, numprocs);
   sgpu_props_from(prop, &p);
   rc = sgpu_cgsolve(g_ctx, phys->D, phys->h, phys->htmp, &p, &st);
-  if (rc != SGPU_OK && rc != SGPU_MAXITER) sgpu_die("sgpu_cgsolve", rc);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER && rc != SGPU_BREAKDOWN) sgpu_die("sgpu_cgsolve", rc);
   if (myproc == 0 && VERBOSE > 2) {
     double res = st.eps0 != 0 ? sqrt(st.eps / st.eps0) : 0;
-    if (st.eps == 0)
+    if (rc == SGPU_BREAKDOWN)
+      printf("Warning... Time step %d, Free-surface iteration broke down after %d steps (non-finite step)\n",
+             prop->n, st.niters);
+    else if (st.eps == 0)
       printf("Warning...Time step %d, norm of free-surface source is 0.\n", prop->n);
     else if (rc == SGPU_MAXITER)
       printf("Warning... Time step %d, Free-surface iteration not converging after %d steps! RES=%e > %.2e\n",
@@ -300,10 +306,13 @@ void sgpu_NonhydrostaticStep(gridT *grid, physT *phys, propT *prop, int myproc, 
                                 (const double *const *)grid->dzf, (const double *const *)phys->utmp2,
                                 (const double *const *)phys->wtmp2, &f, phys->u, phys->w, phys->q, phys->qc,
                                 (const double *const *)phys->stmp3, phys->Cn_W, phys->Cn_W2, &p, &st);
-  if (rc != SGPU_OK && rc != SGPU_MAXITER) sgpu_die("sgpu_nonhydrostatic_step", rc);
+  if (rc != SGPU_OK && rc != SGPU_MAXITER && rc != SGPU_BREAKDOWN) sgpu_die("sgpu_nonhydrostatic_step", rc);
   if (myproc == 0 && VERBOSE > 2) {
     double res = st.eps0 != 0 ? sqrt(st.eps / st.eps0) : 0;
-    if (st.eps == 0)
+    if (rc == SGPU_BREAKDOWN)
+      printf("Warning... Time step %d, Pressure iteration broke down after %d steps (non-finite step)\n", prop->n,
+             st.niters);
+    else if (st.eps == 0)
       printf("Warning...Time step %d, norm of pressure source is 0.\n", prop->n);
     else if (rc == SGPU_MAXITER)
       printf("Warning... Time step %d, Pressure iteration not converging after %d steps! RES=%e > %.2e\n",
