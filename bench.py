@@ -294,6 +294,45 @@ def cpu_baseline_parallel(g, qp, props, seconds: float, threads: int, cost=None)
                       f"solver is serial (-DNOMPI), so the host's cores run one replica each"}
 
 
+def cpu_baseline_instances(probs, props, seconds: float, threads: int):
+    """The oracle port on every host thread for a set of independent problems:
+    one problem per thread (the median-size ones of the set), each CGSolveQ
+    capped so that the run takes about `seconds`; unknown-iterations of all
+    threads ÷ the wall time."""
+    import threading
+    from oracle.oracle import Oracle
+    from suntans_gb300.grid import SolverProps
+    o = Oracle("port")
+    order = np.argsort([p.grid.n_q() for p in probs])
+    mid = len(order) // 2
+    pick = [int(order[(mid + (k + 1) // 2 * (1 if k % 2 else -1)) % len(order)]) for k in range(threads)]
+    setup, per_iter = _oracle_iteration_cost(o, probs[pick[0]], props)
+    m = int(max(2, min(props.qmaxiters, (seconds * 0.5 - setup) / per_iter)))
+    capped = SolverProps(**{**props.__dict__, "qmaxiters": m})
+    work = [0] * threads
+    errors = []
+
+    def one(k):
+        try:
+            pr = probs[pick[k]]
+            work[k] = pr.grid.n_q() * o.cgsolveq(pr, capped)[1]
+        except Exception as e:  # reported after the join
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
+    t = time.perf_counter()
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    wall = time.perf_counter() - t
+    if errors:
+        raise RuntimeError("CPU baseline thread failed: " + errors[0])
+    return {"value": sum(work) / wall, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} problems of the set around its median size, one per thread, oracle CGSolveQ "
+                      f"(qprecond {props.qprecond}) capped at {m} iterations each, {wall:.1f} s wall"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -663,6 +702,9 @@ def bench_cfg4(args):
         k = int(np.argsort(Ns)[len(Ns) // 2])
         line["cpu_baseline"] = cpu_baseline(grids[k], probs[k], None, props, args.cpu_seconds)
         line["cpu_baseline"]["sample"] += " (the median-size problem of the set)"
+        nq_max = max(p.grid.n_q() for p in probs)
+        threads = host_threads(8.0 * nq_max * (7 + grids[0].maxfaces) + 64e6)
+        line["cpu_baseline_all_cores"] = cpu_baseline_instances(probs, props, args.cpu_seconds, threads)
     return line
 
 
