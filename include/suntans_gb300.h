@@ -20,8 +20,8 @@
  * 3315-3316) become in-kernel reductions.  There is no CPU fallback: without a
  * usable CUDA device every entry point returns SGPU_NO_DEVICE.
  *
- * Adapter for the reference's own signatures (gridT/physT/propT) and the
- * two-line call-site patch: INTEGRATION.md and suntans_gb300/shim/.
+ * The adapter with the reference's own signatures (gridT/physT/propT) and the
+ * two-line call-site patch of main/phys.c are in suntans_gb300/shim/.
  */
 #ifndef SUNTANS_GB300_H
 #define SUNTANS_GB300_H
@@ -418,7 +418,8 @@ typedef struct sgpu_noalloc_grid {
  * each call), so calls that overlap on the GPU race and must not be issued.
  * The first call on each device looks up the array's address
  * (cudaGetSymbolAddress, with that device current); make it before any stream
- * capture.  Runs on the current device; blocks until the solve has finished.
+ * capture.  The address is kept per device and context, so the first call
+ * after a cudaDeviceReset looks it up again (also before any capture).  Runs on the current device; blocks until the solve has finished.
  * stats->ms_solve is -1 (no timing events are created). */
 int sgpu_cgsolve_noalloc(const sgpu_noalloc_grid *grid, const double *D, double *h, const double *htmp,
                          const sgpu_props *prop, sgpu_stats *stats, void *stream);

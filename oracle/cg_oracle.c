@@ -49,11 +49,39 @@ static void layout_free(layout_t *L) { free(L->coff); free(L->eoff); }
 /* fcoef row (i,nf) has Nk[i] entries and starts at maxfaces*coff[i] + nf*Nk[i] */
 #define FC(i, nf, k) fcoef[(long)g->maxfaces * L->coff[(i)] + (long)(nf) * g->Nk[(i)] + (k)]
 
+/* Summation order of the inner products.  0 (the default) is the reference's
+   sequential sum in cellp order.  1 sums the same products pairwise (recursive
+   halving of the sequence); it exists only so that the tests can measure how
+   far a solve's iteration count moves when nothing but the order of the
+   inner products' additions changes -- a parallel device reduction cannot
+   reproduce the sequential order. */
+static int g_sum_order = 0;
+void sgo_set_sum_order(int order) { g_sum_order = order; }
+
+static double pairwise_sum(const double *t, long n) {
+  long h;
+  if (n <= 0) return 0.0;
+  if (n == 1) return t[0];
+  h = n / 2;
+  return pairwise_sum(t, h) + pairwise_sum(t + h, n - h);
+}
+
 /* Inner product over computational cells: main/phys.c:3304-3319 (InnerProduct3).
    Sequential sum in cellp order; the serial MPI_Reduce/MPI_Bcast are copies. */
 static double inner3(const sgo_grid *g, const layout_t *L, const double *x, const double *y) {
   double mysum = 0;
   int iptr, i, k;
+  if (g_sum_order == 1) {
+    double *t = (double *)malloc(sizeof(double) * (L->n3 + 1));
+    long n = 0;
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      for (k = g->ctop[i]; k < g->Nk[i]; k++) t[n++] = X3(x, i, k) * X3(y, i, k);
+    }
+    mysum = pairwise_sum(t, n);
+    free(t);
+    return mysum;
+  }
   for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
     i = g->cellp[iptr];
     for (k = g->ctop[i]; k < g->Nk[i]; k++) mysum += X3(x, i, k) * X3(y, i, k);
@@ -65,6 +93,17 @@ static double inner3(const sgo_grid *g, const layout_t *L, const double *x, cons
 static double inner2(const sgo_grid *g, const double *x, const double *y) {
   double mysum = 0;
   int iptr, i;
+  if (g_sum_order == 1) {
+    double *t = (double *)malloc(sizeof(double) * (g->Nc + 1));
+    long n = 0;
+    for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
+      i = g->cellp[iptr];
+      t[n++] = x[i] * y[i];
+    }
+    mysum = pairwise_sum(t, n);
+    free(t);
+    return mysum;
+  }
   for (iptr = g->celldist[0]; iptr < g->celldist[1]; iptr++) {
     i = g->cellp[iptr];
     mysum += x[i] * y[i];

@@ -131,6 +131,9 @@ void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, do
                   const sgo_prop *p, sgo_result *res);
 void sgo_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp,
                  const sgo_prop *p, sgo_result *res);
+/* order of the inner products' additions: 0 sequential (the reference's),
+   1 pairwise (tests only: measures a solve's sensitivity to that order) */
+void sgo_set_sum_order(int order);
 /* single operator pieces, for kernel-level parity */
 void sgo_qcoefficients(const sgo_grid *g, const double *D, const double *c, int qprecond,
                        double *coef, double *fcoef);

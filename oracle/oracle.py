@@ -80,12 +80,39 @@ def build_port() -> str:
     return PORT_SO
 
 
+def _make_args() -> list:
+    env = os.environ.get("SUNTANS_REFDIR")
+    return [f"REFDIR={env}"] if env else []
+
+
 def build_ref() -> Optional[str]:
-    refdir = os.environ.get("SUNTANS_REFDIR", "/root/reference/main")
-    if not os.path.isfile(os.path.join(refdir, "phys.c")):
+    """Builds oracle/_ref from the reference's main/ sources: SUNTANS_REFDIR
+    when set, else the Makefile's default location; None where they are absent."""
+    chk = subprocess.run(["make", "-s", "-C", HERE, "refcheck", *_make_args()], capture_output=True)
+    if chk.returncode != 0:
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", *_make_args()], check=True)
     return REF_SO
+
+
+def ref_dir() -> Optional[str]:
+    """The reference's main/ directory: SUNTANS_REFDIR when set, else the one
+    oracle/_ref was built from (recorded by the Makefile); None on hosts
+    without the reference sources (the GPU machine)."""
+    d = os.environ.get("SUNTANS_REFDIR")
+    if not d:
+        rec = os.path.join(HERE, "_ref", "refdir.txt")
+        if not os.path.isfile(rec):
+            build_ref()  # writes the record where the sources are present
+        if os.path.isfile(rec):
+            d = open(rec).read().strip()
+    return d if d and os.path.isfile(os.path.join(d, "phys.c")) else None
+
+
+def ref_examples_dir() -> Optional[str]:
+    """The reference's examples/ directory, beside main/ (None where absent)."""
+    d = ref_dir()
+    return os.path.join(os.path.dirname(d), "examples") if d else None
 
 
 class Oracle:
@@ -144,6 +171,23 @@ class Oracle:
         self._fn("cgsolve")(C.byref(s), _ptr(D, _dp), _ptr(h, _dp), _ptr(htmp, _dp), C.byref(pr),
                             C.byref(res))
         return h, int(res.niters)
+
+    def iteration_span(self, prob, props, solver="q"):
+        """Iteration counts of the port's solve with the reference's sequential
+        inner products and with pairwise ones: (sequential, pairwise).  A
+        parallel reduction adds in neither order; on an ill-conditioned system
+        the iteration at which the residual crosses the tolerance moves with
+        that order alone (the solution stays within round-off of the
+        reference's).  Port only."""
+        assert self.which == "port"
+        fn = self.cgsolveq if solver == "q" else self.cgsolve
+        n_seq = fn(prob, props)[1]
+        self.lib.sgo_set_sum_order(1)
+        try:
+            n_pair = fn(prob, props)[1]
+        finally:
+            self.lib.sgo_set_sum_order(0)
+        return n_seq, n_pair
 
     # ---- operator pieces ----
     def qcoefficients(self, g, D, c, qprecond):

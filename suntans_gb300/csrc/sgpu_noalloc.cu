@@ -23,7 +23,8 @@
 //     threads) race on the array and give wrong answers.
 //   * the first call on each device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture.
+//     before any stream capture.  The address is kept per device and CUDA
+//     context: a call after cudaDeviceReset (a new context) looks it up again.
 //
 // Semantics are those of CGSolve (main/phys.c:3086-3217), HCoefficients
 // (3252-3269), OperatorH (3335-3349) and HPreconditioner (3227-3235), with the
@@ -33,6 +34,8 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "../../include/suntans_gb300.h"
 #include "sgpu_common.cuh"
@@ -256,20 +259,57 @@ __global__ void __launch_bounds__(kBlock) cgsolve_noalloc_kernel(NAArgs a) {
   }
 }
 
-// device address of g_noalloc_scratch, looked up once per device
+// Device address of g_noalloc_scratch, looked up once per device and context.
+// The address belongs to the module loaded into one CUDA context: after
+// cudaDeviceReset (or any other end of the device's primary context) the array
+// is loaded again at a new address.  So the cached address is keyed by the
+// context's unique id (cuCtxGetId, never reused within a process), reached
+// through the runtime's driver entry points so that the library needs no link
+// against the driver library.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
 static std::mutex g_na_mutex;
 static void* g_na_ptr[64];
+static unsigned long long g_na_ctx[64];
 static bool g_na_done[64];
+static PfnCtxGetCurrent g_ctx_get_current = nullptr;
+static PfnCtxGetId g_ctx_get_id = nullptr;
+
+// id of the context current on this thread; 0 on failure
+static unsigned long long current_context_id() {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess)
+      return 0;
+    g_ctx_get_current = (PfnCtxGetCurrent)f1;
+    g_ctx_get_id = (PfnCtxGetId)f2;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS || c == nullptr) return 0;
+  if (g_ctx_get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 static int noalloc_scratch_ptr(int dev, void** out) {
   if (dev < 0 || dev >= 64) return SGPU_BAD_ARG;
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_done[dev]) {
+  unsigned long long id = current_context_id();
+  if (!g_na_done[dev] || id == 0 || id != g_na_ctx[dev]) {
+    // set-up: the first call on this device (and again after its context changed)
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) return SGPU_CUDA_ERROR;
+    if (id == 0) id = current_context_id();  // the lookup above made the primary context current
     g_na_ptr[dev] = p;
-    g_na_done[dev] = true;
+    g_na_ctx[dev] = id;
+    g_na_done[dev] = (id != 0);
   }
   *out = g_na_ptr[dev];
   return SGPU_OK;

@@ -32,8 +32,8 @@ from suntans_gb300 import gridgen as gg  # noqa: E402
 from suntans_gb300.grid import SolverProps  # noqa: E402
 
 GRID_FIELDS = ("nfaces", "neigh", "face", "Nk", "Nke", "ctop", "cellp", "celldist", "Ac", "df", "dg", "dzz", "dzf")
-REFDIR = os.environ.get("SUNTANS_REFDIR", "/root/reference/main")
-EXAMPLES = os.path.join(os.path.dirname(REFDIR), "examples")
+om.build_ref()
+EXAMPLES = om.ref_examples_dir() or ""
 # fixture name: (example folder, maxFaces of its suntans.dat)
 CASES = {"riverplume_hex": ("riverplume/grids/hex", 7), "riverplume_hybrid": ("riverplume/grids/hybrid", 7)}
 

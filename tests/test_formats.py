@@ -273,7 +273,7 @@ def test_hybrid_grid_round_trip_and_reference(tmp_path):
 # ---------------------------------------------------------------------------
 # the input triangulation (points / edges / cells) of the reference's examples
 # ---------------------------------------------------------------------------
-REF_EXAMPLES = os.path.join(os.path.dirname(os.environ.get("SUNTANS_REFDIR", "/root/reference/main")), "examples")
+REF_EXAMPLES = om.ref_examples_dir() or ""
 # (folder, points, edges, cells, maxFaces): the grids the reference ships with its examples
 MAIN_GRIDS = [
     ("riverplume/grids/tri", "points.dat", "edges.dat", "cells.dat", 3),

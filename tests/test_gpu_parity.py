@@ -2,8 +2,8 @@
 
 Tolerance: relative L2 of the solution over computational cells / active levels
 <= 1e-9 at equal tolerance (1e-10 relative residual), and iteration counts
-within max(2, 2%) of the oracle's (the GPU sums in a different order, which
-shifts the stopping iteration of long unpreconditioned solves slightly).
+within max(4, 3%) of the oracle's (the GPU sums in a different order, which
+shifts the stopping iteration of long solves; iters_close).
 """
 import numpy as np
 import pytest
@@ -17,12 +17,19 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-9
 
 
-def iters_close(n_gpu, n_ref):
+def iters_close(n_gpu, n_ref, n_alt=None):
     """The inner products are summed in a different order on the GPU (a
     deterministic tree over threads) than in the reference (serial over cells),
     so the iteration at which sqrt(eps/eps0) first drops below the tolerance can
-    move by a few iterations; the solution itself is held to TOL below."""
-    return abs(n_gpu - n_ref) <= max(4, int(0.03 * n_ref))
+    move; the solution itself is held to TOL.  n_alt is the oracle's count with
+    pairwise inner products (Oracle.iteration_span): on an ill-conditioned
+    system the order of the additions alone moves the count by more than a few
+    (the reference's riverplume hybrid grid, qprecond 2: 394 sequential, 375
+    pairwise), so the allowance max(4, 3%) is taken around the span of the two."""
+    lo = min(n_ref, n_ref if n_alt is None else n_alt)
+    hi = max(n_ref, n_ref if n_alt is None else n_alt)
+    tol = max(4, int(0.03 * hi))
+    return lo - tol <= n_gpu <= hi + tol
 
 _GRIDS = {}
 
@@ -49,9 +56,9 @@ def test_cgsolveq_parity(gpu_lib, oracle, gname, qprecond):
     q_gpu, st = ctx.cgsolveq(prob, pr)
     m = g.active_mask()
     assert st.status == OK
-    assert iters_close(st.niters, n_ref), (st.niters, n_ref)
     err = rel_l2(q_gpu, q_ref, m)
     assert err <= TOL, err
+    assert iters_close(st.niters, *oracle.iteration_span(prob, pr)), (st.niters, n_ref)
     # entries outside the active set are returned untouched
     assert np.array_equal(q_gpu[~m], prob.q[~m])
     ctx.close()
@@ -68,8 +75,8 @@ def test_cgsolve_parity(gpu_lib, oracle, gname, hprecond):
     h_gpu, st = ctx.cgsolve(prob, pr)
     comp = g.comp_cells()
     assert st.status == OK
-    assert iters_close(st.niters, n_ref), (st.niters, n_ref)
     assert rel_l2(h_gpu[comp], h_ref[comp]) <= TOL
+    assert iters_close(st.niters, *oracle.iteration_span(prob, pr, solver="h")), (st.niters, n_ref)
     bdy = g.cellp[g.celldist[1]:g.celldist[2]]
     assert np.array_equal(h_gpu[bdy], prob.h[bdy])
     ctx.close()

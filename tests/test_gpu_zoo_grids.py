@@ -6,8 +6,9 @@ active levels and iteration counts within the summation-order allowance."""
 import numpy as np
 import pytest
 
+from oracle.oracle import Oracle
 from suntans_gb300.capi import Context, OK
-from tests._cases import rel_l2
+from tests._cases import rel_l2, stopping_ratio
 from tests._golden import example_names, load_example, props_for
 from tests.test_gpu_parity import TOL, iters_close
 
@@ -16,14 +17,22 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("name", example_names())
 def test_example_grid_cgsolveq(gpu_lib, name):
+    """The solution is checked first (relative L2 against the reference's, and
+    the reference's stopping ratio re-evaluated on it), then the iteration
+    count against the span of the oracle's sequential and pairwise counts."""
     g, qp, hp, props, d = load_example(name)
     m = g.active_mask()
+    o = Oracle("port")
     ctx = Context(g)
     for qpc in (0, 1, 2):
-        q, st = ctx.cgsolveq(qp, props_for(props, qprecond=qpc))
+        pr = props_for(props, qprecond=qpc)
+        q, st = ctx.cgsolveq(qp, pr)
         assert st.status == OK
-        assert iters_close(st.niters, int(d[f"n_qp{qpc}"])), (qpc, st.niters, int(d[f"n_qp{qpc}"]))
         assert rel_l2(q, d[f"q_qp{qpc}"], m) <= TOL, qpc
+        assert stopping_ratio(o, qp, q, qpc) < 10 * pr.qepsilon, qpc
+        n_seq, n_pair = o.iteration_span(qp, pr)
+        assert n_seq == int(d[f"n_qp{qpc}"])
+        assert iters_close(st.niters, n_seq, n_pair), (qpc, st.niters, n_seq, n_pair)
     ctx.close()
 
 
@@ -31,11 +40,14 @@ def test_example_grid_cgsolveq(gpu_lib, name):
 def test_example_grid_cgsolve(gpu_lib, name):
     g, qp, hp, props, d = load_example(name)
     comp = g.cellp[g.celldist[0]:g.celldist[1]]
+    o = Oracle("port")
     ctx = Context(g)
     for hpc in (0, 1):
-        h, st = ctx.cgsolve(hp, props_for(props, hprecond=hpc))
+        pr = props_for(props, hprecond=hpc)
+        h, st = ctx.cgsolve(hp, pr)
         assert st.status == OK
-        assert iters_close(st.niters, int(d[f"n_hp{hpc}"])), (hpc, st.niters, int(d[f"n_hp{hpc}"]))
         ref = d[f"h_hp{hpc}"]
         assert np.linalg.norm(h[comp] - ref[comp]) <= TOL * np.linalg.norm(ref[comp]), hpc
+        n_seq, n_pair = o.iteration_span(hp, pr, solver="h")
+        assert iters_close(st.niters, n_seq, n_pair), (hpc, st.niters, n_seq, n_pair)
     ctx.close()

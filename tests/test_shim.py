@@ -9,7 +9,10 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("SUNTANS_REFDIR", "/root/reference/main")
+from oracle import oracle as om  # noqa: E402
+
+om.build_ref()  # records where the reference sources lie, where they are present
+REF = om.ref_dir() or ""
 SHIM = os.path.join(ROOT, "suntans_gb300", "shim")
 
 pytestmark = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "phys.c")),

@@ -7,9 +7,10 @@ caller passes device buffers it owns (here torch tensors stand in for them) and
 the solver's scratch comes from a fixed static array inside the library.
 
 The test calls the entry point through the C ABI twice in a row on the same
-inputs and compares each result with the allocating entry point sgpu_cgsolve,
-within the parity tolerance of the other GPU tests (relative L2 <= 1e-9), and
-checks that a grid beyond the stated capacity is refused with SGPU_TOO_LARGE.
+inputs and compares each result with the allocating entry point sgpu_cgsolve
+and with the reference's own solutions on one of its example grids, within the
+parity tolerance of the other GPU tests (relative L2 <= 1e-9), and checks that
+a grid beyond the stated capacity is refused with SGPU_TOO_LARGE.
 The file name makes pytest collect it last.
 """
 import ctypes as C
@@ -64,6 +65,22 @@ def test_noalloc_matches_allocating_solve_twice(gpu_lib, hprecond):
         assert abs(st.niters - st_ref.niters) <= 2
         assert rel_l2(h[comp], h_ref[comp]) <= TOL
         assert np.array_equal(h[bdy], hp.h[bdy])
+
+
+def test_noalloc_matches_reference_on_example_grid(gpu_lib):
+    """Against the reference's own CGSolve solutions stored with the riverplume
+    hexagon grid (cells of 5-7 faces), two calls in a row, both hprecond modes."""
+    torch = pytest.importorskip("torch")
+    from tests._golden import load_example, props_for
+    lib = load()
+    g, qp, hp, props, d = load_example("riverplume_hex")
+    comp = g.cellp[g.celldist[0]:g.celldist[1]]
+    for hpc in (0, 1):
+        ref = d[f"h_hp{hpc}"]
+        for _ in range(2):
+            rc, h, st = _noalloc_call(lib, g, hp, props_for(props, hprecond=hpc), torch)
+            assert rc == OK and st.status == OK
+            assert rel_l2(h[comp], ref[comp]) <= TOL
 
 
 def test_noalloc_refuses_too_large(gpu_lib):
