@@ -89,7 +89,8 @@ struct sgpu_context {
   // free-surface buffers
   bool h_ready = false;
   double *d_Dh = nullptr, *d_hin = nullptr, *d_bin = nullptr, *d_hcoef = nullptr, *d_hf = nullptr,
-         *d_hx = nullptr, *d_hp = nullptr, *d_hr = nullptr, *d_hz = nullptr, *d_hrt = nullptr;
+         *d_hx = nullptr, *d_hp = nullptr, *d_hr = nullptr, *d_hz = nullptr, *d_hrt = nullptr,
+         *d_hihc = nullptr, *d_hp1 = nullptr;
   int* d_hn = nullptr;
   bool h_uploaded = false, h_solved = false;
 
@@ -377,7 +378,7 @@ int sgpu_phase_times(const sgpu_context* ctx, long long* ns8) {
 
 static int ensure_partials(sgpu_context* ctx, int grid) {
   if (ctx->partials_cap >= grid) return SGPU_OK;
-  int rc = dalloc(ctx, &ctx->d_partials, (size_t)4 * grid);
+  int rc = dalloc(ctx, &ctx->d_partials, (size_t)8 * grid);  // up to 8 doubles per CTA (free surface: 6)
   if (rc) return rc;
   ctx->partials_cap = grid;
   return SGPU_OK;
@@ -613,7 +614,8 @@ static int alloc_h(sgpu_context* ctx) {
   if (ctx->h_ready) return SGPU_OK;
   const size_t nc = ctx->Nc + 1, ncf = (size_t)std::max(ctx->ncomp, 1) * ctx->F;
   int rc;
-  double** v[] = {&ctx->d_hin, &ctx->d_bin, &ctx->d_hcoef, &ctx->d_hx, &ctx->d_hp, &ctx->d_hr, &ctx->d_hz, &ctx->d_hrt};
+  double** v[] = {&ctx->d_hin, &ctx->d_bin, &ctx->d_hcoef, &ctx->d_hx, &ctx->d_hp, &ctx->d_hr, &ctx->d_hz, &ctx->d_hrt,
+                  &ctx->d_hihc, &ctx->d_hp1};
   for (auto pp : v)
     if ((rc = dalloc(ctx, pp, nc))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_hf, ncf))) return rc;
@@ -662,9 +664,12 @@ int sgpu_h_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   DeviceGuard dg(ctx->device);
   int maxg = h_max_grid(ctx->device);
   if (maxg <= 0) return fail(ctx, SGPU_CUDA_ERROR, "occupancy query failed");
-  int grid = ctx->grid_override > 0 ? std::min(ctx->grid_override, maxg) : maxg;
+  // default: one CTA per SM (the barrier's cost grows with the CTAs arriving)
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  int grid = ctx->grid_override > 0 ? std::min(ctx->grid_override, maxg) : std::min(std::max(sms, 1), maxg);
   // no more CTAs than needed to give every thread a cell
-  grid = std::max(1, std::min(grid, (ctx->ncomp + kBlock - 1) / kBlock));
+  grid = std::max(1, std::min(grid, (ctx->ncomp + h_block() - 1) / h_block()));
   int rc = ensure_partials(ctx, grid);
   if (rc) return rc;
   HLaunch L;
@@ -677,6 +682,7 @@ int sgpu_h_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   a.epsilon = prop->epsilon;
   a.resnorm = prop->resnorm;
   a.tmp = prop->grav * std::pow(prop->theta * prop->dt, 2);
+  a.cpc = std::max(1, (ctx->ncomp + grid - 1) / grid);
   a.nbr = ctx->d_nbr;
   a.fedge = ctx->d_fedge;
   a.Ac = ctx->d_Ac;
@@ -686,10 +692,12 @@ int sgpu_h_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   a.h_in = ctx->d_hin;
   a.b_in = ctx->d_bin;
   a.hcoef = ctx->d_hcoef;
+  a.ihcoef = ctx->d_hihc;
   a.hf = ctx->d_hf;
   a.hn = ctx->d_hn;
   a.x = ctx->d_hx;
   a.p = ctx->d_hp;
+  a.p1 = ctx->d_hp1;
   a.r = ctx->d_hr;
   a.z = ctx->d_hz;
   a.rt = ctx->d_hrt;

@@ -63,6 +63,7 @@ struct HArgs {
   double epsilon;
   double resnorm;
   double tmp;           // grav*(theta*dt)^2 (HCoefficients, main/phys.c:3255)
+  int cpc;              // computational cells per CTA (CTA b owns [b*cpc, (b+1)*cpc))
   const int* nbr;       // [ncomp*F] neighbour cell (device order) or -1
   const int* fedge;     // [ncomp*F]
   const double* Ac;     // [ncells]
@@ -72,10 +73,12 @@ struct HArgs {
   const double* h_in;   // [ncells]
   const double* b_in;   // [ncells] right-hand side (htmp)
   double* hcoef;        // [ncomp]
+  double* ihcoef;       // [ncomp] 1/hcoef (the Jacobi step as a product)
   double* hf;           // [F*ncomp]
   int* hn;              // [F*ncomp] neighbour or self (coefficient 0)
   double* x;
-  double* p;
+  double* p;            // the direction, double-buffered with p1
+  double* p1;
   double* r;
   double* z;
   double* rt;
@@ -86,6 +89,7 @@ struct HArgs {
 int q_max_grid(int qprecond, int device);
 cudaError_t q_launch(const QArgs& a, int qprecond, int grid, cudaStream_t st);
 int h_max_grid(int device);
+int h_block();  // threads per CTA of the free-surface kernel
 cudaError_t h_launch(const HArgs& a, int grid, cudaStream_t st);
 
 }  // namespace sgpu
