@@ -23,7 +23,15 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include "cg_oracle.h"
+
+/* Wall-clock seconds (CLOCK_MONOTONIC), for the timing fields of sgo_result. */
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 typedef struct {
   long *coff;   /* [Nc+1] offsets of cell columns in the ragged arrays */
@@ -276,6 +284,7 @@ void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, do
   int iptr, i, k, n, niters, executed = 0;
   double mu, nu, alpha, alpha0, eps, eps0;
   double *x = q, *p = src, *z, *r, *rtmp, *coef, *fcoef;
+  double t0 = now_s(), t1;
   layout_make(g, L);
   z = (double *)calloc(L->n3 + 1, sizeof(double));
   r = (double *)calloc(L->n3 + 1, sizeof(double));
@@ -319,6 +328,7 @@ void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, do
   if (!pr->resnorm) alpha0 = 1;
   if (pr->qprecond == 2) eps = eps0 = inner3(g, L, r, r);
   else eps = eps0 = alpha0;
+  t1 = now_s();
 
   for (n = 0; n < niters && eps != 0; n++) {
     executed++;
@@ -359,7 +369,10 @@ void sgo_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, do
       for (k = g->ctop[i]; k < g->Nk[i]; k++) X3(x, i, k) /= X3(c, i, k);
     }
   }
-  if (res) { res->niters = executed; res->eps = eps; res->eps0 = eps0; }
+  if (res) {
+    res->niters = executed; res->eps = eps; res->eps0 = eps0;
+    res->t_setup = t1 - t0; res->t_loop = now_s() - t1;
+  }
   free(z); free(r); free(rtmp); free(coef); free(fcoef);
   layout_free(L);
 }
@@ -398,6 +411,7 @@ void sgo_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp, co
   int iptr, i, n, niters, executed = 0;
   double mu, nu, eps, eps0, alpha, alpha0;
   double *x = h, *p = htmp, *r, *rtmp, *z, *hcoef, *hfcoef;
+  double t0 = now_s(), t1;
   r = (double *)calloc(g->Nc + 1, sizeof(double));
   rtmp = (double *)calloc(g->Nc + 1, sizeof(double));
   z = (double *)calloc(g->Nc + 1, sizeof(double));
@@ -437,6 +451,7 @@ void sgo_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp, co
   if (!pr->resnorm) alpha0 = 1;
   if (pr->hprecond == 1) eps = eps0 = inner2(g, r, r);
   else eps = eps0 = alpha0;
+  t1 = now_s();
 
   for (n = 0; n < niters && eps != 0 && alpha != 0; n++) {
     executed++;
@@ -471,7 +486,10 @@ void sgo_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp, co
     else eps = alpha;
     if (sqrt(eps / eps0) < pr->epsilon) break;
   }
-  if (res) { res->niters = executed; res->eps = eps; res->eps0 = eps0; }
+  if (res) {
+    res->niters = executed; res->eps = eps; res->eps0 = eps0;
+    res->t_setup = t1 - t0; res->t_loop = now_s() - t1;
+  }
   free(r); free(rtmp); free(z); free(hcoef); free(hfcoef);
 }
 

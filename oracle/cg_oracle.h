@@ -62,6 +62,9 @@ typedef struct sgo_result {
   int niters;          /* solver iterations executed (operator applications in   
                           the loop; the reference's n, plus one when it broke)   */
   double eps, eps0;    /* last eps and the normaliser eps0                        */
+  double t_setup;      /* seconds before the iteration loop (coefficients,
+                          conditioning, first residual); port only               */
+  double t_loop;       /* seconds in the iteration loop; port only               */
 } sgo_result;
 
 /* The gridT fields the steps on either side of CGSolveQ read in addition:

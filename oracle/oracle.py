@@ -68,7 +68,8 @@ class SgoWpred(C.Structure):
 
 
 class SgoResult(C.Structure):
-    _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double)]
+    _fields_ = [("niters", C.c_int), ("eps", C.c_double), ("eps0", C.c_double),
+                ("t_setup", C.c_double), ("t_loop", C.c_double)]
 
 
 def _ptr(a: np.ndarray, t):
@@ -171,6 +172,35 @@ class Oracle:
         self._fn("cgsolve")(C.byref(s), _ptr(D, _dp), _ptr(h, _dp), _ptr(htmp, _dp), C.byref(pr),
                             C.byref(res))
         return h, int(res.niters)
+
+    def cgsolveq_timed(self, prob, props):
+        """cgsolveq plus the port's own timing: (q, niters, seconds before the
+        iteration loop, seconds in it).  Port only."""
+        assert self.which == "port"
+        g = prob.grid
+        s, keep = self._grid(g)
+        q = np.array(prob.q, dtype=np.float64, copy=True)
+        src = np.array(prob.src, dtype=np.float64, copy=True)
+        c = np.array(prob.c, dtype=np.float64, copy=True)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        pr = self._prop(props)
+        res = SgoResult()
+        self._fn("cgsolveq")(C.byref(s), _ptr(D, _dp), _ptr(q, _dp), _ptr(src, _dp), _ptr(c, _dp),
+                             C.byref(pr), C.byref(res))
+        return q, int(res.niters), float(res.t_setup), float(res.t_loop)
+
+    def cgsolve_timed(self, prob, props):
+        """cgsolve plus the port's own timing: (h, niters, setup s, loop s).  Port only."""
+        assert self.which == "port"
+        g = prob.grid
+        s, keep = self._grid(g)
+        h = np.array(prob.h, dtype=np.float64, copy=True)
+        htmp = np.array(prob.htmp, dtype=np.float64, copy=True)
+        D = np.ascontiguousarray(prob.D, dtype=np.float64)
+        pr = self._prop(props)
+        res = SgoResult()
+        self._fn("cgsolve")(C.byref(s), _ptr(D, _dp), _ptr(h, _dp), _ptr(htmp, _dp), C.byref(pr), C.byref(res))
+        return h, int(res.niters), float(res.t_setup), float(res.t_loop)
 
     def iteration_span(self, prob, props, solver="q"):
         """Iteration counts of the port's solve with the reference's sequential

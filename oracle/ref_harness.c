@@ -170,6 +170,8 @@ void ref_cgsolveq(const sgo_grid *g, const double *D, double *q, double *src, do
     res->niters = g_calls3d - 2 - (pr->qprecond == 1 ? 1 : 0);
     res->eps = -1;
     res->eps0 = -1;
+    res->t_setup = -1;
+    res->t_loop = -1;
   }
   harness_free(&H);
 }
@@ -187,6 +189,8 @@ void ref_cgsolve(const sgo_grid *g, const double *D, double *h, double *htmp, co
     res->niters = g_calls2d - 2;
     res->eps = -1;
     res->eps0 = -1;
+    res->t_setup = -1;
+    res->t_loop = -1;
   }
   harness_free(&H);
 }
@@ -574,6 +578,8 @@ int ref_upredictor(const sgo_grid *g, const sgo_ext *x, const sgo_vgrid *v, cons
     res->niters = g_calls2d - 3;
     res->eps = -1;
     res->eps0 = -1;
+    res->t_setup = -1;
+    res->t_loop = -1;
   }
   harness_free(&H);
   return 0;

@@ -344,4 +344,36 @@ def latency_report(reqs, t_end):
            "mean_unknowns": float(np.mean([r.unknowns for r in done])) if done else None}
     out["unknown_iters_per_s"] = out["unknown_iters"] / t_end if t_end > 0 else 0.0
     out["served_per_s"] = len(done) / t_end if t_end > 0 else 0.0
+    out["tail"] = tail_report(reqs, out["p99_ms"])
     return out
+
+
+def tail_report(reqs, p99_ms):
+    """Where the slowest requests (latency >= p99) spent their time, request by
+    request: waiting for admission (arrival to admission) against being solved
+    (admission to harvest), how many of them were admitted only when the
+    previous request on the same grid had finished (requests on one grid are
+    served one at a time), and their share of the grids and sizes."""
+    done = [r for r in reqs if r.t_done >= 0]
+    if not done or p99_ms is None:
+        return None
+    prev_done = {}
+    behind = {}
+    for r in sorted(reqs, key=lambda x: x.t_arrival):
+        pd = prev_done.get(r.grid)
+        behind[r.rid] = pd is not None and (pd < 0 or pd > r.t_arrival)
+        prev_done[r.grid] = r.t_done
+    slow = [r for r in done if (r.t_done - r.t_arrival) * 1e3 >= p99_ms]
+    if not slow:
+        return None
+    wait = np.array([max(r.t_admit - r.t_arrival, 0.0) for r in slow]) * 1e3
+    serve = np.array([r.t_done - max(r.t_admit, r.t_arrival) for r in slow]) * 1e3
+    grids = {}
+    for r in slow:
+        grids[r.grid] = grids.get(r.grid, 0) + 1
+    return {"requests": len(slow),
+            "mean_admission_wait_ms": float(wait.mean()), "mean_solve_ms": float(serve.mean()),
+            "behind_same_grid": int(sum(behind[r.rid] for r in slow)),
+            "distinct_grids": len(grids), "top_grid_share": max(grids.values()) / len(slow),
+            "mean_unknowns": float(np.mean([r.unknowns for r in slow])),
+            "mean_iters": float(np.mean([r.iters for r in slow]))}

@@ -213,6 +213,21 @@ def test_poisson_stream_and_realtime_loop(Eng):
     rep = latency_report(reqs, srv.t_end)
     assert rep["completed"] == n and rep["p99_ms"] >= rep["p50_ms"] > 0
     assert rep["status_counts"] == {0: n}
+    tail = rep["tail"]
+    assert tail["requests"] >= 1 and 0 <= tail["behind_same_grid"] <= tail["requests"]
+    assert tail["mean_admission_wait_ms"] >= 0 and tail["mean_solve_ms"] >= 0
+
+
+def test_tail_report_counts_requests_behind_their_grid():
+    """A request arriving while an earlier request on its grid is unfinished is
+    counted as waiting behind its grid."""
+    from suntans_gb300.serve import tail_report
+    a = Request(0, 0, 0, 1e-8, 0.0, t_admit=0.0, t_done=1.0, unknowns=10, iters=5)
+    b = Request(1, 0, 1, 1e-8, 0.5, t_admit=1.0, t_done=2.0, unknowns=10, iters=5)  # behind a
+    c = Request(2, 1, 0, 1e-8, 0.0, t_admit=0.0, t_done=0.1, unknowns=10, iters=5)
+    t = tail_report([a, b, c], 1000.0)
+    assert t["requests"] == 2 and t["behind_same_grid"] == 1 and t["distinct_grids"] == 1
+    assert abs(t["mean_admission_wait_ms"] - 250.0) < 1e-9
 
 
 def test_prefetched_sources_equal_direct():
