@@ -91,6 +91,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "step", "upred"])
     ap.add_argument("--no-mixed", action="store_true", help="cfg2: skip the mixed_form measurement")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="cfg2: skip the compact mixed (1M cells), batched (256 problems) and serving forms")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="cfg2: skip the full-size parity against the oracle's FP64 solves")
+    ap.add_argument("--parity-timeout", type=float, default=1200.0)
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--cfg3-points", type=int, default=500_000, help="cfg3: random points (domain scaled to keep the density)")
     ap.add_argument("--rate", type=float, default=2000.0)
@@ -105,7 +110,7 @@ def parse():
     ap.add_argument("--qprecond", type=int, default=1)
     ap.add_argument("--points", type=int, default=200_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-seconds", type=float, default=None,
                     help="--impl reference: seconds of CPU work per step (default: about a minute in all)")
     ap.add_argument("--ref-threads", type=int, default=None,
@@ -203,36 +208,66 @@ def peaks():
 
 
 # ---------------------------------------------------------------------------
-def _oracle_iteration_cost(o, qp, props):
-    """(set-up seconds, seconds per iteration) of the oracle's CGSolveQ on this
-    problem, from two short capped runs (2 and 6 iterations)."""
+def host_cpu():
+    """Model name and core counts of this host (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                model = v.strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except AttributeError:
+        usable = os.cpu_count() or 1
+    return {"cpu_model": model, "host_cores": os.cpu_count(), "usable_cores": usable}
+
+
+def _capped(props, **kw):
     from suntans_gb300.grid import SolverProps
-    ts, ns = [], []
-    for cap in (2, 6):
-        t = time.perf_counter()
-        _, n = o.cgsolveq(qp, SolverProps(**{**props.__dict__, "qmaxiters": cap}))
-        ts.append(time.perf_counter() - t)
-        ns.append(max(n, 1))
-    per_iter = (ts[1] - ts[0]) / (ns[1] - ns[0]) if ns[1] > ns[0] else ts[1] / ns[1]
-    per_iter = max(per_iter, ts[1] / ns[1] * 0.05, 1e-7)
-    return max(ts[1] - ns[1] * per_iter, 0.0), per_iter
+    return SolverProps(**{**props.__dict__, **kw})
+
+
+def _q_iters_for(o, qp, props, seconds: float) -> int:
+    """Iterations of the oracle's CGSolveQ that fill about `seconds` of its
+    iteration loop, priced by a 3-iteration run (set-up excluded)."""
+    _, n, _, tl = o.cgsolveq_timed(qp, _capped(props, qmaxiters=3))
+    per_iter = max(tl / max(n, 1), 1e-7)
+    return int(max(20, min(props.qmaxiters, seconds / per_iter)))
 
 
 def cpu_baseline(g, qp, hp, props, seconds: float):
-    """The oracle port on a bounded sample: CGSolveQ capped at M iterations, one thread."""
+    """The oracle port (bit-identical to the reference's solvers) on one host
+    thread: CGSolveQ capped at the iterations that fill about `seconds`, plus
+    the whole CGSolve when hp is given.  Only the iteration loops are timed
+    (the port's own clock_gettime around them): the set-up (coefficients,
+    conditioning, first residual) is reported beside, not counted."""
     from oracle.oracle import Oracle
-    from suntans_gb300.grid import SolverProps
     o = Oracle("port")
-    setup, per_iter = _oracle_iteration_cost(o, qp, props)
-    m = int(max(2, min(props.qmaxiters, (seconds * 0.8 - setup) / per_iter)))
-    capped = SolverProps(**{**props.__dict__, "qmaxiters": m})
-    t = time.perf_counter()
-    _, nq = o.cgsolveq(qp, capped)
-    tq = time.perf_counter() - t
-    work = g.n_q() * nq
-    return {"value": work / tq, "unit": "unknown-iters/s", "cores": 1, "kind": "port",
-            "sample": f"oracle CGSolveQ (qprecond {props.qprecond}) capped at {nq} iterations on the full "
-                      f"N_q={g.n_q()} grid, {tq:.1f} s, 1 thread"}
+    th = tlh = tsh = 0.0
+    nh = 0
+    if hp is not None:
+        _, nh, tsh, tlh = o.cgsolve_timed(hp, props)
+    m = _q_iters_for(o, qp, props, max(seconds - tlh, 1.0))
+    _, nq, tsq, tlq = o.cgsolveq_timed(qp, _capped(props, qmaxiters=m))
+    work = g.n_q() * nq + (g.n_h() * nh if hp is not None else 0)
+    sample = (f"oracle CGSolveQ (qprecond {props.qprecond}) capped at {nq} iterations on the full N_q={g.n_q()} grid"
+              + (f" plus the whole CGSolve ({nh} iterations, N_h={g.n_h()})" if hp is not None else "")
+              + f"; iteration loops timed, {tlq + tlh:.1f} s (set-up {tsq + tsh:.2f} s not counted), 1 thread")
+    return {"value": work / (tlq + tlh), "unit": "unknown-iters/s", "cores": 1, "kind": "port", "sample": sample,
+            "setup_s": tsq + tsh, **host_cpu()}
 
 
 def host_threads(bytes_per_thread: float) -> int:
@@ -256,25 +291,25 @@ def host_threads(bytes_per_thread: float) -> int:
     return max(1, cores)
 
 
-def cpu_baseline_parallel(g, qp, props, seconds: float, threads: int, cost=None):
-    """The oracle port on every host thread: `threads` independent replicas of
-    the bounded CGSolveQ sample run at once (the reference solver is serial; a
-    host runs one replica per core), unknown-iterations of all replicas ÷ the
-    wall time of the slowest."""
+def cpu_baseline_parallel(g, qp, hp, props, m: int, mh: int, threads: int):
+    """The oracle port on every host thread: `threads` independent replicas
+    (the reference solver is serial; a host runs one replica per core), each
+    running CGSolveQ capped at m iterations and CGSolve capped at mh, at once.
+    Unknown-iterations of all replicas ÷ the longest replica's time in its
+    iteration loops (set-up not counted)."""
     import threading
     from oracle.oracle import Oracle
-    from suntans_gb300.grid import SolverProps
     o = Oracle("port")
-    setup, per_iter = cost or _oracle_iteration_cost(o, qp, props)
-    # replicas share the memory bandwidth: budget for a 2x slowdown per replica
-    m = int(max(2, min(props.qmaxiters, (seconds * 0.5 - setup) / per_iter)))
-    capped = SolverProps(**{**props.__dict__, "qmaxiters": m})
-    iters = [0] * threads
+    out = [None] * threads
     errors = []
 
     def one(k):
         try:
-            iters[k] = o.cgsolveq(qp, capped)[1]
+            _, nq, tsq, tlq = o.cgsolveq_timed(qp, _capped(props, qmaxiters=m))
+            nh, tsh, tlh = 0, 0.0, 0.0
+            if hp is not None and mh > 0:
+                _, nh, tsh, tlh = o.cgsolve_timed(hp, _capped(props, maxiters=mh))
+            out[k] = (nq, nh, tsq + tsh, tlq + tlh)
         except Exception as e:  # reported after the join
             errors.append(repr(e))
 
@@ -287,35 +322,40 @@ def cpu_baseline_parallel(g, qp, props, seconds: float, threads: int, cost=None)
     wall = time.perf_counter() - t
     if errors:
         raise RuntimeError("CPU baseline replica failed: " + errors[0])
-    work = g.n_q() * sum(iters)
-    return {"value": work / wall, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
+    work = sum(g.n_q() * nq + (g.n_h() * nh if hp is not None else 0) for nq, nh, _, _ in out)
+    loop = max(x[3] for x in out)
+    nq0, nh0 = out[0][0], out[0][1]
+    return {"value": work / loop, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
             "sample": f"{threads} concurrent replicas of the oracle CGSolveQ (qprecond {props.qprecond}) capped at "
-                      f"{iters[0]} iterations on the full N_q={g.n_q()} grid, {wall:.1f} s wall; the reference "
-                      f"solver is serial (-DNOMPI), so the host's cores run one replica each"}
+                      f"{nq0} iterations on the full N_q={g.n_q()} grid"
+                      + (f" and CGSolve ({nh0} iterations, N_h={g.n_h()})" if hp is not None and mh > 0 else "")
+                      + f"; iteration loops timed (longest {loop:.1f} s, set-up up to "
+                        f"{max(x[2] for x in out):.1f} s not counted; {wall:.1f} s wall); the reference solver is "
+                        f"serial (-DNOMPI), so the host's cores run one replica each",
+            "loop_s": loop, "wall_s": wall}
 
 
 def cpu_baseline_instances(probs, props, seconds: float, threads: int):
     """The oracle port on every host thread for a set of independent problems:
     one problem per thread (the median-size ones of the set), each CGSolveQ
-    capped so that the run takes about `seconds`; unknown-iterations of all
-    threads ÷ the wall time."""
+    capped so that its iteration loop takes about `seconds`; unknown-iterations
+    of all threads ÷ the longest thread's loop time (set-up not counted)."""
     import threading
     from oracle.oracle import Oracle
-    from suntans_gb300.grid import SolverProps
     o = Oracle("port")
     order = np.argsort([p.grid.n_q() for p in probs])
     mid = len(order) // 2
     pick = [int(order[(mid + (k + 1) // 2 * (1 if k % 2 else -1)) % len(order)]) for k in range(threads)]
-    setup, per_iter = _oracle_iteration_cost(o, probs[pick[0]], props)
-    m = int(max(2, min(props.qmaxiters, (seconds * 0.5 - setup) / per_iter)))
-    capped = SolverProps(**{**props.__dict__, "qmaxiters": m})
-    work = [0] * threads
+    m = _q_iters_for(o, probs[pick[0]], props, 0.5 * seconds)
+    capped = _capped(props, qmaxiters=m)
+    res = [None] * threads
     errors = []
 
     def one(k):
         try:
             pr = probs[pick[k]]
-            work[k] = pr.grid.n_q() * o.cgsolveq(pr, capped)[1]
+            _, n, _, tl = o.cgsolveq_timed(pr, capped)
+            res[k] = (pr.grid.n_q() * n, tl)
         except Exception as e:  # reported after the join
             errors.append(repr(e))
 
@@ -328,39 +368,173 @@ def cpu_baseline_instances(probs, props, seconds: float, threads: int):
     wall = time.perf_counter() - t
     if errors:
         raise RuntimeError("CPU baseline thread failed: " + errors[0])
-    return {"value": sum(work) / wall, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
+    loop = max(x[1] for x in res)
+    return {"value": sum(x[0] for x in res) / loop, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
             "sample": f"{threads} problems of the set around its median size, one per thread, oracle CGSolveQ "
-                      f"(qprecond {props.qprecond}) capped at {m} iterations each, {wall:.1f} s wall"}
+                      f"(qprecond {props.qprecond}) capped at {m} iterations each; iteration loops timed "
+                      f"(longest {loop:.1f} s, {wall:.1f} s wall)", **host_cpu()}
 
 
 def run_reference(args):
+    """The reference's solvers (the oracle port, bit-identical to them) on
+    every host core: per step, one replica per core runs CGSolveQ capped at M
+    iterations and the whole CGSolve, concurrently; the line reports all
+    replicas' unknown-iterations ÷ the longest replica's iteration-loop time.
+    Warm-up steps run 2-iteration solves (page-in only); M is sized so that the
+    K timed steps take about a minute and a half in all."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import oracle as om
     if not om.available("port"):
         om.build_port()
+    from oracle.oracle import Oracle
     g, qp, hp, props, desc = make_workload(args)
-    per_step = []
-    seconds = args.ref_seconds or max(5.0, 60.0 / max(args.steps + args.warmup, 1))
     # per replica: the solver's scratch (z, r, rtmp, coef, F face coefficients) and its copies of q, src, c
     threads = args.ref_threads or host_threads(8.0 * g.n_q() * (7 + g.maxfaces) + 64e6)
-    from oracle.oracle import Oracle
-    cost = _oracle_iteration_cost(Oracle("port"), qp, props)
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline_parallel(g, qp, props, seconds, threads, cost)
-        if i >= args.warmup:
-            per_step.append(r)
+    o = Oracle("port")
+    _, nh_full, _, tlh = o.cgsolve_timed(hp, props)
+    seconds = args.ref_seconds or max(4.0, 90.0 / max(args.steps, 1))
+    # concurrent replicas share the memory bandwidth: budget for a 2x slowdown each
+    m = _q_iters_for(o, qp, props, max(0.5 * seconds - 2 * tlh, 1.0))
+    for _ in range(args.warmup):
+        cpu_baseline_parallel(g, qp, hp, props, 2, 2, threads)
+    per_step = [cpu_baseline_parallel(g, qp, hp, props, m, props.maxiters, threads) for _ in range(args.steps)]
     vals = [r["value"] for r in per_step]
     v = float(np.median(vals))
     line = {"metric": "Poisson CG unknown-iters/s (CGSolveQ+CGSolve, 1e-10 relative residual)", "value": v,
             "unit": "unknown-iters/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": desc, "impl": "reference",
+            "ms_per_step": float(np.median([r["loop_s"] for r in per_step])) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": desc,
+            "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "unknown-iters/s", "cores": threads, "kind": "port",
-                             "sample": per_step[0]["sample"]},
+                             "sample": per_step[0]["sample"], **host_cpu()},
             "e2e": {"value": v, "unit": "unknown-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# parity at full size: the oracle's own FP64 solves, in spawned processes
+# ---------------------------------------------------------------------------
+def _parity_job(kind, params, out_dir, queue):
+    """Runs in a spawned process (after the timed regions have started, so no
+    CPU work overlaps the default workload's timing): rebuilds the workload
+    from its seeds and runs the oracle's full FP64 solves to the same
+    tolerance.  cfg2: CGSolveQ and CGSolve, compared here with the GPU
+    solutions the parent saved.  cfg3: CGSolveQ only; its solution is saved
+    for the parent, which compares the mixed-precision result with it."""
+    try:
+        sys.path.insert(0, ROOT)
+        from oracle.oracle import Oracle
+        o = Oracle("port")
+        out = {"kind": kind}
+        if kind == "cfg2":
+            ns = argparse.Namespace(**params)
+            g, qp, hp, props, _ = make_workload(ns)
+            qr, nq, tsq, tlq = o.cgsolveq_timed(qp, props)
+            hr, nh, tsh, tlh = o.cgsolve_timed(hp, props)
+            d = np.load(os.path.join(out_dir, "gpu_cfg2.npz"))
+            m = g.active_mask()
+            c = g.comp_cells()
+            out["q"] = {**rel_errors(d["q"], qr, g), "iters_oracle": nq, "oracle_loop_s": tlq, "oracle_setup_s": tsq}
+            eh = d["h"][c] - hr[c]
+            out["h"] = {"rel_l2": float(np.linalg.norm(eh) / max(np.linalg.norm(hr[c]), 1e-300)),
+                        "max_abs_rel": float(np.abs(eh).max() / max(np.abs(hr[c]).max(), 1e-300)),
+                        "iters_oracle": nh, "oracle_loop_s": tlh, "oracle_setup_s": tsh}
+            del m
+        else:
+            g, qp, props, _ = make_cfg3(params["points"], params["qprecond"])
+            qr, nq, tsq, tlq = o.cgsolveq_timed(qp, props)
+            np.save(os.path.join(out_dir, "oracle_cfg3_q.npy"), qr)
+            out.update(iters_oracle=nq, oracle_loop_s=tlq, oracle_setup_s=tsq)
+        queue.put(out)
+    except Exception as e:  # reported in the line
+        queue.put({"kind": kind, "error": repr(e)})
+
+
+class ParityJobs:
+    """The spawned oracle processes of the default line."""
+
+    def __init__(self):
+        import multiprocessing as mp
+        import tempfile
+        self.ctx = mp.get_context("spawn")
+        self.queue = self.ctx.Queue()
+        self.dir = tempfile.mkdtemp(prefix="sgpu_parity_")
+        self.procs = []
+
+    def start(self, kind, params):
+        p = self.ctx.Process(target=_parity_job, args=(kind, params, self.dir, self.queue), daemon=True)
+        p.start()
+        self.procs.append(p)
+
+    def results(self, timeout_s: float):
+        out = {}
+        t_end = time.time() + timeout_s
+        for _ in self.procs:
+            try:
+                r = self.queue.get(timeout=max(1.0, t_end - time.time()))
+                out[r["kind"]] = r
+            except Exception:
+                break
+        for p in self.procs:
+            p.join(timeout=5)
+            if p.is_alive():
+                p.terminate()
+        return out
+
+    def close(self):
+        import shutil
+        shutil.rmtree(self.dir, ignore_errors=True)
+
+
+def compact_forms(args, parity_jobs=None):
+    """The three chosen forms in compact runs, for the default line: the mixed
+    form at 1M cells, the 256-problem batch and the serving stream."""
+    forms, keep = {}, {}
+    a3 = argparse.Namespace(**{**vars(args), "steps": 2, "warmup": 1, "no_cpu_baseline": True})
+    try:
+        l3 = bench_cfg3(a3, keep)
+        forms["mixed_1m"] = {
+            "workload": l3["config"]["workload"], "N_q": l3["config"]["N_q"], "qprecond": args.qprecond,
+            "equivalent_unknown_iters_per_s": l3["value"], "raw_unknown_iters_per_s": l3["mixed"]["raw_unknown_iters_per_s"],
+            "iters_inner": l3["mixed"]["iters_inner"], "iters_fp64": l3["iters_fp64"],
+            "plain_fp64_unknown_iters_per_s": l3["plain_fp64_unknown_iters_per_s"],
+            "speedup_vs_plain_fp64": l3["speedup_vs_plain_fp64"], "ms_per_solve": l3["ms_per_step"],
+            "errors_vs_fp64_gpu": {k: l3["mixed"][k] for k in ("rel_l2", "max_abs_rel")},
+            "roofline": l3["roofline"], "e2e": l3["e2e"], "clocks": l3["clocks"]}
+    except Exception as e:
+        forms["mixed_1m"] = {"error": repr(e)}
+    a4 = argparse.Namespace(**{**vars(args), "steps": 2, "warmup": 1, "no_cpu_baseline": True})
+    try:
+        l4 = bench_cfg4(a4)
+        forms["batched_256"] = {
+            "workload": l4["config"]["workload"], "instances": l4["config"]["instances"],
+            "N_q_total": l4["config"]["N_q_total"], "equivalent_unknown_iters_per_s": l4["value"],
+            "raw_unknown_iters_per_s": l4["raw_unknown_iters_per_s"],
+            "plain_fp64_loop_unknown_iters_per_s": l4["plain_fp64_loop_unknown_iters_per_s"],
+            "speedup_vs_plain_fp64_loop": l4["speedup_vs_plain_fp64_loop"], "ms_per_launch": l4["ms_per_step"],
+            "launch_shape": l4["config"]["launch_shape"], "graph": l4["config"]["graph"], "errors": l4["errors"],
+            "roofline": l4["roofline"], "e2e": l4["e2e"], "clocks": l4["clocks"]}
+    except Exception as e:
+        forms["batched_256"] = {"error": repr(e)}
+    a5 = argparse.Namespace(**{**vars(args), "serve_seconds": 3.0, "drain_seconds": 10.0, "sustain_seconds": 10.0})
+    try:
+        l5 = bench_cfg5(a5)
+        lat, lat2 = l5["latency"], l5["latency_at_sustainable_rate"]
+        forms["serving"] = {
+            "workload": l5["config"]["workload"], "unknown_iters_per_s": l5["value"],
+            "offered": {"rate_per_s": lat["rate"], "seconds": lat["seconds"], "p50_ms": lat["p50_ms"],
+                        "p99_ms": lat["p99_ms"], "served_per_s": lat["served_per_s"], "completed": lat["completed"],
+                        "requests": lat["requests"], "device_busy_frac": lat["device_busy_frac"], "tail": lat["tail"]},
+            "at_half_capacity": {"rate_per_s": lat2["rate"], "seconds": lat2["seconds"], "p50_ms": lat2["p50_ms"],
+                                 "p99_ms": lat2["p99_ms"], "unknown_iters_per_s": lat2["unknown_iters_per_s"],
+                                 "completed": lat2["completed"], "requests": lat2["requests"],
+                                 "device_busy_frac": lat2["device_busy_frac"], "tail": lat2["tail"]},
+            "hbm_budget_gb": l5["config"]["hbm_budget_gb"], "e2e": l5["e2e"], "clocks": l5["clocks"]}
+    except Exception as e:
+        forms["serving"] = {"error": repr(e)}
+    return forms, keep
 
 
 # ---------------------------------------------------------------------------
@@ -467,9 +641,53 @@ def run_ours(args):
         line["mixed_form"] = mf
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g, qp, hp, props, args.cpu_seconds)
+    ctx.close()
+    full = args.workload == "cfg2" and rank == 0 and world == 1
+    jobs = None
+    if full and not args.no_parity:
+        # the oracle's full FP64 solves run in spawned processes from here on,
+        # beside the forms below (device-timed), never beside the timing above
+        jobs = ParityJobs()
+        np.savez(os.path.join(jobs.dir, "gpu_cfg2.npz"), q=q, h=h)
+        jobs.start("cfg2", {"workload": "cfg2", "points": args.points, "qprecond": args.qprecond})
+        if not args.no_forms:
+            jobs.start("cfg3", {"points": args.cfg3_points, "qprecond": args.qprecond})
+    if full and not args.no_forms:
+        forms, keep = compact_forms(args)
+        line["forms"] = forms
+        srv = forms.get("serving", {})
+        if "offered" in srv:
+            line["latency_p99_ms"] = {"offered_rate": srv["offered"]["p99_ms"],
+                                      "at_half_capacity": srv["at_half_capacity"]["p99_ms"]}
+    else:
+        keep = {}
+    if jobs is not None:
+        res = jobs.results(timeout_s=args.parity_timeout)
+        par = {"oracle": "the oracle port (bit-identical to the reference's CGSolveQ/CGSolve), full FP64 solves "
+                         "to the same tolerance, one host core each, after the timed region"}
+        r2 = res.get("cfg2")
+        if r2 is None:
+            par["cfg2"] = {"error": "oracle job did not finish"}
+        elif "error" in r2:
+            par["cfg2"] = r2
+        else:
+            r2["q"]["iters_gpu"] = int(np.median(nq))
+            r2["h"]["iters_gpu"] = int(np.median(nh))
+            par["cfg2"] = {"q_qprecond%d" % props.qprecond: r2["q"], "h_hprecond1": r2["h"], "tolerance": 1e-9}
+        if not args.no_forms:
+            r3 = res.get("cfg3")
+            if r3 is None or "error" in r3 or "q_mix" not in keep:
+                par["mixed_1m"] = r3 or {"error": "oracle job did not finish"}
+            else:
+                qo = np.load(os.path.join(jobs.dir, "oracle_cfg3_q.npy"))
+                par["mixed_1m"] = {"q_mixed_vs_fp64_oracle": rel_errors(keep["q_mix"], qo, keep["grid"]),
+                                   "q_fp64_gpu_vs_fp64_oracle": rel_errors(keep["q64"], qo, keep["grid"]),
+                                   "iters_oracle": r3["iters_oracle"], "oracle_loop_s": r3["oracle_loop_s"],
+                                   "tolerance": 1e-9}
+        jobs.close()
+        line["parity"] = par
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -547,16 +765,24 @@ def _props(qprecond, tol=1e-10, maxiters=20000):
                        epsilon=tol, resnorm=1.0, dt=20.0, theta=0.55)
 
 
-def bench_cfg3(args):
+def make_cfg3(points: int, qprecond: int):
+    """The mixed-precision configuration: Delaunay seamount from `points`
+    random points in 50 km x 25 km (domain scaled to keep the density),
+    Nkmax 40 stretched 1.02; pressure right-hand side from a seeded N(0, 0.05)
+    face velocity."""
     from suntans_gb300 import gridgen as gg
+    scale = (points / 500_000) ** 0.5
+    g = gg.delaunay_seamount(points, 50_000.0 * scale, 25_000.0 * scale, Nkmax=40, rstretch=1.02, seed=3,
+                             H0=50.0, amp=30.0, sigma=2000.0, h_sigma=0.01)
+    qp = gg.make_q_problem(g, seed=13, sigma_u=0.05, dt=20.0)
+    return g, qp, _props(qprecond), scale
+
+
+def bench_cfg3(args, keep=None):
     from suntans_gb300.batch import Batch, capacity_for
     from suntans_gb300.capi import Context
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    scale = (args.cfg3_points / 500_000) ** 0.5
-    g = gg.delaunay_seamount(args.cfg3_points, 50_000.0 * scale, 25_000.0 * scale, Nkmax=40, rstretch=1.02, seed=3,
-                             H0=50.0, amp=30.0, sigma=2000.0, h_sigma=0.01)
-    qp = gg.make_q_problem(g, seed=13, sigma_u=0.05, dt=20.0)
-    props = _props(args.qprecond)
+    g, qp, props, scale = make_cfg3(args.cfg3_points, args.qprecond)
     N = g.n_q()
     # FP64 plain solve of the same problem: iteration count, reference solution, plain rate
     ctx = Context(g, device=local)
@@ -566,7 +792,9 @@ def bench_cfg3(args):
     q64 = ctx.q_download(qp.q)
     plain_rate = N * s64.niters / (s64.ms_solve / 1e3)
     ctx.close()
-    mf, clocks, _ = mixed_form(qp, args.qprecond, args.steps, args.warmup, 1e-10, 20000, local, q64, s64.niters)
+    mf, clocks, q_mix = mixed_form(qp, args.qprecond, args.steps, args.warmup, 1e-10, 20000, local, q64, s64.niters)
+    if keep is not None:
+        keep.update(q_mix=q_mix, q64=q64, grid=g)
     peak, peak_kind = peaks()
     # end to end through the public API: add (host arrays in), solve, result (host array out)
     t0 = time.perf_counter()
@@ -747,7 +975,8 @@ def bench_cfg5(args):
     # (the saturated run completes the cheaper requests first, so its served rate
     # overstates what the stream can sustain; half of it keeps the queue bounded)
     sus_rate = max(1.0, 0.5 * rep["served_per_s"])
-    rep2, _, _ = stream(sus_rate, max(10.0, 200.0 / sus_rate), 8)
+    sus_s = getattr(args, "sustain_seconds", None) or max(10.0, 200.0 / sus_rate)
+    rep2, _, _ = stream(sus_rate, sus_s, 8)
     b.close()
     launches = rep["launches"]
     line = {"metric": "Poisson CG unknown-iters/s under an open-loop request stream; p50/p99 latency",

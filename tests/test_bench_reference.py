@@ -21,6 +21,7 @@ def test_reference_arm_line():
     assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1
     cb = d["cpu_baseline"]
     assert cb["cores"] == 2 and cb["kind"] == "port" and cb["value"] == d["value"]
+    assert "CGSolve (" in cb["sample"] and "host_cores" in cb and "cpu_model" in cb
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
@@ -29,3 +30,30 @@ def test_host_threads_respects_memory():
     import bench
     assert bench.host_threads(1.0) >= 1
     assert bench.host_threads(1e18) == 1
+
+
+def test_parity_job_compares_with_the_oracle():
+    """The default line's parity leg: a spawned process rebuilds the workload
+    from its seeds, runs the oracle's full FP64 solves and compares them with
+    the solutions saved by the parent (here the oracle's own, so 0 error)."""
+    sys.path.insert(0, ROOT)
+    import argparse
+    import numpy as np
+    import bench
+    from oracle.oracle import Oracle
+    params = {"workload": "cfg2", "points": 1500, "qprecond": 1}
+    g, qp, hp, props, _ = bench.make_workload(argparse.Namespace(**params))
+    o = Oracle("port")
+    q, _ = o.cgsolveq(qp, props)
+    h, _ = o.cgsolve(hp, props)
+    jobs = bench.ParityJobs()
+    try:
+        np.savez(os.path.join(jobs.dir, "gpu_cfg2.npz"), q=q, h=h)
+        jobs.start("cfg2", params)
+        res = jobs.results(timeout_s=300)
+    finally:
+        jobs.close()
+    r = res["cfg2"]
+    assert "error" not in r, r
+    assert r["q"]["rel_l2"] == 0.0 and r["h"]["rel_l2"] == 0.0
+    assert r["q"]["iters_oracle"] > 2 and r["h"]["iters_oracle"] > 2
