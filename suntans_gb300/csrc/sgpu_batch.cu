@@ -503,7 +503,7 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   if (q >= 2 && !mbar_wait(&P.empty[b], ((q >> 1) - 1) & 1, lim)) *err = 1;
   const int par = pi.par;
   const int n4 = (d.nslots + 3) & ~3;
-  unsigned char* st = P.stage[b];
+  unsigned char* st = b ? P.stage[1] : P.stage[0];
   StageDesc* sd = stage_desc(st);
   sd->base = d.base;
   sd->nslots = d.nslots;
@@ -723,27 +723,31 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     return;
   }
   constexpr int NV = (PH == 1 && QP == 2) ? 2 : 1;
-  DF dacc[NV];
-  double acc[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) df_zero(dacc[v]);
+  // The accumulators are scalars, not arrays: an array captured by reference
+  // in the flush lambda below would live in local memory, and every
+  // accumulation of the phase loops would load and store it there.
+  DF dacc0, dacc1;
+  df_zero(dacc0);
+  df_zero(dacc1);
   // Per-warp flush of the instance's partial sums: a fixed shuffle tree, then
   // lane 0 stores the warp's value into the CTA's slot.  No barrier, fence or
   // atomic: the owner CTA collects the slots at the end of the phase.
   // `enc` is the slot, bitwise complemented when this CTA owns the instance.
   if (threadIdx.x == 0) *P.nown = 0;
   auto do_flush = [&](int inst, int enc) {
+    double v0 = df_value(dacc0), v1 = df_value(dacc1);
+    df_zero(dacc0);
+    df_zero(dacc1);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      acc[v] = df_value(dacc[v]);
-      df_zero(dacc[v]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
+    for (int o = 16; o > 0; o >>= 1) {
+      v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+      if (NV == 2) v1 += __shfl_xor_sync(0xffffffffu, v1, o);
     }
     const int slot = enc < 0 ? ~enc : enc;
-    if (lane == 0)
-#pragma unroll
-      for (int v = 0; v < NV; ++v) st_partial(a.tpw + ((size_t)slot * 8 + warp) * 2 + v, acc[v]);
+    if (lane == 0) {
+      st_partial(a.tpw + ((size_t)slot * 8 + warp) * 2, v0);
+      if (NV == 2) st_partial(a.tpw + ((size_t)slot * 8 + warp) * 2 + 1, v1);
+    }
     if (enc < 0 && threadIdx.x == 0) P.own[(*P.nown)++] = inst;
   };
   int cur = -1, cur_enc = 0;
@@ -751,7 +755,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     const uint32_t q = P.seq;
     const int b = q & 1;
     if (!mbar_wait(&P.full[b], (q >> 1) & 1, lim)) err = 1;
-    unsigned char* st = P.stage[b];
+    unsigned char* st = b ? P.stage[1] : P.stage[0];
     const StageDesc sd = *stage_desc(st);
     if (sd.inst != cur) {
       if (cur >= 0) do_flush(cur, cur_enc);
@@ -808,7 +812,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         const int u = base + threadIdx.x + qq * kCompute;
         a.z32[u] = yv[qq];
         pnew[u] = pv[qq];
-        df_addprod(dacc[0], pv[qq], yv[qq]);
+        df_addprod(dacc0, pv[qq], yv[qq]);
       }
     } else {
       const float* sp = stage_stream(st, 0);
@@ -833,10 +837,10 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
           if (QP == 2) {
             *(float4*)(sr + s0) = ro;
           } else {
-            df_addprod(dacc[0], ro.x, ro.x);
-            df_addprod(dacc[0], ro.y, ro.y);
-            df_addprod(dacc[0], ro.z, ro.z);
-            df_addprod(dacc[0], ro.w, ro.w);
+            df_addprod(dacc0, ro.x, ro.x);
+            df_addprod(dacc0, ro.y, ro.y);
+            df_addprod(dacc0, ro.z, ro.z);
+            df_addprod(dacc0, ro.w, ro.w);
           }
         }
       }
@@ -892,8 +896,8 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
           const float sv = (k >= (cn[c] & 0xffff)) ? stib[s] : 0.f;
           a.s32[base + s] = sv;
           const float r = sr[s];
-          df_addprod(dacc[0], r, sv);
-          df_addprod(dacc[NV - 1], r, r);
+          df_addprod(dacc0, r, sv);
+          df_addprod(NV == 2 ? dacc1 : dacc0, r, r);
         }
         csync();
       }
