@@ -864,7 +864,7 @@ def bench_cfg4(args):
     plain_rate = float((Ns * it64).sum() / loop_s)
     # launch shape
     if args.no_autotune:
-        best, table = {"ctas_per_sm": 3, "tile_slots": 1024}, []
+        best, table = {"ctas_per_sm": 3, "tile_slots": 1024, "x_in_apply": 1}, []
     else:
         best, table = autotune(probs, qprecond=args.qprecond, tol=tol, maxiters=maxiters, device=local)
 
@@ -872,6 +872,7 @@ def bench_cfg4(args):
         b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
         b.set(ctas=best["ctas_per_sm"] * sm_count(local))
         b.set_tile_slots(best["tile_slots"])
+        b.set_fusion(best.get("x_in_apply", 1))
         return b
 
     b = make_batch()

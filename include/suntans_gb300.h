@@ -379,6 +379,12 @@ int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);
  * from now on; a column longer than this still gets a tile of its own.
  * Smaller tiles spread small problems over more CTAs. */
 int sgpu_batch_set_tile_slots(sgpu_batch *b, int tile_slots);
+/* Tuning: where the FP32 solution update x += nu p runs.  1 (default): in the
+ * next operator-apply pass, which streams p anyway (fewer bytes per
+ * iteration, a larger pipeline stage); 0: in the vector-update pass.  The
+ * results are the same bits either way.  Refused while a problem is in
+ * mid-solve.  (A tuning knob of this engine; the reference has none.) */
+int sgpu_batch_set_fusion(sgpu_batch *b, int x_in_apply);
 void *sgpu_batch_stream(sgpu_batch *b);
 
 /* Device time of the last launch per phase (ns): [1] operator apply, [2]

@@ -1,21 +1,27 @@
 """Launch-shape autotuner of the batched pressure solver.
 
-The batched kernel's shape has two runtime knobs:
+The batched kernel's shape has three runtime knobs:
 
 * CTAs per SM (1..3 resident at the kernel's register budget): more CTAs hide
   the latency of the face gathers, fewer make the per-iteration grid barrier
-  cheaper;
-* storage slots per tile (the unit of work a CTA's eight compute warps take at
-  once; with the 1024-slot maximum a warp owns 128 slots, i.e. several columns
-  of a 10..60-level grid).  Small tiles spread a batch of small problems over
-  more CTAs; large tiles amortise the tile header and the pipeline hand-offs.
+  cheaper and leave each CTA more shared memory;
+* storage slots per tile, i.e. slots per compute lane (256, 512 or 1024
+  slots: 1, 2 or 4 slots per lane of the CTA's eight compute warps, each
+  warp covering 32, 64 or 128 consecutive levels -- part of a column, or
+  several columns of a 10..60-level grid).  Small tiles spread a batch of
+  small problems over more CTAs; large tiles amortise the tile header and the
+  pipeline hand-offs;
+* fusion: where the FP32 solution update x += nu p runs -- fused into the
+  next operator-apply pass, which streams p anyway (13 instead of 14 FP32
+  values per unknown-iteration, a larger pipeline stage), or kept in the
+  vector-update pass.  The two give the same bits.
 
-`autotune` measures unknown-iterations per second for every pair on the
-caller's own problems (a short run of `iters` iterations after the set-up
-phase, every instance active) and returns the fastest.  A pair whose tile
-count exceeds what that many CTAs can list is recorded as infeasible.  The
-pipeline depth and the fusion of the CG steps into two passes per iteration
-are fixed in the kernel; they are not swept.
+`autotune` measures unknown-iterations per second for every combination on
+the caller's own problems (a short run of `iters` iterations after the set-up
+phase, every instance active) and returns the fastest.  A combination whose
+tile count exceeds what that many CTAs can list is recorded as infeasible.
+The pipeline depth (two stages) and the two passes per iteration are fixed in
+the kernel.
 """
 from __future__ import annotations
 
@@ -26,6 +32,7 @@ from .capi import OOM, SolverError
 
 CTAS_PER_SM = (1, 2, 3)
 TILE_SLOTS = (256, 512, 1024)
+FUSION = (1, 0)
 
 
 def sm_count(device=0) -> int:
@@ -34,8 +41,9 @@ def sm_count(device=0) -> int:
 
 
 def autotune(problems, qprecond=1, tol=1e-10, maxiters=20000, iters=12, ctas_per_sm=CTAS_PER_SM,
-             tile_slots=TILE_SLOTS, device=0, sample=None):
-    """Returns (best, table): best = {"ctas_per_sm", "tile_slots", "rate", "ms"}; table lists every candidate.
+             tile_slots=TILE_SLOTS, fusion=FUSION, device=0, sample=None):
+    """Returns (best, table): best = {"ctas_per_sm", "tile_slots", "x_in_apply", "rate", "ms"}; table lists
+    every candidate.
 
     problems: QProblem list (all share maxfaces).  sample: use at most this many
     problems (evenly spaced after sorting by size), None = all."""
@@ -46,10 +54,11 @@ def autotune(problems, qprecond=1, tol=1e-10, maxiters=20000, iters=12, ctas_per
     F = probs[0].grid.maxfaces
     nsm = sm_count(device)
     table = []
-    for ts in tile_slots:
+    for ts, fx in [(t, f) for t in tile_slots for f in fusion]:
         b = Batch(qprecond=qprecond, maxfaces=F, device=device, **capacity_for([p.grid for p in probs]))
         try:
             b.set_tile_slots(ts)
+            b.set_fusion(fx)
             for p in probs:
                 b.add(p, tol=tol, maxiters=maxiters)
             started = False
@@ -63,11 +72,11 @@ def autotune(problems, qprecond=1, tol=1e-10, maxiters=20000, iters=12, ctas_per
                 except SolverError as e:
                     if e.code != OOM:  # more tiles than this CTA count can list: not a candidate
                         raise
-                    table.append({"ctas_per_sm": cps, "tile_slots": ts, "rate": 0.0, "ms": None,
-                                  "infeasible": str(e)})
+                    table.append({"ctas_per_sm": cps, "tile_slots": ts, "x_in_apply": fx, "rate": 0.0,
+                                  "ms": None, "infeasible": str(e)})
                     continue
-                table.append({"ctas_per_sm": cps, "tile_slots": ts, "rate": work / (ms / 1e3) if ms > 0 else 0.0,
-                              "ms": ms})
+                table.append({"ctas_per_sm": cps, "tile_slots": ts, "x_in_apply": fx,
+                              "rate": work / (ms / 1e3) if ms > 0 else 0.0, "ms": ms})
         finally:
             b.close()
     best = max(table, key=lambda r: r["rate"])

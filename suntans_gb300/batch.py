@@ -66,6 +66,13 @@ class Batch:
         if rc != OK:
             raise SolverError(rc, "sgpu_batch_set")
 
+    def set_fusion(self, x_in_apply: int):
+        """Where the FP32 solution update runs: 1 in the next apply pass
+        (default), 0 in the update pass; same bits either way."""
+        rc = self.lib.sgpu_batch_set_fusion(self.h, int(x_in_apply))
+        if rc != OK:
+            raise SolverError(rc, "sgpu_batch_set_fusion")
+
     def set_tile_slots(self, n: int):
         """Storage slots per tile for problems added from now on (4..1024)."""
         rc = self.lib.sgpu_batch_set_tile_slots(self.h, int(n))

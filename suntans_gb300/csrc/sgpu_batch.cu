@@ -407,7 +407,8 @@ __device__ __forceinline__ bool take_partial(double* p, long long lim, double& o
 // the pipelined phases
 // ---------------------------------------------------------------------------
 // One pipeline stage in shared memory: a 32-byte descriptor written by the
-// producer, the tile header (capacity kHdrCap - 32), and up to 4 FP32 streams.
+// producer, the tile header (room for the launch's largest header), and the
+// FP32 streams.
 // The descriptor carries what the compute warps need of the tile's instance
 // (its scalars and its partial-sum slot), so that they never wait on a global
 // load when the instance changes.
@@ -421,12 +422,13 @@ static_assert(sizeof(StageDesc) == 32, "stage descriptor is 32 bytes");
 constexpr int kStageHdrOff = 32;
 __device__ __forceinline__ StageDesc* stage_desc(unsigned char* stage) { return (StageDesc*)(stage); }
 __device__ __forceinline__ unsigned char* stage_hdr(unsigned char* stage) { return stage + kStageHdrOff; }
-__device__ __forceinline__ float* stage_stream(unsigned char* stage, int k) {
-  return (float*)(stage + kHdrCap + k * kStreamBytes);
+__device__ __forceinline__ float* stage_stream(unsigned char* stage, int hcap, int k) {
+  return (float*)(stage + hcap + k * kStreamBytes);
 }
 
 struct Pipe {
   unsigned char* stage[2];
+  int hcap;          // bytes before the streams of a stage (BatchArgs::hdr_cap)
   uint64_t* full;    // [2]
   uint64_t* empty;   // [2]
   int* list;         // tiles of this CTA for the current phase
@@ -477,7 +479,7 @@ __device__ __forceinline__ void build_list(const BatchArgs& a, Pipe& P, Want&& w
 // Instance fields the producer hands to the compute warps with each tile.
 struct ProdInst {
   int inst, par, slot, owner;
-  float mu, nu;
+  float mu, nu, nux;
 };
 __device__ __forceinline__ ProdInst prod_inst(const BatchArgs& a, int i) {
   const BInst& I = a.inst[i];
@@ -490,6 +492,7 @@ __device__ __forceinline__ ProdInst prod_inst(const BatchArgs& a, int i) {
   r.owner = (l == 0);
   r.mu = (float)(*(volatile const double*)&I.mu);
   r.nu = (float)(*(volatile const double*)&I.nu);
+  r.nux = (float)(*(volatile const double*)&I.nu_x);
   return r;
 }
 
@@ -512,28 +515,32 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   sd->slot = pi.slot;
   sd->owner = pi.owner;
   sd->mu = pi.mu;
-  sd->nu = pi.nu;
+  const bool xa = a.x_in_apply != 0;
+  sd->nu = PH == 0 ? (xa ? pi.nux : 0.f) : pi.nu;  // apply: the pending solution increment's nu
   const bool hdr = (PH == 0) || (QP == 2);
   uint32_t bytes = 0;
-  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + a.F * 4 * n4;
-  else bytes = (hdr ? d.hdr_bytes : 0) + 4 * 4 * n4;
+  if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + a.F * 4 * n4 + (xa ? 4 * n4 : 0);
+  else bytes = (hdr ? d.hdr_bytes : 0) + (xa ? 2 : 4) * 4 * n4;
   fence_proxy_async();
   mbar_arrive_expect_tx(&P.full[b], bytes);
   if (hdr) bulk_g2s(stage_hdr(st), a.hdrs + d.hdr, d.hdr_bytes, &P.full[b]);
   if (PH == 0) {
     const float* pold = par ? a.pb32 : a.pa32;
     const float* S = (QP == 2) ? a.s32 : a.r32;
-    bulk_g2s(stage_stream(st, 0), pold + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, 1), S + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, 0), pold + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, 1), S + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
     for (int f = 0; f < a.F; ++f)
-      bulk_g2s(stage_stream(st, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
+      bulk_g2s(stage_stream(st, P.hcap, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
+    if (xa) bulk_g2s(stage_stream(st, P.hcap, 3 + a.F), a.x32 + d.base, 4 * n4, &P.full[b]);
   } else {
-    const float* p = par ? a.pb32 : a.pa32;  // the direction written by phase A
-    bulk_g2s(stage_stream(st, 0), p + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, 1), a.x32 + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, 2), a.z32 + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, 3), a.r32 + d.base, 4 * n4, &P.full[b]);
+    if (!xa) {
+      const float* p = par ? a.pb32 : a.pa32;  // the direction written by phase A
+      bulk_g2s(stage_stream(st, P.hcap, 0), p + d.base, 4 * n4, &P.full[b]);
+      bulk_g2s(stage_stream(st, P.hcap, 1), a.x32 + d.base, 4 * n4, &P.full[b]);
+    }
+    bulk_g2s(stage_stream(st, P.hcap, 2), a.z32 + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, 3), a.r32 + d.base, 4 * n4, &P.full[b]);
   }
   P.seq = q + 1;
 }
@@ -548,8 +555,6 @@ __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char
   const int F = a.F;
   const int* fns = (const int*)(hd + L.o_fns);
   const int* fkk = (const int*)(hd + L.o_fkk);
-  const float* fD = (const float*)(hd + L.o_fD);
-  const int* fes = (const int*)(hd + L.o_fes);
   const float pu = __fmaf_rn(mu, sp[s], sS[s]);
   pu_out = pu;
   float y;
@@ -621,8 +626,6 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
   const int* cn = (const int*)(hd + L.o_cn);
   const int* fns = (const int*)(hd + L.o_fns);
   const int* fkk = (const int*)(hd + L.o_fkk);
-  const float* fD = (const float*)(hd + L.o_fD);
-  const int* fes = (const int*)(hd + L.o_fes);
   const unsigned char* cmap = hd + L.o_cmap;
   int cc[Q], kv[Q], ctop[Q], nk[Q], sv[Q];
 #pragma unroll
@@ -772,13 +775,26 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       const HdrLayout L = hdr_layout(ncols, a.F, len);
       const unsigned short* start = (const unsigned short*)(hd + L.o_start);
       const int* cn = (const int*)(hd + L.o_cn);
-      const float* sp = stage_stream(st, 0);
-      const float* sS = stage_stream(st, 1);
-      const float* sc = stage_stream(st, 2);
-      const float* sf = stage_stream(st, 3);
+      const float* sp = stage_stream(st, P.hcap, 0);
+      const float* sS = stage_stream(st, P.hcap, 1);
+      const float* sc = stage_stream(st, P.hcap, 2);
+      const float* sf = stage_stream(st, P.hcap, 3);
       const float* pold = sd.par ? a.pb32 : a.pa32;
       float* pnew = sd.par ? a.pa32 : a.pb32;
       const float* S = (QP == 2) ? a.s32 : a.r32;
+      {
+        // the previous update phase's solution increment, deferred to here
+        // where its direction (p_old) is staged anyway: x32 += nu p_old, 4
+        // consecutive slots per thread (padding slots hold zeros in every stream)
+        const int s0 = 4 * (int)threadIdx.x;
+        if (nu != 0.f && s0 < len) {
+          const float* sx = stage_stream(st, P.hcap, 3 + a.F);
+          const float4 p4 = *(const float4*)(sp + s0);
+          const float4 x4 = *(const float4*)(sx + s0);
+          *(float4*)(a.x32 + base + s0) = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y),
+                                                      __fmaf_rn(nu, p4.z, x4.z), __fmaf_rn(nu, p4.w, x4.w));
+        }
+      }
       float yv[Q], pv[Q];
       bool on[Q];
       if (a.F == 3) {
@@ -815,24 +831,25 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         df_addprod(dacc0, pv[qq], yv[qq]);
       }
     } else {
-      const float* sp = stage_stream(st, 0);
-      const float* sx = stage_stream(st, 1);
-      const float* sz = stage_stream(st, 2);
-      float* sr = stage_stream(st, 3);
+      const float* sz = stage_stream(st, P.hcap, 2);
+      float* sr = stage_stream(st, P.hcap, 3);
       {
         // 4 consecutive slots per thread: float4 in shared memory and global
-        // (padding slots hold zeros in every stream and stay zero)
+        // (padding slots hold zeros in every stream and stay zero).  The
+        // solution increment nu p is deferred to the next apply phase (or to
+        // the reliable update), where p is streamed anyway.
         const int s0 = 4 * (int)threadIdx.x;
         if (s0 < len) {
-          const float4 p4 = *(const float4*)(sp + s0);
-          const float4 x4 = *(const float4*)(sx + s0);
+          if (!a.x_in_apply) {
+            const float4 p4 = *(const float4*)(stage_stream(st, P.hcap, 0) + s0);
+            const float4 x4 = *(const float4*)(stage_stream(st, P.hcap, 1) + s0);
+            *(float4*)(a.x32 + base + s0) = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y),
+                                                        __fmaf_rn(nu, p4.z, x4.z), __fmaf_rn(nu, p4.w, x4.w));
+          }
           const float4 z4 = *(const float4*)(sz + s0);
           const float4 r4 = *(const float4*)(sr + s0);
-          const float4 xo = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y), __fmaf_rn(nu, p4.z, x4.z),
-                                        __fmaf_rn(nu, p4.w, x4.w));
           const float4 ro = make_float4(__fmaf_rn(-nu, z4.x, r4.x), __fmaf_rn(-nu, z4.y, r4.y),
                                         __fmaf_rn(-nu, z4.z, r4.z), __fmaf_rn(-nu, z4.w, r4.w));
-          *(float4*)(a.x32 + base + s0) = xo;
           *(float4*)(a.r32 + base + s0) = ro;
           if (QP == 2) {
             *(float4*)(sr + s0) = ro;
@@ -849,9 +866,9 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         // streams of the stage are no longer needed, so they are refilled
         // (coalesced) with the Thomas factors tw, tib and the coefficients.
         csync();
-        float* stw = stage_stream(st, 0);
-        float* stib = stage_stream(st, 1);
-        float* scf = stage_stream(st, 2);
+        float* stw = stage_stream(st, P.hcap, 0);
+        float* stib = stage_stream(st, P.hcap, 1);
+        float* scf = stage_stream(st, P.hcap, 2);
         const int n4 = (len + 3) & ~3;
         for (int s = threadIdx.x; s < n4 + 4; s += kCompute) {
           if (s < n4) {
@@ -983,6 +1000,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   const long long lim = ctl->timeout_ns;
 
   Pipe P;
+  P.hcap = a.hdr_cap;
   P.stage[0] = dyn;
   P.stage[1] = dyn + a.stage_bytes;
   P.full = (uint64_t*)(dyn + 2 * a.stage_bytes);
@@ -1177,6 +1195,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
             I->eps_ref = eps0;
             I->mu = 0.0;
             I->nu = 0.0;
+            I->nu_x = 0.0;
             I->n = 0;
             I->nrel = 0;
             I->flags = 0;
@@ -1203,6 +1222,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
     // ---- A: p_new = S + mu p_old (on the fly), z = A p_new, p.z ----
     build_list(a, P, is_run, s_wsum);
     pipelined_phase<QP, 0>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
+      In->nu_x = 0.0;  // this phase's tiles added the pending solution increment
       const double alpha = In->alpha;
       In->alpha_prev = alpha;
       In->mu = 1 / alpha;  // mu = 1/alpha before nu (2484-2485)
@@ -1225,6 +1245,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
       const double mu = In->mu * alpha;  // mu *= alpha (2498/2509)
       In->mu = mu;
       In->alpha = alpha;
+      In->nu_x = a.x_in_apply ? In->nu : 0.0;  // x32 += nu p now pending (next apply phase or R1)
       const double eps = (QP == 2) ? tot[1] : alpha;
       In->eps = eps;
       const int n = In->n + 1;
@@ -1259,12 +1280,16 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
 
     if (ld_volatile_int(&a.gflags[2])) {
       auto flagged = [&](int i) { return inst_flags(a, i) != 0; };
-      // ---- R1: x64 += x32, x32 = 0 for flagged instances ----
+      // ---- R1: x64 += x32 (+ the pending nu p), x32 = 0 for flagged instances ----
       if (compute)
         for_tiles(a, flagged, [&](int t, int i) {
           const TileDesc d = a.tiles[t];
+          const BInst& I = a.inst[i];
+          const float nux = (float)(*(volatile const double*)&I.nu_x);
+          const float* p = ld_volatile_int(&I.par) ? a.pb32 : a.pa32;  // the direction of the last update phase
           for (int u = d.base + tid; u < d.base + d.nslots; u += kCompute) {
-            a.x64[u] += f2d(a.x32[u]);
+            const float x = nux != 0.f ? __fmaf_rn(nux, p[u], a.x32[u]) : a.x32[u];
+            a.x64[u] += f2d(x);
             a.x32[u] = 0.f;
           }
         });
@@ -1298,6 +1323,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
               csync();
             },
             [&](BInst* In, const double* tot) {
+              In->nu_x = 0.0;  // R1 added the pending solution increment
               if (!(In->flags & 1)) {
                 In->flags = 0;
                 return;
@@ -1485,6 +1511,7 @@ struct sgpu_batch {
   long long last_work = 0;
   bool attr_set[3] = {false, false, false};
   int streams = 4;                    // FP32 streams per pipeline stage
+  int x_in_apply = 1;                 // the solution update's place (BatchArgs::x_in_apply)
   int dyn_smem = kDynSmem;            // dynamic shared memory of the kernel
 };
 
@@ -1537,7 +1564,7 @@ static int batch_max_grid(sgpu_batch* b) {
   if (!b->attr_set[b->qprecond]) {
     // the largest stage configuration any batch may use, so that batches of
     // different face counts sharing the kernel never find the limit too low
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_bytes(3 + kMaxF)) !=
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_bytes(4 + kMaxF)) !=
         cudaSuccess)
       return 0;
     b->attr_set[b->qprecond] = true;
@@ -1564,7 +1591,7 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   b->device = device;
   b->qprecond = qprecond;
   b->F = maxfaces;
-  b->streams = 3 + maxfaces;
+  b->streams = 4 + maxfaces;
   b->dyn_smem = dyn_smem_bytes(b->streams);
   // tiles are 4-slot aligned: reserve room for the padding (< 4 slots per tile)
   const long long tiles_est = max_cols + max_slots / kBTSlots + 2LL * max_instances + 2;
@@ -1862,8 +1889,6 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
     int* cn = (int*)(h + L.o_cn);
     int* fns = (int*)(h + L.o_fns);
     int* fkk = (int*)(h + L.o_fkk);
-    float* fD = (float*)(h + L.o_fD);
-    int* fes = (int*)(h + L.o_fes);
     unsigned char* cmap = h + L.o_cmap;
     for (int cc = 0; cc < ncols; ++cc) {
       const int j = T.c0 + cc;
@@ -1874,8 +1899,6 @@ int sgpu_batch_add(sgpu_batch* b, const sgpu_grid_desc* g, const int* ctop, cons
         const BFace& fc = v_face[(size_t)j * F + f];
         fns[cc * F + f] = fc.ns;
         fkk[cc * F + f] = fc.ns < 0 ? 0 : ((int)fc.kmin | ((int)fc.kmax << 16));
-        fD[cc * F + f] = fc.D;
-        fes[cc * F + f] = fc.es;
       }
     }
     st[ncols] = (unsigned short)T.nslots;
@@ -1964,6 +1987,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     if (key[x] != key[y]) return key[x] > key[y];
     return b->inst[x].unk > b->inst[y].unk;
   });
+  int max_hdr = 0;
   for (int i : order) {
     HostInst& H = b->inst[i];
     BInst& I = b->h_inst[i];
@@ -1976,6 +2000,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
       if (d.hdr != nb || d.base != base || d.inst != i) tiles_changed = true;
       d.hdr = nb;
       d.hdr_bytes = T.hdr_bytes;
+      max_hdr = std::max(max_hdr, T.hdr_bytes);
       d.base = base;
       d.nslots = T.nslots;
       d.inst = i;
@@ -1996,6 +2021,14 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     b->last_work = 0;
     return SGPU_OK;
   }
+  // stages sized to this launch's largest tile header: the streams start
+  // right after it (a 1024-slot tile of 40-level columns has a ~3 KB header,
+  // far below the 10 KB a tile of 128 shallow columns needs), which leaves
+  // room for three CTAs per SM with the apply phase's 4 + F streams
+  const int hdr_cap = std::min(kHdrCap, (kStageHdrOff + max_hdr + 127) & ~127);
+  const int streams = b->x_in_apply ? b->streams : std::max(b->streams - 1, 4);
+  const int stage_bytes = std::max(stage_bytes_for(hdr_cap, streams), (int)((sizeof(TileSmem) + 127) & ~127));
+  b->dyn_smem = dyn_smem_bytes_for(stage_bytes);
   int maxg = batch_max_grid(b);
   if (maxg <= 0) return bfail(b, SGPU_CUDA_ERROR, "occupancy query failed");
   int grid = b->grid_override > 0 ? std::min(b->grid_override, maxg) : maxg;
@@ -2027,7 +2060,9 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     if ((e = cudaMemcpyAsync(b->d_gflags, b->h_gflags, 4 * sizeof(int), cudaMemcpyHostToDevice, st))) return e;
     BatchArgs a = b->a;
     a.F = b->F;
-    a.stage_bytes = stage_bytes_for(b->streams);
+    a.stage_bytes = stage_bytes;
+    a.hdr_cap = hdr_cap;
+    a.x_in_apply = b->x_in_apply;
     a.ntiles = ntiles;
     a.ninst = ninst;
     a.max_iters_chunk = chunk;
@@ -2249,6 +2284,18 @@ int sgpu_batch_set(sgpu_batch* b, double delta, int grid, long long timeout_ns) 
   if (delta > 0) b->delta = delta;
   if (grid >= 0) b->grid_override = grid;
   if (timeout_ns > 0) b->timeout_ns = timeout_ns;
+  return SGPU_OK;
+}
+
+int sgpu_batch_set_fusion(sgpu_batch* b, int x_in_apply) {
+  if (!b || (x_in_apply != 0 && x_in_apply != 1)) return SGPU_BAD_ARG;
+  if (b->inflight) return bfail(b, SGPU_BAD_ARG, "a launch is in flight");
+  // a problem in mid-solve may hold a deferred solution increment (nu_x) that
+  // only the deferring form applies: change the form between solves only
+  for (int i = 0; i < b->max_inst; ++i)
+    if (b->inst[i].live && b->h_inst[i].state == INST_RUN && x_in_apply != b->x_in_apply)
+      return bfail(b, SGPU_BAD_ARG, "problem %d is in mid-solve", i);
+  b->x_in_apply = x_in_apply;
   return SGPU_OK;
 }
 

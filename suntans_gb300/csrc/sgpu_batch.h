@@ -21,13 +21,17 @@ constexpr int kHdrCap = 10240;   // bytes of a tile header (see tile header layo
 constexpr int kStreamFloats = kBTSlots + 4;                 // one FP32 stream of a tile (+1 group)
 constexpr int kStreamBytes = kStreamFloats * 4;             // 4112, a multiple of 16
 constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // the smallest pipeline stage (4 streams)
-// A stage holds the header and `streams` = 3 + F FP32 streams (p, s, coef and
-// one face-weight stream per face; the update phase uses 4 of them).
+// A stage holds the descriptor and header (at most kHdrCap bytes; each launch
+// sizes it to its largest tile header) and `streams` = 4 + F FP32 streams (p,
+// s, coef, one face-weight stream per face and x; the update phase uses 2 of
+// them, and 4 as scratch for qprecond 2).
 __host__ __device__ constexpr int stage_bytes_for(int streams) { return kHdrCap + streams * kStreamBytes; }
+__host__ __device__ constexpr int stage_bytes_for(int hdr_cap, int streams) { return hdr_cap + streams * kStreamBytes; }
 static_assert(kBTCols <= 256, "the header's slot-to-column map holds one byte per slot");
 constexpr int kListCap = 512;    // tiles per CTA per phase
 // dynamic shared memory of the kernel: 2 stages, 4 mbarriers (32 B), the tile list
 __host__ __device__ constexpr int dyn_smem_bytes(int streams) { return 2 * stage_bytes_for(streams) + 32 + 4 * kListCap; }
+__host__ __device__ constexpr int dyn_smem_bytes_for(int stage_bytes) { return 2 * stage_bytes + 32 + 4 * kListCap; }
 constexpr int kDynSmem = dyn_smem_bytes(4);
 
 // Tile header (global, built on the host when an instance is added; all
@@ -37,12 +41,10 @@ constexpr int kDynSmem = dyn_smem_bytes(4);
 //   o_cn      int cn[ncols]                   ctop | nk << 16
 //   o_fns     int fns[ncols*F]                neighbour's first slot (-1: none)
 //   o_fkk     int fkk[ncols*F]                kmin | kmax << 16 (empty when no neighbour)
-//   o_fD      float fD[ncols*F]               D of the edge
-//   o_fes     int fes[ncols*F]                edge's first slot (dzf*D storage)
 //   o_cmap    unsigned char cmap[nslots]      column of each slot of the tile
 __host__ __device__ __forceinline__ int pad16(int b) { return (b + 15) & ~15; }
 struct HdrLayout {
-  int o_start, o_cn, o_fns, o_fkk, o_fD, o_fes, o_cmap, bytes;
+  int o_start, o_cn, o_fns, o_fkk, o_cmap, bytes;
 };
 __host__ __device__ __forceinline__ HdrLayout hdr_layout(int ncols, int F, int nslots) {
   HdrLayout L;
@@ -51,9 +53,7 @@ __host__ __device__ __forceinline__ HdrLayout hdr_layout(int ncols, int F, int n
   const int sf = pad16(4 * ncols * F);
   L.o_fns = L.o_cn + pad16(4 * ncols);
   L.o_fkk = L.o_fns + sf;
-  L.o_fD = L.o_fkk + sf;
-  L.o_fes = L.o_fD + sf;
-  L.o_cmap = L.o_fes + sf;
+  L.o_cmap = L.o_fkk + sf;  // the face weights travel as streams, not in the header
   L.bytes = L.o_cmap + pad16(nslots);
   return L;
 }
@@ -93,6 +93,10 @@ struct __align__(64) BInst {
   double alpha, eps, eps0, eps_ref;   // CG scalars (FP64)
   double mu, nu;
   double alpha_prev;
+  double nu_x;         // the solution increment nu_x * p still to add to x32 (p = the
+                       // direction of the last update phase): the next apply phase
+                       // adds it where it streams that direction anyway, or the
+                       // reliable update adds it; 0 when nothing is pending
 };
 
 // Column metadata (one entry per computational column, global column index),
@@ -115,7 +119,10 @@ struct BFace {
 
 struct BatchArgs {
   int F;
-  int stage_bytes;     // bytes of one pipeline stage (stage_bytes_for(streams))
+  int stage_bytes;     // bytes of one pipeline stage: hdr_cap + streams * kStreamBytes
+  int hdr_cap;         // bytes before a stage's streams: descriptor + the launch's largest header
+  int x_in_apply;      // 1: the solution update x32 += nu p runs in the next apply pass, where
+                       // p is streamed anyway; 0: in the update pass (streams p and x there)
   int ntiles;
   int ninst;           // instance slots in use (some may be EMPTY/DONE)
   int max_iters_chunk; // global iterations allowed in this launch

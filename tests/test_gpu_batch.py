@@ -261,3 +261,56 @@ def test_overlapped_launch_wait_equals_solo(gpu_lib):
     assert np.array_equal(results["first2"][0], ref[2][0])
     assert results[2][1].niters == ref_re[1].niters and np.array_equal(results[2][0], ref_re[0])
     b.close()
+
+
+@pytest.mark.parametrize("qprecond", [0, 1, 2])
+def test_fusion_forms_equal_bitwise(gpu_lib, qprecond):
+    """The solution update run in the next apply pass (x_in_apply 1, the
+    default) or in the update pass (0): the same FP32 operations on the same
+    operands, so the same bits and iteration counts; also across chunked
+    launches (the increment deferred past a launch boundary and into the
+    reliable updates), and MAXITER stops."""
+    grids = tri_grids()
+    probs = [gg.make_q_problem(g, seed=60 + k, q0_sigma=0.01) for k, g in enumerate(grids)]
+    out = {}
+    for form in (0, 1):
+        for chunk in (0, 7):
+            b = Batch(qprecond=qprecond, maxfaces=3, **capacity_for(grids))
+            b.set_fusion(form)
+            ids = [b.add(p, maxiters=4000 if k else 25) for k, p in enumerate(probs)]
+            while True:
+                running, _, _ = b.run(max_iters=chunk)
+                if running == 0:
+                    break
+            out[(form, chunk)] = [b.result(i, p.q) for i, p in zip(ids, probs)]
+            b.close()
+    ref = out[(0, 0)]
+    assert ref[0][1].status == MAXITER
+    for key, res in out.items():
+        for (q, st), (q0, st0) in zip(res, ref):
+            assert st.status == st0.status and st.niters == st0.niters, key
+            assert np.array_equal(q, q0), key
+
+
+def test_fusion_change_refused_mid_solve(gpu_lib):
+    g = tri_grids()[1]
+    b = Batch(qprecond=1, maxfaces=3, **capacity_for([g]))
+    b.add(gg.make_q_problem(g, seed=3))
+    b.run(max_iters=3)
+    with pytest.raises(Exception):
+        b.set_fusion(0)
+    b.set_fusion(1)  # unchanged: accepted
+    b.close()
+
+
+def test_autotune_sweeps_the_three_knobs(gpu_lib):
+    """CTAs per SM, slots per tile and the fusion of the solution update are
+    all swept; the chosen shape is a measured, feasible one."""
+    from suntans_gb300.autotune import autotune
+    grids = tri_grids()
+    probs = [gg.make_q_problem(g, seed=70 + k) for k, g in enumerate(grids)]
+    best, table = autotune(probs, qprecond=1, iters=4, ctas_per_sm=(1, 2), tile_slots=(512, 1024))
+    assert len(table) == 2 * 2 * 2
+    assert {(r["ctas_per_sm"], r["tile_slots"], r["x_in_apply"]) for r in table} == \
+        {(c, t, f) for c in (1, 2) for t in (512, 1024) for f in (0, 1)}
+    assert best["rate"] > 0 and best["rate"] == max(r["rate"] for r in table)
