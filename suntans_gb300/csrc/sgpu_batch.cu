@@ -422,13 +422,14 @@ static_assert(sizeof(StageDesc) == 32, "stage descriptor is 32 bytes");
 constexpr int kStageHdrOff = 32;
 __device__ __forceinline__ StageDesc* stage_desc(unsigned char* stage) { return (StageDesc*)(stage); }
 __device__ __forceinline__ unsigned char* stage_hdr(unsigned char* stage) { return stage + kStageHdrOff; }
-__device__ __forceinline__ float* stage_stream(unsigned char* stage, int hcap, int k) {
-  return (float*)(stage + hcap + k * kStreamBytes);
+__device__ __forceinline__ float* stage_stream(unsigned char* stage, int hcap, int sfl, int k) {
+  return (float*)(stage + hcap + k * 4 * sfl);
 }
 
 struct Pipe {
   unsigned char* stage[2];
   int hcap;          // bytes before the streams of a stage (BatchArgs::hdr_cap)
+  int sfl;           // floats per stream (BatchArgs::stream_floats)
   uint64_t* full;    // [2]
   uint64_t* empty;   // [2]
   int* list;         // tiles of this CTA for the current phase
@@ -527,20 +528,20 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   if (PH == 0) {
     const float* pold = par ? a.pb32 : a.pa32;
     const float* S = (QP == 2) ? a.s32 : a.r32;
-    bulk_g2s(stage_stream(st, P.hcap, 0), pold + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, P.hcap, 1), S + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, P.hcap, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 0), pold + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 1), S + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
     for (int f = 0; f < a.F; ++f)
-      bulk_g2s(stage_stream(st, P.hcap, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
-    if (xa) bulk_g2s(stage_stream(st, P.hcap, 3 + a.F), a.x32 + d.base, 4 * n4, &P.full[b]);
+      bulk_g2s(stage_stream(st, P.hcap, P.sfl, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
+    if (xa) bulk_g2s(stage_stream(st, P.hcap, P.sfl, 3 + a.F), a.x32 + d.base, 4 * n4, &P.full[b]);
   } else {
     if (!xa) {
       const float* p = par ? a.pb32 : a.pa32;  // the direction written by phase A
-      bulk_g2s(stage_stream(st, P.hcap, 0), p + d.base, 4 * n4, &P.full[b]);
-      bulk_g2s(stage_stream(st, P.hcap, 1), a.x32 + d.base, 4 * n4, &P.full[b]);
+      bulk_g2s(stage_stream(st, P.hcap, P.sfl, 0), p + d.base, 4 * n4, &P.full[b]);
+      bulk_g2s(stage_stream(st, P.hcap, P.sfl, 1), a.x32 + d.base, 4 * n4, &P.full[b]);
     }
-    bulk_g2s(stage_stream(st, P.hcap, 2), a.z32 + d.base, 4 * n4, &P.full[b]);
-    bulk_g2s(stage_stream(st, P.hcap, 3), a.r32 + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 2), a.z32 + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 3), a.r32 + d.base, 4 * n4, &P.full[b]);
   }
   P.seq = q + 1;
 }
@@ -565,7 +566,7 @@ __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char
       if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
       const int n = fns[c * F + f] + k;
       const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      y = __fmaf_rn(sf[f * kStreamFloats + s], pn, y);  // staged face weight stream f
+      y = __fmaf_rn(sf[f * a.stream_floats + s], pn, y);  // staged face weight stream f
     }
     if (k > ctop) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
     if (k < nk - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
@@ -576,7 +577,7 @@ __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char
       if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
       const int n = fns[c * F + f] + k;
       const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      y = __fmaf_rn(pn - pu, sf[f * kStreamFloats + s], y);  // staged dzf*D of the edge level
+      y = __fmaf_rn(pn - pu, sf[f * a.stream_floats + s], y);  // staged dzf*D of the edge level
     }
     const float c0 = sc[s];
     if (ctop < nk - 1) {
@@ -653,9 +654,9 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
       const int n = ok ? fns[e] + kv[q] : base + sv[q];
       pn[q][f] = __fmaf_rn(mu, pold[n], S[n]);
       if (QP == 1) {
-        wn[q][f] = sf[f * kStreamFloats + sv[q]];  // staged face weight (0 where the face does not couple)
+        wn[q][f] = sf[f * a.stream_floats + sv[q]];  // staged face weight (0 where the face does not couple)
       } else {
-        wn[q][f] = sf[f * kStreamFloats + sv[q]];  // staged dzf*D of the edge level (0 likewise)
+        wn[q][f] = sf[f * a.stream_floats + sv[q]];  // staged dzf*D of the edge level (0 likewise)
       }
     }
   }
@@ -775,10 +776,10 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       const HdrLayout L = hdr_layout(ncols, a.F, len);
       const unsigned short* start = (const unsigned short*)(hd + L.o_start);
       const int* cn = (const int*)(hd + L.o_cn);
-      const float* sp = stage_stream(st, P.hcap, 0);
-      const float* sS = stage_stream(st, P.hcap, 1);
-      const float* sc = stage_stream(st, P.hcap, 2);
-      const float* sf = stage_stream(st, P.hcap, 3);
+      const float* sp = stage_stream(st, P.hcap, P.sfl, 0);
+      const float* sS = stage_stream(st, P.hcap, P.sfl, 1);
+      const float* sc = stage_stream(st, P.hcap, P.sfl, 2);
+      const float* sf = stage_stream(st, P.hcap, P.sfl, 3);
       const float* pold = sd.par ? a.pb32 : a.pa32;
       float* pnew = sd.par ? a.pa32 : a.pb32;
       const float* S = (QP == 2) ? a.s32 : a.r32;
@@ -788,7 +789,7 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         // consecutive slots per thread (padding slots hold zeros in every stream)
         const int s0 = 4 * (int)threadIdx.x;
         if (nu != 0.f && s0 < len) {
-          const float* sx = stage_stream(st, P.hcap, 3 + a.F);
+          const float* sx = stage_stream(st, P.hcap, P.sfl, 3 + a.F);
           const float4 p4 = *(const float4*)(sp + s0);
           const float4 x4 = *(const float4*)(sx + s0);
           *(float4*)(a.x32 + base + s0) = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y),
@@ -831,8 +832,8 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         df_addprod(dacc0, pv[qq], yv[qq]);
       }
     } else {
-      const float* sz = stage_stream(st, P.hcap, 2);
-      float* sr = stage_stream(st, P.hcap, 3);
+      const float* sz = stage_stream(st, P.hcap, P.sfl, 2);
+      float* sr = stage_stream(st, P.hcap, P.sfl, 3);
       {
         // 4 consecutive slots per thread: float4 in shared memory and global
         // (padding slots hold zeros in every stream and stay zero).  The
@@ -841,8 +842,8 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         const int s0 = 4 * (int)threadIdx.x;
         if (s0 < len) {
           if (!a.x_in_apply) {
-            const float4 p4 = *(const float4*)(stage_stream(st, P.hcap, 0) + s0);
-            const float4 x4 = *(const float4*)(stage_stream(st, P.hcap, 1) + s0);
+            const float4 p4 = *(const float4*)(stage_stream(st, P.hcap, P.sfl, 0) + s0);
+            const float4 x4 = *(const float4*)(stage_stream(st, P.hcap, P.sfl, 1) + s0);
             *(float4*)(a.x32 + base + s0) = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y),
                                                         __fmaf_rn(nu, p4.z, x4.z), __fmaf_rn(nu, p4.w, x4.w));
           }
@@ -866,9 +867,9 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         // streams of the stage are no longer needed, so they are refilled
         // (coalesced) with the Thomas factors tw, tib and the coefficients.
         csync();
-        float* stw = stage_stream(st, P.hcap, 0);
-        float* stib = stage_stream(st, P.hcap, 1);
-        float* scf = stage_stream(st, P.hcap, 2);
+        float* stw = stage_stream(st, P.hcap, P.sfl, 0);
+        float* stib = stage_stream(st, P.hcap, P.sfl, 1);
+        float* scf = stage_stream(st, P.hcap, P.sfl, 2);
         const int n4 = (len + 3) & ~3;
         for (int s = threadIdx.x; s < n4 + 4; s += kCompute) {
           if (s < n4) {
@@ -1001,6 +1002,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
 
   Pipe P;
   P.hcap = a.hdr_cap;
+  P.sfl = a.stream_floats;
   P.stage[0] = dyn;
   P.stage[1] = dyn + a.stage_bytes;
   P.full = (uint64_t*)(dyn + 2 * a.stage_bytes);
@@ -1987,7 +1989,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     if (key[x] != key[y]) return key[x] > key[y];
     return b->inst[x].unk > b->inst[y].unk;
   });
-  int max_hdr = 0;
+  int max_hdr = 0, max_slots = 0;
   for (int i : order) {
     HostInst& H = b->inst[i];
     BInst& I = b->h_inst[i];
@@ -2001,6 +2003,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
       d.hdr = nb;
       d.hdr_bytes = T.hdr_bytes;
       max_hdr = std::max(max_hdr, T.hdr_bytes);
+      max_slots = std::max(max_slots, T.nslots);
       d.base = base;
       d.nslots = T.nslots;
       d.inst = i;
@@ -2027,7 +2030,11 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
   // room for three CTAs per SM with the apply phase's 4 + F streams
   const int hdr_cap = std::min(kHdrCap, (kStageHdrOff + max_hdr + 127) & ~127);
   const int streams = b->x_in_apply ? b->streams : std::max(b->streams - 1, 4);
-  const int stage_bytes = std::max(stage_bytes_for(hdr_cap, streams), (int)((sizeof(TileSmem) + 127) & ~127));
+  // streams sized to the launch's largest tile (+1 group of 4: the vertical
+  // coefficient stream reads one slot past the tile)
+  const int stream_floats = std::min(kStreamFloats, ((max_slots + 3) & ~3) + 4);
+  const int stage_bytes =
+      std::max(hdr_cap + streams * 4 * stream_floats, (int)((sizeof(TileSmem) + 127) & ~127));
   b->dyn_smem = dyn_smem_bytes_for(stage_bytes);
   int maxg = batch_max_grid(b);
   if (maxg <= 0) return bfail(b, SGPU_CUDA_ERROR, "occupancy query failed");
@@ -2062,6 +2069,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     a.F = b->F;
     a.stage_bytes = stage_bytes;
     a.hdr_cap = hdr_cap;
+    a.stream_floats = stream_floats;
     a.x_in_apply = b->x_in_apply;
     a.ntiles = ntiles;
     a.ninst = ninst;

@@ -121,6 +121,7 @@ struct BatchArgs {
   int F;
   int stage_bytes;     // bytes of one pipeline stage: hdr_cap + streams * kStreamBytes
   int hdr_cap;         // bytes before a stage's streams: descriptor + the launch's largest header
+  int stream_floats;   // floats per stage stream: the launch's largest tile + 4
   int x_in_apply;      // 1: the solution update x32 += nu p runs in the next apply pass, where
                        // p is streamed anyway; 0: in the update pass (streams p and x there)
   int ntiles;

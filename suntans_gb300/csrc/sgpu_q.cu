@@ -26,6 +26,17 @@
 #include "sgpu_common.cuh"
 #include "sgpu_q.h"
 
+// unroll factor of the flat apply loop (slots of one thread in flight together)
+#ifndef SGPU_Q_UNROLL
+#define SGPU_Q_UNROLL 1
+#endif
+#define SGPU_Q_PRAGMA(x) _Pragma(#x)
+#define SGPU_Q_UNROLL_N(n) SGPU_Q_PRAGMA(unroll n)
+#define SGPU_Q_APPLY_UNROLL SGPU_Q_UNROLL_N(SGPU_Q_UNROLL)
+#ifndef SGPU_Q_MINB
+#define SGPU_Q_MINB 6
+#endif
+
 namespace sgpu {
 
 struct TileCtx {
@@ -222,7 +233,7 @@ __device__ __forceinline__ void column_factor(const QArgs& a, int off, int ctop,
 // the persistent kernel
 // ---------------------------------------------------------------------------
 template <int QP>
-__global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
+__global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) {
   __shared__ int s_start[kMaxTileCols + 1];
   __shared__ double s_red[4 * (kBlock / 32)];
   __shared__ TriSmem s_tri;
@@ -440,14 +451,14 @@ __global__ void __launch_bounds__(kBlock) cgsolveq_kernel(QArgs a) {
       double part[1] = {0.0};
       const int T = G * kBlock;
       if (F == 3) {
-#pragma unroll 4
+SGPU_Q_APPLY_UNROLL
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
           const double zu = apply_flat<QP, 3>(a, a.p, u);
           a.z[u] = zu;
           part[0] += a.p[u] * zu;
         }
       } else if (F == 4) {
-#pragma unroll 4
+SGPU_Q_APPLY_UNROLL
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
           const double zu = apply_flat<QP, 4>(a, a.p, u);
           a.z[u] = zu;
