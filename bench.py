@@ -12,7 +12,9 @@ Workloads (--workload):
         (hprecond 1), each to a 1e-10 relative residual, in FP64.  The line
         also carries "mixed_form": the same pressure problem through the
         mixed-precision batched solver (one instance), against the FP64 solve.
-  cfg1  the 64x16 quad channel (1024 cells, Nkmax 32), FP64.
+  cfg1  the 64x16 lock-exchange channel (1024 quad cells, Nkmax 32): every
+        solve of the reference model's own 10-step run, re-run through the C
+        ABI; latency per solve and parity with the reference's solutions.
   cfg3  mixed precision at 1M triangles (500k points, 50 km x 25 km, Nkmax 40,
         ~4e7 unknowns): one pressure solve per step; errors against the FP64
         GPU solve of the same problem (itself matched to the oracle).
@@ -122,12 +124,15 @@ def make_workload(args):
     from suntans_gb300 import gridgen as gg
     from suntans_gb300.grid import SolverProps
     if args.workload == "cfg1":
-        g = gg.quad_channel(64, 16, dx=10.0, dy=10.0, depth=20.0, Nkmax=32, h_sigma=1e-3, seed=1)
-        qp = gg.make_q_problem(g, seed=11, sigma_u=0.01, dt=1.0)
-        hp = gg.make_h_problem(g, seed=12)
-        props = SolverProps(qprecond=args.qprecond, qmaxiters=1000, qepsilon=1e-10, hprecond=1,
-                            maxiters=1000, epsilon=1e-10, resnorm=1.0, dt=1.0, theta=0.55)
-        desc = {"workload": "quad channel 64x16 cells (dx=dy=10 m), flat 20 m, Nkmax=32, lock-exchange config",
+        # the solves of step 10 of the reference model's own 10-step lock-exchange run
+        from tests._golden import load_lockexchange
+        d, props, grid_at, q_problem, h_problem = load_lockexchange()
+        qp, _, _ = q_problem(10)
+        hp, _, _ = h_problem(10)
+        g = qp.grid
+        hp.grid = g
+        desc = {"workload": "lock-exchange channel 64x16 quad cells (dx=dy=10 m), flat 20 m, Nkmax=32: the "
+                            "CGSolveQ/CGSolve inputs of step 10 of the reference model's own 10-step run",
                 "cells": g.Nc, "Nkmax": 32}
     else:
         g = gg.delaunay_seamount(args.points, 20_000.0, 10_000.0, Nkmax=50, rstretch=1.02, seed=1,
@@ -778,6 +783,86 @@ def make_cfg3(points: int, qprecond: int):
     return g, qp, _props(qprecond), scale
 
 
+def bench_cfg1(args):
+    """The 64 x 16 lock-exchange channel: every solve the reference model made
+    in its own 10-step run (tests/golden/runs/lockexchange_cfg1.npz: the
+    pressure solves of steps 1, 5 and 10, the free-surface solves of all ten),
+    re-run through the drop-in C ABI.  The working set (~4 MB) lives in L2, so
+    the figure is the latency per solve, beside the parity with the
+    reference's own solutions."""
+    import torch
+    from oracle.oracle import Oracle
+    from suntans_gb300.capi import Context
+    from tests._golden import load_lockexchange
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    d, props, grid_at, q_problem, h_problem = load_lockexchange()
+    rows = {"q": [], "h": []}
+    sampler = ClockSampler(local)
+    sampler.start()
+    for kind, steps, make in (("q", d["q_steps"], q_problem), ("h", d["h_steps"], h_problem)):
+        for s in steps:
+            p, ref, n_ref = make(int(s))
+            g = p.grid
+            ctx = Context(g, device=local)
+            if kind == "q":
+                ctx.q_upload(p)
+                dev = [ctx.q_solve(props) for _ in range(max(args.warmup, 1) + args.steps)][max(args.warmup, 1):]
+                t0 = time.perf_counter()
+                x, st = ctx.cgsolveq(p, props)
+                e2e = time.perf_counter() - t0
+                m = g.active_mask()
+            else:
+                ctx.h_upload(p)
+                dev = [ctx.h_solve(props) for _ in range(max(args.warmup, 1) + args.steps)][max(args.warmup, 1):]
+                t0 = time.perf_counter()
+                x, st = ctx.cgsolve(p, props)
+                e2e = time.perf_counter() - t0
+                m = np.zeros(g.Nc, dtype=bool)
+                m[g.comp_cells()] = True
+            ctx.close()
+            err = float(np.linalg.norm((x - ref)[m]) / np.linalg.norm(ref[m]))
+            rows[kind].append({"step": int(s), "ms_device": float(np.median([v.ms_solve for v in dev])),
+                               "ms_e2e": e2e * 1e3, "iters": int(st.niters), "iters_reference": n_ref,
+                               "rel_l2_vs_reference": err, "unknowns": int(st.unknowns)})
+    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    work = sum(r["unknowns"] * r["iters"] for k in rows for r in rows[k])
+    t_dev = sum(r["ms_device"] for k in rows for r in rows[k]) / 1e3
+    t_e2e = sum(r["ms_e2e"] for k in rows for r in rows[k]) / 1e3
+    line = {"metric": "Poisson CG latency per solve (CGSolveQ, CGSolve) on the reference run's own solves, "
+                      "1e-10 relative residual",
+            "value": work / t_dev, "unit": "unknown-iters/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 1), "ms_per_step": t_dev * 1e3 / len(rows["q"] + rows["h"]),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "the reference model's own solver inputs (lock-exchange run)",
+            "config": {"workload": "lock-exchange channel 64x16 quad cells (dx=dy=10 m), flat 20 m, Nkmax=32, "
+                                   "10 nonhydrostatic steps of the reference model (dt 1 s); qprecond 1, hprecond 1",
+                       "l2": "working set ~4 MB, L2-resident: latency, not %HBM"},
+            "cgsolveq": {"ms_device_p50": float(np.median([r["ms_device"] for r in rows["q"]])),
+                         "ms_e2e_p50": float(np.median([r["ms_e2e"] for r in rows["q"]])), "solves": rows["q"]},
+            "cgsolve": {"ms_device_p50": float(np.median([r["ms_device"] for r in rows["h"]])),
+                        "ms_e2e_p50": float(np.median([r["ms_e2e"] for r in rows["h"]])), "solves": rows["h"]},
+            "max_rel_l2_vs_reference": max(r["rel_l2_vs_reference"] for k in rows for r in rows[k]),
+            "e2e": {"value": work / t_e2e, "unit": "unknown-iters/s",
+                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+            "gpu_launches": len(rows["q"] + rows["h"]) * (args.steps + 1), "clocks": clocks}
+    if not args.no_cpu_baseline:
+        o = Oracle("port")
+        t, w = 0.0, 0
+        for s in d["q_steps"]:
+            p, _, _ = q_problem(int(s))
+            _, n, _, tl = o.cgsolveq_timed(p, props)
+            t, w = t + tl, w + p.grid.n_q() * n
+        for s in d["h_steps"]:
+            p, _, _ = h_problem(int(s))
+            _, n, _, tl = o.cgsolve_timed(p, props)
+            t, w = t + tl, w + p.grid.n_h() * n
+        line["cpu_baseline"] = {"value": w / t, "unit": "unknown-iters/s", "cores": 1, "kind": "port",
+                                "sample": "the oracle (bit-identical to the reference's solvers) on the same solves, "
+                                          f"iteration loops timed, {t:.2f} s", **host_cpu()}
+    return line
+
+
 def bench_cfg3(args, keep=None):
     from suntans_gb300.batch import Batch, capacity_for
     from suntans_gb300.capi import Context
@@ -1164,12 +1249,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload in ("cfg3", "cfg4", "cfg5", "step", "upred"):
+    elif args.workload in ("cfg1", "cfg3", "cfg4", "cfg5", "step", "upred"):
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         import __graft_entry__
         __graft_entry__.build()
-        fn = {"cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5, "step": bench_step,
+        fn = {"cfg1": bench_cfg1, "cfg3": bench_cfg3, "cfg4": bench_cfg4, "cfg5": bench_cfg5, "step": bench_step,
               "upred": bench_upred}[args.workload]
         line = fn(args)
         if int(os.environ.get("RANK", "0")) == 0:

@@ -85,3 +85,38 @@ def wpred_fields(g, d, tag):
 
 def props_for(props, **kw):
     return SolverProps(**{**props, **kw})
+
+
+LOCKX = os.path.join(HERE, "runs", "lockexchange_cfg1.npz")
+
+
+def load_lockexchange():
+    """The 64 x 16 lock-exchange channel's solver fixture (make_lockexchange_golden.py):
+    returns (d, props, grid_at, q_problem, h_problem) where grid_at(step)
+    builds the solver grid with that step's ctop/dzz/dzf and the problem
+    builders return (problem, reference solution, reference iterations)."""
+    d = dict(np.load(LOCKX))
+    Nc, Ne, mf, Nkmax = (int(v) for v in d["sizes"])
+    pv = d["props"]
+    props = SolverProps(qprecond=int(pv[9]), qmaxiters=int(pv[7]), qepsilon=float(pv[4]), hprecond=int(pv[8]),
+                        maxiters=int(pv[6]), epsilon=float(pv[3]), resnorm=float(pv[5]), grav=float(pv[2]),
+                        theta=float(pv[1]), dt=float(pv[0]))
+    base = {k: d[k] for k in ("nfaces", "neigh", "face", "Nk", "Nke", "cellp", "celldist", "Ac", "df", "dg")}
+    first_q = int(d["q_steps"][0])
+
+    def grid_at(step):
+        qs = step if f"q{step}_ctop" in d else first_q
+        return SunGrid(Nc=Nc, Ne=Ne, maxfaces=mf, Nkmax=Nkmax, ctop=d[f"q{qs}_ctop"], dzz=d[f"q{qs}_dzz"],
+                       dzf=d[f"q{qs}_dzf"], name=f"lockexchange_step{step}", **base)
+
+    def q_problem(step):
+        g = grid_at(step)
+        p = QProblem(grid=g, D=d[f"q{step}_D"], src=d[f"q{step}_src"], q=d[f"q{step}_q_in"], c=np.ones(g.n3))
+        return p, d[f"q{step}_q_out"], int(d[f"q{step}_niters"][0])
+
+    def h_problem(step):
+        g = grid_at(step)
+        p = HProblem(grid=g, D=d[f"h{step}_D"], htmp=d[f"h{step}_htmp"], h=d[f"h{step}_h_in"])
+        return p, d[f"h{step}_h_out"], int(d[f"h{step}_niters"][0])
+
+    return d, props, grid_at, q_problem, h_problem

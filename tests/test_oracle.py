@@ -323,3 +323,21 @@ def test_summation_order_moves_iterations_not_solution(port):
         port.lib.sgo_set_sum_order(0)
     assert n == n_pair
     assert rel_l2(q, d["q_qp2"], g.active_mask()) <= 1e-9
+
+
+def test_port_matches_lockexchange_run_bitwise(port):
+    """The lock-exchange channel fixture records the reference model's own
+    solves over a 10-step nonhydrostatic run (make_lockexchange_golden.py):
+    the port, given each solve's recorded inputs, returns the reference's
+    solution bit for bit with its iteration count."""
+    from tests._golden import load_lockexchange
+    d, props, grid_at, q_problem, h_problem = load_lockexchange()
+    assert list(d["q_steps"]) == [1, 5, 10] and list(d["h_steps"]) == list(range(1, 11))
+    for s in d["q_steps"]:
+        p, ref, n = q_problem(int(s))
+        q, nq = port.cgsolveq(p, props)
+        assert nq == n and np.array_equal(q, ref)
+    for s in d["h_steps"]:
+        p, ref, n = h_problem(int(s))
+        h, nh = port.cgsolve(p, props)
+        assert nh == n and np.array_equal(h, ref)
