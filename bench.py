@@ -76,7 +76,7 @@ def q_bytes_per_unknown_iter(qprecond: int, F: int) -> int:
 # cases of the same constructions; a launch's traffic grows in proportion to
 # unknowns × iterations, so `traffic` below scales these to the launch timed.
 # profiles/cgsolveq_kernel_fp64_seamount50k.md, profiles/batch_kernel_mixed_seamount250k.md
-MEASURED_TRAFFIC_PER_UNKNOWN_ITER = {"cgsolveq_kernel<1>": 110.7, "batch_kernel<1>": 60.6}
+MEASURED_TRAFFIC_PER_UNKNOWN_ITER = {"cgsolveq_kernel<1>": 110.7, "batch_kernel<1>": 55.3}
 
 
 def h_bytes_per_unknown_iter(F: int) -> int:
