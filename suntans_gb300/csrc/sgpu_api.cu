@@ -521,7 +521,15 @@ int sgpu_q_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   DeviceGuard dg(ctx->device);
   int maxg = q_max_grid(prop->qprecond, ctx->device);
   if (maxg <= 0) return fail(ctx, SGPU_CUDA_ERROR, "occupancy query failed");
-  int grid = ctx->grid_override > 0 ? std::min(ctx->grid_override, maxg) : maxg;
+  // a full wave for large problems; small ones (a few hundred thousand
+  // unknowns) take fewer CTAs -- at least one per SM, at least 8 slots per
+  // thread -- since their iterations are bound by the grid barriers, whose
+  // cost grows with the CTAs arriving
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const long long want = (ctx->n3c + 8LL * kBlock - 1) / (8LL * kBlock);
+  int grid = ctx->grid_override > 0 ? std::min(ctx->grid_override, maxg)
+                                    : (int)std::min<long long>(maxg, std::max<long long>(sms, want));
   int rc = ensure_partials(ctx, grid);
   if (rc) return rc;
   QLaunch L;
