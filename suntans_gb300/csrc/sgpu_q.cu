@@ -235,12 +235,21 @@ __device__ __forceinline__ void column_factor(const QArgs& a, int off, int ctop,
 template <int QP>
 __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) {
   __shared__ int s_start[kMaxTileCols + 1];
-  __shared__ double s_red[4 * (kBlock / 32)];
+  __shared__ double s_red[2 * kBlock + 2];
+  __shared__ double s_sc[4];  // scalars from thread 0: mu, nu, done
   __shared__ TriSmem s_tri;
   SolveCtl* ctl = a.ctl;
   const int G = gridDim.x;
   const int F = a.F;
   const int tid = threadIdx.x;
+  // Barriers: arrive-and-wait on a monotonic counter; after each, one warp of
+  // every CTA sums the published per-CTA partials in the same order and
+  // thread 0 runs the scalar recurrences (identical in every CTA), leaving
+  // mu, nu and the loop flag in shared memory.  Partials rotate between two
+  // buffers so that no CTA overwrites a set another is still reading.
+  unsigned int nbar = 0;
+  double* partA = a.partials;          // [2][G]: p.z
+  double* partB = a.partials + 2 * G;  // [2][2][G]: r.r or r.s, r.r
 
   // ---- S1: working vectors, face metadata, coefficients / conditioner ----
   for (int t = blockIdx.x; t < a.ntiles; t += G) {
@@ -337,7 +346,7 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
     a.p[u] = a.src_in[u];
     if (QP == 1) a.c[u] = a.c_in[u];
   }
-  if (!grid_sync(ctl, 1, [] {})) return;
+  if (!grid_wait(ctl, ++nbar * G, 1)) return;
 
   // ---- S2 (qprecond 1): scaled coefficients (QCoefficients 3427-3452) ----
   if (QP == 1) {
@@ -366,10 +375,13 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
       }
       __syncthreads();
     }
-    if (!grid_sync(ctl, 2, [] {})) return;
+    if (!grid_wait(ctl, ++nbar * G, 2)) return;
   }
 
   // ---- S3: z = A x; r = p - z; p = r or M^-1 r; alpha0, eps0 (2444-2475) ----
+  // thread 0 of every CTA keeps the scalar state (the same in every CTA)
+  double alpha = 0.0, eps = 0.0, eps0 = 0.0, mu_t = 0.0;
+  int status = SGPU_OK;
   {
     double part[2] = {0.0, 0.0};
     for (int t = blockIdx.x; t < a.ntiles; t += G) {
@@ -408,31 +420,22 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
       }
       __syncthreads();
     }
-    block_sum<2>(part, s_red);
+    cta_sum<2, kBlock>(part, s_red);
     if (tid == 0) {
-      a.partials[blockIdx.x] = part[0];
-      a.partials[G + blockIdx.x] = part[1];
+      partB[2 * G + blockIdx.x] = part[0];
+      partB[3 * G + blockIdx.x] = part[1];
     }
-    const double resnorm = a.resnorm;
-    if (!grid_sync(ctl, 3, [&] {
-          double tot[2];
-          reduce_partials<2>(a.partials, G, G, tot, s_red);
-          if (tid == 0) {
-            double alpha = tot[0], alpha0 = tot[0];
-            if (!resnorm) alpha0 = 1;
-            double eps, eps0;
-            if (QP == 2) eps = eps0 = tot[1];
-            else eps = eps0 = alpha0;
-            ctl->alpha = alpha;
-            ctl->alpha0 = alpha0;
-            ctl->eps = eps;
-            ctl->eps0 = eps0;
-            ctl->n = 0;
-            ctl->done = (a.maxiters <= 0 || eps == 0) ? 1 : 0;
-            __threadfence();
-          }
-        }))
-      return;
+    if (!grid_wait(ctl, ++nbar * G, 3)) return;
+    grid_sum<2>(partB + 2 * G, G, [&](const double* tot) {
+      alpha = tot[0];
+      double alpha0 = tot[0];
+      if (!a.resnorm) alpha0 = 1;
+      if (QP == 2) eps = eps0 = tot[1];
+      else eps = eps0 = alpha0;
+      s_sc[0] = 0.0;
+      s_sc[1] = 0.0;
+      s_sc[2] = (a.maxiters <= 0 || eps == 0) ? 1.0 : 0.0;
+    });
   }
 
   // ---- the CG loop (2478-2525) ----
@@ -441,8 +444,9 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
   // write of p fewer per iteration.  When the loop ends after B, the last one
   // is still pending and is done at the end.
   bool x_pending = false;
+  int n = 0;
   for (;;) {
-    if (ld_volatile_int(&ctl->done)) break;
+    if (s_sc[2] != 0.0) break;
     // A: z = A p, p.z -- flat over the computational storage: slot u of
     // thread g is u = g + i*T (T = all threads), its column from the static
     // slot-to-column index, so no tile barrier or column search stands between
@@ -471,29 +475,23 @@ SGPU_Q_APPLY_UNROLL
           part[0] += a.p[u] * zu;
         }
       }
-      block_sum<1>(part, s_red);
-      if (tid == 0) a.partials[blockIdx.x] = part[0];
-      if (!grid_sync(ctl, 4, [&] {
-            double tot[1];
-            reduce_partials<1>(a.partials, G, G, tot, s_red);
-            if (tid == 0) {
-              const double alpha = *(volatile double*)&ctl->alpha;
-              ctl->mu = 1 / alpha;
-              const double nu = alpha / tot[0];
-              ctl->nu = nu;
-              if (!isfinite(nu)) {
-                ctl->status = SGPU_BREAKDOWN;
-                ctl->done = 1;
-              }
-              __threadfence();
-            }
-          }))
-        return;
-      if (ld_volatile_int(&ctl->done)) break;
+      cta_sum<1, kBlock>(part, s_red);
+      if (tid == 0) partA[(n & 1) * G + blockIdx.x] = part[0];
+      if (!grid_wait(ctl, ++nbar * G, 4)) return;
+      grid_sum<1>(partA + (n & 1) * G, G, [&](const double* tot) {
+        mu_t = 1 / alpha;
+        const double nu = alpha / tot[0];
+        s_sc[1] = nu;
+        if (!isfinite(nu)) {
+          status = SGPU_BREAKDOWN;
+          s_sc[2] = 1.0;
+        }
+      });
+      if (s_sc[2] != 0.0) break;
     }
-    // B: x += nu p; r -= nu z; [rt = M^-1 r]; alpha, eps
+    // B: r -= nu z; [rt = M^-1 r]; alpha, eps
     {
-      const double nu = *(volatile double*)&ctl->nu;
+      const double nu = s_sc[1];
       double part[2] = {0.0, 0.0};
       if (QP != 2) {
         const int T = G * kBlock;
@@ -535,48 +533,38 @@ SGPU_Q_APPLY_UNROLL
         }
         __syncthreads();
       }
-      block_sum<2>(part, s_red);
+      cta_sum<2, kBlock>(part, s_red);
       if (tid == 0) {
-        a.partials[blockIdx.x] = part[0];
-        a.partials[G + blockIdx.x] = part[1];
+        partB[(size_t)(n & 1) * 2 * G + blockIdx.x] = part[0];
+        partB[(size_t)(n & 1) * 2 * G + G + blockIdx.x] = part[1];
       }
-      const double qeps = a.qepsilon;
-      const int maxit = a.maxiters;
-      if (!grid_sync(ctl, 5, [&] {
-            double tot[2];
-            reduce_partials<2>(a.partials, G, G, tot, s_red);
-            if (tid == 0) {
-              const double alpha = tot[0];
-              double mu = *(volatile double*)&ctl->mu;
-              mu *= alpha;
-              ctl->mu = mu;
-              ctl->alpha = alpha;
-              const double eps = (QP == 2) ? tot[1] : alpha;
-              ctl->eps = eps;
-              const int n = ctl->n + 1;
-              ctl->n = n;
-              const double eps0 = ctl->eps0;
-              int done = 0;
-              if (sqrt(eps / eps0) < qeps) done = 1;
-              else if (n >= maxit || eps == 0) done = 1;
-              if (!isfinite(alpha)) {
-                ctl->status = SGPU_BREAKDOWN;
-                done = 1;
-              }
-              if (done && n >= maxit && !(sqrt(eps / eps0) < qeps) && ctl->status == SGPU_OK)
-                ctl->status = SGPU_MAXITER;
-              ctl->done = done;
-              __threadfence();
-            }
-          }))
-        return;
+      if (!grid_wait(ctl, ++nbar * G, 5)) return;
+      grid_sum<2>(partB + (size_t)(n & 1) * 2 * G, G, [&](const double* tot) {
+        alpha = tot[0];
+        mu_t *= alpha;
+        s_sc[0] = mu_t;
+        eps = (QP == 2) ? tot[1] : alpha;
+        const bool conv = sqrt(eps / eps0) < a.qepsilon;
+        double done = 0.0;
+        if (conv || eps == 0) done = 1.0;
+        else if (n + 1 >= a.maxiters) {
+          status = SGPU_MAXITER;
+          done = 1.0;
+        }
+        if (!isfinite(alpha)) {
+          status = SGPU_BREAKDOWN;
+          done = 1.0;
+        }
+        s_sc[2] = done;
+      });
       x_pending = true;
-      if (ld_volatile_int(&ctl->done)) break;
+      ++n;
+      if (s_sc[2] != 0.0) break;
     }
     // C: x += nu p; p = r + mu p  (or rt + mu p)
     {
-      const double mu = *(volatile double*)&ctl->mu;
-      const double nu = *(volatile double*)&ctl->nu;
+      const double mu = s_sc[0];
+      const double nu = s_sc[1];
       const double* src = (QP == 2) ? a.rt : a.r;
       const int T = G * kBlock;
 #pragma unroll 4
@@ -586,10 +574,20 @@ SGPU_Q_APPLY_UNROLL
         a.p[u] = src[u] + mu * pu;
       }
       x_pending = false;
-      if (!grid_sync(ctl, 6, [] {})) return;
+      if (!grid_wait(ctl, ++nbar * G, 6)) return;
     }
   }
-  const double nu_last = *(volatile double*)&ctl->nu;
+  const double nu_last = s_sc[1];
+  if (blockIdx.x == 0 && tid == 0) {
+    ctl->alpha = alpha;
+    ctl->eps = eps;
+    ctl->eps0 = eps0;
+    ctl->mu = mu_t;
+    ctl->nu = nu_last;
+    ctl->n = n;
+    if (status != SGPU_OK) atomicCAS(&ctl->status, SGPU_OK, status);
+    ctl->done = 1;
+  }
 
   // ---- the pending x update, and the rescale (2539-2546), each slot by one thread ----
   if (QP == 1) {
