@@ -106,6 +106,11 @@ def parse():
     ap.add_argument("--pool", type=int, default=64)
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--chunk", type=int, default=32)
+    ap.add_argument("--sustain-rate", type=float, default=None,
+                    help="cfg5: rate of the second (unsaturated) stream (default: half the served rate)")
+    ap.add_argument("--copies", type=int, default=2,
+                    help="cfg5: resident copies a hot grid may have (1: one request per grid at a time, "
+                         "results bit-identical alone and in the mix)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--graph", action="store_true",
                     help="cfg5: replay launches from CUDA graphs (re-captured whenever the set of problems changes)")
@@ -1030,10 +1035,11 @@ def bench_cfg5(args):
     pool = gg.serving_pool(n=args.pool, seed=5, workers=None)
     grids = [p[0].grid for p in pool]
     need = sum(request_bytes(g, args.qprecond) for g in grids)
-    b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
+    b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local,
+              **capacity_for(grids * args.copies))
     b.use_graph(args.graph)
     srv = Server(pool, b, args.budget_gb * 1e9, lambda g: request_bytes(g, args.qprecond), chunk=args.chunk,
-                 maxiters=5000, keep_q=False)
+                 maxiters=5000, keep_q=False, copies=args.copies)
     # warm-up: one untimed request per grid (cold starts; every grid resident)
     srv.run([Request(-1 - k, k, 0, 1e-8, 0.0) for k in range(len(pool))], realtime=False)
     warm_launches = srv.launches
@@ -1060,7 +1066,7 @@ def bench_cfg5(args):
     # again at a rate the measured capacity sustains (latency without a growing queue)
     # (the saturated run completes the cheaper requests first, so its served rate
     # overstates what the stream can sustain; half of it keeps the queue bounded)
-    sus_rate = max(1.0, 0.5 * rep["served_per_s"])
+    sus_rate = getattr(args, "sustain_rate", None) or max(1.0, 0.5 * rep["served_per_s"])
     sus_s = getattr(args, "sustain_seconds", None) or max(10.0, 200.0 / sus_rate)
     rep2, _, _ = stream(sus_rate, sus_s, 8)
     b.close()
@@ -1075,7 +1081,7 @@ def bench_cfg5(args):
                                    f"{len(pool[0])} right-hand sides mixed per request, tolerance from "
                                    "{1e-8, 1e-10}, warm starts",
                        "hbm_budget_gb": args.budget_gb, "pool_resident_gb": need / 1e9, "chunk_iters": args.chunk,
-                       "qprecond": args.qprecond, "step": "one launch of the serving loop",
+                       "qprecond": args.qprecond, "step": "one launch of the serving loop", "copies": args.copies,
                        "drain_limit_s": args.drain_seconds, "graph": args.graph},
             "latency": rep, "latency_at_sustainable_rate": rep2, "evictions": srv.evictions,
             "e2e": {"value": rep["unknown_iters_per_s"], "unit": "unknown-iters/s",

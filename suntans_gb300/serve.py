@@ -54,6 +54,8 @@ class Request:
     unknowns: int = 0
     launch_done: int = -1  # serving-loop launch after which the result was harvested
     warm: bool = False     # started from the grid's resident previous solution
+    copy: int = -1         # the resident copy of the grid that served it
+    warm_from: int = -1    # rid of the request whose solution was its initial guess (-1: cold)
     q: np.ndarray | None = None
 
 
@@ -113,10 +115,23 @@ class PrefetchedSources:
 
 class Server:
     """pool[g] is a list of QProblem on grid g (its stored right-hand sides).
-    sources: callable request -> right-hand side (default: request_src)."""
+    sources: callable request -> right-hand side (default: request_src).
+
+    copies: resident copies a grid may have.  With 1 (the default) a grid's
+    requests are served one at a time in arrival order, each warm-started from
+    the previous one's solution, so every result is the same bits alone or in
+    any mix.  The tail of the request stream comes from that queue (a hot
+    grid's requests wait behind one another; `tail_report`).  With copies > 1
+    a request arriving while its grid is busy goes to an idle copy of the grid
+    (warm-started from that copy's last solution) or, budget allowing, to a
+    new copy, warm-started from the grid's latest finished solution (cold when
+    it has none): the queue goes, and each result is still a solve of its own
+    request to its tolerance from the initial guess it was given
+    (Request.warm_from) -- the same within the tolerance, not the same bits,
+    as when served alone."""
 
     def __init__(self, pool, engine, budget_bytes, request_bytes, chunk=64, maxiters=20000, keep_q=True,
-                 clock=time.perf_counter, sources=None):
+                 clock=time.perf_counter, sources=None, copies=1):
         self.pool = pool
         self.engine = engine
         self.budget = float(budget_bytes)
@@ -125,8 +140,12 @@ class Server:
         self.maxiters = int(maxiters)
         self.keep_q = keep_q
         self.clock = clock
-        self.resident = collections.OrderedDict()  # grid -> instance id (LRU order)
-        self.busy = {}                             # grid -> Request in flight
+        self.copies = max(1, int(copies))
+        self.resident = collections.OrderedDict()  # (grid, copy) -> instance id (LRU order)
+        self.busy = {}                             # (grid, copy) -> Request in flight
+        self.ncopy = collections.Counter()         # grid -> resident copies
+        self.copy_last = {}                        # (grid, copy) -> rid of its last finished request
+        self.grid_last = {}                        # grid -> (rid, solution) of its latest finished request
         self.used = 0
         self.evictions = 0
         self.launches = 0
@@ -140,26 +159,33 @@ class Server:
 
     # -- admission --------------------------------------------------------
     def _evict_one(self, avoid) -> bool:
-        for g, iid in self.resident.items():
-            if g not in self.busy and g != avoid:
+        for key, iid in self.resident.items():
+            if key not in self.busy and key[0] != avoid:
                 self.engine.release(iid)
-                del self.resident[g]
-                self.used -= self.rbytes[g]
+                del self.resident[key]
+                self.ncopy[key[0]] -= 1
+                self.used -= self.rbytes[key[0]]
                 self.evictions += 1
                 return True
         return False
 
+    def _busy_grids(self):
+        return {key[0] for key in self.busy}
+
     def _admit(self, r: Request) -> bool:
         g = r.grid
-        if g in self.busy:
-            return False
-        if g in self.resident:
-            iid = self.resident.pop(g)
-            self.resident[g] = iid  # most recently used
+        idle = [key for key in self.resident if key[0] == g and key not in self.busy]
+        if idle:
+            key = idle[-1]  # the most recently used copy
+            iid = self.resident.pop(key)
+            self.resident[key] = iid
             self.engine.resubmit(iid, self.sources(r), tol=r.tol, maxiters=self.maxiters, warm=True)
             self.resubmits += 1
             r.warm = True
+            r.warm_from = self.copy_last.get(key, -1)
         else:
+            if self.ncopy[g] >= self.copies:
+                return False
             if self.rbytes[g] > self.budget:
                 raise SolverError(OOM, f"grid {g} needs {self.rbytes[g]} bytes, budget {self.budget:.0f}")
             while self.used + self.rbytes[g] > self.budget:
@@ -168,6 +194,10 @@ class Server:
             prob = self.pool[g][r.rhs]
             if r.mix != 0.0:
                 prob = type(prob)(**{**prob.__dict__, "src": self.sources(r)})
+            last = self.grid_last.get(g) if self.copies > 1 else None
+            if last is not None:
+                # a further copy of a grid in use starts from its latest solution
+                prob = type(prob)(**{**prob.__dict__, "q": last[1]})
             while True:
                 try:
                     iid = self.engine.add(prob, tol=r.tol, maxiters=self.maxiters)
@@ -177,17 +207,27 @@ class Server:
                         raise
                     if not self._evict_one(g):
                         return False
-            self.resident[g] = iid
+            c = 0
+            while (g, c) in self.resident:
+                c += 1
+            key = (g, c)
+            if last is not None:
+                r.warm = True
+                r.warm_from = last[0]
+            self.resident[key] = iid
+            self.ncopy[g] += 1
             self.used += self.rbytes[g]
-        self.busy[g] = r
+        self.busy[key] = r
+        r.copy = key[1]
         r.t_admit = self.clock() - self.t0
         return True
 
     def _harvest(self, only=None):
-        for g, r in list(self.busy.items()):
+        for key, r in list(self.busy.items()):
+            g = key[0]
             if only is not None and g not in only:
                 continue
-            iid = self.resident[g]
+            iid = self.resident[key]
             if self.engine.state(iid) == 3:  # INST_DONE
                 if self.keep_q:
                     q, st = self.engine.result(iid, self.pool[g][r.rhs].q, release=False)
@@ -200,7 +240,25 @@ class Server:
                 r.iters, r.status, r.unknowns = int(st.niters), int(st.status), int(st.unknowns)
                 if self.keep_q:
                     r.q = q
-                del self.busy[g]
+                self.copy_last[key] = r.rid
+                if self.copies > 1:
+                    self.grid_last[g] = (r.rid, q if self.keep_q else self.qbuf[g])
+                del self.busy[key]
+
+    def _admit_waiting(self, queues):
+        """Admits waiting requests, oldest first across grids; a grid takes as
+        many of its waiting requests as it has idle or new copies (one at a
+        time with copies = 1: a grid's later requests wait for its earlier
+        ones).  Returns how many."""
+        n = 0
+        heads = sorted((q[0].t_arrival, g) for g, q in queues.items() if q)
+        for _, g in heads:
+            while queues.get(g) and self._admit(queues[g][0]):
+                queues[g].popleft()
+                n += 1
+            if g in queues and not queues[g]:
+                del queues[g]
+        return n
 
     # -- the loop -----------------------------------------------------------
     def run(self, requests, realtime=True, drain_limit=None):
@@ -226,16 +284,9 @@ class Server:
                 queues.setdefault(reqs[i].grid, collections.deque()).append(reqs[i])
                 npending += 1
                 i += 1
-            # admit the oldest waiting request of every idle grid, oldest first;
-            # a grid's later requests wait for its earlier ones
+            # admit waiting requests, oldest first (_admit_waiting)
             t1 = self.clock()
-            heads = sorted((q[0].t_arrival, g) for g, q in queues.items() if q and g not in self.busy)
-            for _, g in heads:
-                if self._admit(queues[g][0]):
-                    queues[g].popleft()
-                    npending -= 1
-                    if not queues[g]:
-                        del queues[g]
+            npending -= self._admit_waiting(queues)
             t2 = self.clock()
             self.host_s["admit"] += t2 - t1
             if self.busy:
@@ -260,19 +311,6 @@ class Server:
         self.t_end = self.clock() - self.t0
         return reqs
 
-
-    def _admit_waiting(self, queues):
-        """Admits the oldest waiting request of every idle grid, oldest first
-        (a grid's later requests wait for its earlier ones); returns how many."""
-        n = 0
-        heads = sorted((q[0].t_arrival, g) for g, q in queues.items() if q and g not in self.busy)
-        for _, g in heads:
-            if self._admit(queues[g][0]):
-                queues[g].popleft()
-                n += 1
-                if not queues[g]:
-                    del queues[g]
-        return n
 
     def _run_overlapped(self, requests, realtime, drain_limit):
         reqs = sorted(requests, key=lambda r: r.t_arrival)

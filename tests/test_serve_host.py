@@ -264,3 +264,27 @@ def test_overlapped_loop_admits_during_launches():
     assert all(r.t_done >= 0 for r in reqs)
     assert srv.launches == 20 and srv.work == sum(r.iters * r.unknowns for r in reqs)
     assert seen[0] == [0, 1]
+
+
+@pytest.mark.parametrize("Eng", ENGINES)
+def test_copies_serve_a_hot_grid_in_parallel(Eng):
+    """With copies = 2, three requests on one grid arriving together: the first
+    two run at once on two resident copies (the second cold), the third waits
+    for an idle copy and warm-starts there; with copies = 1 they run one after
+    another.  Copies count against the budget like any resident grid."""
+    pool = fake_pool([100, 100])
+    for copies, launches_max in ((1, 3 * 5), (2, 2 * 5)):
+        eng = Eng(10_000)
+        srv = Server(pool, eng, 1e12, rbytes, chunk=8, keep_q=False, copies=copies)
+        reqs = [Request(k, 0, k % 2, 1e-8, 0.0) for k in range(3)]
+        srv.run(reqs, realtime=False)
+        assert all(r.t_done >= 0 and r.iters > 0 for r in reqs)
+        assert srv.ncopy[0] == copies and srv.used == copies * rbytes(pool[0][0].grid)
+        assert [r.warm for r in reqs] == ([False, True, True] if copies == 1 else [False, False, True])
+        assert srv.launches <= launches_max
+    # budget for one copy only: the second copy is not created, nothing is evicted
+    eng = FakeEngine(10_000)
+    srv = Server(pool, eng, 1.5 * rbytes(pool[0][0].grid), rbytes, chunk=8, keep_q=False, copies=2)
+    reqs = [Request(k, 0, 0, 1e-8, 0.0) for k in range(2)]
+    srv.run(reqs, realtime=False)
+    assert srv.ncopy[0] == 1 and srv.evictions == 0 and all(r.t_done >= 0 for r in reqs)
