@@ -1054,7 +1054,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
           a.z32[u] = 0.f;
           if (QP == 2) a.s32[u] = 0.f;
           if (QP == 1) {
-            double cc = 1.0;
+            double cc = 1.0, akeep = 0.0;
             if (act) {
               double diag = 0.0;
               for (int f = 0; f < F; ++f) {
@@ -1063,6 +1063,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
                 diag += dz * a.face[(size_t)(ti.c0 + c) * F + f].D64;
               }
               const double ak = (k == ctop) ? Ac / dz : 2 * Ac / (dz + a.dzz64[u - 1]);
+              akeep = ak;  // the unscaled vertical coefficient, scaled in S2
               if (ctop < nk - 1) {
                 if (k == ctop) diag += 2 * ak + 2 * Ac / (a.dzz64[u + 1] + dz);
                 else if (k == nk - 1) diag += ak;
@@ -1071,11 +1072,15 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
               if (diag <= 0) diag = 1;
               cc = sqrt(diag);
             }
-            a.c64[u] = cc;
-            a.cinv32[u] = (float)(1.0 / cc);
-            a.fz32[u] = (float)(dz / cc);
+            // c64 holds 1/c: one FP64 division per slot here instead of five
+            // in the scaled coefficients (S2) and one in the rescale
+            const double ic = 1.0 / cc;
+            a.c64[u] = ic;
+            a.coef64[u] = akeep;
+            a.cinv32[u] = (float)ic;
+            a.fz32[u] = (float)(dz * ic);
             a.x64[u] = act ? a.q64[u] * cc : 0.0;
-            a.b64[u] = act ? a.src64[u] / cc : 0.0;
+            a.b64[u] = act ? a.src64[u] * ic : 0.0;
           } else {
             double cf = 0.0;
             if (k == ctop) cf = Ac / dz;
@@ -1111,8 +1116,9 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
           a.pb32[u] = 0.f;
           if (QP == 2) a.s32[u] = 0.f;
           if (QP == 1) {
-            a.c64[u] = a.cin64[u];
-            a.cinv32[u] = (float)(1.0 / a.cin64[u]);
+            const double ic = 1.0 / a.cin64[u];
+            a.c64[u] = ic;
+            a.cinv32[u] = (float)ic;
           }
         }
       }
@@ -1134,17 +1140,18 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
             const int ctop = sm.ctop[c];
             const double Ac = a.colAc[ti.c0 + c];
             const double dz = a.dzz64[u];
-            const double cu = a.c64[u];
+            const double icu = a.c64[u];  // 1/c
+            const double ak = a.coef64[u];  // Ac/dzz or 2 Ac/(dzz + dzz above), from S1
             double cf = 0.0;
-            if (k == ctop) cf = Ac / dz / cu;
-            else if (k > ctop) cf = 2 * Ac / (dz + a.dzz64[u - 1]) / (cu * a.c64[u - 1]);
+            if (k == ctop) cf = ak * icu;
+            else if (k > ctop) cf = ak * (icu * a.c64[u - 1]);
             a.coef64[u] = cf;
             a.coef32[u] = (float)cf;
             for (int f = 0; f < F; ++f) {
               const int kk = sm.fkk[c * F + f];
               double v = 0.0;
               if (k >= ctop && k >= (kk & 0xffff) && k < (kk >> 16))
-                v = dz * a.face[(size_t)(ti.c0 + c) * F + f].D64 / (cu * a.c64[sm.fns[c * F + f] + k]);
+                v = dz * a.face[(size_t)(ti.c0 + c) * F + f].D64 * (icu * a.c64[sm.fns[c * F + f] + k]);
               a.fc64[(size_t)F * u + f] = v;
               // the FP32 weight the inner apply uses: (dzz/c_u) * (D * (1/c_n)), as formed
               // from the FP32 copies (0 where the face does not couple the level)
@@ -1364,7 +1371,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
 __global__ void finalize_q_kernel(const double* __restrict__ x64, const double* __restrict__ c64,
                                   double* __restrict__ q64, int s0, int n, int scaled) {
   for (int u = s0 + blockIdx.x * blockDim.x + threadIdx.x; u < s0 + n; u += gridDim.x * blockDim.x)
-    q64[u] = scaled ? x64[u] / c64[u] : x64[u];
+    q64[u] = scaled ? x64[u] * c64[u] : x64[u];  // c64 holds 1/c
 }
 
 }  // namespace sgpu
@@ -2211,7 +2218,7 @@ int sgpu_batch_result(sgpu_batch* b, int id, double* const* q, sgpu_stats* st, i
         const int i = H.dev2cell[j], k0 = H.ctop[i];
         const long long o = H.coff[j];
         if (scaled)
-          for (int k = k0; k < H.Nk[i]; ++k) q[i][k] = x[o + k] / c[o + k];
+          for (int k = k0; k < H.Nk[i]; ++k) q[i][k] = x[o + k] * c[o + k];  // c64 holds 1/c
         else
           std::memcpy(q[i] + k0, x + o + k0, sizeof(double) * (H.Nk[i] - k0));
       }

@@ -142,7 +142,7 @@ struct BatchArgs {
   const double* q64;     // [nslots] warm start (and fixed values at boundary columns)
   const double* cin64;   // [nslots] c at boundary columns (qprecond 1)
   const double* dzfD64;  // [nedge_slots] dzf*D per edge level (qprecond 0/2)
-  double* c64;           // [nslots] sqrt|diag| (qprecond 1), 1 elsewhere
+  double* c64;           // [nslots] 1/sqrt|diag| (qprecond 1: 1/c), 1 elsewhere
   double* coef64;        // [nslots+4] vertical coefficient (scaled for qprecond 1)
   double* fc64;          // [F*nslots] face coefficients of the FP64 operator (qprecond 1)
   double* x64;           // [nslots] FP64 iterate (scaled variables for qprecond 1)
