@@ -511,6 +511,7 @@ def compact_forms(args, parity_jobs=None):
             "iters_inner": l3["mixed"]["iters_inner"], "iters_fp64": l3["iters_fp64"],
             "plain_fp64_unknown_iters_per_s": l3["plain_fp64_unknown_iters_per_s"],
             "speedup_vs_plain_fp64": l3["speedup_vs_plain_fp64"], "ms_per_solve": l3["ms_per_step"],
+            "shape": l3["mixed"].get("shape"),
             "errors_vs_fp64_gpu": {k: l3["mixed"][k] for k in ("rel_l2", "max_abs_rel")},
             "roofline": l3["roofline"], "e2e": l3["e2e"], "clocks": l3["clocks"]}
     except Exception as e:
@@ -642,8 +643,9 @@ def run_ours(args):
         # the same pressure problem through the mixed-precision batched solver
         q64 = ctx.q_download(qp.q)
         it64 = int(np.median(nq))
+        shape, _ = mixed_shape(qp, props.qprecond, props.qepsilon, props.qmaxiters, local)
         mf, _, _ = mixed_form(qp, props.qprecond, max(2, min(args.steps, 5)), 3, props.qepsilon, props.qmaxiters,
-                              local, q64, it64)
+                              local, q64, it64, shape=shape)
         plain_q_rate = g.n_q() * it64 / (q_launch_ms / 1e3)
         mf["plain_fp64_q_unknown_iters_per_s"] = plain_q_rate
         mf["speedup_vs_plain_fp64"] = mf["equivalent_unknown_iters_per_s"] / plain_q_rate
@@ -744,12 +746,28 @@ def batch_timed(b, ids, steps, warmup, tol, maxiters, device):
     return ev0.elapsed_time(ev1), per, clocks
 
 
-def mixed_form(prob, qprecond, steps, warmup, tol, maxiters, device, q64=None, iters64=None):
-    """One problem through the batched mixed-precision solver: timing, iterations, errors."""
+def mixed_shape(prob, qprecond, tol, maxiters, device):
+    """The batched solver's launch shape for one large problem, picked by the
+    engine's autotuner: the iteration form (one pass, or two with the solution
+    update in the apply pass) at 2 and 3 CTAs per SM, 1024-slot tiles."""
+    from suntans_gb300.autotune import autotune
+    best, table = autotune([prob], qprecond=qprecond, tol=tol, maxiters=maxiters, iters=8, ctas_per_sm=(2, 3),
+                           tile_slots=(1024,), fusion=(2, 1), device=device)
+    return best, table
+
+
+def mixed_form(prob, qprecond, steps, warmup, tol, maxiters, device, q64=None, iters64=None, shape=None):
+    """One problem through the batched mixed-precision solver: timing, iterations, errors.
+    shape: an autotuner result (CTAs per SM, slots per tile, form), None = the engine's defaults."""
+    from suntans_gb300.autotune import sm_count
     from suntans_gb300.batch import Batch, capacity_for
     g = prob.grid
     b = Batch(qprecond=qprecond, maxfaces=g.maxfaces, device=device, **capacity_for([g]))
     try:
+        if shape is not None:
+            b.set(ctas=shape["ctas_per_sm"] * sm_count(device))
+            b.set_tile_slots(shape["tile_slots"])
+            b.set_fusion(shape["fusion"])
         b.use_graph(True)
         iid = b.add(prob, tol=tol, maxiters=maxiters)
         ms_total, per, clocks = batch_timed(b, [iid], steps, max(warmup, 1), tol, maxiters, device)
@@ -760,6 +778,8 @@ def mixed_form(prob, qprecond, steps, warmup, tol, maxiters, device, q64=None, i
     N = g.n_q()
     out = {"ms_per_solve": ms_total / steps, "iters_inner": int(st.niters), "status": int(st.status),
            "raw_unknown_iters_per_s": N * st.niters / t}
+    if shape is not None:
+        out["shape"] = {k: shape[k] for k in ("ctas_per_sm", "tile_slots", "fusion")}
     if iters64 is not None:
         out["iters_fp64"] = int(iters64)
         out["equivalent_unknown_iters_per_s"] = N * iters64 / t
@@ -869,6 +889,7 @@ def bench_cfg1(args):
 
 
 def bench_cfg3(args, keep=None):
+    from suntans_gb300.autotune import sm_count
     from suntans_gb300.batch import Batch, capacity_for
     from suntans_gb300.capi import Context
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -882,13 +903,18 @@ def bench_cfg3(args, keep=None):
     q64 = ctx.q_download(qp.q)
     plain_rate = N * s64.niters / (s64.ms_solve / 1e3)
     ctx.close()
-    mf, clocks, q_mix = mixed_form(qp, args.qprecond, args.steps, args.warmup, 1e-10, 20000, local, q64, s64.niters)
+    shape, shape_table = mixed_shape(qp, args.qprecond, 1e-10, 20000, local)
+    mf, clocks, q_mix = mixed_form(qp, args.qprecond, args.steps, args.warmup, 1e-10, 20000, local, q64, s64.niters,
+                                   shape=shape)
     if keep is not None:
         keep.update(q_mix=q_mix, q64=q64, grid=g)
     peak, peak_kind = peaks()
     # end to end through the public API: add (host arrays in), solve, result (host array out)
     t0 = time.perf_counter()
     b = Batch(qprecond=args.qprecond, maxfaces=g.maxfaces, device=local, **capacity_for([g]))
+    b.set(ctas=shape["ctas_per_sm"] * sm_count(local))
+    b.set_tile_slots(shape["tile_slots"])
+    b.set_fusion(shape["fusion"])
     iid = b.add(qp, tol=1e-10, maxiters=20000)
     b.run()
     q, st = b.result(iid, qp.q)
@@ -905,6 +931,7 @@ def bench_cfg3(args, keep=None):
                        "cells": g.Nc, "N_q": N, "qprecond": args.qprecond, "tolerance": 1e-10,
                        "l2": "not flushed: working set > 129 MB L2"},
             "mixed": mf, "plain_fp64_unknown_iters_per_s": plain_rate, "iters_fp64": int(s64.niters),
+            "autotune": [{k: r[k] for k in ("ctas_per_sm", "tile_slots", "fusion", "rate")} for r in shape_table],
             "speedup_vs_plain_fp64": mf["equivalent_unknown_iters_per_s"] / plain_rate,
             "roofline": {"bound": "hbm", "achieved": mf["achieved_gbs_fp32_inner"], "peak": peak, "unit": "GB/s",
                          "frac": mf["achieved_gbs_fp32_inner"] / peak,
@@ -954,7 +981,7 @@ def bench_cfg4(args):
     plain_rate = float((Ns * it64).sum() / loop_s)
     # launch shape
     if args.no_autotune:
-        best, table = {"ctas_per_sm": 3, "tile_slots": 1024, "x_in_apply": 1}, []
+        best, table = {"ctas_per_sm": 3, "tile_slots": 1024, "fusion": 1}, []
     else:
         best, table = autotune(probs, qprecond=args.qprecond, tol=tol, maxiters=maxiters, device=local)
 
@@ -962,7 +989,7 @@ def bench_cfg4(args):
         b = Batch(qprecond=args.qprecond, maxfaces=grids[0].maxfaces, device=local, **capacity_for(grids))
         b.set(ctas=best["ctas_per_sm"] * sm_count(local))
         b.set_tile_slots(best["tile_slots"])
-        b.set_fusion(best.get("x_in_apply", 1))
+        b.set_fusion(best.get("fusion", 1))
         return b
 
     b = make_batch()

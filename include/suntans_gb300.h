@@ -379,12 +379,18 @@ int sgpu_batch_set(sgpu_batch *b, double delta, int ctas, long long timeout_ns);
  * from now on; a column longer than this still gets a tile of its own.
  * Smaller tiles spread small problems over more CTAs. */
 int sgpu_batch_set_tile_slots(sgpu_batch *b, int tile_slots);
-/* Tuning: where the FP32 solution update x += nu p runs.  1 (default): in the
- * next operator-apply pass, which streams p anyway (fewer bytes per
- * iteration, a larger pipeline stage); 0: in the vector-update pass.  The
- * results are the same bits either way.  Refused while a problem is in
- * mid-solve.  (A tuning knob of this engine; the reference has none.) */
-int sgpu_batch_set_fusion(sgpu_batch *b, int x_in_apply);
+/* Tuning: the form of a CG iteration.  1 (default): two passes (operator
+ * apply; vector update) with the FP32 solution update x += nu p run in the
+ * next apply pass, which streams p anyway (fewer bytes per iteration, a
+ * larger pipeline stage); 0: two passes with the update in the vector-update
+ * pass -- the same bits as 1.  2 (qprecond 0/1; qprecond 2 runs it as 1): one
+ * pass per iteration -- the residual step, the solution update, the new
+ * direction and the operator apply in one sweep with one grid barrier, the
+ * next mu from the sweep's own inner products (|r - nu z|^2 = r.r - 2 nu r.z
+ * + nu^2 z.z); the same stopping rule on the FP64 true residual, iterates
+ * that round differently.  Refused while a problem is in mid-solve under
+ * another form.  (A tuning knob of this engine; the reference has none.) */
+int sgpu_batch_set_fusion(sgpu_batch *b, int form);
 void *sgpu_batch_stream(sgpu_batch *b);
 
 /* Device time of the last launch per phase (ns): [1] operator apply, [2]

@@ -11,17 +11,20 @@ The batched kernel's shape has three runtime knobs:
   several columns of a 10..60-level grid).  Small tiles spread a batch of
   small problems over more CTAs; large tiles amortise the tile header and the
   pipeline hand-offs;
-* fusion: where the FP32 solution update x += nu p runs -- fused into the
-  next operator-apply pass, which streams p anyway (13 instead of 14 FP32
-  values per unknown-iteration, a larger pipeline stage), or kept in the
-  vector-update pass.  The two give the same bits.
+* fusion, the form of an iteration: two passes (operator apply; vector
+  update) with the FP32 solution update x += nu p fused into the next apply
+  pass, which streams p anyway (13 instead of 14 FP32 values per
+  unknown-iteration, a larger pipeline stage), or kept in the update pass --
+  the two give the same bits; or one pass per iteration (qprecond 0/1: the
+  residual step, the solution update, the new direction and the operator in
+  one sweep, the next mu from the sweep's own inner products; 12 values, one
+  grid barrier instead of two, a stage of 5 + F streams).
 
 `autotune` measures unknown-iterations per second for every combination on
 the caller's own problems (a short run of `iters` iterations after the set-up
 phase, every instance active) and returns the fastest.  A combination whose
 tile count exceeds what that many CTAs can list is recorded as infeasible.
-The pipeline depth (two stages) and the two passes per iteration are fixed in
-the kernel.
+The pipeline depth (two stages) is fixed in the kernel.
 """
 from __future__ import annotations
 
@@ -32,7 +35,7 @@ from .capi import OOM, SolverError
 
 CTAS_PER_SM = (1, 2, 3)
 TILE_SLOTS = (256, 512, 1024)
-FUSION = (1, 0)
+FUSION = (2, 1, 0)
 
 
 def sm_count(device=0) -> int:
@@ -42,7 +45,7 @@ def sm_count(device=0) -> int:
 
 def autotune(problems, qprecond=1, tol=1e-10, maxiters=20000, iters=12, ctas_per_sm=CTAS_PER_SM,
              tile_slots=TILE_SLOTS, fusion=FUSION, device=0, sample=None):
-    """Returns (best, table): best = {"ctas_per_sm", "tile_slots", "x_in_apply", "rate", "ms"}; table lists
+    """Returns (best, table): best = {"ctas_per_sm", "tile_slots", "fusion", "rate", "ms"}; table lists
     every candidate.
 
     problems: QProblem list (all share maxfaces).  sample: use at most this many
@@ -72,10 +75,10 @@ def autotune(problems, qprecond=1, tol=1e-10, maxiters=20000, iters=12, ctas_per
                 except SolverError as e:
                     if e.code != OOM:  # more tiles than this CTA count can list: not a candidate
                         raise
-                    table.append({"ctas_per_sm": cps, "tile_slots": ts, "x_in_apply": fx, "rate": 0.0,
+                    table.append({"ctas_per_sm": cps, "tile_slots": ts, "fusion": fx, "rate": 0.0,
                                   "ms": None, "infeasible": str(e)})
                     continue
-                table.append({"ctas_per_sm": cps, "tile_slots": ts, "x_in_apply": fx,
+                table.append({"ctas_per_sm": cps, "tile_slots": ts, "fusion": fx,
                               "rate": work / (ms / 1e3) if ms > 0 else 0.0, "ms": ms})
         finally:
             b.close()

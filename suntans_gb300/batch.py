@@ -66,10 +66,13 @@ class Batch:
         if rc != OK:
             raise SolverError(rc, "sgpu_batch_set")
 
-    def set_fusion(self, x_in_apply: int):
-        """Where the FP32 solution update runs: 1 in the next apply pass
-        (default), 0 in the update pass; same bits either way."""
-        rc = self.lib.sgpu_batch_set_fusion(self.h, int(x_in_apply))
+    def set_fusion(self, form: int):
+        """The form of a CG iteration: 1 (default) two passes with the FP32
+        solution update run in the next apply pass, 0 two passes with it in
+        the update pass (the same bits as 1), 2 one pass per iteration with
+        the two reductions merged (qprecond 0/1; qprecond 2 runs it as 1).
+        Refused while a problem is in mid-solve under another form."""
+        rc = self.lib.sgpu_batch_set_fusion(self.h, int(form))
         if rc != OK:
             raise SolverError(rc, "sgpu_batch_set_fusion")
 

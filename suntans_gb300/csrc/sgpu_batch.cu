@@ -497,8 +497,15 @@ __device__ __forceinline__ ProdInst prod_inst(const BatchArgs& a, int i) {
   return r;
 }
 
+// Residual and A p buffers: the one-pass form alternates between two of each
+// (a pass reads the neighbours' old values while it writes its own new ones);
+// the two-pass form updates r in place and writes z in the apply pass only.
+__device__ __forceinline__ float* rbuf(const BatchArgs& a, int par) { return (a.one_pass && par) ? a.r2_32 : a.r32; }
+__device__ __forceinline__ float* zbuf(const BatchArgs& a, int par) { return (a.one_pass && par) ? a.z2_32 : a.z32; }
+
 // Producer: fill stage seq&1 with tile descriptor d of instance fields pi.
-// PH 0 = apply, 1 = update.
+// PH 0 = apply, 1 = update, 2 = the one-pass form's single sweep (streams p,
+// r, coef, the F face weights, z and x of the current buffers).
 template <int QP, int PH>
 __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileDesc& d, const ProdInst& pi,
                                         long long lim, int* err) {
@@ -518,14 +525,24 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   sd->mu = pi.mu;
   const bool xa = a.x_in_apply != 0;
   sd->nu = PH == 0 ? (xa ? pi.nux : 0.f) : pi.nu;  // apply: the pending solution increment's nu
-  const bool hdr = (PH == 0) || (QP == 2);
+  const bool hdr = (PH != 1) || (QP == 2);
   uint32_t bytes = 0;
   if (PH == 0) bytes = d.hdr_bytes + 2 * 4 * n4 + 4 * (n4 + 4) + a.F * 4 * n4 + (xa ? 4 * n4 : 0);
+  else if (PH == 2) bytes = d.hdr_bytes + 4 * 4 * n4 + 4 * (n4 + 4) + a.F * 4 * n4;
   else bytes = (hdr ? d.hdr_bytes : 0) + (xa ? 2 : 4) * 4 * n4;
   fence_proxy_async();
   mbar_arrive_expect_tx(&P.full[b], bytes);
   if (hdr) bulk_g2s(stage_hdr(st), a.hdrs + d.hdr, d.hdr_bytes, &P.full[b]);
-  if (PH == 0) {
+  if (PH == 2) {
+    const float* pold = par ? a.pb32 : a.pa32;
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 0), pold + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 1), rbuf(a, par) + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 2), a.coef32 + d.base, 4 * (n4 + 4), &P.full[b]);
+    for (int f = 0; f < a.F; ++f)
+      bulk_g2s(stage_stream(st, P.hcap, P.sfl, 3 + f), a.fw32 + (size_t)f * a.fw_stride + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 3 + a.F), zbuf(a, par) + d.base, 4 * n4, &P.full[b]);
+    bulk_g2s(stage_stream(st, P.hcap, P.sfl, 4 + a.F), a.x32 + d.base, 4 * n4, &P.full[b]);
+  } else if (PH == 0) {
     const float* pold = par ? a.pb32 : a.pa32;
     const float* S = (QP == 2) ? a.s32 : a.r32;
     bulk_g2s(stage_stream(st, P.hcap, P.sfl, 0), pold + d.base, 4 * n4, &P.full[b]);
@@ -546,17 +563,32 @@ __device__ __forceinline__ void produce(const BatchArgs& a, Pipe& P, const TileD
   P.seq = q + 1;
 }
 
+// The direction of a slot, formed where it is used.  Two-pass form: p_new =
+// S + mu p_old (S = r, or s for qprecond 2).  One-pass form (M): the pending
+// residual step first, r_new = r - nu z, then p_new = r_new + mu p_old.  A slot
+// and each of its neighbours evaluate the same two roundings on the same
+// operands, so every reader sees the value the slot's owner stores.
+template <bool M>
+__device__ __forceinline__ float res_new(float nu, float r, float z) {
+  return M ? __fmaf_rn(-nu, z, r) : r;
+}
+
 // FP32 apply of one active slot from a staged tile (own data in shared
-// memory, neighbours from global).  p_new = S + mu p_old on the fly.
-template <int QP>
+// memory, neighbours from global).  p_new formed on the fly (res_new above);
+// M: sz / zold are the staged / global z and ru_out receives r_new of the slot.
+template <int QP, bool M>
 __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char* hd, const HdrLayout& L, int c,
-                                         int s, int k, int ctop, int nk, float mu, const float* sp, const float* sS,
-                                         const float* sc, const float* sf, const float* __restrict__ pold,
-                                         const float* __restrict__ S, float& pu_out) {
+                                         int s, int k, int ctop, int nk, float mu, float nu, const float* sp,
+                                         const float* sS, const float* sz, const float* sc, const float* sf,
+                                         const float* __restrict__ pold, const float* __restrict__ S,
+                                         const float* __restrict__ zold, float& pu_out, float& ru_out) {
   const int F = a.F;
   const int* fns = (const int*)(hd + L.o_fns);
   const int* fkk = (const int*)(hd + L.o_fkk);
-  const float pu = __fmaf_rn(mu, sp[s], sS[s]);
+  auto own = [&](int t) { return __fmaf_rn(mu, sp[t], res_new<M>(nu, sS[t], M ? sz[t] : 0.f)); };
+  auto nbr = [&](int n) { return __fmaf_rn(mu, pold[n], res_new<M>(nu, S[n], M ? zold[n] : 0.f)); };
+  ru_out = res_new<M>(nu, sS[s], M ? sz[s] : 0.f);
+  const float pu = __fmaf_rn(mu, sp[s], ru_out);
   pu_out = pu;
   float y;
   if (QP == 1) {
@@ -565,33 +597,31 @@ __device__ __forceinline__ float apply32(const BatchArgs& a, const unsigned char
       const int kk = fkk[c * F + f];
       if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
       const int n = fns[c * F + f] + k;
-      const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      y = __fmaf_rn(sf[f * a.stream_floats + s], pn, y);  // staged face weight stream f
+      y = __fmaf_rn(sf[f * a.stream_floats + s], nbr(n), y);  // staged face weight stream f
     }
-    if (k > ctop) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
-    if (k < nk - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
+    if (k > ctop) y = __fmaf_rn(sc[s], own(s - 1), y);
+    if (k < nk - 1) y = __fmaf_rn(sc[s + 1], own(s + 1), y);
   } else {
     y = 0.f;
     for (int f = 0; f < F; ++f) {
       const int kk = fkk[c * F + f];
       if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
       const int n = fns[c * F + f] + k;
-      const float pn = __fmaf_rn(mu, pold[n], S[n]);
-      y = __fmaf_rn(pn - pu, sf[f * a.stream_floats + s], y);  // staged dzf*D of the edge level
+      y = __fmaf_rn(nbr(n) - pu, sf[f * a.stream_floats + s], y);  // staged dzf*D of the edge level
     }
     const float c0 = sc[s];
     if (ctop < nk - 1) {
       if (k == ctop) {
         const float c1 = sc[s + 1];
-        const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+        const float pp = own(s + 1);
         y += (-2.f * c0 - c1) * pu + c1 * pp;
       } else if (k == nk - 1) {
-        const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
+        const float pm = own(s - 1);
         y += c0 * pm - c0 * pu;
       } else {
         const float c1 = sc[s + 1];
-        const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
-        const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+        const float pm = own(s - 1);
+        const float pp = own(s + 1);
         y += c0 * pm - (c0 + c1) * pu + c1 * pp;
       }
     } else {
@@ -615,19 +645,22 @@ __device__ __forceinline__ int hcol_of(const unsigned short* start, int ncols, i
 // compile-time face count: every neighbour gather of the 4 slots is
 // independent of the others, so all of them are in flight together.  A face
 // that does not couple a level gathers the slot itself (a valid address) with
-// a zero weight.
-template <int QP, int FF>
+// a zero weight.  M: the one-pass formation (res_new), rv receives r_new.
+template <int QP, int FF, bool M, class Emit>
 __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned char* hd, const HdrLayout& L,
-                                             int ncols, int len, int base, float mu, const float* sp, const float* sS,
-                                             const float* sc, const float* sf, const float* __restrict__ pold,
-                                             const float* __restrict__ S, float (&yv)[kBTSlots / kCompute],
-                                             float (&pv)[kBTSlots / kCompute], bool (&on)[kBTSlots / kCompute]) {
+                                             int ncols, int len, int base, float mu, float nu, const float* sp,
+                                             const float* sS, const float* sz, const float* sc, const float* sf,
+                                             const float* __restrict__ pold, const float* __restrict__ S,
+                                             const float* __restrict__ zold, float (&yv)[kBTSlots / kCompute],
+                                             float (&pv)[kBTSlots / kCompute], bool (&on)[kBTSlots / kCompute],
+                                             Emit&& emit) {
   constexpr int Q = kBTSlots / kCompute;
   const unsigned short* start = (const unsigned short*)(hd + L.o_start);
   const int* cn = (const int*)(hd + L.o_cn);
   const int* fns = (const int*)(hd + L.o_fns);
   const int* fkk = (const int*)(hd + L.o_fkk);
   const unsigned char* cmap = hd + L.o_cmap;
+  auto own = [&](int t) { return __fmaf_rn(mu, sp[t], res_new<M>(nu, sS[t], M ? sz[t] : 0.f)); };
   int cc[Q], kv[Q], ctop[Q], nk[Q], sv[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -642,60 +675,70 @@ __device__ __forceinline__ void apply_tile32(const BatchArgs& a, const unsigned 
     nk[q] = w >> 16;
     on[q] = in && kv[q] >= ctop[q];
   }
-  // gathers
-  float pn[Q][FF], wn[Q][FF];
+  // gathers, then the slots' applies; the one-pass form (three gathers per
+  // face instead of two) takes the slots in two halves to stay in registers
+  constexpr int NG = M ? 2 : 1, QG = Q / NG;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
+  for (int g = 0; g < NG; ++g) {
+  float pn[QG][FF], wn[QG][FF];
+#pragma unroll
+  for (int qi = 0; qi < QG; ++qi) {
+    const int q = g * QG + qi;
 #pragma unroll
     for (int f = 0; f < FF; ++f) {
       const int e = cc[q] * FF + f;
       const int kk = fkk[e];
       const bool ok = on[q] && kv[q] >= (kk & 0xffff) && kv[q] < (kk >> 16);
       const int n = ok ? fns[e] + kv[q] : base + sv[q];
-      pn[q][f] = __fmaf_rn(mu, pold[n], S[n]);
-      if (QP == 1) {
-        wn[q][f] = sf[f * a.stream_floats + sv[q]];  // staged face weight (0 where the face does not couple)
-      } else {
-        wn[q][f] = sf[f * a.stream_floats + sv[q]];  // staged dzf*D of the edge level (0 likewise)
-      }
+      pn[qi][f] = __fmaf_rn(mu, pold[n], res_new<M>(nu, S[n], M ? zold[n] : 0.f));
+      // staged face weight: (dzz/c_u) D (1/c_n) for qprecond 1, dzf*D of the
+      // edge level otherwise (0 where the face does not couple)
+      wn[qi][f] = sf[f * a.stream_floats + sv[q]];
     }
   }
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
+  for (int qi = 0; qi < QG; ++qi) {
+    const int q = g * QG + qi;
     const int s = sv[q], k = kv[q];
-    const float pu = __fmaf_rn(mu, sp[s], sS[s]);
-    pv[q] = pu;
+    const float ru = res_new<M>(nu, sS[s], M ? sz[s] : 0.f);
+    const float pu = __fmaf_rn(mu, sp[s], ru);
     float y;
     if (QP == 1) {
       y = -pu;
 #pragma unroll
-      for (int f = 0; f < FF; ++f) y = __fmaf_rn(wn[q][f], pn[q][f], y);
-      if (k > ctop[q]) y = __fmaf_rn(sc[s], __fmaf_rn(mu, sp[s - 1], sS[s - 1]), y);
-      if (k < nk[q] - 1) y = __fmaf_rn(sc[s + 1], __fmaf_rn(mu, sp[s + 1], sS[s + 1]), y);
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(wn[qi][f], pn[qi][f], y);
+      if (k > ctop[q]) y = __fmaf_rn(sc[s], own(s - 1), y);
+      if (k < nk[q] - 1) y = __fmaf_rn(sc[s + 1], own(s + 1), y);
     } else {
       y = 0.f;
 #pragma unroll
-      for (int f = 0; f < FF; ++f) y = __fmaf_rn(pn[q][f] - pu, wn[q][f], y);
+      for (int f = 0; f < FF; ++f) y = __fmaf_rn(pn[qi][f] - pu, wn[qi][f], y);
       const float c0 = sc[s];
       if (ctop[q] < nk[q] - 1) {
         if (k == ctop[q]) {
           const float c1 = sc[s + 1];
-          const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+          const float pp = own(s + 1);
           y += (-2.f * c0 - c1) * pu + c1 * pp;
         } else if (k == nk[q] - 1) {
-          const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
+          const float pm = own(s - 1);
           y += c0 * pm - c0 * pu;
         } else {
           const float c1 = sc[s + 1];
-          const float pm = __fmaf_rn(mu, sp[s - 1], sS[s - 1]);
-          const float pp = __fmaf_rn(mu, sp[s + 1], sS[s + 1]);
+          const float pm = own(s - 1);
+          const float pp = own(s + 1);
           y += c0 * pm - (c0 + c1) * pu + c1 * pp;
         }
       } else {
         y -= 2.f * c0 * pu;
       }
     }
-    yv[q] = on[q] ? y : 0.f;
+    if (M) {
+      emit(q, on[q], y, pu, ru);
+    } else {
+      yv[q] = on[q] ? y : 0.f;
+      pv[q] = pu;
+    }
+  }
   }
 }
 
@@ -726,31 +769,47 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     if (lane == 0 && err) atomicCAS(&a.ctl->status, SGPU_OK, SGPU_TIMEOUT);
     return;
   }
-  constexpr int NV = (PH == 1 && QP == 2) ? 2 : 1;
+  // sums per phase: apply p.z; update r.r (qprecond 2: r.s, r.r); one pass
+  // p.z, r.r, r.z, z.z
+  constexpr int NV = PH == 2 ? 4 : ((PH == 1 && QP == 2) ? 2 : 1);
+  static_assert(NV <= kPwVals, "warp slots hold kPwVals sums");
   // The accumulators are scalars, not arrays: an array captured by reference
   // in the flush lambda below would live in local memory, and every
   // accumulation of the phase loops would load and store it there.
-  DF dacc0, dacc1;
+  DF dacc0, dacc1, dacc2, dacc3;
   df_zero(dacc0);
   df_zero(dacc1);
+  df_zero(dacc2);
+  df_zero(dacc3);
   // Per-warp flush of the instance's partial sums: a fixed shuffle tree, then
   // lane 0 stores the warp's value into the CTA's slot.  No barrier, fence or
   // atomic: the owner CTA collects the slots at the end of the phase.
   // `enc` is the slot, bitwise complemented when this CTA owns the instance.
   if (threadIdx.x == 0) *P.nown = 0;
   auto do_flush = [&](int inst, int enc) {
-    double v0 = df_value(dacc0), v1 = df_value(dacc1);
+    double v0 = df_value(dacc0), v1 = df_value(dacc1), v2 = df_value(dacc2), v3 = df_value(dacc3);
     df_zero(dacc0);
     df_zero(dacc1);
+    df_zero(dacc2);
+    df_zero(dacc3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-      if (NV == 2) v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+      if (NV >= 2) v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+      if (NV == 4) {
+        v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+        v3 += __shfl_xor_sync(0xffffffffu, v3, o);
+      }
     }
     const int slot = enc < 0 ? ~enc : enc;
     if (lane == 0) {
-      st_partial(a.tpw + ((size_t)slot * 8 + warp) * 2, v0);
-      if (NV == 2) st_partial(a.tpw + ((size_t)slot * 8 + warp) * 2 + 1, v1);
+      double* w = a.tpw + ((size_t)slot * 8 + warp) * kPwVals;
+      st_partial(w, v0);
+      if (NV >= 2) st_partial(w + 1, v1);
+      if (NV == 4) {
+        st_partial(w + 2, v2);
+        st_partial(w + 3, v3);
+      }
     }
     if (enc < 0 && threadIdx.x == 0) P.own[(*P.nown)++] = inst;
   };
@@ -770,7 +829,8 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     const int len = sd.nslots;
     const int base = sd.base;
     constexpr int Q = kBTSlots / kCompute;
-    if (PH == 0) {
+    if (PH == 0 || PH == 2) {
+      constexpr bool M = PH == 2;
       const unsigned char* hd = stage_hdr(st);
       const int ncols = ((const int*)hd)[0];
       const HdrLayout L = hdr_layout(ncols, a.F, len);
@@ -780,28 +840,53 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       const float* sS = stage_stream(st, P.hcap, P.sfl, 1);
       const float* sc = stage_stream(st, P.hcap, P.sfl, 2);
       const float* sf = stage_stream(st, P.hcap, P.sfl, 3);
+      const float* sz = M ? stage_stream(st, P.hcap, P.sfl, 3 + a.F) : nullptr;
       const float* pold = sd.par ? a.pb32 : a.pa32;
       float* pnew = sd.par ? a.pa32 : a.pb32;
-      const float* S = (QP == 2) ? a.s32 : a.r32;
+      const float* S = M ? rbuf(a, sd.par) : ((QP == 2) ? a.s32 : a.r32);
+      const float* zold = M ? zbuf(a, sd.par) : nullptr;
+      float* rnew = M ? rbuf(a, sd.par ^ 1) : nullptr;
+      float* znew = M ? zbuf(a, sd.par ^ 1) : a.z32;
+      // the pending solution increment x32 += nu p_old, applied here where its
+      // direction is staged anyway: 4 consecutive slots per thread (padding
+      // slots hold zeros in every stream).  Two-pass form: nu is the previous
+      // update phase's step; one pass: the step this pass also applies to r.
+      const float mu_p = mu, nu_r = M ? nu : 0.f;
       {
-        // the previous update phase's solution increment, deferred to here
-        // where its direction (p_old) is staged anyway: x32 += nu p_old, 4
-        // consecutive slots per thread (padding slots hold zeros in every stream)
         const int s0 = 4 * (int)threadIdx.x;
         if (nu != 0.f && s0 < len) {
-          const float* sx = stage_stream(st, P.hcap, P.sfl, 3 + a.F);
+          const float* sx = stage_stream(st, P.hcap, P.sfl, M ? 4 + a.F : 3 + a.F);
           const float4 p4 = *(const float4*)(sp + s0);
           const float4 x4 = *(const float4*)(sx + s0);
           *(float4*)(a.x32 + base + s0) = make_float4(__fmaf_rn(nu, p4.x, x4.x), __fmaf_rn(nu, p4.y, x4.y),
                                                       __fmaf_rn(nu, p4.z, x4.z), __fmaf_rn(nu, p4.w, x4.w));
         }
       }
+      // Two-pass apply: z and p_new are stored after the stage is handed back.
+      // One pass: each slot's r_new, p_new and z are stored and summed as soon
+      // as they are formed (four slots' worth of them would not fit in
+      // registers beside the gathers).
       float yv[Q], pv[Q];
       bool on[Q];
+      // (captures scalars only: an array captured here would live in local memory)
+      const int ubase = base + (int)threadIdx.x;
+      auto emit = [&](int qq, bool o, float y, float pu, float ru) {
+        if (!o) return;
+        const int u = ubase + qq * kCompute;
+        znew[u] = y;
+        pnew[u] = pu;
+        rnew[u] = ru;
+        df_addprod(dacc0, pu, y);
+        df_addprod(dacc1, ru, ru);
+        df_addprod(dacc2, ru, y);
+        df_addprod(dacc3, y, y);
+      };
       if (a.F == 3) {
-        apply_tile32<QP, 3>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, yv, pv, on);
+        apply_tile32<QP, 3, M>(a, hd, L, ncols, len, base, mu_p, nu_r, sp, sS, sz, sc, sf, pold, S, zold, yv, pv, on,
+                               emit);
       } else if (a.F == 4) {
-        apply_tile32<QP, 4>(a, hd, L, ncols, len, base, mu, sp, sS, sc, sf, pold, S, yv, pv, on);
+        apply_tile32<QP, 4, M>(a, hd, L, ncols, len, base, mu_p, nu_r, sp, sS, sz, sc, sf, pold, S, zold, yv, pv, on,
+                               emit);
       } else {
 #pragma unroll
         for (int qq = 0; qq < Q; ++qq) {
@@ -815,7 +900,10 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
             const int ctop = cn[c] & 0xffff, nk = cn[c] >> 16;
             if (k >= ctop) {
               on[qq] = true;
-              yv[qq] = apply32<QP>(a, hd, L, c, s, k, ctop, nk, mu, sp, sS, sc, sf, pold, S, pv[qq]);
+              float ru;
+              yv[qq] = apply32<QP, M>(a, hd, L, c, s, k, ctop, nk, mu_p, nu_r, sp, sS, sz, sc, sf, pold, S, zold,
+                                      pv[qq], ru);
+              if (M) emit(qq, true, yv[qq], pv[qq], ru);
             }
           }
         }
@@ -823,13 +911,15 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
       // the stage is no longer read: hand it back to the producer
       __syncwarp();
       if (lane == 0) mbar_arrive(&P.empty[b]);
+      if (!M) {
 #pragma unroll
-      for (int qq = 0; qq < Q; ++qq) {
-        if (!on[qq]) continue;
-        const int u = base + threadIdx.x + qq * kCompute;
-        a.z32[u] = yv[qq];
-        pnew[u] = pv[qq];
-        df_addprod(dacc0, pv[qq], yv[qq]);
+        for (int qq = 0; qq < Q; ++qq) {
+          if (!on[qq]) continue;
+          const int u = base + threadIdx.x + qq * kCompute;
+          znew[u] = yv[qq];
+          pnew[u] = pv[qq];
+          df_addprod(dacc0, pv[qq], yv[qq]);
+        }
       }
     } else {
       const float* sz = stage_stream(st, P.hcap, P.sfl, 2);
@@ -943,14 +1033,14 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
     double v[NV];
 #pragma unroll
     for (int vv = 0; vv < NV; ++vv) v[vv] = 0.0;
-    volatile long long* base = (volatile long long*)(a.tpw + (size_t)t0 * 16);
+    volatile long long* base = (volatile long long*)(a.tpw + (size_t)t0 * 8 * kPwVals);
     for (int e0 = threadIdx.x; e0 < m8; e0 += kPer * kCompute) {
       long long bits[kPer][NV];
 #pragma unroll
       for (int k = 0; k < kPer; ++k) {
         const int e = e0 + k * kCompute;
 #pragma unroll
-        for (int vv = 0; vv < NV; ++vv) bits[k][vv] = e < m8 ? base[2 * e + vv] : 0;
+        for (int vv = 0; vv < NV; ++vv) bits[k][vv] = e < m8 ? base[kPwVals * e + vv] : 0;
       }
 #pragma unroll
       for (int k = 0; k < kPer; ++k) {
@@ -960,9 +1050,9 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
         for (int vv = 0; vv < NV; ++vv) {
           double x;
           if (bits[k][vv] != kEmptyPartial) {
-            base[2 * e + vv] = kEmptyPartial;
+            base[kPwVals * e + vv] = kEmptyPartial;
             x = __longlong_as_double(bits[k][vv]);
-          } else if (!take_partial((double*)(base + 2 * e + vv), lim, x)) {
+          } else if (!take_partial((double*)(base + kPwVals * e + vv), lim, x)) {
             err = 1;
           }
           v[vv] += x;
@@ -986,8 +1076,12 @@ __device__ __forceinline__ void pipelined_phase(const BatchArgs& a, Pipe& P, dou
 #ifndef SGPU_BATCH_MINB
 #define SGPU_BATCH_MINB 3
 #endif
-template <int QP>
-__global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchArgs a) {
+// ONE: the one-pass form, a kernel of its own: its sweep keeps four
+// double-float sums, three gathers per face and the new r, p and z live,
+// which needs ~96 registers (2 CTAs per SM); the two-pass kernel fits in 72
+// (3 CTAs per SM).
+template <int QP, int ONE>
+__global__ void __launch_bounds__(kThreads, ONE ? 2 : SGPU_BATCH_MINB) batch_kernel(BatchArgs a) {
   extern __shared__ __align__(128) unsigned char dyn[];
   __shared__ double s_red[4 * 8];
   __shared__ int s_flag;
@@ -1024,7 +1118,8 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
 
   // every partial-sum slot of this launch starts empty (a grid barrier orders
   // this before the first flush: in the set-up phases, or just below)
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + tid; e < (size_t)a.ntiles * 16; e += (size_t)gridDim.x * blockDim.x)
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + tid; e < (size_t)a.ntiles * 8 * kPwVals;
+       e += (size_t)gridDim.x * blockDim.x)
     ((long long*)a.tpw)[e] = kEmptyPartial;
   if (!ld_volatile_int(&a.gflags[1]))
     if (!grid_sync(ctl, 5, [] {})) return;
@@ -1053,6 +1148,10 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
           a.x32[u] = 0.f;
           a.z32[u] = 0.f;
           if (QP == 2) a.s32[u] = 0.f;
+          else {
+            a.r2_32[u] = 0.f;
+            a.z2_32[u] = 0.f;
+          }
           if (QP == 1) {
             double cc = 1.0, akeep = 0.0;
             if (act) {
@@ -1114,7 +1213,12 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
           a.r32[u] = 0.f;
           a.pa32[u] = 0.f;
           a.pb32[u] = 0.f;
+          a.z32[u] = 0.f;
           if (QP == 2) a.s32[u] = 0.f;
+          else {
+            a.r2_32[u] = 0.f;
+            a.z2_32[u] = 0.f;
+          }
           if (QP == 1) {
             const double ic = 1.0 / a.cin64[u];
             a.c64[u] = ic;
@@ -1228,64 +1332,137 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
   for (int it = 0; it < a.max_iters_chunk; ++it) {
     if (!ld_volatile_int(&a.gflags[3])) break;
 
-    // ---- A: p_new = S + mu p_old (on the fly), z = A p_new, p.z ----
-    build_list(a, P, is_run, s_wsum);
-    pipelined_phase<QP, 0>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
-      In->nu_x = 0.0;  // this phase's tiles added the pending solution increment
-      const double alpha = In->alpha;
-      In->alpha_prev = alpha;
-      In->mu = 1 / alpha;  // mu = 1/alpha before nu (2484-2485)
-      const double nu = alpha / tot[0];
-      In->nu = nu;
-      In->par ^= 1;
-      if (!isfinite(nu)) {
-        In->status = SGPU_BREAKDOWN;
-        In->flags = 2;  // final merge
-        In->state = INST_DONE;
-        atomicOr(&a.gflags[0], 1);
-      }
-    });
-    if (!grid_sync(ctl, 1, [] {})) return;
-
-    // ---- B: x32 += nu p, r -= nu z, preconditioner, r.s, r.r ----
-    build_list(a, P, is_run, s_wsum);
-    pipelined_phase<QP, 1>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
-      const double alpha = tot[0];
-      const double mu = In->mu * alpha;  // mu *= alpha (2498/2509)
-      In->mu = mu;
-      In->alpha = alpha;
-      In->nu_x = a.x_in_apply ? In->nu : 0.0;  // x32 += nu p now pending (next apply phase or R1)
-      const double eps = (QP == 2) ? tot[1] : alpha;
-      In->eps = eps;
-      const int n = In->n + 1;
-      In->n = n;
-      int flags = 0;
-      if (!isfinite(alpha) || !isfinite(mu)) {
-        In->status = SGPU_BREAKDOWN;
-        In->state = INST_DONE;
-        flags = 2;
-      } else if (eps == 0) {
-        In->state = INST_DONE;
-        flags = 2;
-      } else if (eps < In->tol2 * In->eps0 || eps < a.delta2 * In->eps_ref) {
-        flags = 1;  // verify / refresh with the FP64 true residual
-      } else if (n >= In->maxiters) {
-        In->status = SGPU_MAXITER;
-        In->state = INST_DONE;
-        flags = 2;
-      }
-      if (flags == 1 && n >= In->maxiters) flags = 1 | 4;  // last chance: verify, else stop
-      In->flags = flags;
-      if (flags) atomicOr(&a.gflags[0], 1);
-    });
-    if (!grid_sync(ctl, 2, [&] {
-          if (tid == 0) {
-            a.gflags[2] = a.gflags[0];
-            a.gflags[0] = 0;
-            __threadfence();
+    if (QP != 2 && ONE) {
+      // ---- one pass: r_j = r - nu z, x += nu p_old, p_j = r_j + mu p_old,
+      //      z_j = A p_j; p.z, r.r, r.z, z.z ----
+      // CG with the two reductions of an iteration merged (the residual step
+      // of iteration j-1 is taken in the sweep of iteration j): nu_j =
+      // r_j.r_j / p_j.z_j as in the two-pass form, and the next mu from
+      // |r_j - nu_j z_j|^2 = r.r - 2 nu r.z + nu^2 z.z of this sweep's own
+      // vectors.  The convergence test sees r_j.r_j one sweep after the
+      // two-pass form would, so a solve takes one sweep more than its
+      // iteration count.
+      build_list(a, P, is_run, s_wsum);
+      pipelined_phase<QP, 2>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
+        const double pz = tot[0], rr = tot[1], rz = tot[2], zz = tot[3];
+        const bool moved = In->nu != 0.0;  // this sweep took the pending step (not the first, nor one after a refresh)
+        const int n = In->n + (moved ? 1 : 0);
+        In->n = n;
+        In->nu_x = 0.0;
+        const double eps = rr;
+        In->eps = eps;
+        int flags = 0;
+        if (!isfinite(rr) || !isfinite(pz)) {
+          In->status = SGPU_BREAKDOWN;
+          In->state = INST_DONE;
+          flags = 2;
+        } else if (moved) {
+          if (eps == 0) {
+            In->state = INST_DONE;
+            flags = 2;
+          } else if (eps < In->tol2 * In->eps0 || eps < a.delta2 * In->eps_ref) {
+            flags = 1;  // verify / refresh with the FP64 true residual
+          } else if (n >= In->maxiters) {
+            In->status = SGPU_MAXITER;
+            In->state = INST_DONE;
+            flags = 2;
           }
-        }))
-      return;
+          if (flags == 1 && n >= In->maxiters) flags = 1 | 4;  // last chance: verify, else stop
+        }
+        if (flags == 0) {
+          const double nu = rr / pz;
+          double rnext = rr - 2.0 * nu * rz + nu * nu * zz;
+          if (!(rnext > 0.0)) rnext = 0.0;  // cancellation at convergence: restart the direction
+          if (!isfinite(nu)) {
+            In->status = SGPU_BREAKDOWN;
+            In->state = INST_DONE;
+            flags = 2;
+          } else {
+            In->alpha = rr;
+            In->nu = nu;
+            In->mu = rnext / rr;
+            In->par ^= 1;  // the sweep wrote the other buffers of p, r and z
+          }
+        } else if (flags & 1) {
+          // refresh: this sweep's direction is dropped.  R2 writes the true
+          // residual over the residual this sweep read (buffer par, kept), and
+          // the next sweep forms p_j again from it with mu = rho_true / rho_{j-1}
+          // and the direction p_{j-1} still in buffer par; x32 holds x_j, so
+          // nothing is pending.
+          In->alpha_prev = In->alpha;
+          In->nu = 0.0;
+        }
+        In->flags = flags;
+        if (flags) atomicOr(&a.gflags[0], 1);
+      });
+      if (!grid_sync(ctl, 2, [&] {
+            if (tid == 0) {
+              a.gflags[2] = a.gflags[0];
+              a.gflags[0] = 0;
+              __threadfence();
+            }
+          }))
+        return;
+    } else {
+      // ---- A: p_new = S + mu p_old (on the fly), z = A p_new, p.z ----
+      build_list(a, P, is_run, s_wsum);
+      pipelined_phase<QP, 0>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
+        In->nu_x = 0.0;  // this phase's tiles added the pending solution increment
+        const double alpha = In->alpha;
+        In->alpha_prev = alpha;
+        In->mu = 1 / alpha;  // mu = 1/alpha before nu (2484-2485)
+        const double nu = alpha / tot[0];
+        In->nu = nu;
+        In->par ^= 1;
+        if (!isfinite(nu)) {
+          In->status = SGPU_BREAKDOWN;
+          In->flags = 2;  // final merge
+          In->state = INST_DONE;
+          atomicOr(&a.gflags[0], 1);
+        }
+      });
+      if (!grid_sync(ctl, 1, [] {})) return;
+
+      // ---- B: x32 += nu p, r -= nu z, preconditioner, r.s, r.r ----
+      build_list(a, P, is_run, s_wsum);
+      pipelined_phase<QP, 1>(a, P, s_red, &s_flag, lim, [&](BInst* In, const double* tot) {
+        const double alpha = tot[0];
+        const double mu = In->mu * alpha;  // mu *= alpha (2498/2509)
+        In->mu = mu;
+        In->alpha = alpha;
+        In->nu_x = a.x_in_apply ? In->nu : 0.0;  // x32 += nu p now pending (next apply phase or R1)
+        const double eps = (QP == 2) ? tot[1] : alpha;
+        In->eps = eps;
+        const int n = In->n + 1;
+        In->n = n;
+        int flags = 0;
+        if (!isfinite(alpha) || !isfinite(mu)) {
+          In->status = SGPU_BREAKDOWN;
+          In->state = INST_DONE;
+          flags = 2;
+        } else if (eps == 0) {
+          In->state = INST_DONE;
+          flags = 2;
+        } else if (eps < In->tol2 * In->eps0 || eps < a.delta2 * In->eps_ref) {
+          flags = 1;  // verify / refresh with the FP64 true residual
+        } else if (n >= In->maxiters) {
+          In->status = SGPU_MAXITER;
+          In->state = INST_DONE;
+          flags = 2;
+        }
+        if (flags == 1 && n >= In->maxiters) flags = 1 | 4;  // last chance: verify, else stop
+        In->flags = flags;
+        if (flags) atomicOr(&a.gflags[0], 1);
+      });
+      if (!grid_sync(ctl, 2, [&] {
+            if (tid == 0) {
+              a.gflags[2] = a.gflags[0];
+              a.gflags[0] = 0;
+              __threadfence();
+            }
+          }))
+        return;
+    }
 
     if (ld_volatile_int(&a.gflags[2])) {
       auto flagged = [&](int i) { return inst_flags(a, i) != 0; };
@@ -1311,6 +1488,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
               TileInfo ti;
               load_tile(a, t, ti, sm);
               const int len = ti.end - ti.base;
+              float* rout = rbuf(a, ld_volatile_int(&a.inst[i].par));  // the residual the next sweep reads
               for (int s = tid; s < len; s += kCompute) {
                 const int c = col_of(sm.start, sm.ncols, s);
                 const int k = s - sm.start[c];
@@ -1318,7 +1496,7 @@ __global__ void __launch_bounds__(kThreads, SGPU_BATCH_MINB) batch_kernel(BatchA
                 const int ctop = sm.ctop[c], nk = sm.nk[c];
                 if (k < ctop) continue;
                 const double r = a.b64[u] - apply64<QP>(a, sm, c, u, k, ctop, nk, a.x64);
-                a.r32[u] = (float)r;
+                rout[u] = (float)r;
                 if (QP == 2) acc[1] += r * r;
                 else acc[0] += r * r;
               }
@@ -1500,6 +1678,9 @@ struct sgpu_batch {
   bool use_graph = false, graph_failed = false;
   cudaGraphExec_t gexec = nullptr;
   int g_ntiles = -1, g_ninst = -1, g_grid = -1, g_chunk = -1;
+  // the captured launch's by-value arguments that the key above does not fix
+  int g_stage = -1, g_hdr = -1, g_sfl = -1, g_fusion = -1;
+  double g_delta = -1.0;
   long long graph_launches = 0;
   // device
   std::vector<void*> allocs;
@@ -1518,9 +1699,10 @@ struct sgpu_batch {
   int ntiles = 0;
   double last_ms = 0.0;
   long long last_work = 0;
-  bool attr_set[3] = {false, false, false};
+  bool attr_set[3][2] = {};
   int streams = 4;                    // FP32 streams per pipeline stage
   int x_in_apply = 1;                 // the solution update's place (BatchArgs::x_in_apply)
+  int fusion = 1;                     // sgpu_batch_set_fusion's form: 0, 1 or 2 (one pass; qprecond 0/1)
   int dyn_smem = kDynSmem;            // dynamic shared memory of the kernel
 };
 
@@ -1563,20 +1745,23 @@ struct Guard {
   }
 };
 
-const void* kernel_of(int qp) {
-  return qp == 1 ? (const void*)batch_kernel<1> : qp == 2 ? (const void*)batch_kernel<2> : (const void*)batch_kernel<0>;
+const void* kernel_of(int qp, bool one) {
+  if (one) return qp == 1 ? (const void*)batch_kernel<1, 1> : (const void*)batch_kernel<0, 1>;
+  return qp == 1 ? (const void*)batch_kernel<1, 0>
+                 : qp == 2 ? (const void*)batch_kernel<2, 0> : (const void*)batch_kernel<0, 0>;
 }
 }  // namespace
 
-static int batch_max_grid(sgpu_batch* b) {
-  const void* fn = kernel_of(b->qprecond);
-  if (!b->attr_set[b->qprecond]) {
-    // the largest stage configuration any batch may use, so that batches of
-    // different face counts sharing the kernel never find the limit too low
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_bytes(4 + kMaxF)) !=
+static int batch_max_grid(sgpu_batch* b, bool one) {
+  const void* fn = kernel_of(b->qprecond, one);
+  if (!b->attr_set[b->qprecond][one]) {
+    // the largest stage configuration any batch may use (the one-pass form's
+    // 5 + F streams at 8 faces), so that batches of different face counts and
+    // forms sharing the kernel never find the limit too low
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_bytes(5 + kMaxF)) !=
         cudaSuccess)
       return 0;
-    b->attr_set[b->qprecond] = true;
+    b->attr_set[b->qprecond][one] = true;
   }
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -1674,13 +1859,18 @@ int sgpu_batch_create(int device, int qprecond, int maxfaces, long long max_slot
   if ((rc = balloc(b, &a.pb32, S))) return rc;
   if ((rc = balloc(b, &a.x32, S))) return rc;
   if ((rc = balloc(b, &a.z32, S))) return rc;
+  if (qprecond != 2) {
+    if ((rc = balloc(b, &a.r2_32, S))) return rc;
+    if ((rc = balloc(b, &a.z2_32, S))) return rc;
+  }
   if ((rc = balloc(b, &a.tpart, 2 * ((size_t)b->max_tiles + 1)))) return rc;
-  if ((rc = balloc(b, &a.tpw, 16 * ((size_t)b->max_tiles + 1)))) return rc;
+  if ((rc = balloc(b, &a.tpw, 8 * kPwVals * ((size_t)b->max_tiles + 1)))) return rc;
   if ((rc = balloc(b, &b->d_inst, (size_t)max_instances))) return rc;
   if ((rc = balloc(b, &b->d_ctl, 1))) return rc;
   if ((rc = balloc(b, &b->d_gflags, 4))) return rc;
   // padding slots are copied by the bulk copies but never used: keep them finite
-  float* f32s[] = {a.fz32, a.cinv32, a.coef32, a.r32, a.pa32, a.pb32, a.x32, a.z32, a.s32, a.tw32, a.tib32};
+  float* f32s[] = {a.fz32, a.cinv32, a.coef32, a.r32, a.pa32, a.pb32, a.x32, a.z32, a.r2_32, a.z2_32, a.s32,
+                   a.tw32, a.tib32};
   for (float* p : f32s)
     if (p) BCK(cudaMemsetAsync(p, 0, S * sizeof(float), b->stream));
   BCK(cudaMemsetAsync(a.coef64, 0, S * sizeof(double), b->stream));
@@ -2036,14 +2226,15 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
   // far below the 10 KB a tile of 128 shallow columns needs), which leaves
   // room for three CTAs per SM with the apply phase's 4 + F streams
   const int hdr_cap = std::min(kHdrCap, (kStageHdrOff + max_hdr + 127) & ~127);
-  const int streams = b->x_in_apply ? b->streams : std::max(b->streams - 1, 4);
+  const bool one_pass = b->fusion == 2 && b->qprecond != 2;
+  const int streams = one_pass ? b->streams + 1 : (b->x_in_apply ? b->streams : std::max(b->streams - 1, 4));
   // streams sized to the launch's largest tile (+1 group of 4: the vertical
   // coefficient stream reads one slot past the tile)
   const int stream_floats = std::min(kStreamFloats, ((max_slots + 3) & ~3) + 4);
   const int stage_bytes =
       std::max(hdr_cap + streams * 4 * stream_floats, (int)((sizeof(TileSmem) + 127) & ~127));
   b->dyn_smem = dyn_smem_bytes_for(stage_bytes);
-  int maxg = batch_max_grid(b);
+  int maxg = batch_max_grid(b, one_pass);
   if (maxg <= 0) return bfail(b, SGPU_CUDA_ERROR, "occupancy query failed");
   int grid = b->grid_override > 0 ? std::min(b->grid_override, maxg) : maxg;
   grid = std::max(1, std::min(grid, ntiles));
@@ -2063,6 +2254,8 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
   b->h_gflags[3] = any_run;
   const int chunk = max_iters > 0 ? max_iters : 0x7fffffff;
   const bool key_same = b->g_ntiles == ntiles && b->g_ninst == ninst && b->g_grid == grid && b->g_chunk == chunk &&
+                        b->g_stage == stage_bytes && b->g_hdr == hdr_cap && b->g_sfl == stream_floats &&
+                        b->g_fusion == b->fusion && b->g_delta == b->delta &&
                         !tiles_changed;
   cudaStream_t st = b->stream;
   auto enqueue = [&]() -> cudaError_t {
@@ -2078,6 +2271,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     a.hdr_cap = hdr_cap;
     a.stream_floats = stream_floats;
     a.x_in_apply = b->x_in_apply;
+    a.one_pass = one_pass ? 1 : 0;
     a.ntiles = ntiles;
     a.ninst = ninst;
     a.max_iters_chunk = chunk;
@@ -2096,7 +2290,7 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
     // the instance table and status come back in sgpu_batch_wait, after the
     // stream has drained: a device-to-host copy queued behind the kernel here
     // would hold up the read-backs of finished problems on the other stream
-    return cudaLaunchKernelExC(&cfg, kernel_of(b->qprecond), args);
+    return cudaLaunchKernelExC(&cfg, kernel_of(b->qprecond, one_pass), args);
   };
   std::memcpy(b->h_inst_up, b->h_inst, sizeof(BInst) * ninst);
   BCK(cudaEventRecord(b->ev0, st));
@@ -2126,6 +2320,11 @@ int sgpu_batch_launch(sgpu_batch* b, int max_iters) {
         b->g_ninst = ninst;
         b->g_grid = grid;
         b->g_chunk = chunk;
+        b->g_stage = stage_bytes;
+        b->g_hdr = hdr_cap;
+        b->g_sfl = stream_floats;
+        b->g_fusion = b->fusion;
+        b->g_delta = b->delta;
       }
     }
     if (b->gexec) {
@@ -2302,15 +2501,17 @@ int sgpu_batch_set(sgpu_batch* b, double delta, int grid, long long timeout_ns) 
   return SGPU_OK;
 }
 
-int sgpu_batch_set_fusion(sgpu_batch* b, int x_in_apply) {
-  if (!b || (x_in_apply != 0 && x_in_apply != 1)) return SGPU_BAD_ARG;
+int sgpu_batch_set_fusion(sgpu_batch* b, int form) {
+  if (!b || form < 0 || form > 2) return SGPU_BAD_ARG;
   if (b->inflight) return bfail(b, SGPU_BAD_ARG, "a launch is in flight");
-  // a problem in mid-solve may hold a deferred solution increment (nu_x) that
-  // only the deferring form applies: change the form between solves only
+  // a problem in mid-solve holds state that only its form reads (a deferred
+  // solution increment, the one-pass form's pending step and buffer parity):
+  // change the form between solves only
   for (int i = 0; i < b->max_inst; ++i)
-    if (b->inst[i].live && b->h_inst[i].state == INST_RUN && x_in_apply != b->x_in_apply)
+    if (b->inst[i].live && b->h_inst[i].state == INST_RUN && form != b->fusion)
       return bfail(b, SGPU_BAD_ARG, "problem %d is in mid-solve", i);
-  b->x_in_apply = x_in_apply;
+  b->fusion = form;
+  b->x_in_apply = form >= 1 ? 1 : 0;  // qprecond 2 runs form 2 as form 1
   return SGPU_OK;
 }
 

@@ -24,11 +24,12 @@ constexpr int kBufBytes = kHdrCap + 4 * kStreamBytes;       // the smallest pipe
 // A stage holds the descriptor and header (at most kHdrCap bytes; each launch
 // sizes it to its largest tile header) and `streams` = 4 + F FP32 streams (p,
 // s, coef, one face-weight stream per face and x; the update phase uses 2 of
-// them, and 4 as scratch for qprecond 2).
+// them, and 4 as scratch for qprecond 2), or 5 + F in the one-pass form (+ z).
 __host__ __device__ constexpr int stage_bytes_for(int streams) { return kHdrCap + streams * kStreamBytes; }
 __host__ __device__ constexpr int stage_bytes_for(int hdr_cap, int streams) { return hdr_cap + streams * kStreamBytes; }
 static_assert(kBTCols <= 256, "the header's slot-to-column map holds one byte per slot");
 constexpr int kListCap = 512;    // tiles per CTA per phase
+constexpr int kPwVals = 4;       // partial sums per warp slot (the one-pass form reduces four)
 // dynamic shared memory of the kernel: 2 stages, 4 mbarriers (32 B), the tile list
 __host__ __device__ constexpr int dyn_smem_bytes(int streams) { return 2 * stage_bytes_for(streams) + 32 + 4 * kListCap; }
 __host__ __device__ constexpr int dyn_smem_bytes_for(int stage_bytes) { return 2 * stage_bytes + 32 + 4 * kListCap; }
@@ -87,7 +88,8 @@ struct __align__(64) BInst {
   int status;          // SGPU_* code
   int flags;           // bit0: reliable update now; bit1: final merge; bit2: last chance at maxiters
   int cnt;             // tiles finished in the current phase (the last flush reduces)
-  int par;             // which p buffer holds the current direction
+  int par;             // which p buffer holds the current direction (and, in the one-pass
+                       // form, which r and z buffers hold the current residual and A p)
   int nrel;            // reliable updates done
   int s2;              // end of the instance's storage (boundary columns in [s1, s2))
   double alpha, eps, eps0, eps_ref;   // CG scalars (FP64)
@@ -96,7 +98,9 @@ struct __align__(64) BInst {
   double nu_x;         // the solution increment nu_x * p still to add to x32 (p = the
                        // direction of the last update phase): the next apply phase
                        // adds it where it streams that direction anyway, or the
-                       // reliable update adds it; 0 when nothing is pending
+                       // reliable update adds it; 0 when nothing is pending.  The
+                       // one-pass form keeps its pending step in nu instead (applied
+                       // to r and x by the next pass) and leaves nu_x at 0
 };
 
 // Column metadata (one entry per computational column, global column index),
@@ -124,6 +128,9 @@ struct BatchArgs {
   int stream_floats;   // floats per stage stream: the launch's largest tile + 4
   int x_in_apply;      // 1: the solution update x32 += nu p runs in the next apply pass, where
                        // p is streamed anyway; 0: in the update pass (streams p and x there)
+  int one_pass;        // 1 (qprecond 0/1): one pass per iteration -- r -= nu z, x += nu p,
+                       // p = r + mu p and z = A p in one sweep, mu from the pass's inner
+                       // products (r, z and p double-buffered); 0: the two passes above
   int ntiles;
   int ninst;           // instance slots in use (some may be EMPTY/DONE)
   int max_iters_chunk; // global iterations allowed in this launch
@@ -162,9 +169,11 @@ struct BatchArgs {
   float* pb32;
   float* x32;            // [nslots] FP32 correction accumulated since the last reliable update
   float* z32;            // [nslots]
+  float* r2_32;          // [nslots] second residual buffer (one-pass form; qprecond 0/1)
+  float* z2_32;          // [nslots] second A p buffer (one-pass form; qprecond 0/1)
   // per-CTA partial sums [ntiles*2] of the simple phases and instance table
   double* tpart;
-  double* tpw;           // [ntiles*8*2] per-warp partial sums of the pipelined phases
+  double* tpw;           // [ntiles*8*kPwVals] per-warp partial sums of the pipelined phases
   BInst* inst;
   SolveCtl* ctl;         // grid barrier
   int* gflags;           // [4]: 0 any reliable flag, 2 its snapshot, 3 any instance running

@@ -50,14 +50,16 @@ def tri_grids():
     ]
 
 
+@pytest.mark.parametrize("form", [1, 2])
 @pytest.mark.parametrize("qprecond", [0, 1, 2])
 @pytest.mark.parametrize("gname", ["quad16x8", "quad64x16x32", "tri3000_partial", "tri400_shallow"])
-def test_single_problem_matches_oracle(gpu_lib, oracle, qprecond, gname):
+def test_single_problem_matches_oracle(gpu_lib, oracle, qprecond, gname, form):
     g = dict(grid_cases())[gname]()
     prob = gg.make_q_problem(g, seed=1, q0_sigma=0.01)
     pr = q_props(qprecond)
     q_ref, n_ref = oracle.cgsolveq(prob, pr)
     b = Batch(qprecond=qprecond, maxfaces=g.maxfaces, **capacity_for([g]))
+    b.set_fusion(form)
     i = b.add(prob, tol=pr.qepsilon, maxiters=pr.qmaxiters)
     running, ms, work = b.run()
     assert running == 0
@@ -265,15 +267,15 @@ def test_overlapped_launch_wait_equals_solo(gpu_lib):
 
 @pytest.mark.parametrize("qprecond", [0, 1, 2])
 def test_fusion_forms_equal_bitwise(gpu_lib, qprecond):
-    """The solution update run in the next apply pass (x_in_apply 1, the
-    default) or in the update pass (0): the same FP32 operations on the same
-    operands, so the same bits and iteration counts; also across chunked
-    launches (the increment deferred past a launch boundary and into the
-    reliable updates), and MAXITER stops."""
+    """The solution update run in the next apply pass (form 1, the default) or
+    in the update pass (0): the same FP32 operations on the same operands, so
+    the same bits and iteration counts; also across chunked launches (the
+    increment deferred past a launch boundary and into the reliable updates),
+    and MAXITER stops.  qprecond 2 runs the one-pass form (2) as form 1."""
     grids = tri_grids()
     probs = [gg.make_q_problem(g, seed=60 + k, q0_sigma=0.01) for k, g in enumerate(grids)]
     out = {}
-    for form in (0, 1):
+    for form in ((0, 1, 2) if qprecond == 2 else (0, 1)):
         for chunk in (0, 7):
             b = Batch(qprecond=qprecond, maxfaces=3, **capacity_for(grids))
             b.set_fusion(form)
@@ -290,6 +292,60 @@ def test_fusion_forms_equal_bitwise(gpu_lib, qprecond):
         for (q, st), (q0, st0) in zip(res, ref):
             assert st.status == st0.status and st.niters == st0.niters, key
             assert np.array_equal(q, q0), key
+
+
+@pytest.mark.parametrize("qprecond", [0, 1])
+def test_one_pass_form_matches_oracle(gpu_lib, oracle, qprecond):
+    """The one-pass form (2): every problem meets the reference's stopping rule
+    on the FP64 true residual and the accuracy bar of the two-pass form against
+    the oracle, with iteration counts within the same bounds; its bits do not
+    depend on chunked launches (the pending step and the buffer parity carried
+    across launch boundaries and reliable updates) and a MAXITER stop is
+    reported at the limit."""
+    grids = tri_grids()
+    probs = [gg.make_q_problem(g, seed=80 + k, q0_sigma=0.01) for k, g in enumerate(grids)]
+    pr = q_props(qprecond)
+    out = {}
+    for chunk in (0, 7):
+        b = Batch(qprecond=qprecond, maxfaces=3, **capacity_for(grids))
+        b.set_fusion(2)
+        ids = [b.add(p, tol=pr.qepsilon, maxiters=25 if k == 0 else pr.qmaxiters) for k, p in enumerate(probs)]
+        while True:
+            running, _, _ = b.run(max_iters=chunk)
+            if running == 0:
+                break
+        out[chunk] = [b.result(i, p.q) for i, p in zip(ids, probs)]
+        b.close()
+    for (q, st), (q0, st0) in zip(out[7], out[0]):
+        assert st.status == st0.status and st.niters == st0.niters
+        assert np.array_equal(q, q0)
+    assert out[0][0][1].status == MAXITER and out[0][0][1].niters == 25
+    for p, (q, st) in list(zip(probs, out[0]))[1:]:
+        q_ref, n_ref = oracle.cgsolveq(p, pr)
+        assert st.status == OK
+        assert close_iters(st.niters, n_ref, qprecond), (st.niters, n_ref)
+        check_accuracy(oracle, p, q, q_ref, qprecond)
+        m = p.grid.active_mask()
+        assert np.array_equal(q[~m], p.q[~m])
+
+
+def test_one_pass_form_alone_equals_in_batch(gpu_lib):
+    """A problem's one-pass solve does not depend on the rest of the batch."""
+    grids = tri_grids()
+    probs = [gg.make_q_problem(g, seed=90 + k) for k, g in enumerate(grids)]
+    b = Batch(qprecond=1, maxfaces=3, **capacity_for([grids[1]]))
+    b.set_fusion(2)
+    i = b.add(probs[1])
+    b.run()
+    alone = b.result(i, probs[1].q)
+    b.close()
+    b = Batch(qprecond=1, maxfaces=3, **capacity_for(grids))
+    b.set_fusion(2)
+    ids = [b.add(p) for p in probs]
+    b.run()
+    q, st = b.result(ids[1], probs[1].q)
+    b.close()
+    assert st.niters == alone[1].niters and np.array_equal(q, alone[0])
 
 
 def test_fusion_change_refused_mid_solve(gpu_lib):
@@ -310,7 +366,7 @@ def test_autotune_sweeps_the_three_knobs(gpu_lib):
     grids = tri_grids()
     probs = [gg.make_q_problem(g, seed=70 + k) for k, g in enumerate(grids)]
     best, table = autotune(probs, qprecond=1, iters=4, ctas_per_sm=(1, 2), tile_slots=(512, 1024))
-    assert len(table) == 2 * 2 * 2
-    assert {(r["ctas_per_sm"], r["tile_slots"], r["x_in_apply"]) for r in table} == \
-        {(c, t, f) for c in (1, 2) for t in (512, 1024) for f in (0, 1)}
+    assert len(table) == 2 * 2 * 3
+    assert {(r["ctas_per_sm"], r["tile_slots"], r["fusion"]) for r in table} == \
+        {(c, t, f) for c in (1, 2) for t in (512, 1024) for f in (0, 1, 2)}
     assert best["rate"] > 0 and best["rate"] == max(r["rate"] for r in table)
