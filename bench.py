@@ -112,6 +112,8 @@ def parse():
                     help="cfg5: resident copies a hot grid may have (1: one request per grid at a time, "
                          "results bit-identical alone and in the mix)")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--mixed-shape", default=None,
+                    help="cfg2/cfg3 mixed form: FORM,CTAS_PER_SM,TILE_SLOTS instead of the autotuner's pick")
     ap.add_argument("--graph", action="store_true",
                     help="cfg5: replay launches from CUDA graphs (re-captured whenever the set of problems changes)")
     ap.add_argument("--qprecond", type=int, default=1)
@@ -643,7 +645,7 @@ def run_ours(args):
         # the same pressure problem through the mixed-precision batched solver
         q64 = ctx.q_download(qp.q)
         it64 = int(np.median(nq))
-        shape, _ = mixed_shape(qp, props.qprecond, props.qepsilon, props.qmaxiters, local)
+        shape, _ = mixed_shape(qp, props.qprecond, props.qepsilon, props.qmaxiters, local, args.mixed_shape)
         mf, _, _ = mixed_form(qp, props.qprecond, max(2, min(args.steps, 5)), 3, props.qepsilon, props.qmaxiters,
                               local, q64, it64, shape=shape)
         plain_q_rate = g.n_q() * it64 / (q_launch_ms / 1e3)
@@ -746,11 +748,15 @@ def batch_timed(b, ids, steps, warmup, tol, maxiters, device):
     return ev0.elapsed_time(ev1), per, clocks
 
 
-def mixed_shape(prob, qprecond, tol, maxiters, device):
+def mixed_shape(prob, qprecond, tol, maxiters, device, fixed=None):
     """The batched solver's launch shape for one large problem, picked by the
     engine's autotuner: the iteration form (one pass, or two with the solution
-    update in the apply pass) at 2 and 3 CTAs per SM, 1024-slot tiles."""
+    update in the apply pass) at 2 and 3 CTAs per SM, 1024-slot tiles.
+    fixed: "FORM,CTAS_PER_SM,TILE_SLOTS" to skip the search."""
     from suntans_gb300.autotune import autotune
+    if fixed:
+        f, c, t = (int(v) for v in fixed.split(","))
+        return {"fusion": f, "ctas_per_sm": c, "tile_slots": t, "rate": None}, []
     best, table = autotune([prob], qprecond=qprecond, tol=tol, maxiters=maxiters, iters=8, ctas_per_sm=(2, 3),
                            tile_slots=(1024,), fusion=(2, 1), device=device)
     return best, table
@@ -903,7 +909,7 @@ def bench_cfg3(args, keep=None):
     q64 = ctx.q_download(qp.q)
     plain_rate = N * s64.niters / (s64.ms_solve / 1e3)
     ctx.close()
-    shape, shape_table = mixed_shape(qp, args.qprecond, 1e-10, 20000, local)
+    shape, shape_table = mixed_shape(qp, args.qprecond, 1e-10, 20000, local, args.mixed_shape)
     mf, clocks, q_mix = mixed_form(qp, args.qprecond, args.steps, args.warmup, 1e-10, 20000, local, q64, s64.niters,
                                    shape=shape)
     if keep is not None:

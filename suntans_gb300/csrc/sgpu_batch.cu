@@ -1134,6 +1134,22 @@ __global__ void __launch_bounds__(kThreads, ONE ? 2 : SGPU_BATCH_MINB) batch_ker
         TileInfo ti;
         load_tile(a, t, ti, sm);
         const int len = ti.end - ti.base;
+        if (QP == 1) {
+          // the unscaled vertical coefficient of every wet slot first (one FP64
+          // division per slot): a slot's diagonal also needs the coefficient
+          // of the slot below, 2 Ac/(dzz[k+1] + dzz[k]), which is that slot's
+          // own -- the same operands in the same order, so the same bits
+          for (int s = tid; s < len; s += kCompute) {
+            const int c = col_of(sm.start, sm.ncols, s);
+            const int k = s - sm.start[c];
+            const int u = ti.base + s;
+            const int ctop = sm.ctop[c];
+            const double dz = a.dzz64[u];
+            const double Ac = a.colAc[ti.c0 + c];
+            a.coef64[u] = k < ctop ? 0.0 : (k == ctop) ? Ac / dz : 2 * Ac / (dz + a.dzz64[u - 1]);
+          }
+          csync();
+        }
         for (int s = tid; s < len; s += kCompute) {
           const int c = col_of(sm.start, sm.ncols, s);
           const int k = s - sm.start[c];
@@ -1153,7 +1169,7 @@ __global__ void __launch_bounds__(kThreads, ONE ? 2 : SGPU_BATCH_MINB) batch_ker
             a.z2_32[u] = 0.f;
           }
           if (QP == 1) {
-            double cc = 1.0, akeep = 0.0;
+            double cc = 1.0;
             if (act) {
               double diag = 0.0;
               for (int f = 0; f < F; ++f) {
@@ -1161,12 +1177,11 @@ __global__ void __launch_bounds__(kThreads, ONE ? 2 : SGPU_BATCH_MINB) batch_ker
                 if (k < (kk & 0xffff) || k >= (kk >> 16)) continue;
                 diag += dz * a.face[(size_t)(ti.c0 + c) * F + f].D64;
               }
-              const double ak = (k == ctop) ? Ac / dz : 2 * Ac / (dz + a.dzz64[u - 1]);
-              akeep = ak;  // the unscaled vertical coefficient, scaled in S2
+              const double ak = a.coef64[u];  // Ac/dzz or 2 Ac/(dzz + dzz above); scaled in S2
               if (ctop < nk - 1) {
-                if (k == ctop) diag += 2 * ak + 2 * Ac / (a.dzz64[u + 1] + dz);
+                if (k == ctop) diag += 2 * ak + a.coef64[u + 1];
                 else if (k == nk - 1) diag += ak;
-                else diag += ak + 2 * Ac / (a.dzz64[u + 1] + dz);
+                else diag += ak + a.coef64[u + 1];
               }
               if (diag <= 0) diag = 1;
               cc = sqrt(diag);
@@ -1175,7 +1190,6 @@ __global__ void __launch_bounds__(kThreads, ONE ? 2 : SGPU_BATCH_MINB) batch_ker
             // in the scaled coefficients (S2) and one in the rescale
             const double ic = 1.0 / cc;
             a.c64[u] = ic;
-            a.coef64[u] = akeep;
             a.cinv32[u] = (float)ic;
             a.fz32[u] = (float)(dz * ic);
             a.x64[u] = act ? a.q64[u] * cc : 0.0;
