@@ -86,7 +86,10 @@ __device__ __forceinline__ double apply_slot(const QArgs& a, const double* __res
       if (k >= kmin && k < kmax) y += xin[a.fnoff[j * F + f] + k] * a.fc[(size_t)f * a.n3c + u];
     }
     if (k > ctop && k < nk - 1) {
-      y += a.coef[u] * xin[u - 1] + a.coef[u + 1] * xin[u + 1];
+      // the two vertical terms as two FMAs into y (GB300's FP64 pipe is the
+      // kernel's limit: a product, an FMA and an add would be three)
+      y = __fma_rn(a.coef[u], xin[u - 1], y);
+      y = __fma_rn(a.coef[u + 1], xin[u + 1], y);
     } else if (ctop < nk - 1) {
       if (k == ctop) y += a.coef[u + 1] * xin[u + 1];
       else y += a.coef[u] * xin[u - 1];  // k == nk-1
@@ -140,15 +143,16 @@ __device__ __forceinline__ double apply_flat(const QArgs& a, const double* __res
     const bool ok = act && meta >= 0 && k >= (meta & 0xffff) && k < (meta >> 16);
     const int n = ok ? a.fnoff[j * F + f] + k : u;
     const double w = a.fc[(size_t)f * a.n3c + u];
-    if (QP == 1) y += xin[n] * w;
-    else y += (xin[n] - xu) * w;
+    if (QP == 1) y = __fma_rn(xin[n], w, y);
+    else y = __fma_rn(xin[n] - xu, w, y);
   }
   const double xm = xin[u > 0 ? u - 1 : 0], xp = xin[u + 1];
   const double c0 = a.coef[u], c1 = a.coef[u + 1];
   if (QP == 1) {
     const double cm = (act && k > ctop) ? c0 : 0.0;
     const double cp = (act && k < nk - 1) ? c1 : 0.0;
-    y += cm * xm + cp * xp;
+    y = __fma_rn(cm, xm, y);  // two FMAs, as in apply_slot
+    y = __fma_rn(cp, xp, y);
   } else if (ctop < nk - 1) {
     if (k == ctop) y += (-2 * c0 - c1) * xu + c1 * xp;
     else if (k == nk - 1) y += c0 * xm - c0 * xu;
@@ -439,6 +443,9 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
   }
 
   // ---- the CG loop (2478-2525) ----
+  // Every update and inner-product term is one explicit FMA: the loop is
+  // bound by GB300's FP64 pipe, and a product and a sum issued apart would
+  // cost two of its slots.
   // x += nu p (2506-2507) is carried out in C, where p is read anyway, before
   // p changes: the same operation on the same operands, one read and one
   // write of p fewer per iteration.  When the loop ends after B, the last one
@@ -459,20 +466,20 @@ SGPU_Q_APPLY_UNROLL
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
           const double zu = apply_flat<QP, 3>(a, a.p, u);
           a.z[u] = zu;
-          part[0] += a.p[u] * zu;
+          part[0] = __fma_rn(a.p[u], zu, part[0]);
         }
       } else if (F == 4) {
 SGPU_Q_APPLY_UNROLL
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
           const double zu = apply_flat<QP, 4>(a, a.p, u);
           a.z[u] = zu;
-          part[0] += a.p[u] * zu;
+          part[0] = __fma_rn(a.p[u], zu, part[0]);
         }
       } else {
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
           const double zu = apply_flat<QP, 0>(a, a.p, u);
           a.z[u] = zu;
-          part[0] += a.p[u] * zu;
+          part[0] = __fma_rn(a.p[u], zu, part[0]);
         }
       }
       cta_sum<1, kBlock>(part, s_red);
@@ -497,9 +504,9 @@ SGPU_Q_APPLY_UNROLL
         const int T = G * kBlock;
 #pragma unroll 4
         for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
-          const double ru = a.r[u] - nu * a.z[u];
+          const double ru = __fma_rn(-nu, a.z[u], a.r[u]);
           a.r[u] = ru;
-          part[0] += ru * ru;
+          part[0] = __fma_rn(ru, ru, part[0]);
         }
       }
       // qprecond 2: the tile's r, Thomas factors and coefficients are staged
@@ -570,8 +577,8 @@ SGPU_Q_APPLY_UNROLL
 #pragma unroll 4
       for (int u = blockIdx.x * kBlock + tid; u < a.n3c; u += T) {
         const double pu = a.p[u];
-        a.x[u] += nu * pu;
-        a.p[u] = src[u] + mu * pu;
+        a.x[u] = __fma_rn(nu, pu, a.x[u]);
+        a.p[u] = __fma_rn(mu, pu, src[u]);
       }
       x_pending = false;
       if (!grid_wait(ctl, ++nbar * G, 6)) return;
