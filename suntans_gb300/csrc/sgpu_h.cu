@@ -221,14 +221,14 @@ __global__ void __launch_bounds__(kHBlock, 1) cgsolve_kernel(HArgs a) {
           const double w0 = HF(f, j0), w1 = HF(f, j1);
           const double q0 = (k0 >= lo && k0 < hi) ? sp[k0 - lo] : hdir(sv, po, mu, k0);
           const double q1 = (k1 >= lo && k1 < hi) ? sp[k1 - lo] : hdir(sv, po, mu, k1);
-          y0 -= w0 * q0;
-          y1 -= w1 * q1;
+          y0 = __fma_rn(-w0, q0, y0);
+          y1 = __fma_rn(-w1, q1, y1);
         }
         sz[j0 - lo] = y0;
-        pz += p0 * y0;
+        pz = __fma_rn(p0, y0, pz);
         if (two) {
           sz[j1 - lo] = y1;
-          pz += p1 * y1;
+          pz = __fma_rn(p1, y1, pz);
         }
       });
     } else {
@@ -239,16 +239,16 @@ __global__ void __launch_bounds__(kHBlock, 1) cgsolve_kernel(HArgs a) {
           const size_t o0 = (size_t)f * nc + j0, o1 = (size_t)f * nc + j1;
           const int k0 = hn[o0], k1 = hn[o1];
           const double w0 = hf[o0], w1 = hf[o1];
-          y0 -= w0 * hdir(sv, po, mu, k0);
-          y1 -= w1 * hdir(sv, po, mu, k1);
+          y0 = __fma_rn(-w0, hdir(sv, po, mu, k0), y0);
+          y1 = __fma_rn(-w1, hdir(sv, po, mu, k1), y1);
         }
         pn[j0] = p0;
         z[j0] = y0;
-        pz += p0 * y0;
+        pz = __fma_rn(p0, y0, pz);
         if (two) {
           pn[j1] = p1;
           z[j1] = y1;
-          pz += p1 * y1;
+          pz = __fma_rn(p1, y1, pz);
         }
       });
     }
@@ -276,8 +276,9 @@ __global__ void __launch_bounds__(kHBlock, 1) cgsolve_kernel(HArgs a) {
     cells2(lo + tid, hi, kHBlock, [&](int j0, int j1, bool two) {
       const double pa = SM ? sp[j0 - lo] : pn[j0], pb = SM ? sp[j1 - lo] : pn[j1];
       const double za = SM ? sz[j0 - lo] : z[j0], zb = SM ? sz[j1 - lo] : z[j1];
-      const double ra = r[j0] - nu * za, rb = r[j1] - nu * zb;
-      const double xa = x[j0] + nu * pa, xb = x[j1] + nu * pb;
+      // one explicit FMA per update and inner-product term (FP64-pipe bound)
+      const double ra = __fma_rn(-nu, za, r[j0]), rb = __fma_rn(-nu, zb, r[j1]);
+      const double xa = __fma_rn(nu, pa, x[j0]), xb = __fma_rn(nu, pb, x[j1]);
       double sa = 0.0, sb = 0.0;
       if (HP == 1) {
         sa = ra * IHC(j0);
@@ -287,20 +288,20 @@ __global__ void __launch_bounds__(kHBlock, 1) cgsolve_kernel(HArgs a) {
       r[j0] = ra;
       if (HP == 1) {
         rt[j0] = sa;
-        rs += ra * sa;
-        rr += ra * ra;
+        rs = __fma_rn(ra, sa, rs);
+        rr = __fma_rn(ra, ra, rr);
       } else {
-        rs += ra * ra;
+        rs = __fma_rn(ra, ra, rs);
       }
       if (two) {
         x[j1] = xb;
         r[j1] = rb;
         if (HP == 1) {
           rt[j1] = sb;
-          rs += rb * sb;
-          rr += rb * rb;
+          rs = __fma_rn(rb, sb, rs);
+          rr = __fma_rn(rb, rb, rr);
         } else {
-          rs += rb * rb;
+          rs = __fma_rn(rb, rb, rs);
         }
       }
     });
