@@ -139,9 +139,9 @@ __device__ __forceinline__ double apply_flat(const QArgs& a, const double* __res
   double y = (QP == 1) ? -xu : 0.0;
 #pragma unroll
   for (int f = 0; f < F; ++f) {
-    const int meta = a.fmeta[j * F + f];
-    const bool ok = act && meta >= 0 && k >= (meta & 0xffff) && k < (meta >> 16);
-    const int n = ok ? a.fnoff[j * F + f] + k : u;
+    // the neighbour slot comes straight from the slot (set-up S1), so the
+    // gather waits on one load, not on the slot's column metadata first
+    const int n = a.nslot[(size_t)f * a.n3c + u];
     const double w = a.fc[(size_t)f * a.n3c + u];
     if (QP == 1) y = __fma_rn(xin[n], w, y);
     else y = __fma_rn(xin[n] - xu, w, y);
@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
             a.fnoff[j * F + f] = a.dcoff[nb];
           }
           const bool on = act && k >= kmin && k < kmax;
+          a.nslot[(size_t)f * a.n3c + u] = on ? a.dcoff[nb] + k : u;
           if (QP != 1) {
             a.fc[(size_t)f * a.n3c + u] = on ? a.dzf[a.eoff[e] + k] * a.D[e] : 0.0;
           } else {
@@ -295,6 +296,7 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
             a.fmeta[j * F + f] = -1;
             a.fnoff[j * F + f] = 0;
           }
+          a.nslot[(size_t)f * a.n3c + u] = u;
           a.fc[(size_t)f * a.n3c + u] = 0.0;
         }
       }

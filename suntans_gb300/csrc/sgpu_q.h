@@ -39,6 +39,8 @@ struct QArgs {
   int* fnoff;           // [ncomp*F] neighbour column storage offset
   double* coef;         // [n3+1]
   double* fc;           // [F*n3c]
+  int* nslot;           // [F*n3c] neighbour slot of each slot and face (the slot
+                        // itself where the face does not couple: fc is 0 there)
   double* c;            // [n3]
   double* tw;           // [n3c] Thomas multipliers
   double* tib;          // [n3c] Thomas inverse pivots
