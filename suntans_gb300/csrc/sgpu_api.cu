@@ -52,6 +52,7 @@ struct sgpu_context {
   // pressure solve buffers
   bool q_ready = false;
   int *d_ctop = nullptr, *d_fmeta = nullptr, *d_fnoff = nullptr, *d_nslot = nullptr;
+  unsigned char* d_sflag = nullptr;
   double *d_dzz = nullptr, *d_dzf = nullptr, *d_Dq = nullptr, *d_qin = nullptr, *d_srcin = nullptr,
          *d_cin = nullptr, *d_coef = nullptr, *d_fc = nullptr, *d_c = nullptr, *d_tw = nullptr,
          *d_tib = nullptr, *d_x = nullptr, *d_p = nullptr, *d_r = nullptr, *d_z = nullptr, *d_rt = nullptr;
@@ -399,6 +400,7 @@ static int alloc_q(sgpu_context* ctx) {
   if ((rc = dalloc(ctx, &ctx->d_tib, n3c))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_fc, n3c * ctx->F))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_nslot, n3c * ctx->F))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_sflag, n3c))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_dzf, ctx->ne3 + 1))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_Dq, ctx->Ne + 1))) return rc;
   CK(cudaMemsetAsync(ctx->d_coef, 0, n3 * sizeof(double), ctx->stream));
@@ -565,6 +567,7 @@ int sgpu_q_solve(sgpu_context* ctx, const sgpu_props* prop, sgpu_stats* st) {
   a.coef = ctx->d_coef;
   a.fc = ctx->d_fc;
   a.nslot = ctx->d_nslot;
+  a.sflag = ctx->d_sflag;
   a.c = ctx->d_c;
   a.tw = ctx->d_tw;
   a.tib = ctx->d_tib;

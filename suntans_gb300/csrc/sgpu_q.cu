@@ -131,10 +131,9 @@ __device__ __forceinline__ double apply_slot(const QArgs& a, const double* __res
 template <int QP, int FF>
 __device__ __forceinline__ double apply_flat(const QArgs& a, const double* __restrict__ xin, int u) {
   const int F = FF ? FF : a.F;
-  const int j = a.slotcol[u];
-  const int k = u - a.dcoff[j];
-  const int ctop = a.ctop[j], nk = a.nk[j];
-  const bool act = k >= ctop;
+  // the slot's wet / upper / lower-neighbour bits (set-up S1): no column lookup
+  const int fl = a.sflag[u];
+  const bool act = fl & 1, up = fl & 2, dn = fl & 4;
   const double xu = xin[u];
   double y = (QP == 1) ? -xu : 0.0;
 #pragma unroll
@@ -149,13 +148,13 @@ __device__ __forceinline__ double apply_flat(const QArgs& a, const double* __res
   const double xm = xin[u > 0 ? u - 1 : 0], xp = xin[u + 1];
   const double c0 = a.coef[u], c1 = a.coef[u + 1];
   if (QP == 1) {
-    const double cm = (act && k > ctop) ? c0 : 0.0;
-    const double cp = (act && k < nk - 1) ? c1 : 0.0;
+    const double cm = up ? c0 : 0.0;
+    const double cp = dn ? c1 : 0.0;
     y = __fma_rn(cm, xm, y);  // two FMAs, as in apply_slot
     y = __fma_rn(cp, xp, y);
-  } else if (ctop < nk - 1) {
-    if (k == ctop) y += (-2 * c0 - c1) * xu + c1 * xp;
-    else if (k == nk - 1) y += c0 * xm - c0 * xu;
+  } else if (up || dn) {  // ctop < nk - 1
+    if (!up) y += (-2 * c0 - c1) * xu + c1 * xp;  // k == ctop
+    else if (!dn) y += c0 * xm - c0 * xu;         // k == nk - 1
     else y += c0 * xm - (c0 + c1) * xu + c1 * xp;
   } else {
     y -= 2.0 * c0 * xu;
@@ -267,6 +266,7 @@ __global__ void __launch_bounds__(kBlock, SGPU_Q_MINB) cgsolveq_kernel(QArgs a) 
       const int ctop = a.ctop[j];
       const int nk = a.nk[j];
       const bool act = k >= ctop;
+      a.sflag[u] = (unsigned char)((act ? 1 : 0) | (act && k > ctop ? 2 : 0) | (act && k < nk - 1 ? 4 : 0));
       a.z[u] = 0.0;
       a.r[u] = 0.0;
       a.rt[u] = 0.0;

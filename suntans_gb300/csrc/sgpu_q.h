@@ -41,6 +41,7 @@ struct QArgs {
   double* fc;           // [F*n3c]
   int* nslot;           // [F*n3c] neighbour slot of each slot and face (the slot
                         // itself where the face does not couple: fc is 0 there)
+  unsigned char* sflag; // [n3c] bit 0: wet (k >= ctop); bit 1: k > ctop; bit 2: k < nk-1
   double* c;            // [n3]
   double* tw;           // [n3c] Thomas multipliers
   double* tib;          // [n3c] Thomas inverse pivots
