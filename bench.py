@@ -76,7 +76,14 @@ def q_bytes_per_unknown_iter(qprecond: int, F: int) -> int:
 # cases of the same constructions; a launch's traffic grows in proportion to
 # unknowns × iterations, so `traffic` below scales these to the launch timed.
 # profiles/cgsolveq_kernel_fp64_seamount50k.md, profiles/batch_kernel_mixed_seamount250k.md
-MEASURED_TRAFFIC_PER_UNKNOWN_ITER = {"cgsolveq_kernel<1>": 110.7, "batch_kernel<1>": 55.3}
+# (two-pass form), profiles/batch_kernel_onepass_seamount125k.md (one-pass form)
+MEASURED_TRAFFIC_PER_UNKNOWN_ITER = {"cgsolveq_kernel<1>": 119.2, "batch_kernel<1, 0>": 55.3,
+                                     "batch_kernel<1, 1>": 51.8}
+
+
+def batch_kernel_name(qprecond: int, fusion) -> str:
+    """The batched solver's kernel for a launch shape's form (2: the one-pass kernel)."""
+    return f"batch_kernel<{qprecond}, {1 if fusion == 2 and qprecond != 2 else 0}>"
 
 
 def h_bytes_per_unknown_iter(F: int) -> int:
@@ -941,8 +948,9 @@ def bench_cfg3(args, keep=None):
             "speedup_vs_plain_fp64": mf["equivalent_unknown_iters_per_s"] / plain_rate,
             "roofline": {"bound": "hbm", "achieved": mf["achieved_gbs_fp32_inner"], "peak": peak, "unit": "GB/s",
                          "frac": mf["achieved_gbs_fp32_inner"] / peak,
-                         "traffic": traffic(f"batch_kernel<{args.qprecond}>", N * mf["iters_inner"]),
-                         "kernel": f"batch_kernel<{args.qprecond}>",
+                         "traffic": traffic(batch_kernel_name(args.qprecond, shape["fusion"]),
+                                            N * mf["iters_inner"]),
+                         "kernel": batch_kernel_name(args.qprecond, shape["fusion"]),
                          "bytes_per_unknown_iter": FP32_BYTES_PER_UNKNOWN_ITER, "peak_kind": peak_kind},
             "e2e": {"value": N * st.niters / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 8 * N},
@@ -1044,8 +1052,9 @@ def bench_cfg4(args):
                        "status_ok": int(sum(st.status == 0 for _, st in res))},
             "autotune": table,
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": traffic(f"batch_kernel<{args.qprecond}>", float((Ns * itm).sum())),
-                         "kernel": f"batch_kernel<{args.qprecond}>",
+                         "traffic": traffic(batch_kernel_name(args.qprecond, best.get("fusion", 1)),
+                                            float((Ns * itm).sum())),
+                         "kernel": batch_kernel_name(args.qprecond, best.get("fusion", 1)),
                          "bytes_per_unknown_iter": FP32_BYTES_PER_UNKNOWN_ITER, "peak_kind": peak_kind},
             "e2e": {"value": e2e_work / e2e_s, "unit": "unknown-iters/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(8 * Ns.sum())},
