@@ -618,15 +618,22 @@ def run_ours(args):
     peak, peak_kind = peaks()
 
     # ---- end to end through the drop-in calls with host arrays ----
+    # The calls as the reference model makes them: row pointers into the
+    # caller's own storage, solutions written in place.  Each step restores
+    # the initial guesses first (the caller's state before the step, outside
+    # the timed calls), so every step solves the same systems.
     e2e_work = 0
-    t0 = time.perf_counter()
+    e2e_s = 0.0
     h2d = d2h = 0
     e2e_steps = max(1, min(args.steps, 3))
+    drop = ctx.dropin(qp, hp)
     for _ in range(e2e_steps):
-        q, sq = ctx.cgsolveq(qp, props)
-        h, sh = ctx.cgsolve(hp, props)
+        drop.reset()
+        t0 = time.perf_counter()
+        sq = drop.q_call(props)
+        sh = drop.h_call(props)
+        e2e_s += time.perf_counter() - t0
         e2e_work += sq.unknowns * sq.niters + sh.unknowns * sh.niters
-    e2e_s = time.perf_counter() - t0
     n3, ne3 = g.n3, int(g.Nke.sum())
     n3b = int(g.Nk[g.cellp[g.celldist[1]:]].sum())  # c goes up only at the type-3 boundary columns
     h2d = 8 * (3 * n3 + n3b + ne3 + g.Ne) + 4 * g.Nc + 8 * (2 * g.Nc + g.Ne)

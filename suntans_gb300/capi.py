@@ -187,6 +187,47 @@ def _vp(a: np.ndarray):
     return a.ctypes.data_as(_dpp)
 
 
+class DropIn:
+    """sgpu_cgsolveq / sgpu_cgsolve on caller-owned storage (Context.dropin):
+    q_call() and h_call() solve in place and return Stats; reset() restores the
+    initial guesses (the caller's state before the step)."""
+
+    def __init__(self, ctx, qprob, hprob):
+        g = ctx.grid
+        self.ctx = ctx
+        self.q0 = np.array(qprob.q, dtype=np.float64, copy=True)
+        self.q = self.q0.copy()
+        self.h0 = np.array(hprob.h, dtype=np.float64, copy=True)
+        self.h = self.h0.copy()
+        self.keep, self.P = ctx._q_ptrs(qprob, self.q)
+        self.Dq = np.ascontiguousarray(qprob.D, dtype=np.float64)
+        self.ctop = np.ascontiguousarray(g.ctop, dtype=np.int32)
+        self.htmp = np.ascontiguousarray(hprob.htmp, dtype=np.float64)
+        self.Dh = np.ascontiguousarray(hprob.D, dtype=np.float64)
+
+    def reset(self):
+        np.copyto(self.q, self.q0)
+        np.copyto(self.h, self.h0)
+
+    def q_call(self, props) -> "Stats":
+        st = Stats()
+        pr = props_struct(props)
+        P = self.P
+        rc = self.ctx.lib.sgpu_cgsolveq(self.ctx.h, self.ctop.ctypes.data_as(_ip), _vp(P["dzz"]), _vp(P["dzf"]),
+                                        self.Dq.ctypes.data_as(_dp), _vp(P["q"]), _vp(P["src"]), _vp(P["c"]),
+                                        C.byref(pr), C.byref(st))
+        self.ctx._check(rc, "sgpu_cgsolveq")
+        return st
+
+    def h_call(self, props) -> "Stats":
+        st = Stats()
+        pr = props_struct(props)
+        rc = self.ctx.lib.sgpu_cgsolve(self.ctx.h, self.Dh.ctypes.data_as(_dp), self.h.ctypes.data_as(_dp),
+                                       self.htmp.ctypes.data_as(_dp), C.byref(pr), C.byref(st))
+        self.ctx._check(rc, "sgpu_cgsolve")
+        return st
+
+
 class SolverError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"{msg} (status {code})")
@@ -594,6 +635,13 @@ class Context:
                                    htmp.ctypes.data_as(_dp), C.byref(pr), C.byref(st))
         self._check(rc, "sgpu_cgsolve")
         return h, st
+
+    def dropin(self, qprob, hprob):
+        """The two drop-in calls as the reference model makes them: the caller
+        owns its rows (here flat copies of the problems' fields, with row
+        pointers built once, as phys->qc, grid->dzz ... are), and each call
+        solves in place -- q rows (CGSolveQ) and h (CGSolve) overwritten."""
+        return DropIn(self, qprob, hprob)
 
     def h_upload(self, prob):
         h = np.ascontiguousarray(prob.h, dtype=np.float64)

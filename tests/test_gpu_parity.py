@@ -130,6 +130,27 @@ def test_repeat_is_bitwise_deterministic(gpu_lib):
     assert sa.niters == sb.niters and np.array_equal(a, b)
 
 
+def test_dropin_in_place_matches_copying_call(gpu_lib):
+    """The calls as the reference model makes them (row pointers into the
+    caller's storage, solutions written in place; the bench's end-to-end
+    leg) give the bits of the copying wrapper, and reset() restores the
+    caller's initial guesses so repeated steps solve the same systems."""
+    g = grid("tri3000_partial")
+    qp = gg.make_q_problem(g, seed=21, q0_sigma=0.01)
+    hp = gg.make_h_problem(g, seed=22)
+    ctx = Context(g)
+    q_ref, sq_ref = ctx.cgsolveq(qp, q_props(1))
+    h_ref, sh_ref = ctx.cgsolve(hp, h_props(1))
+    drop = ctx.dropin(qp, hp)
+    for _ in range(2):
+        drop.reset()
+        assert np.array_equal(drop.q, qp.q) and np.array_equal(drop.h, hp.h)
+        sq = drop.q_call(q_props(1))
+        sh = drop.h_call(h_props(1))
+        assert sq.niters == sq_ref.niters and np.array_equal(drop.q, q_ref)
+        assert sh.niters == sh_ref.niters and np.array_equal(drop.h, h_ref)
+
+
 def test_staged_solve_repeatable(gpu_lib, oracle):
     """upload once, solve twice on the resident inputs, download: same answer as the drop-in."""
     g = grid("quad64x16x32")
