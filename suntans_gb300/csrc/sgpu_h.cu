@@ -52,9 +52,14 @@
 
 namespace sgpu {
 
-constexpr int kHBlock = 512;  // threads per CTA of the free-surface kernel
+#ifndef SGPU_H_BLOCK
+#define SGPU_H_BLOCK 512
+#endif
+constexpr int kHBlock = SGPU_H_BLOCK;  // threads per CTA of the free-surface kernel (one CTA per SM)
 constexpr size_t kHStaticSmem = sizeof(double) * (2 * kHBlock + 2 + 8) + 64;
-constexpr size_t kHMaxDynSmem = 216 * 1024;  // the CTA's cells' vectors and coefficients
+// the CTA's cells' vectors and coefficients: what the 227 KB a CTA may hold
+// leaves beside the static arrays
+constexpr size_t kHMaxDynSmem = (227 * 1024 - kHStaticSmem) & ~(size_t)1023;
 
 // The per-thread cell loop over [b, e) with step BS, two cells per step so
 // that their gathers are in flight together: body(j0, j1, two) with j1 valid
