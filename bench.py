@@ -634,6 +634,7 @@ def run_ours(args):
         sh = drop.h_call(props)
         e2e_s += time.perf_counter() - t0
         e2e_work += sq.unknowns * sq.niters + sh.unknowns * sh.niters
+    q, h = drop.q, drop.h  # the drop-in solutions, checked against the oracle below
     n3, ne3 = g.n3, int(g.Nke.sum())
     n3b = int(g.Nk[g.cellp[g.celldist[1]:]].sum())  # c goes up only at the type-3 boundary columns
     h2d = 8 * (3 * n3 + n3b + ne3 + g.Ne) + 4 * g.Nc + 8 * (2 * g.Nc + g.Ne)
