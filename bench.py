@@ -115,6 +115,10 @@ def parse():
     ap.add_argument("--chunk", type=int, default=32)
     ap.add_argument("--sustain-rate", type=float, default=None,
                     help="cfg5: rate of the second (unsaturated) stream (default: half the served rate)")
+    ap.add_argument("--stride-cap", type=int, default=1,
+                    help="serving: largest stride for problems much larger than the smallest in flight (1 = off)")
+    ap.add_argument("--stride-ratio", type=float, default=8.0,
+                    help="serving: size ratio to the smallest problem in flight per doubling of the stride")
     ap.add_argument("--copies", type=int, default=2,
                     help="cfg5: resident copies a hot grid may have (1: one request per grid at a time, "
                          "results bit-identical alone and in the mix)")
@@ -1089,7 +1093,8 @@ def bench_cfg5(args):
               **capacity_for(grids * args.copies))
     b.use_graph(args.graph)
     srv = Server(pool, b, args.budget_gb * 1e9, lambda g: request_bytes(g, args.qprecond), chunk=args.chunk,
-                 maxiters=5000, keep_q=False, copies=args.copies)
+                 maxiters=5000, keep_q=False, copies=args.copies,
+                 stride_cap=getattr(args, "stride_cap", 1), stride_ratio=getattr(args, "stride_ratio", 8.0))
     # warm-up: one untimed request per grid (cold starts; every grid resident)
     srv.run([Request(-1 - k, k, 0, 1e-8, 0.0) for k in range(len(pool))], realtime=False)
     warm_launches = srv.launches
@@ -1132,6 +1137,7 @@ def bench_cfg5(args):
                                    "{1e-8, 1e-10}, warm starts",
                        "hbm_budget_gb": args.budget_gb, "pool_resident_gb": need / 1e9, "chunk_iters": args.chunk,
                        "qprecond": args.qprecond, "step": "one launch of the serving loop", "copies": args.copies,
+                       "stride_cap": getattr(args, "stride_cap", 1), "stride_ratio": getattr(args, "stride_ratio", 8.0),
                        "drain_limit_s": args.drain_seconds, "graph": args.graph},
             "latency": rep, "latency_at_sustainable_rate": rep2, "evictions": srv.evictions,
             "e2e": {"value": rep["unknown_iters_per_s"], "unit": "unknown-iters/s",

@@ -391,6 +391,15 @@ int sgpu_batch_set_tile_slots(sgpu_batch *b, int tile_slots);
  * that round differently.  Refused while a problem is in mid-solve under
  * another form.  (A tuning knob of this engine; the reference has none.) */
 int sgpu_batch_set_fusion(sgpu_batch *b, int form);
+/* Scheduling: problem `id` advances only on the global iterations it of a
+ * launch with it % stride == 0 (1, the default: on every one; 1..64).  Every
+ * global iteration costs time in proportion to the work of the problems that
+ * take part, so giving large problems a stride > 1 while small ones are in
+ * flight lets the small ones finish sooner.  A problem's own iterates, and so
+ * its result bits and iteration count, do not depend on its stride.  May be
+ * changed between launches, also in mid-solve.  (A scheduling knob of this
+ * engine; the reference has none.) */
+int sgpu_batch_set_stride(sgpu_batch *b, int id, int stride);
 void *sgpu_batch_stream(sgpu_batch *b);
 
 /* Device time of the last launch per phase (ns): [1] operator apply, [2]

@@ -76,6 +76,13 @@ class Batch:
         if rc != OK:
             raise SolverError(rc, "sgpu_batch_set_fusion")
 
+    def set_stride(self, i: int, stride: int):
+        """Problem i advances on every stride-th global iteration of a launch
+        (1 = every one); its result bits do not depend on it."""
+        rc = self.lib.sgpu_batch_set_stride(self.h, int(i), int(stride))
+        if rc != OK:
+            raise SolverError(rc, "sgpu_batch_set_stride")
+
     def set_tile_slots(self, n: int):
         """Storage slots per tile for problems added from now on (4..1024)."""
         rc = self.lib.sgpu_batch_set_tile_slots(self.h, int(n))

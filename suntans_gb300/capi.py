@@ -32,7 +32,7 @@ EXPORTS = [
     "sgpu_upredictor_grid", "sgpu_upredictor_vertical", "sgpu_upredictor_rhs", "sgpu_upredictor_finish",
     "sgpu_upredictor",
     "sgpu_batch_create", "sgpu_batch_destroy", "sgpu_batch_last_error", "sgpu_batch_bytes_per_request",
-    "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_launch", "sgpu_batch_wait", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set", "sgpu_batch_set_tile_slots", "sgpu_batch_set_fusion",
+    "sgpu_batch_add", "sgpu_batch_run", "sgpu_batch_launch", "sgpu_batch_wait", "sgpu_batch_state", "sgpu_batch_result", "sgpu_batch_set", "sgpu_batch_set_tile_slots", "sgpu_batch_set_fusion", "sgpu_batch_set_stride",
     "sgpu_batch_stream", "sgpu_batch_phase_times", "sgpu_batch_resubmit", "sgpu_batch_use_graph",
     "sgpu_batch_graph_launches",
 ]
@@ -160,6 +160,7 @@ def load() -> C.CDLL:
     lib.sgpu_batch_set.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_longlong]
     lib.sgpu_batch_set_tile_slots.argtypes = [C.c_void_p, C.c_int]
     lib.sgpu_batch_set_fusion.argtypes = [C.c_void_p, C.c_int]
+    lib.sgpu_batch_set_stride.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.sgpu_batch_stream.argtypes = [C.c_void_p]
     lib.sgpu_batch_stream.restype = C.c_void_p
     lib.sgpu_batch_phase_times.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]

@@ -1342,9 +1342,19 @@ __global__ void __launch_bounds__(kThreads, ONE ? 2 : SGPU_BATCH_MINB) batch_ker
   }
 
   // ============================ iterations ==============================
-  auto is_run = [&](int i) { return inst_state(a, i) == INST_RUN; };
+  // A running instance takes part in global iteration it unless its stride
+  // skips it (the same decision in every CTA: it and the stride are uniform);
+  // a skipped iteration leaves the instance's state untouched, so its own
+  // iteration sequence, and its bits, do not depend on the stride.
+  int it_now = 0;
+  auto is_run = [&](int i) {
+    if (inst_state(a, i) != INST_RUN) return false;
+    const int st = ld_volatile_int(&a.inst[i].stride);
+    return st <= 1 || it_now % st == 0;
+  };
   for (int it = 0; it < a.max_iters_chunk; ++it) {
     if (!ld_volatile_int(&a.gflags[3])) break;
+    it_now = it;
 
     if (QP != 2 && ONE) {
       // ---- one pass: r_j = r - nu z, x += nu p_old, p_j = r_j + mu p_old,
@@ -2526,6 +2536,13 @@ int sgpu_batch_set_fusion(sgpu_batch* b, int form) {
       return bfail(b, SGPU_BAD_ARG, "problem %d is in mid-solve", i);
   b->fusion = form;
   b->x_in_apply = form >= 1 ? 1 : 0;  // qprecond 2 runs form 2 as form 1
+  return SGPU_OK;
+}
+
+int sgpu_batch_set_stride(sgpu_batch* b, int id, int stride) {
+  if (!b || id < 0 || id >= b->max_inst || !b->inst[id].live || stride < 1 || stride > 64) return SGPU_BAD_ARG;
+  if (b->inflight) return bfail(b, SGPU_BAD_ARG, "a launch is in flight");
+  b->h_inst[id].stride = stride;  // uploaded with the instance table at the next launch
   return SGPU_OK;
 }
 

@@ -92,6 +92,8 @@ struct __align__(64) BInst {
                        // form, which r and z buffers hold the current residual and A p)
   int nrel;            // reliable updates done
   int s2;              // end of the instance's storage (boundary columns in [s1, s2))
+  int stride;          // iterates on a launch's global iterations it with it % stride == 0
+                       // (0 or 1: on every one); sgpu_batch_set_stride
   double alpha, eps, eps0, eps_ref;   // CG scalars (FP64)
   double mu, nu;
   double alpha_prev;

@@ -131,7 +131,7 @@ class Server:
     as when served alone."""
 
     def __init__(self, pool, engine, budget_bytes, request_bytes, chunk=64, maxiters=20000, keep_q=True,
-                 clock=time.perf_counter, sources=None, copies=1):
+                 clock=time.perf_counter, sources=None, copies=1, stride_cap=1, stride_ratio=8.0):
         self.pool = pool
         self.engine = engine
         self.budget = float(budget_bytes)
@@ -155,6 +155,10 @@ class Server:
         self.t0 = self.clock()
         self.sources = sources or (lambda r: request_src(pool, r))
         self.qbuf = {}  # grid -> reusable result buffer when results are not kept
+        # size-aware sharing of the lockstep launches (_set_strides)
+        self.stride_cap = max(1, int(stride_cap))
+        self.stride_ratio = float(stride_ratio)
+        self.stride_of = {}  # instance id -> stride last set
         self.host_s = {"admit": 0.0, "launch": 0.0, "harvest": 0.0}  # wall time by loop part
 
     # -- admission --------------------------------------------------------
@@ -162,6 +166,7 @@ class Server:
         for key, iid in self.resident.items():
             if key not in self.busy and key[0] != avoid:
                 self.engine.release(iid)
+                self.stride_of.pop(iid, None)  # the id may be reused by a later add (stride 1)
                 del self.resident[key]
                 self.ncopy[key[0]] -= 1
                 self.used -= self.rbytes[key[0]]
@@ -245,6 +250,30 @@ class Server:
                     self.grid_last[g] = (r.rid, q if self.keep_q else self.qbuf[g])
                 del self.busy[key]
 
+    def _set_strides(self):
+        """Every global iteration of a launch costs time in proportion to the
+        unknowns of the problems taking part, so in lockstep a small request
+        pays for the large ones beside it.  With stride_cap > 1 a problem in
+        flight with at least stride_ratio x s times the storage of the
+        smallest one in flight advances only on every s-th global iteration
+        (s = 2, 4, ... up to stride_cap): small requests finish sooner, large
+        ones later, and no result changes (the engine's strides leave every
+        problem's own iterates alone)."""
+        if self.stride_cap <= 1 or not hasattr(self.engine, "set_stride"):
+            return
+        sizes = {key: self.pool[key[0]][0].grid.n3 for key in self.busy}  # storage slots
+        if not sizes:
+            return
+        smallest = min(sizes.values())
+        for key, n in sizes.items():
+            s = 1
+            while s < self.stride_cap and n >= self.stride_ratio * smallest * s:
+                s *= 2
+            iid = self.resident[key]
+            if self.stride_of.get(iid, 1) != s:
+                self.engine.set_stride(iid, s)
+                self.stride_of[iid] = s
+
     def _admit_waiting(self, queues):
         """Admits waiting requests, oldest first across grids; a grid takes as
         many of its waiting requests as it has idle or new copies (one at a
@@ -290,6 +319,7 @@ class Server:
             t2 = self.clock()
             self.host_s["admit"] += t2 - t1
             if self.busy:
+                self._set_strides()
                 _, ms, work = self.engine.run(max_iters=self.chunk)
                 t3 = self.clock()
                 self.launches += 1
@@ -343,6 +373,7 @@ class Server:
             t4 = self.clock()
             self.host_s["admit"] += t4 - t3
             if self.busy:
+                self._set_strides()
                 self.engine.launch(max_iters=self.chunk)
                 inflight = True
                 # the other finished problems are read back while this launch runs

@@ -348,6 +348,45 @@ def test_one_pass_form_alone_equals_in_batch(gpu_lib):
     assert st.niters == alone[1].niters and np.array_equal(q, alone[0])
 
 
+@pytest.mark.parametrize("form", [1, 2])
+def test_stride_pauses_problems_without_changing_their_bits(gpu_lib, form):
+    """A problem with stride s takes part in every s-th global iteration of a
+    launch (the first launch of 12: strides 3 and 2 give 4 and 6 iterations,
+    counted in the launch's work), and its result and iteration count are
+    those of the unstrided batch, bit for bit; a stride may change in
+    mid-solve."""
+    grids = tri_grids()
+    probs = [gg.make_q_problem(g, seed=100 + k) for k, g in enumerate(grids)]
+    N = [g.n_q() for g in grids]
+    out = {}
+    for strided in (False, True):
+        b = Batch(qprecond=1, maxfaces=3, **capacity_for(grids))
+        b.set_fusion(form)
+        ids = [b.add(p) for p in probs]
+        if strided:
+            b.set_stride(ids[1], 3)
+            b.set_stride(ids[2], 2)
+        running, _, work = b.run(max_iters=12)
+        assert running == len(probs)
+        sweeps = [12, 4, 6, 12] if strided else [12] * 4
+        if form == 1:
+            assert work == sum(n * k for n, k in zip(N, sweeps)), (work, sweeps)
+        else:
+            # the one-pass form's first sweep forms the first direction and
+            # counts no iteration (nor does a sweep after a reliable update)
+            expect = sum(n * (k - 1) for n, k in zip(N, sweeps))
+            assert expect - 2 * max(N) <= work <= expect, (work, expect)
+        if strided:
+            b.set_stride(ids[1], 1)  # changed in mid-solve
+        while b.run()[0]:
+            pass
+        out[strided] = [b.result(i, p.q) for i, p in zip(ids, probs)]
+        b.close()
+    for (q, st), (q0, st0) in zip(out[True], out[False]):
+        assert st.status == st0.status == OK and st.niters == st0.niters
+        assert np.array_equal(q, q0)
+
+
 def test_fusion_change_refused_mid_solve(gpu_lib):
     g = tri_grids()[1]
     b = Batch(qprecond=1, maxfaces=3, **capacity_for([g]))

@@ -288,3 +288,58 @@ def test_copies_serve_a_hot_grid_in_parallel(Eng):
     reqs = [Request(k, 0, 0, 1e-8, 0.0) for k in range(2)]
     srv.run(reqs, realtime=False)
     assert srv.ncopy[0] == 1 and srv.evictions == 0 and all(r.t_done >= 0 for r in reqs)
+
+
+class StridedEngine(FakeEngine):
+    """FakeEngine whose launches honour per-problem strides (a problem with
+    stride s advances on every s-th global iteration of a launch)."""
+
+    def __init__(self, cap):
+        super().__init__(cap)
+        self.strides = {}
+        self.log = []
+
+    def set_stride(self, i, s):
+        self.strides[i] = s
+        self.log.append((i, s))
+
+    def run(self, max_iters=0):
+        work, running = 0, 0
+        for i, I in self.inst.items():
+            if I["state"] in (1, 2):
+                s = self.strides.get(i, 1)
+                cap = I["left"] if max_iters <= 0 else -(-max_iters // s)
+                k = min(I["left"], cap)
+                I["left"] -= k
+                I["it"] += k
+                work += k * I["n"]
+                I["state"] = 3 if I["left"] == 0 else 2
+                running += I["state"] != 3
+        return running, 0.1, work
+
+    def release(self, i):
+        super().release(i)
+        self.strides.pop(i, None)
+
+
+def test_strides_slow_large_problems_while_small_ones_are_in_flight():
+    """stride_cap 4, ratio 8: beside a 100-unknown problem, one of 1000 gets
+    stride 2 and one of 5000 stride 4; alone, a large problem runs at stride 1
+    again; with the default stride_cap nothing is set."""
+    pool = fake_pool([100, 1000, 5000], rhs=1)
+    eng = StridedEngine(10 ** 9)
+    srv = Server(pool, eng, 1e12, rbytes, chunk=8, keep_q=False, stride_cap=4, stride_ratio=8.0)
+    reqs = [Request(k, k, 0, 1e-10, 0.0) for k in range(3)]
+    srv.run(reqs, realtime=False)
+    first = dict(eng.log[:2])
+    assert first == {1: 2, 2: 4}, eng.log
+    # once the small request is done the large ones go back to stride 1
+    assert (1, 1) in eng.log[2:] or (2, 1) in eng.log[2:], eng.log
+    assert all(r.t_done >= 0 and r.iters == 80 for r in reqs)
+    # 80 iterations at chunk 8: the small request in launch 10; beside it the
+    # others advanced 40 (stride 2) and 20 (stride 4), then 8 per launch
+    assert [r.launch_done for r in reqs] == [10, 15, 18]
+    eng2 = StridedEngine(10 ** 9)
+    Server(pool, eng2, 1e12, rbytes, chunk=8, keep_q=False).run([Request(k, k, 0, 1e-10, 0.0) for k in range(3)],
+                                                                  realtime=False)
+    assert eng2.log == []
