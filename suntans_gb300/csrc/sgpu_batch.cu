@@ -34,10 +34,13 @@
 // r.s, r.r) -- the producer streams each tile's header and its contiguous FP32
 // streams into a two-stage shared-memory ring with bulk asynchronous copies
 // (cp.async.bulk + mbarrier), so the compute warps never wait on metadata
-// chains.  Only when some problem asks for it run the reliable-update phases
-// R1 (x64 += x32) and R2 (FP64 true residual).  Each phase ends at a grid
-// barrier; per-problem reductions finish before it in the CTA that completes
-// the problem's last tile.
+// chains.  The one-pass form (qprecond 0/1, a kernel instantiation of its
+// own) does an iteration in one such sweep: the pending residual step, the
+// solution update, the new direction and z = A p, with the next mu from the
+// sweep's r.r, r.z and z.z.  Only when some problem asks for it run the
+// reliable-update phases R1 (x64 += x32) and R2 (FP64 true residual).  Each
+// phase ends at a grid barrier; per-problem reductions are collected by the
+// CTA that holds the problem's first tile.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
