@@ -39,8 +39,9 @@
 // solution update, the new direction and z = A p, with the next mu from the
 // sweep's r.r, r.z and z.z.  Only when some problem asks for it run the
 // reliable-update phases R1 (x64 += x32) and R2 (FP64 true residual).  Each
-// phase ends at a grid barrier; per-problem reductions are collected by the
-// CTA that holds the problem's first tile.
+// phase ends at a grid barrier; per-problem reductions finish before it, in
+// the CTA holding the problem's first tile (pipelined phases) or in the CTA
+// that completes its last tile (set-up and residual phases).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
