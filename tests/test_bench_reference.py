@@ -57,3 +57,18 @@ def test_parity_job_compares_with_the_oracle():
     assert "error" not in r, r
     assert r["q"]["rel_l2"] == 0.0 and r["h"]["rel_l2"] == 0.0
     assert r["q"]["iters_oracle"] > 2 and r["h"]["iters_oracle"] > 2
+
+
+def test_roofline_traffic_names_the_kernel_of_the_form():
+    """The mixed lines name the batched kernel of the form the autotuner
+    picked (the one-pass form has a kernel of its own, qprecond 0/1 only) and
+    scale that kernel's measured bytes per unknown-iteration."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.batch_kernel_name(1, 2) == "batch_kernel<1, 1>"
+    assert bench.batch_kernel_name(1, 1) == "batch_kernel<1, 0>"
+    assert bench.batch_kernel_name(1, 0) == "batch_kernel<1, 0>"
+    assert bench.batch_kernel_name(2, 2) == "batch_kernel<2, 0>"
+    for k in ("cgsolveq_kernel<1>", "batch_kernel<1, 0>", "batch_kernel<1, 1>"):
+        assert bench.traffic(k, 1000) == 1000 * bench.MEASURED_TRAFFIC_PER_UNKNOWN_ITER[k]
+    assert bench.traffic("batch_kernel<2, 0>", 1000) is None
